@@ -1,0 +1,147 @@
+"""The CPU oracle against the reference's golden vector and independent definitions."""
+import json
+import os
+
+import numpy as np
+import pytest
+import scipy.fft as sf
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _hc(x):
+    n = x.shape[0]
+    X = np.fft.rfft(x, axis=0)
+    hc = np.zeros_like(x)
+    hc[: n // 2 + 1] = X.real[: n // 2 + 1]
+    for k in range(1, (n + 1) // 2):
+        hc[n - k] = X.imag[k]
+    return hc
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 8, 13, 16, 48, 64, 97, 112, 384])
+def test_r2r_kinds_match_scipy(n):
+    """FFTW r2r semantics (src/fft.f90:260-313 kinds) vs pocketfft and numpy."""
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((n, 4))
+    cases = [(O.R2HC, _hc(x)), (O.HC2R, None),
+             (O.REDFT10, sf.dct(x, 2, axis=0)), (O.REDFT01, sf.dct(x, 3, axis=0)),
+             (O.RODFT10, sf.dst(x, 2, axis=0)), (O.RODFT01, sf.dst(x, 3, axis=0)),
+             (O.REDFT11, sf.dct(x, 4, axis=0)), (O.RODFT11, sf.dst(x, 4, axis=0)),
+             (O.RODFT00, sf.dst(x, 1, axis=0))]
+    if n >= 2:
+        cases.append((O.REDFT00, sf.dct(x, 1, axis=0)))
+    for kind, ref in cases:
+        if kind == O.HC2R:
+            y = O.r2r(O.HC2R, _hc(x))
+            ref = x * n
+        else:
+            y = O.r2r(kind, x)
+        err = np.abs(y - ref).max() / np.abs(ref).max()
+        assert err < 5e-15 * max(1.0, np.log2(max(n, 2))), (kind, err)
+
+
+def test_r2r_direct_sums_long_double():
+    """DCT-II / DST-II against O(N^2) sums in extended precision."""
+    n = 24
+    x = np.random.default_rng(1).standard_normal(n)
+    j = np.arange(n, dtype=np.longdouble)
+    k = j[:, None]
+    pi = np.longdouble(np.pi)
+    dct2 = 2 * (np.cos(pi * (2 * j + 1) * k / (2 * n)) * x.astype(np.longdouble)).sum(axis=1)
+    dst2 = 2 * (np.sin(pi * (2 * j + 1) * (k + 1) / (2 * n)) * x.astype(np.longdouble)).sum(axis=1)
+    assert np.abs(O.r2r(O.REDFT10, x) - dct2.astype(float)).max() < 1e-14
+    assert np.abs(O.r2r(O.RODFT10, x) - dst2.astype(float)).max() < 1e-14
+
+
+def test_eigenvalues_tridmatrix():
+    """src/initsolver.f90:85-187 on a few BC pairs."""
+    lam = O.eigenvalues(8, "PP", "c")
+    assert np.allclose(lam, -2 * (1 - np.cos(2 * np.arange(8) * np.pi / 8)))
+    lam = O.eigenvalues(8, "NN", "c")
+    assert np.allclose(lam, -2 * (1 - np.cos(np.arange(8) * np.pi / 8)))
+    lam = O.eigenvalues(8, "DD", "f")
+    assert lam[-1] == 0.0 and np.allclose(lam[:-1], -2 * (1 - np.cos(np.arange(1, 8) * np.pi / 8)))
+    dzc, dzf, zc, zf = O.initgrid(1, 16, 1.4, 2.0, False)
+    assert abs(zf[16] - 2.0) < 1e-14 and np.all(dzf[1:17] > 0)
+    a, b, c = O.tridmatrix("NN", 16, 1 / dzc, 1 / dzf, "c")
+    assert b[0] == -c[0] and b[-1] == -a[-1]
+
+
+def _poisson_residual(n, dli, dzci, dzfi, cbc, p, rhs):
+    """lap(p) - rhs on the interior (the operator of src/debug.f90:91-132)."""
+    from numpy import s_
+    i, j, k = s_[1:n[0] + 1], s_[1:n[1] + 1], s_[1:n[2] + 1]
+    lap = ((p[2:, j, k] - 2 * p[i, j, k] + p[:-2, j, k]) * dli[0] ** 2
+           + (p[i, 2:, k] - 2 * p[i, j, k] + p[i, :-2, k]) * dli[1] ** 2
+           + ((p[i, j, 2:] - p[i, j, k]) * dzci[1:n[2] + 1] - (p[i, j, k] - p[i, j, :-2]) * dzci[0:n[2]])
+           * dzfi[1:n[2] + 1])
+    return lap - rhs[i, j, k]
+
+
+@pytest.mark.parametrize("cbc", ["PPPPNN", "PPNNNN", "NNDDPP", "DDNNDD", "PPPPPP"])
+def test_solver_inverts_laplacian(cbc):
+    """solver() output satisfies the 7-point Poisson equation with the BC ghosts of boundp."""
+    n = [12, 10, 9]
+    l = [1.3, 0.7, 2.0]
+    dl = [l[d] / n[d] for d in range(3)]
+    dli = [1 / x for x in dl]
+    zper = cbc[4:] == "PP"
+    dzc, dzf, zc, zf = O.initgrid(1, n[2], 0.0 if zper else 1.4, l[2], zper)
+    dzci, dzfi = 1 / dzc, 1 / dzf
+    s = O.initsolver(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc")
+    rng = np.random.default_rng(3)
+    p = O.field(n)
+    p[1:-1, 1:-1, 1:-1] = rng.standard_normal(n)
+    if "D" not in cbc:  # compatible RHS: remove the volume-weighted mean
+        wts = dzf[1:-1][None, None, :] * np.ones(n)
+        p[1:-1, 1:-1, 1:-1] -= (p[1:-1, 1:-1, 1:-1] * wts).sum() / wts.sum()
+    rhs = p.copy()
+    O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], cbc, "ccc", p)
+    is_bound = [1, 1] + [0 if cbc[2 * d:2 * d + 2] == "PP" else 1 for d in (1, 2) for _ in (0, 1)]
+    O.boundp(cbc, n, [0.] * 6, is_bound, dl, dzc, p)
+    res = _poisson_residual(n, dli, dzci, dzfi, cbc, p, rhs)
+    assert np.abs(res).max() < 1e-9 * np.abs(rhs).max() * max(dli) ** 2 / 10
+
+
+def test_projection_is_divergence_free():
+    """src/sanity.f90:206-284: noise velocity -> fillps -> solver -> correc -> chkdiv < small."""
+    n = [16, 12, 10]
+    l = [1.0, 1.0, 1.0]
+    cbcvel = "PPDDDD" * 3
+    cbcpre = "PPNNNN"
+    dl = [l[d] / n[d] for d in range(3)]
+    dli = [1 / x for x in dl]
+    dzc, dzf, zc, zf = O.initgrid(1, n[2], 1.2, l[2], False)
+    dzci, dzfi = 1 / dzc, 1 / dzf
+    s = O.initsolver(n, dli, dzci, dzfi, cbcpre, [0.] * 6, "ccc")
+    is_bound = [1, 1, 1, 1, 1, 1]
+    u, v, w, p = O.field(n), O.field(n), O.field(n), O.field(n)
+    for f, seed in ((u, 123), (v, 456), (w, 789)):
+        O.add_noise(n, seed, 0.5, f)
+    dt = np.arccos(np.float32(-1.0)).astype(np.float64)
+    O.bounduvw(cbcvel, n, [0.] * 18, is_bound, dl, dzc, dzf, u, v, w, False, O.HALO_LOWER)
+    O.fillps(n, dli, dzfi, 1 / dt, u, v, w, p)
+    O.updt_rhs_b("ccc", cbcpre, n, is_bound, s["rhsb"], p)
+    O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], cbcpre, "ccc", p)
+    O.boundp(cbcpre, n, [0.] * 6, is_bound, dl, dzc, p)
+    O.correc(n, dli, dzci, dt, p, u, v, w)
+    O.bounduvw(cbcvel, n, [0.] * 18, is_bound, dl, dzc, dzf, u, v, w, True, O.HALO_UPPER, O.HALO_NONE)
+    divtot, divmax = O.chkdiv(n, l, dli, dzfi, u, v, w)
+    small = np.finfo(float).eps * 10 ** (np.finfo(float).precision // 2)
+    assert divmax < small
+
+
+def test_lid_driven_cavity_golden():
+    """Pin: the reference's own regression (tests/lid_driven_cavity/test.py:5-8), 1500 steps."""
+    case = json.load(open(os.path.join(GOLD, "ldc_re1000_case.json")))
+    ref = np.loadtxt(os.path.join(GOLD, "ldc_re1000_vprofile.txt"))
+    r = O.Run(case)
+    r.start()
+    r.step(case["nstep"])
+    n = case["ng"]
+    prof = r.v[1, n[1] // 2 + 1, 1:n[2] + 1]
+    np.testing.assert_allclose(r.grid()["zc"][1:n[2] + 1], ref[:, 0], rtol=1e-7)
+    np.testing.assert_allclose(prof, ref[:, 1], rtol=1e-7, atol=0)
