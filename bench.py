@@ -1,0 +1,310 @@
+"""Benchmark: Poisson solves/s and RK3-step Mcell/s at 512^3 on one GB300.
+
+Workload (headline `value`): the Poisson/pressure solve of the reference's
+src/solver_gpu.f90 on a 512^3 channel-type grid -- periodic x and y (FFT),
+Neumann z walls on a tanh-stretched grid (gr = 1.4), Lx = 4*pi, Ly = 2*pi,
+Lz = 2 -- FP64, with a seeded N(0,1) right-hand side (mean removed).  One step
+is one in-place solve of the device field (inputs resident in HBM; every field
+touched is 1 GB, far larger than the 129 MB L2).  Secondary: one full RK3 time
+step (src/main.f90:437-473) of the 512^3 triperiodic Taylor-Green vortex.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's solver (the
+oracle, OpenMP on all host cores) on the same workload: the reference itself is
+Fortran + MPI + FFTW and cannot be built on these machines.
+
+Multi-GPU: the solve does not shard without an all-to-all; N ranks run N
+independent replicas (weak scaling) and `value` is the total solves/s.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Poisson solves/s & RK3-step Mcell/s at 512^3; FP32+refine vs FP64 at equal error"
+N_DEFAULT = 512
+L_CH = (4 * np.pi, 2 * np.pi, 2.0)
+BYTES_PER_CELL_PASS = 16  # each of the five passes reads and writes one FP64 value per cell
+
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_for(kernel, workload):
+    """DRAM bytes per launch from a committed ncu summary, if one exists for this kernel+workload."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        return t.get(workload, {}).get(kernel)
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"cans_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, val in zip(names, r[3:7]):
+                if val.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(rows[0][1]), "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def make_rhs(n, dzf, device, seed=20260101):
+    """seeded N(0,1) RHS with the volume-weighted mean removed (compatible with Neumann z)"""
+    import torch
+    from cans_gb300 import cans
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    p = cans.field(n, device)
+    inner = torch.randn((n[2], n[1], n[0]), generator=g, device=device, dtype=torch.float64)
+    w = torch.tensor(dzf[1:-1], device=device, dtype=torch.float64)[:, None, None]
+    inner -= (inner * w).sum() / (w.sum() * n[0] * n[1])
+    p[1:-1, 1:-1, 1:-1] = inner
+    return p
+
+
+def bench_ours(args, rank, world):
+    import torch
+    from cans_gb300 import cans
+    from cans_gb300.driver import Simulation, initgrid
+    dev = f"cuda:{rank % max(1, torch.cuda.device_count())}"
+    torch.cuda.set_device(dev)
+    n = [args.size] * 3
+    dl = [L_CH[d] / n[d] for d in range(3)]
+    dli = [1. / x for x in dl]
+    dzc, dzf, zc, zf = initgrid(1, n[2], 1.4, L_CH[2], False)
+    plan = cans.Plan(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc")
+    p = make_rhs(n, dzf, dev)
+    ncell = n[0] * n[1] * n[2]
+    for _ in range(args.warmup):
+        plan.solve(p)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    plan.set_timing(True)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = cans.launch_count()
+    with Clocks(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(args.steps):
+            plan.solve(p)
+        e1.record(st)
+        torch.cuda.synchronize()
+    launches = cans.launch_count() - l0
+    ms = e0.elapsed_time(e1) / args.steps
+    pass_ms, nrec = plan.get_timing()
+    plan.set_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world / (ms * 1e-3)
+    # roofline of the dominant pass
+    names = ["solve_xfwd", "solve_yfwd", "solve_zthomas", "solve_ybwd", "solve_xbwd"]
+    top = int(np.argmax(pass_ms))
+    hbm, kind = peaks()
+    achieved = BYTES_PER_CELL_PASS * ncell / (pass_ms[top] * 1e-3) / 1e9
+    workload = f"poisson_{n[0]}x{n[1]}x{n[2]}_PPPPNN_fp64"
+    roof = {"bound": "hbm", "kernel": names[top], "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "peak_source": kind,
+            "traffic": traffic_for(names[top], workload),
+            "algorithmic_bytes_per_launch": BYTES_PER_CELL_PASS * ncell,
+            "pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)},
+            "solve_achieved_gbs": round(5 * BYTES_PER_CELL_PASS * ncell / (ms * 1e-3) / 1e9, 1)}
+    # end-to-end through the C ABI with host buffers: H2D rhs, solve, D2H solution
+    host_in = torch.empty(p.shape, dtype=torch.float64, pin_memory=True)
+    host_in.copy_(make_rhs(n, dzf, dev, seed=7).cpu())
+    host_out = torch.empty_like(host_in, pin_memory=True)
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ke2e = max(1, min(args.steps, 5))
+    e2.record(st)
+    for _ in range(ke2e):
+        p.copy_(host_in, non_blocking=True)
+        plan.solve(p)
+        host_out.copy_(p, non_blocking=True)
+    e3.record(st)
+    torch.cuda.synchronize()
+    ms_e2e = e2.elapsed_time(e3) / ke2e
+    nbytes = p.numel() * 8
+    e2e = {"value": round(world / (ms_e2e * 1e-3), 3), "unit": "solves/s", "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes}
+    del host_in, host_out
+    # secondary: RK3 step of the 512^3 Taylor-Green vortex (all kernels of one time step)
+    rk3 = None
+    if not args.skip_rk3:
+        del p, plan
+        torch.cuda.empty_cache()
+        rk3 = bench_rk3(args.size, dev, max(1, min(args.steps, 5)))
+    out = {"metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) RHS, mean removed)",
+           "config": {"workload": workload, "grid": n, "bc_pressure": "PP,PP,NN", "z_grid": "tanh gr=1.4",
+                      "domain": [round(x, 6) for x in L_CH], "precision": "fp64",
+                      "l2": "working set 4+ GB per solve >> 129 MB L2 (no flush needed)",
+                      "parallelism": f"replicas x{world}"},
+           "e2e": e2e, "roofline": roof, "clocks": clk.summary(), "gpu_launches": launches}
+    if rk3:
+        out["rk3_step"] = rk3
+    return out
+
+
+def bench_rk3(size, dev, steps):
+    import torch
+    from cans_gb300 import cans
+    from cans_gb300.driver import Simulation
+    n = size
+    case = dict(ng=[n, n, n], l=[2 * np.pi] * 3, gtype=1, gr=0., cfl=0.5, dtmax=1e5, dt_f=-1., visci=1600.,
+                icheck=0, cbcvel="PP" * 9, cbcpre="PP" * 3, bcvel=[0.] * 18, bcpre=[0.] * 6)
+    sim = Simulation(case, device=dev)
+    dl = 2 * np.pi / n
+    x = (torch.arange(1, n + 1, device=dev, dtype=torch.float64) - 0.5) * dl
+    xf = torch.arange(1, n + 1, device=dev, dtype=torch.float64) * dl
+    # initflow 'tgv' (src/initflow.f90:102-117) with the analytic pressure
+    Z, Y, X = torch.meshgrid(x, x, xf, indexing="ij")
+    sim.u[1:-1, 1:-1, 1:-1] = torch.sin(X) * torch.cos(Y) * torch.cos(Z)
+    Z, Y, X = torch.meshgrid(x, xf, x, indexing="ij")
+    sim.v[1:-1, 1:-1, 1:-1] = -torch.cos(X) * torch.sin(Y) * torch.cos(Z)
+    Z, Y, X = torch.meshgrid(x, x, x, indexing="ij")
+    sim.p[1:-1, 1:-1, 1:-1] = (torch.cos(2 * X) + torch.cos(2 * Y)) * (torch.cos(2 * Z) + 2.) / 16.
+    del X, Y, Z
+    sim.start()
+    sim.step(1)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = cans.launch_count()
+    e0.record(st)
+    sim.step(steps)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"workload": f"tgv_{n}^3_rk3_fp64", "value": round(n ** 3 / (ms * 1e-3) / 1e6, 2), "unit": "Mcell/s",
+            "ms_per_step": round(ms, 3), "steps": steps, "gpu_launches_per_step": (cans.launch_count() - l0) // steps}
+
+
+def bench_cpu(size, steps, warmup, threads=None):
+    """The oracle (CPU restatement of src/solver.f90 with FFTW r2r semantics), all host cores."""
+    from oracle import oracle as O
+    if threads:
+        O.set_num_threads(threads)
+    n = [size] * 3
+    dl = [L_CH[d] / n[d] for d in range(3)]
+    dli = [1. / x for x in dl]
+    dzc, dzf, zc, zf = O.initgrid(1, n[2], 1.4, L_CH[2], False)
+    s = O.initsolver(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc")
+    p = O.field(n)
+    rng = np.random.default_rng(20260101)
+    p[1:-1, 1:-1, 1:-1] = rng.standard_normal(n)
+    times = []
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], "PPPPNN", "ccc", p)
+        if it >= warmup:
+            times.append(time.perf_counter() - t0)
+    sec = float(np.mean(times))
+    return sec, O.num_threads()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=N_DEFAULT)
+    ap.add_argument("--skip-rk3", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sec, cores = bench_cpu(args.size, args.steps, min(args.warmup, 1))
+        val = 1.0 / sec
+        out = {"metric": METRIC, "impl": "reference", "value": round(val, 5), "unit": "solves/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2),
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+               "data": "synthetic (seeded N(0,1) RHS)",
+               "config": {"workload": f"poisson_{args.size}x{args.size}x{args.size}_PPPPNN_fp64",
+                          "grid": [args.size] * 3, "bc_pressure": "PP,PP,NN", "z_grid": "tanh gr=1.4"},
+               "cpu_baseline": {"value": round(val, 5), "unit": "solves/s", "cores": cores, "kind": "port",
+                                "sample": f"{args.steps} full {args.size}^3 solves of the C/OpenMP restatement "
+                                          "of src/solver.f90 (reference Fortran/MPI/FFTW build unavailable)"},
+               "e2e": {"value": round(val, 5), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = bench_ours(args, rank, world)
+    if rank == 0:
+        if not args.skip_cpu:
+            sec, cores = bench_cpu(args.size, 1, 0)
+            out["cpu_baseline"] = {"value": round(1.0 / sec, 5), "unit": "solves/s", "cores": cores, "kind": "port",
+                                   "sample": f"1 full {args.size}^3 solve of the C/OpenMP restatement of "
+                                             "src/solver.f90 on the host cores"}
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,268 @@
+"""Python host mirror of the CaNS routines on the pressure-correction path.
+
+Binds the C ABI of libcans_gb300.so (include/cans_gb300.h) with ctypes.  The
+function names, argument order and meaning follow the reference Fortran
+routines (src/initsolver.f90, src/solver_gpu.f90, src/fillps.f90, ...); device
+memory comes from torch (plumbing only: every computation runs in the library's
+own CUDA kernels).  There is no CPU fallback: importing this module on a
+machine without the built library raises.
+
+Field layout: haloed fields are torch float64 CUDA tensors of shape
+(n3+2, n2+2, n1+2) -- the same bytes as the reference's Fortran arrays
+p(0:n1+1, 0:n2+1, 0:n3+1).  `fview(t)` returns the Fortran-indexed numpy view
+[i, j, k] of a tensor copied to the host.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK, EINVAL, ENOMEM, ECUDA, ENOTSUP, ETIMEOUT, ENONFINITE = range(7)
+FP64, FP32 = 0, 1
+HALO_LOWER, HALO_NONE, HALO_UPPER, HALO_BOTH = -1, 0, 1, 2
+
+_lib = None
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_V = C.c_void_p
+
+
+class CansError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        super().__init__(f"{where}: {lib().cans_strerror(status).decode()} (status {status})")
+
+
+def lib_path():
+    return _build.LIB
+
+
+def lib():
+    """Load libcans_gb300.so (building it first if this tree has nvcc and no library)."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            path = _build.build()
+        _lib = C.CDLL(path)
+        _setup(_lib)
+    return _lib
+
+
+def _setup(L):
+    L.cans_strerror.restype = C.c_char_p
+    L.cans_strerror.argtypes = [C.c_int]
+    L.cans_version.restype = C.c_char_p
+    L.cans_initgrid.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, _D, _D, _D, _D]
+    L.cans_initsolver.argtypes = [_I, _D, _D, _D, C.c_char_p, _D, C.c_char_p, C.c_int, _V, C.POINTER(_V),
+                                  _D, _D, _D, _D, _D, _D]
+    L.cans_plan_destroy.argtypes = [_V]
+    L.cans_plan_device_bytes.argtypes = [_V]
+    L.cans_plan_device_bytes.restype = C.c_longlong
+    L.cans_plan_set_timing.argtypes = [_V, C.c_int]
+    L.cans_plan_get_timing.argtypes = [_V, _D, _I]
+    L.cans_launch_count.restype = C.c_longlong
+    L.cans_solver.argtypes = [_V, _V]
+    L.cans_solver_f32.argtypes = [_V, _V]
+    L.cans_solver_refined.argtypes = [_V, _V, _D, _V, _V, C.c_double, C.c_int, _I, _D]
+    L.cans_solve_helmholtz.argtypes = [_V, C.c_double, _I, _V]
+    L.cans_fillps.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
+    L.cans_correc.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
+    L.cans_updatep.argtypes = [_I, _D, _V, _V, C.c_double, C.c_int, _V, _V, _V]
+    L.cans_rk.argtypes = [_D, _I, _D, _V, _V, _V, _V, C.c_double, C.c_double, _V, _I, _D, _D, C.c_int,
+                          _V, _V, _V, _V, _V, _V, _D, _V, _V]
+    L.cans_bounduvw.argtypes = [C.c_char_p, _I, _D, _I, _D, _D, _D, _V, _V, _V, C.c_int, C.c_int, C.c_int, _V]
+    L.cans_boundp.argtypes = [C.c_char_p, _I, _D, _I, _D, _D, _V, C.c_int, _V]
+    L.cans_updt_rhs_b.argtypes = [C.c_char_p, C.c_char_p, _I, _I, _D, _V, C.c_double, C.c_int, _V]
+    L.cans_chkdiv.argtypes = [_I, _D, _D, _V, _V, _V, _V, _D, _D, _V]
+    L.cans_chkdt.argtypes = [_I, _D, _V, _V, C.c_double, C.c_double, C.c_int, C.c_int, _V, _V, _V, _D, _V]
+    L.cans_bulk_mean.argtypes = [_I, _V, _V, _D, _V]
+
+
+def _check(rc, where):
+    if rc != OK:
+        raise CansError(rc, where)
+
+
+def _ints(v):
+    return (C.c_int * len(v))(*[int(x) for x in v])
+
+
+def _dbls(v):
+    return (C.c_double * len(v))(*[float(x) for x in v])
+
+
+def _chars(s):
+    return s.encode() if isinstance(s, str) else bytes(s)
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _hp(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_D)
+
+
+def _stream(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+# ------------------------------------------------------------------------------ fields
+def field(n, device="cuda", dtype=None):
+    import torch
+    return torch.zeros((n[2] + 2, n[1] + 2, n[0] + 2), dtype=dtype or torch.float64, device=device)
+
+
+def to_device(arr_f, device="cuda", dtype=None):
+    """Fortran-indexed numpy array [i, j, k] -> device tensor (k, j, i)."""
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(arr_f).transpose(2, 1, 0))).to(
+        device=device, dtype=dtype or torch.float64)
+
+
+def fview(t):
+    """device tensor (k, j, i) -> Fortran-indexed numpy array [i, j, k] (host copy)."""
+    return t.detach().cpu().numpy().transpose(2, 1, 0)
+
+
+# ------------------------------------------------------------------------------ solver plan
+class Plan:
+    """initsolver + the device plan (src/initsolver.f90:15, src/fft.f90:25)."""
+
+    def __init__(self, ng, dli, dzci_g, dzfi_g, cbc, bc, c_or_f="ccc", precision=FP64, stream=None):
+        ng = [int(x) for x in ng]
+        self.ng = ng
+        self.cbc, self.c_or_f = cbc, c_or_f
+        self.lambdaxy = np.zeros((ng[0], ng[1]), order="F")
+        self.a, self.b, self.c = np.zeros(ng[2]), np.zeros(ng[2]), np.zeros(ng[2])
+        normfft = C.c_double()
+        rhsb = (C.c_double * 6)()
+        h = C.c_void_p()
+        dzci_g, pzc = _hp(dzci_g)
+        dzfi_g, pzf = _hp(dzfi_g)
+        rc = lib().cans_initsolver(_ints(ng), _dbls(dli), pzc, pzf, _chars(cbc), _dbls(bc), _chars(c_or_f),
+                                   int(precision), _stream(stream), C.byref(h),
+                                   self.lambdaxy.ctypes.data_as(_D), self.a.ctypes.data_as(_D),
+                                   self.b.ctypes.data_as(_D), self.c.ctypes.data_as(_D), C.byref(normfft), rhsb)
+        _check(rc, "cans_initsolver")
+        self._h = h
+        self.normfft = normfft.value
+        self.rhsb = np.array(list(rhsb))
+        self.precision = precision
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.cans_plan_destroy(h)
+            self._h = None
+
+    @property
+    def device_bytes(self):
+        return lib().cans_plan_device_bytes(self._h)
+
+    def set_timing(self, enable=True):
+        _check(lib().cans_plan_set_timing(self._h, int(enable)), "cans_plan_set_timing")
+
+    def get_timing(self):
+        """mean ms per pass (x-fwd, y-fwd, z, y-bwd, x-bwd) over the solves since the last call"""
+        ms = (C.c_double * 5)()
+        cnt = C.c_int()
+        _check(lib().cans_plan_get_timing(self._h, ms, C.byref(cnt)), "cans_plan_get_timing")
+        return list(ms), cnt.value
+
+    def solve(self, p):
+        """solver (src/solver_gpu.f90:34) in place on a haloed float64 (or float32) field."""
+        import torch
+        if p.dtype == torch.float32:
+            _check(lib().cans_solver_f32(self._h, _ptr(p)), "cans_solver_f32")
+        else:
+            _check(lib().cans_solver(self._h, _ptr(p)), "cans_solver")
+        return p
+
+    def solve_refined(self, p, dli, dzci, dzfi, rtol=1e-13, max_iter=6):
+        it, rr = C.c_int(), C.c_double()
+        _check(lib().cans_solver_refined(self._h, _ptr(p), _dbls(dli), _ptr(dzci), _ptr(dzfi), rtol, max_iter,
+                                         C.byref(it), C.byref(rr)), "cans_solver_refined")
+        return it.value, rr.value
+
+    def solve_helmholtz(self, alpha, is_bound, p):
+        """solve_helmholtz (src/solve_helmholtz.f90:28), 3D variant."""
+        _check(lib().cans_solve_helmholtz(self._h, float(alpha), _ints(is_bound), _ptr(p)), "cans_solve_helmholtz")
+        return p
+
+
+# ------------------------------------------------------------------------------ kernels
+def launch_count():
+    return lib().cans_launch_count()
+
+
+def fillps(n, dli, dzfi, dti, u, v, w, p, stream=None):
+    _check(lib().cans_fillps(_ints(n), _dbls(dli), _ptr(dzfi), float(dti), _ptr(u), _ptr(v), _ptr(w), _ptr(p),
+                             _stream(stream)), "cans_fillps")
+
+
+def correc(n, dli, dzci, dt, p, u, v, w, stream=None):
+    _check(lib().cans_correc(_ints(n), _dbls(dli), _ptr(dzci), float(dt), _ptr(p), _ptr(u), _ptr(v), _ptr(w),
+                             _stream(stream)), "cans_correc")
+
+
+def updatep(n, dli, dzci, dzfi, alpha, is_impdiff, pp, p, stream=None):
+    _check(lib().cans_updatep(_ints(n), _dbls(dli), _ptr(dzci), _ptr(dzfi), float(alpha), int(is_impdiff), _ptr(pp),
+                              _ptr(p), _stream(stream)), "cans_updatep")
+
+
+def rk(rkpar, n, dli, dzci, dzfi, gvr_c, gvr_f, dt, visc, p, is_forced, velf, bforce, is_impdiff,
+       dudtrko, dvdtrko, dwdtrko, u, v, w, work=None, stream=None):
+    f = (C.c_double * 3)()
+    _check(lib().cans_rk(_dbls(rkpar), _ints(n), _dbls(dli), _ptr(dzci), _ptr(dzfi), _ptr(gvr_c), _ptr(gvr_f),
+                         float(dt), float(visc), _ptr(p), _ints(is_forced), _dbls(velf), _dbls(bforce),
+                         int(is_impdiff), _ptr(dudtrko), _ptr(dvdtrko), _ptr(dwdtrko), _ptr(u), _ptr(v), _ptr(w),
+                         f, _ptr(work), _stream(stream)), "cans_rk")
+    return np.array(list(f))
+
+
+def bounduvw(cbc, n, bc, is_bound, dl, dzc_h, dzf_h, u, v, w, keep_norm=False, halos_norm=HALO_BOTH,
+             halos_tang=HALO_BOTH, stream=None):
+    dzc_h, pc = _hp(dzc_h)
+    dzf_h, pf = _hp(dzf_h)
+    _check(lib().cans_bounduvw(_chars(cbc), _ints(n), _dbls(bc), _ints(is_bound), _dbls(dl), pc, pf, _ptr(u),
+                               _ptr(v), _ptr(w), int(keep_norm), int(halos_norm), int(halos_tang), _stream(stream)),
+           "cans_bounduvw")
+
+
+def boundp(cbc, n, bc, is_bound, dl, dzc_h, p, halo_side=HALO_BOTH, stream=None):
+    dzc_h, pc = _hp(dzc_h)
+    _check(lib().cans_boundp(_chars(cbc), _ints(n), _dbls(bc), _ints(is_bound), _dbls(dl), pc, _ptr(p),
+                             int(halo_side), _stream(stream)), "cans_boundp")
+
+
+def updt_rhs_b(c_or_f, cbc, n, is_bound, rhsb, p, alpha=None, stream=None):
+    _check(lib().cans_updt_rhs_b(_chars(c_or_f), _chars(cbc), _ints(n), _ints(is_bound), _dbls(rhsb), _ptr(p),
+                                 0. if alpha is None else float(alpha), 0 if alpha is None else 1, _stream(stream)),
+           "cans_updt_rhs_b")
+
+
+def chkdiv(n, l, dli, dzfi, u, v, w, stream=None):
+    a, b = C.c_double(), C.c_double()
+    _check(lib().cans_chkdiv(_ints(n), _dbls(l), _dbls(dli), _ptr(dzfi), _ptr(u), _ptr(v), _ptr(w), C.byref(a),
+                             C.byref(b), _stream(stream)), "cans_chkdiv")
+    return a.value, b.value
+
+
+def chkdt(n, dl, dzci, dzfi, visc, alpha, is_impdiff, is_impdiff_1d, u, v, w, stream=None):
+    r = C.c_double()
+    _check(lib().cans_chkdt(_ints(n), _dbls(dl), _ptr(dzci), _ptr(dzfi), float(visc), float(alpha), int(is_impdiff),
+                            int(is_impdiff_1d), _ptr(u), _ptr(v), _ptr(w), C.byref(r), _stream(stream)), "cans_chkdt")
+    return r.value
+
+
+def bulk_mean(n, gvr, p, stream=None):
+    r = C.c_double()
+    _check(lib().cans_bulk_mean(_ints(n), _ptr(gvr), _ptr(p), C.byref(r), _stream(stream)), "cans_bulk_mean")
+    return r.value

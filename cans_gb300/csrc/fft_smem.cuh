@@ -1,0 +1,270 @@
+// Shared-memory Stockham FFT core and the FFTW-semantics r2r pre/post-processing
+// used by the x/y transform passes of the Poisson solve (sm_103a).
+//
+// Every r2r kind of src/fft.f90:260-313 is reduced to a batched complex FFT of
+// length m on the lines held by one CTA:
+//   - "pairs" kinds pack two real lines as z = x + i y (two-for-one), so one complex
+//     FFT transforms two lines (R2HC/HC2R, REDFT10/01 and RODFT10/01 by Makhoul's
+//     reordering, RODFT00 and REDFT00 by odd/even extension);
+//   - REDFT11/RODFT11 transform one line per complex FFT of length 2n.
+// The complex FFT is the mixed-radix Stockham auto-sort formulation: stage with
+// radix R and span Ns reads x[jb + r*m/R], applies exp(s*2*pi*i*r*(jb%Ns)/(Ns*R)),
+// does a length-R DFT and writes y[(jb/Ns)*Ns*R + jb%Ns + r*Ns].
+#pragma once
+#include "cans_internal.cuh"
+
+struct DirParams {
+  int n;         // grid points along the direction
+  int nt;        // transformed points (n, or n-1 for face-centred DD)
+  int m;         // complex FFT length
+  int kind;      // r2r kind of this pass
+  int pairs;     // 1: two real lines per complex sequence
+  int ncx;       // complex sequences per CTA
+  int lpb;       // real lines per CTA
+  int ld;        // complex line stride in shared memory (m + 1)
+  int sld;       // real staging line stride (nt + 1)
+  int nstages;
+  int radix[12];
+  const void *tw;    // T2[m]  exp(-2 pi i e / m)
+  const void *post;  // T2[nt] exp(-i pi k/(2 nt)) (Makhoul) | exp(-i pi (2k+1)/(4n)) (kinds 11)
+  const void *pre;   // T2[nt] exp(-i pi j/(2n)) (kinds 11)
+};
+
+// ---------------------------------------------------------------------------------- DFT_R
+template <int R> struct RootTab;  // cos/sin(2 pi e / R), e = 0..R-1
+template <> struct RootTab<3> {
+  static __device__ __forceinline__ double c(int e) { const double t[3] = {1.0, -0.5, -0.5}; return t[e]; }
+  static __device__ __forceinline__ double s(int e) {
+    const double t[3] = {0.0, 0.86602540378443864676, -0.86602540378443864676}; return t[e]; }
+};
+template <> struct RootTab<5> {
+  static __device__ __forceinline__ double c(int e) {
+    const double t[5] = {1.0, 0.30901699437494742410, -0.80901699437494742410, -0.80901699437494742410,
+                         0.30901699437494742410};
+    return t[e]; }
+  static __device__ __forceinline__ double s(int e) {
+    const double t[5] = {0.0, 0.95105651629515357212, 0.58778525229247312917, -0.58778525229247312917,
+                         -0.95105651629515357212};
+    return t[e]; }
+};
+template <> struct RootTab<7> {
+  static __device__ __forceinline__ double c(int e) {
+    const double t[7] = {1.0, 0.62348980185873353053, -0.22252093395631440429, -0.90096886790241912624,
+                         -0.90096886790241912624, -0.22252093395631440429, 0.62348980185873353053};
+    return t[e]; }
+  static __device__ __forceinline__ double s(int e) {
+    const double t[7] = {0.0, 0.78183148246802980871, 0.97492791218182360702, 0.43388373911755812048,
+                         -0.43388373911755812048, -0.97492791218182360702, -0.78183148246802980871};
+    return t[e]; }
+};
+
+// generic O(R^2) DFT for odd prime R: y_s = sum_q v_q exp(SIGN*2*pi*i*q*s/R)
+template <int R, int SIGN, typename T2>
+__device__ __forceinline__ void dft_generic(T2 (&v)[R]) {
+  using T = decltype(T2::x);
+  T2 y[R];
+#pragma unroll
+  for (int s = 0; s < R; ++s) {
+    T2 acc = v[0];
+#pragma unroll
+    for (int q = 1; q < R; ++q) {
+      const int e = (q * s) % R;
+      const T c = (T)RootTab<R>::c(e), sn = (T)(SIGN * RootTab<R>::s(e));
+      acc.x += v[q].x * c - v[q].y * sn;
+      acc.y += v[q].x * sn + v[q].y * c;
+    }
+    y[s] = acc;
+  }
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = y[s];
+}
+
+template <int SIGN, typename T2>
+__device__ __forceinline__ void dft4(T2 &x0, T2 &x1, T2 &x2, T2 &x3) {
+  T2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = cmul_i<SIGN>(csub(x1, x3));
+  x0 = cadd(t0, t2); x2 = csub(t0, t2); x1 = cadd(t1, t3); x3 = csub(t1, t3);
+}
+
+template <int R, int SIGN, typename T2>
+__device__ __forceinline__ void dft(T2 (&v)[R]) {
+  using T = decltype(T2::x);
+  if constexpr (R == 2) {
+    T2 a = v[0]; v[0] = cadd(a, v[1]); v[1] = csub(a, v[1]);
+  } else if constexpr (R == 4) {
+    dft4<SIGN>(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    const T c = (T)0.70710678118654752440;
+    T2 a0 = cadd(v[0], v[4]), a1 = cadd(v[1], v[5]), a2 = cadd(v[2], v[6]), a3 = cadd(v[3], v[7]);
+    T2 b0 = csub(v[0], v[4]), b1 = csub(v[1], v[5]), b2 = csub(v[2], v[6]), b3 = csub(v[3], v[7]);
+    // b1 *= W8, b2 *= W8^2, b3 *= W8^3 with W8 = exp(SIGN*i*pi/4)
+    b1 = cmk<T2>(c * (b1.x - SIGN * b1.y), c * (b1.y + SIGN * b1.x));
+    b2 = cmul_i<SIGN>(b2);
+    b3 = cmk<T2>(-c * (b3.x + SIGN * b3.y), c * (SIGN * b3.x - b3.y));
+    dft4<SIGN>(a0, a1, a2, a3);
+    dft4<SIGN>(b0, b1, b2, b3);
+    v[0] = a0; v[2] = a1; v[4] = a2; v[6] = a3;
+    v[1] = b0; v[3] = b1; v[5] = b2; v[7] = b3;
+  } else {
+    dft_generic<R, SIGN>(v);
+  }
+}
+
+// one Stockham stage over all ncx lines held by the CTA
+template <int R, int SIGN, typename T2>
+__device__ __forceinline__ void fft_stage(const T2 *__restrict__ src, T2 *__restrict__ dst, int m, int nlines,
+                                          int ld, int Ns, const T2 *__restrict__ tw) {
+  const int nb = m / R, total = nb * nlines, tws = m / (Ns * R);
+  for (int b = threadIdx.x; b < total; b += blockDim.x) {
+    const int line = b / nb, jb = b - line * nb;
+    const T2 *s = src + line * ld;
+    T2 *d = dst + line * ld;
+    const int k = jb % Ns;
+    T2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      v[r] = s[jb + r * nb];
+      if (r > 0 && Ns > 1) {
+        T2 w = __ldg(&tw[r * k * tws]);
+        if (SIGN > 0) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    dft<R, SIGN>(v);
+    const int idxD = (jb / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[idxD + r * Ns] = v[r];
+  }
+}
+
+// batched complex FFT of the CTA's lines; data starts in A; returns the buffer holding the result
+template <int SIGN, typename T2>
+__device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P) {
+  const T2 *tw = reinterpret_cast<const T2 *>(P.tw);
+  T2 *src = A, *dst = B;
+  int Ns = 1;
+  for (int s = 0; s < P.nstages; ++s) {
+    const int R = P.radix[s];
+    switch (R) {
+      case 2: fft_stage<2, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
+      case 3: fft_stage<3, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
+      case 4: fft_stage<4, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
+      case 5: fft_stage<5, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
+      case 7: fft_stage<7, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
+      default: fft_stage<8, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
+    }
+    __syncthreads();
+    Ns *= R;
+    T2 *t = src; src = dst; dst = t;
+  }
+  return src;
+}
+
+// ------------------------------------------------------------------------ r2r pre-processing
+// staging: real line r at stg[r*sld + i], i < nt.  Fills the complex sequences A[q*ld + k], k < m.
+template <typename T>
+__device__ void r2r_pre(const DirParams &P, const T *__restrict__ stg, cplx_t<T> *__restrict__ A) {
+  using T2 = cplx_t<T>;
+  const int m = P.m, nt = P.nt, n = P.nt, sld = P.sld, ld = P.ld;
+  const T2 *tab = reinterpret_cast<const T2 *>(P.post);
+  const T2 *pre = reinterpret_cast<const T2 *>(P.pre);
+  const int total = P.ncx * m;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int q = e / m, k = e - q * m;
+    const T *x0 = stg + (2 * q) * sld, *x1 = x0 + sld;
+    T2 z;
+    switch (P.kind) {
+      case K_R2HC: z = cmk<T2>(x0[k], x1[k]); break;
+      case K_REDFT10:
+      case K_RODFT10: {
+        const int src = (k < (n + 1) / 2) ? 2 * k : 2 * (n - 1 - k) + 1;
+        const T sg = (P.kind == K_RODFT10 && (src & 1)) ? T(-1) : T(1);
+        z = cmk<T2>(sg * x0[src], sg * x1[src]);
+      } break;
+      case K_HC2R: {
+        T2 X, Y;
+        if (k == 0) { X = cmk<T2>(x0[0], T(0)); Y = cmk<T2>(x1[0], T(0)); }
+        else if (2 * k < n) { X = cmk<T2>(x0[k], x0[n - k]); Y = cmk<T2>(x1[k], x1[n - k]); }
+        else if (2 * k == n) { X = cmk<T2>(x0[k], T(0)); Y = cmk<T2>(x1[k], T(0)); }
+        else { X = cmk<T2>(x0[n - k], -x0[k]); Y = cmk<T2>(x1[n - k], -x1[k]); }
+        z = cmk<T2>(X.x - Y.y, X.y + Y.x);
+      } break;
+      case K_REDFT01:
+      case K_RODFT01: {
+        // V_k = exp(+i pi k/(2n)) (x_k - i x_{n-k}), x_n = 0; DST-III reads the reversed line
+        const T2 t = tab[k];  // (cos, -sin)
+        const T c = t.x, s = -t.y;
+        const bool rev = P.kind == K_RODFT01;
+        const int ka = rev ? n - 1 - k : k, kb = rev ? k - 1 : n - k;
+        const T a0 = x0[ka], a1 = x1[ka];
+        const T b0 = k == 0 ? T(0) : x0[kb], b1 = k == 0 ? T(0) : x1[kb];
+        const T2 V0 = cmk<T2>(c * a0 + s * b0, s * a0 - c * b0);
+        const T2 V1 = cmk<T2>(c * a1 + s * b1, s * a1 - c * b1);
+        z = cmk<T2>(V0.x - V1.y, V0.y + V1.x);
+      } break;
+      case K_RODFT00: {
+        if (k == 0 || k == nt + 1) z = cmk<T2>(T(0), T(0));
+        else if (k <= nt) z = cmk<T2>(x0[k - 1], x1[k - 1]);
+        else z = cmk<T2>(-x0[m - 1 - k], -x1[m - 1 - k]);
+      } break;
+      case K_REDFT00: {
+        const int s = k <= nt - 1 ? k : m - k;
+        z = cmk<T2>(x0[s], x1[s]);
+      } break;
+      default: {  // K_REDFT11 / K_RODFT11: one line per sequence, zero-padded to 2n
+        const T *x = stg + q * sld;
+        if (k < n) { const T2 w = pre[k]; z = cmk<T2>(x[k] * w.x, x[k] * w.y); }
+        else z = cmk<T2>(T(0), T(0));
+      } break;
+    }
+    A[q * ld + k] = z;
+  }
+}
+
+// ----------------------------------------------------------------------- r2r post-processing
+// value of output index k (< nt) of real line r from the FFT result Z
+template <typename T>
+__device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__restrict__ Z, int r, int k) {
+  using T2 = cplx_t<T>;
+  const int m = P.m, n = P.nt;
+  const T2 *tab = reinterpret_cast<const T2 *>(P.post);
+  if (!P.pairs) {  // kinds 11
+    const T2 z = Z[r * P.ld + k], w = tab[k];
+    const T re = w.x * z.x - w.y * z.y, im = w.x * z.y + w.y * z.x;
+    return P.kind == K_REDFT11 ? T(2) * re : T(-2) * im;
+  }
+  const int q = r >> 1, wsel = r & 1;
+  const T2 *L = Z + q * P.ld;
+  switch (P.kind) {
+    case K_R2HC: {
+      const T2 a = L[k], b = L[(m - k) % m];
+      if (2 * k <= n) return wsel == 0 ? T(0.5) * (a.x + b.x) : T(0.5) * (a.y + b.y);
+      return wsel == 0 ? T(0.5) * (b.y - a.y) : T(0.5) * (a.x - b.x);
+    }
+    case K_REDFT10:
+    case K_RODFT10: {
+      const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
+      const T2 a = L[kk], b = L[(m - kk) % m], t = tab[kk];
+      const T c = t.x, s = -t.y;
+      return wsel == 0 ? c * (a.x + b.x) + s * (a.y - b.y) : c * (a.y + b.y) - s * (a.x - b.x);
+    }
+    case K_HC2R: {
+      const T2 a = L[k];
+      return wsel == 0 ? a.x : a.y;
+    }
+    case K_REDFT01:
+    case K_RODFT01: {
+      const int pos = (k & 1) == 0 ? (k >> 1) : n - 1 - ((k - 1) >> 1);
+      const T2 a = L[pos];
+      const T v = wsel == 0 ? a.x : a.y;
+      return (P.kind == K_RODFT01 && (k & 1)) ? -v : v;
+    }
+    case K_RODFT00: {
+      const T2 a = L[k + 1];
+      return wsel == 0 ? -a.y : a.x;
+    }
+    default: {  // K_REDFT00
+      const T2 a = L[k];
+      return wsel == 0 ? a.x : a.y;
+    }
+  }
+}

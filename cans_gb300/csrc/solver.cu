@@ -1,0 +1,831 @@
+// Poisson / Helmholtz solve of the CaNS pressure-correction path on one GB300.
+//
+// Reference: src/solver_gpu.f90:34-276 (GPU), src/solver.f90:17-307 (CPU oracle of
+// the algorithm), src/initsolver.f90:15-232, src/fft.f90:25-313, src/solve_helmholtz.f90.
+//
+// Data flow of one solve (five HBM passes, no pencil library):
+//   1. x-forward : rows p(1:n1,j,k) of the haloed field -> r2r along x -> spectral
+//                  buffer S stored transposed per k-plane, S[k][i][j] (j fastest)
+//   2. y-forward : contiguous lines S[k][i][:] -> r2r along y, in place
+//   3. z-solve   : one thread per spectral column (i,j), Thomas elimination over k
+//                  with the LU factors (1/den, c/den) precomputed once per plan
+//                  (they depend only on lambda_xy(i,j), a, b, c), in place
+//   4. y-backward: in place
+//   5. x-backward: S -> r2r along x -> rows of p (interior only)
+// The spectral ordering is FFTW's r2r output ordering, so lambda_xy and the
+// normalisation are exactly those of the CPU path.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <vector>
+
+#include "cans_internal.cuh"
+#include "fft_smem.cuh"
+
+static thread_local cudaError_t g_last_cuda = cudaSuccess;
+void cans_set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+static std::atomic<long long> g_launches{0};
+void cans_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+extern "C" long long cans_launch_count(void) { return g_launches.load(); }
+
+extern "C" const char *cans_strerror(int s) {
+  switch (s) {
+    case CANS_OK: return "ok";
+    case CANS_EINVAL: return "invalid argument";
+    case CANS_ENOMEM: return "device out of memory";
+    case CANS_ECUDA: return g_last_cuda != cudaSuccess ? cudaGetErrorString(g_last_cuda) : "CUDA error";
+    case CANS_ENOTSUP: return "not supported (transform length or boundary-condition combination)";
+    case CANS_ETIMEOUT: return "bounded device wait expired";
+    case CANS_ENONFINITE: return "non-finite value";
+    default: return "unknown status";
+  }
+}
+extern "C" const char *cans_version(void) { return "cans_gb300 0.1 sm_103a"; }
+
+// ====================================================================================
+// host-side set-up maths (restated from src/initsolver.f90 and src/fft.f90)
+// ====================================================================================
+namespace {
+const double kPi = 3.14159265358979323846;
+
+bool bc_ok(char c) { return c == 'P' || c == 'D' || c == 'N'; }
+
+// src/initsolver.f90:85-144, FFTW (CPU) spectral ordering
+void eigenvalues(int n, const char bc[2], char c_or_f, double *lam) {
+  const char b0 = bc[0], b1 = bc[1];
+  if (b0 == 'P' && b1 == 'P') {
+    for (int l = 1; l <= n; l++) lam[l - 1] = -2. * (1. - cos(((double)(2 * (l - 1)) * kPi) / (double)n));
+  } else if (b0 == 'N' && b1 == 'N') {
+    for (int l = 1; l <= n; l++) lam[l - 1] = -2. * (1. - cos(((double)(l - 1) * kPi) / (double)n));
+  } else if (b0 == 'D' && b1 == 'D') {
+    if (c_or_f == 'c') {
+      for (int l = 1; l <= n; l++) lam[l - 1] = -2. * (1. - cos(((double)l * kPi) / (double)n));
+    } else {
+      for (int l = 1; l <= n - 1; l++) lam[l - 1] = -2. * (1. - cos(((double)l * kPi) / (double)n));
+      lam[n - 1] = 0.;
+    }
+  } else {
+    for (int l = 1; l <= n; l++) lam[l - 1] = -2. * (1. - cos(((double)(2 * l - 1) * kPi) / (2. * n)));
+  }
+}
+
+// src/initsolver.f90:146-187
+void tridmatrix(const char bc[2], int n, const double *dzci, const double *dzfi, char c_or_f, double *a,
+                double *b, double *c) {
+  for (int k = 1; k <= n; k++) {
+    if (c_or_f == 'c') { a[k - 1] = dzfi[k] * dzci[k - 1]; c[k - 1] = dzfi[k] * dzci[k]; }
+    else { a[k - 1] = dzfi[k] * dzci[k]; c[k - 1] = dzfi[k + 1] * dzci[k]; }
+    b[k - 1] = -(a[k - 1] + c[k - 1]);
+  }
+  double f[2];
+  for (int ib = 0; ib < 2; ib++) f[ib] = bc[ib] == 'P' ? 0. : (bc[ib] == 'D' ? -1. : 1.);
+  if (c_or_f == 'c') {
+    b[0] = b[0] + f[0] * a[0];
+    b[n - 1] = b[n - 1] + f[1] * c[n - 1];
+  } else {
+    if (bc[0] == 'N') b[0] = b[0] + f[0] * a[0];
+    if (bc[1] == 'N') b[n - 1] = b[n - 1] + f[1] * c[n - 1];
+  }
+}
+
+// src/initsolver.f90:189-232 (the face planes are constant: return the two values)
+void bc_rhs(const char cbc[2], const double bc[2], const double dlc[2], const double dlf[2], char c_or_f,
+            double out[2]) {
+  double f[2];
+  for (int ib = 0; ib < 2; ib++) {
+    const double sgn = ib == 0 ? 1. : -1.;
+    if (cbc[ib] == 'P') f[ib] = 0.;
+    else if (cbc[ib] == 'D') f[ib] = c_or_f == 'c' ? -2. * bc[ib] : -bc[ib];
+    else f[ib] = sgn * (c_or_f == 'c' ? dlc[ib] : dlf[ib]) * bc[ib];
+  }
+  for (int ib = 0; ib < 2; ib++) out[ib] = f[ib] / dlc[ib] / dlf[ib];
+}
+
+// src/fft.f90:260-313
+void find_fft(const char bc[2], char c_or_f, int *kf, int *kb, double norm[2]) {
+  const char b0 = bc[0], b1 = bc[1];
+  norm[0] = 2.; norm[1] = 0.;
+  if (b0 == 'P' && b1 == 'P') { *kf = K_R2HC; *kb = K_HC2R; norm[0] = 1.; return; }
+  if (c_or_f == 'c') {
+    if (b0 == 'N' && b1 == 'N') { *kf = K_REDFT10; *kb = K_REDFT01; }
+    else if (b0 == 'D' && b1 == 'D') { *kf = K_RODFT10; *kb = K_RODFT01; }
+    else if (b0 == 'N' && b1 == 'D') { *kf = K_REDFT11; *kb = K_REDFT11; }
+    else { *kf = K_RODFT11; *kb = K_RODFT11; }
+  } else {
+    if (b0 == 'N' && b1 == 'N') { *kf = K_REDFT00; *kb = K_REDFT00; norm[1] = -1.; }
+    else if (b0 == 'D' && b1 == 'D') { *kf = K_RODFT00; *kb = K_RODFT00; norm[1] = 1.; }
+    else if (b0 == 'N' && b1 == 'D') { *kf = K_REDFT10; *kb = K_REDFT01; }
+    else { *kf = K_RODFT01; *kb = K_RODFT10; }
+  }
+}
+
+// complex FFT length of a kind on nt points
+int fft_len(int kind, int nt) {
+  switch (kind) {
+    case K_REDFT00: return 2 * (nt - 1);
+    case K_RODFT00: return 2 * (nt + 1);
+    case K_REDFT11: case K_RODFT11: return 2 * nt;
+    default: return nt;
+  }
+}
+
+bool factor_radices(int m, int *radix, int *ns) {
+  *ns = 0;
+  if (m == 1) return true;
+  while (m % 8 == 0 && m != 16) { radix[(*ns)++] = 8; m /= 8; }
+  while (m % 4 == 0) { radix[(*ns)++] = 4; m /= 4; }
+  while (m % 2 == 0) { radix[(*ns)++] = 2; m /= 2; }
+  for (int r : {3, 5, 7}) while (m % r == 0) { radix[(*ns)++] = r; m /= r; }
+  return m == 1 && *ns <= 12;
+}
+
+std::vector<double> exp_table(int count, long num_mul, long num_add, long den) {
+  // entries exp(-i*pi*(num_mul*e + num_add)/den), e = 0..count-1, as interleaved (re, im)
+  std::vector<double> t(2 * (size_t)count);
+  for (int e = 0; e < count; e++) {
+    long double ang = 3.14159265358979323846264338327950288L * (long double)(num_mul * e + num_add) / (long double)den;
+    t[2 * e] = (double)cosl(ang);
+    t[2 * e + 1] = -(double)sinl(ang);
+  }
+  return t;
+}
+}  // namespace
+
+
+// ====================================================================================
+// initgrid (src/initgrid.f90:14-118): stretched z grid.  The reference evaluates
+// z0 = (k-0.)/(1.*n) in default (single) precision; reproduced with float.
+// ====================================================================================
+static double gridpoint(int gtype, double alpha, double z0) {
+  if (!(alpha > DBL_EPSILON)) return z0;
+  switch (gtype) {
+    case 2: return 1.0 * (1. + tanh((z0 - 1.0) * alpha) / tanh(alpha / 1.));
+    case 3: return 1. - 1.0 * (1. + tanh((1. - z0 - 1.0) * alpha) / tanh(alpha / 1.));
+    case 4:
+      if (z0 <= 0.5) return 0.5 * ((1. - 1.) + tanh(2. * alpha * (z0 - 0.)) / tanh(alpha));
+      return 0.5 * ((1. + 1.) + tanh(2. * alpha * (z0 - 1.)) / tanh(alpha));
+    default: return 0.5 * (1. + tanh((z0 - 0.5) * alpha) / tanh(alpha / 2.));
+  }
+}
+
+extern "C" int cans_initgrid(int gtype, int n, double gr, double lz, int is_periodic, double *dzc, double *dzf,
+                             double *zc, double *zf) {
+  if (gtype < 1 || gtype > 4 || n < 1 || !dzc || !dzf || !zc || !zf) return CANS_EINVAL;
+  zf[0] = 0.;
+  for (int k = 1; k <= n; k++) zf[k] = gridpoint(gtype, gr, (double)((float)k / (float)n));
+  for (int k = 1; k <= n; k++) zf[k] = zf[k] * lz;
+  if (fabs(gr) < DBL_EPSILON) {
+    for (int k = 0; k <= n + 1; k++) { dzf[k] = lz / (double)n; dzc[k] = lz / (double)n; }
+  } else {
+    for (int k = 1; k <= n; k++) dzf[k] = zf[k] - zf[k - 1];
+    if (!is_periodic) { dzf[0] = dzf[1]; dzf[n + 1] = dzf[n]; }
+    else { dzf[0] = dzf[n]; dzf[n + 1] = dzf[1]; }
+    for (int k = 0; k <= n; k++) dzc[k] = .5 * (dzf[k] + dzf[k + 1]);
+    dzc[n + 1] = is_periodic ? dzc[1] : dzc[n];
+  }
+  zc[0] = -dzc[0] / 2.;
+  zf[0] = 0.;
+  for (int k = 1; k <= n + 1; k++) { zc[k] = zc[k - 1] + dzc[k - 1]; zf[k] = zf[k - 1] + dzf[k]; }
+  return CANS_OK;
+}
+
+// ====================================================================================
+// plan
+// ====================================================================================
+struct DirTables {
+  void *tw = nullptr, *post = nullptr, *pre = nullptr;  // device, precision of the plan
+};
+
+struct Factor {
+  double key = 0.;       // 1/alpha for Helmholtz, NaN-free sentinel 0 for Poisson
+  bool valid = false;
+  double *zinv = nullptr, *dd = nullptr, *p2 = nullptr, *dcl = nullptr;  // device
+  unsigned long long stamp = 0;
+};
+
+struct cans_plan {
+  int n[3];
+  char cbc[6];
+  char c_or_f[3];
+  int precision;
+  cudaStream_t stream;
+  int kf[2], kb[2], nt[2], m[2];
+  int radix[2][12], nstages[2];
+  DirTables tab[2];
+  double normfft;
+  double rhsb[6];
+  int q;             // 1 when the last z row is a Dirichlet face (not solved)
+  int nn;            // rows of the z system (n3 - q)
+  int zper;          // periodic z
+  std::vector<double> lam_h, a_h, b_h, c_h;
+  double *lamcol = nullptr;   // device lambda in spectral column order (i*n2 + j)
+  double *a_d = nullptr, *b_d = nullptr, *c_d = nullptr, *bb_d = nullptr;
+  void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)
+  double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
+  float *R32 = nullptr;
+  Factor fac[4];
+  unsigned long long clock = 0;
+  long long bytes = 0;
+  void *red = nullptr;        // reduction scratch
+  // optional per-pass timing: events recorded between the passes of each solve
+  bool timing = false;
+  std::vector<cudaEvent_t> ev;  // kTimedSolves x (kPasses + 1)
+  int nrec = 0;
+};
+static const int kPasses = 5, kTimedSolves = 256;
+
+template <typename T> DirParams make_params(const cans_plan *P, int d, int fwd) {
+  DirParams q;
+  memset(&q, 0, sizeof(q));
+  q.n = P->n[d];
+  q.nt = P->nt[d];
+  q.m = P->m[d];
+  q.kind = fwd ? P->kf[d] : P->kb[d];
+  q.pairs = (q.kind == K_REDFT11 || q.kind == K_RODFT11) ? 0 : 1;
+  q.ld = q.m + 1;
+  q.sld = q.nt + 1;
+  q.nstages = P->nstages[d];
+  for (int s = 0; s < 12; s++) q.radix[s] = P->radix[d][s];
+  q.tw = P->tab[d].tw;
+  q.post = P->tab[d].post;
+  q.pre = P->tab[d].pre;
+  // complex sequences per CTA: keep the two FFT buffers near 96 KB
+  const size_t per = (size_t)q.ld * sizeof(cplx_t<T>) * 2;
+  int ncx = (int)std::max<size_t>(1, (96 * 1024) / per);
+  ncx = std::min(ncx, 16);
+  q.ncx = ncx;
+  q.lpb = q.pairs ? 2 * ncx : ncx;
+  return q;
+}
+
+template <typename T> size_t smem_bytes(const DirParams &q) {
+  const size_t a = (size_t)q.ncx * q.ld * sizeof(cplx_t<T>);
+  const size_t b = std::max(a, (size_t)q.lpb * q.sld * sizeof(T));
+  return a + b + (size_t)q.lpb * sizeof(T) + 64;
+}
+
+// ====================================================================================
+// kernels
+// ====================================================================================
+// 1. x-forward: haloed rows -> S[k][i][j]
+template <typename T, typename TF>
+__global__ void __launch_bounds__(256) k_xfwd(const TF *__restrict__ p, T *__restrict__ S, int n1, int n2, DirParams P) {
+  using T2 = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)P.ncx * P.ld;
+  T *stg = reinterpret_cast<T *>(B);
+  const size_t bbytes = std::max((size_t)P.ncx * P.ld * sizeof(T2), (size_t)P.lpb * P.sld * sizeof(T));
+  T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
+  const int k = blockIdx.y, j0 = blockIdx.x * P.lpb, lpb = P.lpb, nt = P.nt;
+  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+    const int r = e / nt, i = e - r * nt, j = j0 + r;
+    stg[r * P.sld + i] = (j < n2) ? (T)p[hidx(i + 1, j + 1, k + 1, n1, n2)] : T(0);
+  }
+  if (nt < n1)
+    for (int r = threadIdx.x; r < lpb; r += blockDim.x)
+      pass[r] = (j0 + r < n2) ? (T)p[hidx(n1, j0 + r + 1, k + 1, n1, n2)] : T(0);
+  __syncthreads();
+  r2r_pre<T>(P, stg, A);
+  __syncthreads();
+  const T2 *Z = fft_lines<-1>(A, B, P);
+  T *Sk = S + (size_t)k * n1 * n2;
+  for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
+    const int i = e / lpb, r = e - i * lpb, j = j0 + r;
+    if (j >= n2) continue;
+    Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T>(P, Z, r, i) : pass[r];
+  }
+}
+
+// 2./4. y pass, in place on contiguous lines S[l*n2 .. l*n2+n2-1], l = k*n1 + i
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(256) k_ylines(T *__restrict__ S, long nlines, int n2, DirParams P) {
+  using T2 = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)P.ncx * P.ld;
+  T *stg = reinterpret_cast<T *>(B);
+  const long l0 = (long)blockIdx.x * P.lpb;
+  const int lpb = P.lpb, nt = P.nt;
+  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+    const int r = e / nt, j = e - r * nt;
+    stg[r * P.sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
+  }
+  __syncthreads();
+  r2r_pre<T>(P, stg, A);
+  __syncthreads();
+  const T2 *Z = fft_lines<SIGN>(A, B, P);
+  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+    const int r = e / nt, j = e - r * nt;
+    if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T>(P, Z, r, j);
+  }
+}
+
+// 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k)
+template <typename T, typename TF>
+__global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2, DirParams P) {
+  using T2 = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)P.ncx * P.ld;
+  T *stg = reinterpret_cast<T *>(B);
+  const size_t bbytes = std::max((size_t)P.ncx * P.ld * sizeof(T2), (size_t)P.lpb * P.sld * sizeof(T));
+  T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
+  const int k = blockIdx.y, j0 = blockIdx.x * P.lpb, lpb = P.lpb, nt = P.nt;
+  const T *Sk = S + (size_t)k * n1 * n2;
+  for (int e = threadIdx.x; e < nt * lpb; e += blockDim.x) {
+    const int i = e / lpb, r = e - i * lpb, j = j0 + r;
+    stg[r * P.sld + i] = (j < n2) ? Sk[(size_t)i * n2 + j] : T(0);
+  }
+  if (nt < n1)
+    for (int r = threadIdx.x; r < lpb; r += blockDim.x)
+      pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
+  __syncthreads();
+  r2r_pre<T>(P, stg, A);
+  __syncthreads();
+  const T2 *Z = fft_lines<+1>(A, B, P);
+  for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
+    const int r = e / n1, i = e - r * n1, j = j0 + r;
+    if (j >= n2) continue;
+    p[hidx(i + 1, j + 1, k + 1, n1, n2)] = (TF)((i < nt) ? r2r_post<T>(P, Z, r, i) : pass[r]);
+  }
+}
+
+// z factorisation per spectral column (src/solver.f90:114-307 with the RHS-independent
+// part hoisted): zinv_k = 1/den_k (0 where the singular mode is pinned), dd_k = c_k/den_k;
+// periodic z: the auxiliary Sherman-Morrison solution p2 and the closure denominator.
+__global__ void k_zfactor(const double *__restrict__ lamcol, const double *__restrict__ a,
+                          const double *__restrict__ b, const double *__restrict__ c, long ncol, int nn,
+                          int zper, double *__restrict__ zinv, double *__restrict__ dd, double *__restrict__ p2,
+                          double *__restrict__ dcl) {
+  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const double lam = lamcol[col];
+  double z = 1. / (b[0] + lam);
+  double dprev = c[0] * z;
+  zinv[col] = z;
+  dd[col] = dprev;
+  for (int k = 1; k < nn; k++) {
+    const double den = b[k] + lam - a[k] * dprev;
+    const double pt = DBL_EPSILON * fmax(fabs(b[k] + lam), fabs(a[k] * dprev));
+    const size_t idx = (size_t)k * ncol + col;
+    if (k == nn - 1 && fabs(den) <= pt) {
+      zinv[idx] = 0.; dd[idx] = 0.; dprev = 0.;
+    } else {
+      z = 1. / den;
+      dprev = c[k] * z;
+      zinv[idx] = z; dd[idx] = dprev;
+    }
+  }
+  if (!zper) return;
+  // auxiliary system: rhs (-a_1, 0, ..., 0, -c_nn), same matrix, no pivot pinning
+  double dq = 0., y = 0.;
+  for (int k = 0; k < nn; k++) {
+    double r = 0.;
+    if (k == 0) r = -a[0];
+    if (k == nn - 1) r = r - c[nn - 1];
+    const double zz = 1. / (k == 0 ? b[0] + lam : b[k] + lam - a[k] * dq);
+    dq = c[k] * zz;
+    y = (k == 0) ? r * zz : (r - a[k] * y) * zz;
+    p2[(size_t)k * ncol + col] = y;
+  }
+  for (int k = nn - 2; k >= 0; k--) {
+    const size_t idx = (size_t)k * ncol + col;
+    // recompute d_k of the auxiliary recursion = dd unless the main one was pinned at nn-1
+    const double dk = dd[idx];
+    y = p2[idx] - dk * y;
+    p2[idx] = y;
+  }
+  const double q1 = p2[col], qn = p2[(size_t)(nn - 1) * ncol + col];
+  const double den = b[nn] + lam + c[nn] * q1 + a[nn] * qn;
+  const double pt = DBL_EPSILON * fmax(fabs(b[nn] + lam), fabs(c[nn] * q1 + a[nn] * qn));
+  dcl[col] = fabs(den) <= pt ? 0. : den;
+}
+
+// z solve, FP64 spectral data, in place
+__global__ void __launch_bounds__(128) k_zsolve64(double *__restrict__ S, const double *__restrict__ zinv,
+                                                  const double *__restrict__ dd, const double *__restrict__ p2,
+                                                  const double *__restrict__ dcl, const double *__restrict__ a,
+                                                  const double *__restrict__ c, long ncol, int nn, int zper,
+                                                  double norm) {
+  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  double y = 0.;
+  for (int k = 0; k < nn; k++) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = (S[idx] * norm - a[k] * y) * zinv[idx];
+    S[idx] = y;
+  }
+  for (int k = nn - 2; k >= 0; k--) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = S[idx] - dd[idx] * y;
+    S[idx] = y;
+  }
+  if (zper) {
+    const size_t iN = (size_t)nn * ncol + col;
+    const double den = dcl[col];
+    const double s1 = S[col], sn = S[(size_t)(nn - 1) * ncol + col];
+    const double pN = den == 0. ? 0. : (S[iN] * norm - c[nn] * s1 - a[nn] * sn) / den;
+    S[iN] = pN;
+    for (int k = 0; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      S[idx] = S[idx] + p2[idx] * pN;
+    }
+  }
+}
+
+// z solve on FP32 spectral data: elimination in FP64, forward sweep kept in FP64 in the
+// FP64 scratch W (same layout), result rounded to FP32 on the backward sweep
+__global__ void __launch_bounds__(128) k_zsolve32(float *__restrict__ S, double *__restrict__ W,
+                                                  const double *__restrict__ zinv, const double *__restrict__ dd,
+                                                  const double *__restrict__ p2, const double *__restrict__ dcl,
+                                                  const double *__restrict__ a, const double *__restrict__ c,
+                                                  long ncol, int nn, int zper, double norm) {
+  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  double y = 0.;
+  for (int k = 0; k < nn; k++) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = ((double)S[idx] * norm - a[k] * y) * zinv[idx];
+    W[idx] = y;
+  }
+  double s1 = 0., sn = y;
+  for (int k = nn - 2; k >= 0; k--) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = W[idx] - dd[idx] * y;
+    W[idx] = y;
+  }
+  s1 = nn > 1 ? y : sn;
+  if (zper) {
+    const size_t iN = (size_t)nn * ncol + col;
+    const double den = dcl[col];
+    const double pN = den == 0. ? 0. : ((double)S[iN] * norm - c[nn] * s1 - a[nn] * sn) / den;
+    S[iN] = (float)pN;
+    for (int k = 0; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      S[idx] = (float)(W[idx] + p2[idx] * pN);
+    }
+  } else {
+    for (int k = 0; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      S[idx] = (float)W[idx];
+    }
+  }
+}
+
+// ====================================================================================
+// host: plan construction and solve drivers
+// ====================================================================================
+template <typename T> static int upload_tables(cans_plan *P, int d) {
+  using T2 = cplx_t<T>;
+  const int nt = P->nt[d], m = P->m[d];
+  auto up = [&](const std::vector<double> &v, void **dst) -> int {
+    const size_t cnt = v.size() / 2;
+    std::vector<T2> h(cnt);
+    for (size_t e = 0; e < cnt; e++) { h[e].x = (T)v[2 * e]; h[e].y = (T)v[2 * e + 1]; }
+    CANS_CUDA_TRY(cudaMalloc(dst, std::max<size_t>(1, cnt) * sizeof(T2)));
+    P->bytes += (long long)(cnt * sizeof(T2));
+    CANS_CUDA_TRY(cudaMemcpy(*dst, h.data(), cnt * sizeof(T2), cudaMemcpyHostToDevice));
+    return CANS_OK;
+  };
+  int rc = up(exp_table(m, 2, 0, m), &P->tab[d].tw);  // exp(-2 pi i e/m)
+  if (rc) return rc;
+  const int kind = P->kf[d];
+  if (kind == K_REDFT11 || kind == K_RODFT11) {
+    if ((rc = up(exp_table(nt, 1, 0, 2L * nt), &P->tab[d].pre))) return rc;      // exp(-i pi j/(2n))
+    if ((rc = up(exp_table(nt, 2, 1, 4L * nt), &P->tab[d].post))) return rc;    // exp(-i pi (2k+1)/(4n))
+  } else {
+    if ((rc = up(exp_table(std::max(nt, 1), 1, 0, 2L * nt), &P->tab[d].post))) return rc;  // exp(-i pi k/(2n))
+  }
+  return CANS_OK;
+}
+
+static void free_factor(Factor &f) {
+  cudaFree(f.zinv); cudaFree(f.dd); cudaFree(f.p2); cudaFree(f.dcl);
+  f = Factor();
+}
+
+extern "C" int cans_plan_destroy(cans_plan *P) {
+  if (!P) return CANS_OK;
+  for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
+  for (auto &f : P->fac) free_factor(f);
+  cudaFree(P->lamcol); cudaFree(P->a_d); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
+  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red);
+  for (auto &e : P->ev) cudaEventDestroy(e);
+  delete P;
+  return CANS_OK;
+}
+
+extern "C" long long cans_plan_device_bytes(const cans_plan *P) { return P ? P->bytes : 0; }
+
+// get (or build) the factorisation for the diagonal shift `key` (0 = Poisson: b as is)
+static int get_factor(cans_plan *P, double key, bool helm, Factor **out) {
+  const long ncol = (long)P->n[0] * P->n[1];
+  const int nn = P->zper ? P->nn - 1 : P->nn;
+  for (auto &f : P->fac)
+    if (f.valid && f.key == key && (helm || key == 0.)) { f.stamp = ++P->clock; *out = &f; return CANS_OK; }
+  Factor *slot = &P->fac[0];
+  for (auto &f : P->fac) {
+    if (!f.valid) { slot = &f; break; }
+    if (f.stamp < slot->stamp) slot = &f;
+  }
+  if (!slot->zinv) {
+    const size_t cells = (size_t)ncol * std::max(nn, 1);
+    CANS_CUDA_TRY(cudaMalloc(&slot->zinv, cells * sizeof(double)));
+    CANS_CUDA_TRY(cudaMalloc(&slot->dd, cells * sizeof(double)));
+    P->bytes += (long long)(2 * cells * sizeof(double));
+    if (P->zper) {
+      CANS_CUDA_TRY(cudaMalloc(&slot->p2, cells * sizeof(double)));
+      CANS_CUDA_TRY(cudaMalloc(&slot->dcl, ncol * sizeof(double)));
+      P->bytes += (long long)((cells + ncol) * sizeof(double));
+    }
+  }
+  const double *b = P->b_d;
+  if (helm) {
+    std::vector<double> bb(P->n[2]);
+    for (int k = 0; k < P->n[2]; k++) bb[k] = P->b_h[k] + key;
+    CANS_CUDA_TRY(cudaMemcpyAsync(P->bb_d, bb.data(), bb.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                  P->stream));
+    CANS_CUDA_TRY(cudaStreamSynchronize(P->stream));
+    b = P->bb_d;
+  }
+  const int tpb = 128;
+  k_zfactor<<<(unsigned)((ncol + tpb - 1) / tpb), tpb, 0, P->stream>>>(P->lamcol, P->a_d, b, P->c_d, ncol, nn,
+                                                                       P->zper, slot->zinv, slot->dd, slot->p2,
+                                                                       slot->dcl);
+  CANS_LAUNCH_CHECK();
+  slot->key = key;
+  slot->valid = true;
+  slot->stamp = ++P->clock;
+  *out = slot;
+  return CANS_OK;
+}
+
+template <typename T> static int set_smem(const void *fn, size_t bytes) {
+  CANS_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return CANS_OK;
+}
+
+template <typename T, typename TF> static int launch_xfwd(cans_plan *P, const TF *p) {
+  DirParams q = make_params<T>(P, 0, 1);
+  const size_t sm = smem_bytes<T>(q);
+  int rc = set_smem<T>((const void *)k_xfwd<T, TF>, sm);
+  if (rc) return rc;
+  dim3 grid((P->n[1] + q.lpb - 1) / q.lpb, P->n[2]);
+  k_xfwd<T, TF><<<grid, 256, sm, P->stream>>>(p, (T *)P->S, P->n[0], P->n[1], q);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+template <typename T, typename TF> static int launch_xbwd(cans_plan *P, TF *p) {
+  DirParams q = make_params<T>(P, 0, 0);
+  const size_t sm = smem_bytes<T>(q);
+  int rc = set_smem<T>((const void *)k_xbwd<T, TF>, sm);
+  if (rc) return rc;
+  dim3 grid((P->n[1] + q.lpb - 1) / q.lpb, P->n[2]);
+  k_xbwd<T, TF><<<grid, 256, sm, P->stream>>>((const T *)P->S, p, P->n[0], P->n[1], q);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+template <typename T> static int launch_y(cans_plan *P, int fwd) {
+  DirParams q = make_params<T>(P, 1, fwd);
+  const size_t sm = smem_bytes<T>(q);
+  const long nlines = (long)P->n[0] * P->n[2];
+  const unsigned grid = (unsigned)((nlines + q.lpb - 1) / q.lpb);
+  if (fwd) {
+    int rc = set_smem<T>((const void *)k_ylines<T, -1>, sm);
+    if (rc) return rc;
+    k_ylines<T, -1><<<grid, 256, sm, P->stream>>>((T *)P->S, nlines, P->n[1], q);
+  } else {
+    int rc = set_smem<T>((const void *)k_ylines<T, +1>, sm);
+    if (rc) return rc;
+    k_ylines<T, +1><<<grid, 256, sm, P->stream>>>((T *)P->S, nlines, P->n[1], q);
+  }
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+static int launch_z(cans_plan *P, const Factor *F, double norm, bool f32) {
+  const long ncol = (long)P->n[0] * P->n[1];
+  const int nn = P->zper ? P->nn - 1 : P->nn;
+  const int tpb = 128;
+  const unsigned grid = (unsigned)((ncol + tpb - 1) / tpb);
+  if (!f32)
+    k_zsolve64<<<grid, tpb, 0, P->stream>>>((double *)P->S, F->zinv, F->dd, F->p2, F->dcl, P->a_d, P->c_d, ncol,
+                                            nn, P->zper, norm);
+  else
+    k_zsolve32<<<grid, tpb, 0, P->stream>>>((float *)P->S, P->R64, F->zinv, F->dd, F->p2, F->dcl, P->a_d, P->c_d,
+                                            ncol, nn, P->zper, norm);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+// full solve: T = arithmetic of the transforms, TF = element type of the field
+static void mark(cans_plan *P, int pass) {
+  if (!P->timing || P->nrec >= kTimedSolves) return;
+  cudaEventRecord(P->ev[(size_t)P->nrec * (kPasses + 1) + pass], P->stream);
+  if (pass == kPasses) P->nrec++;
+}
+
+template <typename T, typename TF> static int solve_impl(cans_plan *P, TF *p, double key, bool helm, double norm) {
+  Factor *F = nullptr;
+  int rc;
+  if ((rc = get_factor(P, key, helm, &F))) return rc;
+  mark(P, 0);
+  if ((rc = launch_xfwd<T, TF>(P, p))) return rc;
+  mark(P, 1);
+  if ((rc = launch_y<T>(P, 1))) return rc;
+  mark(P, 2);
+  if ((rc = launch_z(P, F, norm, sizeof(T) == 4))) return rc;
+  mark(P, 3);
+  if ((rc = launch_y<T>(P, 0))) return rc;
+  mark(P, 4);
+  if ((rc = launch_xbwd<T, TF>(P, p))) return rc;
+  mark(P, 5);
+  return CANS_OK;
+}
+
+extern "C" int cans_plan_set_timing(cans_plan *P, int enable) {
+  if (!P) return CANS_EINVAL;
+  if (enable && P->ev.empty()) {
+    P->ev.resize((size_t)kTimedSolves * (kPasses + 1));
+    for (auto &e : P->ev) CANS_CUDA_TRY(cudaEventCreate(&e));
+  }
+  P->timing = enable != 0;
+  P->nrec = 0;
+  return CANS_OK;
+}
+
+extern "C" int cans_plan_get_timing(cans_plan *P, double ms[5], int *nsolves) {
+  if (!P || !ms) return CANS_EINVAL;
+  for (int q = 0; q < kPasses; q++) ms[q] = 0.;
+  if (nsolves) *nsolves = P->nrec;
+  if (P->nrec == 0) return CANS_OK;
+  CANS_CUDA_TRY(cudaStreamSynchronize(P->stream));
+  for (int s = 0; s < P->nrec; s++)
+    for (int q = 0; q < kPasses; q++) {
+      float t = 0.f;
+      CANS_CUDA_TRY(cudaEventElapsedTime(&t, P->ev[(size_t)s * (kPasses + 1) + q], P->ev[(size_t)s * (kPasses + 1) + q + 1]));
+      ms[q] += t;
+    }
+  for (int q = 0; q < kPasses; q++) ms[q] /= P->nrec;
+  P->nrec = 0;
+  return CANS_OK;
+}
+
+extern "C" int cans_initsolver(const int ng[3], const double dli[3], const double *dzci_g, const double *dzfi_g,
+                               const char cbc[6], const double bc[6], const char c_or_f[3], int precision,
+                               void *stream, cans_plan **plan, double *lambdaxy, double *a, double *b, double *c,
+                               double *normfft, double rhsb[6]) {
+  if (!ng || !dli || !dzci_g || !dzfi_g || !cbc || !bc || !c_or_f || !plan) return CANS_EINVAL;
+  *plan = nullptr;
+  if (ng[0] < 1 || ng[1] < 1 || ng[2] < 2) return CANS_EINVAL;
+  if (precision != CANS_FP64 && precision != CANS_FP32) return CANS_EINVAL;
+  for (int e = 0; e < 6; e++) if (!bc_ok(cbc[e])) return CANS_EINVAL;
+  for (int d = 0; d < 3; d++) if (c_or_f[d] != 'c' && c_or_f[d] != 'f') return CANS_EINVAL;
+  for (int d = 0; d < 3; d++)
+    if ((cbc[2 * d] == 'P') != (cbc[2 * d + 1] == 'P')) return CANS_EINVAL;
+  cans_plan *P = new cans_plan();
+  for (int d = 0; d < 3; d++) P->n[d] = ng[d];
+  memcpy(P->cbc, cbc, 6);
+  memcpy(P->c_or_f, c_or_f, 3);
+  P->precision = precision;
+  P->stream = as_stream(stream);
+  const int n1 = ng[0], n2 = ng[1], n3 = ng[2];
+  // eigenvalues, z coefficients, boundary values (src/initsolver.f90:15-83)
+  std::vector<double> lx(n1), ly(n2);
+  eigenvalues(n1, cbc + 0, c_or_f[0], lx.data());
+  for (int i = 0; i < n1; i++) lx[i] = lx[i] * (dli[0] * dli[0]);
+  eigenvalues(n2, cbc + 2, c_or_f[1], ly.data());
+  for (int j = 0; j < n2; j++) ly[j] = ly[j] * (dli[1] * dli[1]);
+  P->lam_h.resize((size_t)n1 * n2);
+  for (int j = 0; j < n2; j++)
+    for (int i = 0; i < n1; i++) P->lam_h[i + (size_t)n1 * j] = lx[i] + ly[j];
+  P->a_h.resize(n3); P->b_h.resize(n3); P->c_h.resize(n3);
+  tridmatrix(cbc + 4, n3, dzci_g, dzfi_g, c_or_f[2], P->a_h.data(), P->b_h.data(), P->c_h.data());
+  double dl[3], dlc[2], dlf[2];
+  for (int d = 0; d < 3; d++) dl[d] = 1. / dli[d];
+  for (int d = 0; d < 2; d++) {
+    dlc[0] = dlc[1] = dl[d]; dlf[0] = dlf[1] = dl[d];
+    bc_rhs(cbc + 2 * d, bc + 2 * d, dlc, dlf, c_or_f[d], P->rhsb + 2 * d);
+  }
+  if (c_or_f[2] == 'c') { dlc[0] = 1. / dzci_g[0]; dlc[1] = 1. / dzci_g[n3]; }
+  else { dlc[0] = 1. / dzci_g[1]; dlc[1] = 1. / dzci_g[n3 - 1]; }
+  dlf[0] = 1. / dzfi_g[1]; dlf[1] = 1. / dzfi_g[n3];
+  bc_rhs(cbc + 4, bc + 4, dlc, dlf, c_or_f[2], P->rhsb + 4);
+  // transforms (src/fft.f90:25-209)
+  double nf = 1.;
+  for (int d = 0; d < 2; d++) {
+    double norm[2];
+    find_fft(cbc + 2 * d, c_or_f[d], &P->kf[d], &P->kb[d], norm);
+    const int ix = (cbc[2 * d] == 'D' && cbc[2 * d + 1] == 'D' && c_or_f[d] == 'f') ? 1 : 0;
+    P->nt[d] = ng[d] - ix;
+    nf = nf * norm[0] * ((double)ng[d] + norm[1] - (double)ix);
+    if (P->nt[d] < 1 || (P->kf[d] == K_REDFT00 && P->nt[d] < 2)) { delete P; return CANS_ENOTSUP; }
+    P->m[d] = fft_len(P->kf[d], P->nt[d]);
+    if (!factor_radices(P->m[d], P->radix[d], &P->nstages[d]) || P->m[d] > 4096) { delete P; return CANS_ENOTSUP; }
+  }
+  P->normfft = 1. / nf;
+  P->q = (c_or_f[2] == 'f' && cbc[5] == 'D') ? 1 : 0;
+  P->nn = n3 - P->q;
+  P->zper = cbc[4] == 'P' && cbc[5] == 'P';
+  if (P->zper && P->nn < 2) { delete P; return CANS_ENOTSUP; }
+  // host outputs
+  if (lambdaxy) memcpy(lambdaxy, P->lam_h.data(), sizeof(double) * P->lam_h.size());
+  if (a) memcpy(a, P->a_h.data(), sizeof(double) * n3);
+  if (b) memcpy(b, P->b_h.data(), sizeof(double) * n3);
+  if (c) memcpy(c, P->c_h.data(), sizeof(double) * n3);
+  if (normfft) *normfft = P->normfft;
+  if (rhsb) memcpy(rhsb, P->rhsb, sizeof(double) * 6);
+  // device state
+  int rc = CANS_OK;
+  auto fail = [&](int r) { cans_plan_destroy(P); return r; };
+  std::vector<double> lamcol((size_t)n1 * n2);
+  for (int i = 0; i < n1; i++)
+    for (int j = 0; j < n2; j++) lamcol[(size_t)i * n2 + j] = P->lam_h[i + (size_t)n1 * j];
+  const size_t ncell = (size_t)n1 * n2 * n3;
+  const size_t esz = precision == CANS_FP64 ? sizeof(double) : sizeof(float);
+  cudaError_t e;
+  if ((e = cudaMalloc(&P->lamcol, lamcol.size() * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&P->a_d, n3 * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&P->b_d, n3 * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&P->c_d, n3 * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&P->bb_d, n3 * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&P->S, ncell * esz)) != cudaSuccess ||
+      (e = cudaMalloc(&P->red, 4096)) != cudaSuccess) {
+    cans_set_last_cuda_error(e);
+    return fail(e == cudaErrorMemoryAllocation ? CANS_ENOMEM : CANS_ECUDA);
+  }
+  P->bytes += (long long)(lamcol.size() * sizeof(double) + 4 * n3 * sizeof(double) + ncell * esz + 4096);
+  if (precision == CANS_FP32) {
+    if ((e = cudaMalloc(&P->R64, ncell * sizeof(double))) != cudaSuccess) {
+      cans_set_last_cuda_error(e);
+      return fail(CANS_ENOMEM);
+    }
+    P->bytes += (long long)(ncell * sizeof(double));
+  }
+  if (cudaMemcpy(P->lamcol, lamcol.data(), lamcol.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(P->a_d, P->a_h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(P->b_d, P->b_h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(P->c_d, P->c_h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(CANS_ECUDA);
+  for (int d = 0; d < 2; d++) {
+    rc = precision == CANS_FP64 ? upload_tables<double>(P, d) : upload_tables<float>(P, d);
+    if (rc) return fail(rc);
+  }
+  Factor *F;
+  if ((rc = get_factor(P, 0., false, &F))) return fail(rc);
+  *plan = P;
+  return CANS_OK;
+}
+
+extern "C" int cans_solver(cans_plan *P, double *p) {
+  if (!P || !p) return CANS_EINVAL;
+  if (P->precision != CANS_FP64) return solve_impl<float, double>(P, p, 0., false, P->normfft);
+  return solve_impl<double, double>(P, p, 0., false, P->normfft);
+}
+
+extern "C" int cans_solver_f32(cans_plan *P, float *p) {
+  if (!P || !p) return CANS_EINVAL;
+  if (P->precision != CANS_FP32) return CANS_EINVAL;
+  return solve_impl<float, float>(P, p, 0., false, P->normfft);
+}
+
+// updt_rhs_b with alpha for the Helmholtz wrapper (src/bound.f90:514-598)
+__global__ void k_rhsb_face(double *p, int n1, int n2, int n3, int dir, int plane, double val) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e1 = dir == 0 ? n2 : n1, e2 = dir == 2 ? n2 : n3;
+  if (t >= e1 * e2) return;
+  const int a = t % e1 + 1, b = t / e1 + 1;
+  size_t idx = dir == 0 ? hidx(plane, a, b, n1, n2) : (dir == 1 ? hidx(a, plane, b, n1, n2) : hidx(a, b, plane, n1, n2));
+  p[idx] = p[idx] + val;
+}
+
+int cans_rhsb_add(const char c_or_f[3], const char cbc[6], const int n[3], const int is_bound[6],
+                  const double rhsb[6], double *p, double norm, cudaStream_t st) {
+  for (int d = 0; d < 3; d++) {
+    const int q = (c_or_f[d] == 'f' && cbc[1 + 2 * d] == 'D') ? 1 : 0;
+    for (int ib = 0; ib < 2; ib++) {
+      if (!is_bound[ib + 2 * d]) continue;
+      const int plane = ib == 0 ? 1 : n[d] - q;
+      const int e1 = d == 0 ? n[1] : n[0], e2 = d == 2 ? n[1] : n[2];
+      const int cnt = e1 * e2;
+      k_rhsb_face<<<(cnt + 255) / 256, 256, 0, st>>>(p, n[0], n[1], n[2], d, plane, rhsb[ib + 2 * d] * norm);
+      CANS_LAUNCH_CHECK();
+    }
+  }
+  return CANS_OK;
+}
+
+extern "C" int cans_solve_helmholtz(cans_plan *P, double alpha, const int is_bound[6], double *p) {
+  if (!P || !p || !is_bound || alpha == 0.) return CANS_EINVAL;
+  int rc = cans_rhsb_add(P->c_or_f, P->cbc, P->n, is_bound, P->rhsb, p, alpha, P->stream);
+  if (rc) return rc;
+  const double alphai = 1. / alpha;
+  if (P->precision != CANS_FP64) return solve_impl<float, double>(P, p, alphai, true, P->normfft * alphai);
+  return solve_impl<double, double>(P, p, alphai, true, P->normfft * alphai);
+}

@@ -1,0 +1,680 @@
+// Projection, momentum and boundary-condition kernels of the CaNS pressure-correction
+// path (FP64), one GB300.  Every kernel keeps the reference's arithmetic order so the
+// results agree with the CPU path to rounding.
+//
+//   fillps    src/fillps.f90:13-51
+//   correc    src/correc.f90:13-60        (one pass over the haloed box for u, v, w)
+//   updatep   src/updatep.f90:14-88
+//   rk        src/rk.f90:24-333 + mom_xyz_ad src/mom.f90:771-1019 + bulk forcing
+//   bounds    src/bound.f90:17-598 (one GPU: periodic halos are local copies)
+//   checks    src/chkdiv.f90, src/chkdt.f90, src/utils.f90 (deterministic two-level
+//             FP64 reductions)
+#include <math.h>
+#include <string.h>
+
+#include <cfloat>
+#include <vector>
+
+#include "cans_internal.cuh"
+
+namespace {
+constexpr int kTB = 256;
+
+struct Dims {
+  int n1, n2, n3;
+};
+
+__device__ __forceinline__ bool cell3(long t, const Dims &d, int &i, int &j, int &k) {
+  const long nx = d.n1, ny = d.n2;
+  if (t >= nx * ny * d.n3) return false;
+  i = (int)(t % nx) + 1;
+  const long r = t / nx;
+  j = (int)(r % ny) + 1;
+  k = (int)(r / ny) + 1;
+  return true;
+}
+
+unsigned blocks_for(long count, int tb = kTB) { return (unsigned)((count + tb - 1) / tb); }
+}  // namespace
+
+// ------------------------------------------------------------------------------ fillps
+__global__ void __launch_bounds__(kTB) k_fillps(Dims d, double dti, double dtidxi, double dtidyi,
+                                                const double *__restrict__ dzfi, const double *__restrict__ u,
+                                                const double *__restrict__ v, const double *__restrict__ w,
+                                                double *__restrict__ p) {
+  int i, j, k;
+  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t c = hidx(i, j, k, n1, n2);
+  p[c] = ((w[c] - w[hidx(i, j, k - 1, n1, n2)]) * dti * dzfi[k] + (v[c] - v[hidx(i, j - 1, k, n1, n2)]) * dtidyi) +
+         (u[c] - u[hidx(i - 1, j, k, n1, n2)]) * dtidxi;
+}
+
+extern "C" int cans_fillps(const int n[3], const double dli[3], const double *dzfi, double dti, const double *u,
+                           const double *v, const double *w, double *p, void *stream) {
+  if (!n || !dli || !dzfi || !u || !v || !w || !p || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  Dims d{n[0], n[1], n[2]};
+  const long cnt = (long)n[0] * n[1] * n[2];
+  k_fillps<<<blocks_for(cnt), kTB, 0, as_stream(stream)>>>(d, dti, dti * dli[0], dti * dli[1], dzfi, u, v, w, p);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ correc
+// one thread per haloed cell; u for i<=n1, v for j<=n2, w for k<=n3 (the reference's ranges)
+__global__ void __launch_bounds__(kTB) k_correc(Dims d, double fi, double fj, double dt,
+                                                const double *__restrict__ dzci, const double *__restrict__ p,
+                                                double *__restrict__ u, double *__restrict__ v,
+                                                double *__restrict__ w) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nx = d.n1 + 2, ny = d.n2 + 2;
+  if (t >= nx * ny * (d.n3 + 2)) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / (nx * ny));
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t c = (size_t)t;
+  const double pc = p[c];
+  if (i <= d.n1) u[c] = u[c] - fi * (p[c + 1] - pc);
+  if (j <= d.n2) v[c] = v[c] - fj * (p[hidx(i, j + 1, k, n1, n2)] - pc);
+  if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * (p[hidx(i, j, k + 1, n1, n2)] - pc);
+}
+
+extern "C" int cans_correc(const int n[3], const double dli[3], const double *dzci, double dt, const double *p,
+                           double *u, double *v, double *w, void *stream) {
+  if (!n || !dli || !dzci || !p || !u || !v || !w || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  Dims d{n[0], n[1], n[2]};
+  const long cnt = (long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+  k_correc<<<blocks_for(cnt), kTB, 0, as_stream(stream)>>>(d, dt * dli[0], dt * dli[1], dt, dzci, p, u, v, w);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ updatep
+__global__ void __launch_bounds__(kTB) k_updatep(Dims d, double dxi, double dyi, double alpha, int impl,
+                                                 const double *__restrict__ dzci, const double *__restrict__ dzfi,
+                                                 const double *__restrict__ pp, double *__restrict__ p) {
+  int i, j, k;
+  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t c = hidx(i, j, k, n1, n2);
+  if (impl) {
+    const double ppc = pp[c];
+    double lap = 0.;
+    lap = lap + ((pp[c + 1] - 2. * ppc + pp[c - 1]) * (dxi * dxi) +
+                 (pp[hidx(i, j + 1, k, n1, n2)] - 2. * ppc + pp[hidx(i, j - 1, k, n1, n2)]) * (dyi * dyi));
+    lap = lap + ((pp[hidx(i, j, k + 1, n1, n2)] - ppc) * dzci[k] - (ppc - pp[hidx(i, j, k - 1, n1, n2)]) * dzci[k - 1]) *
+                    dzfi[k];
+    p[c] = p[c] + ppc + alpha * lap;
+  } else {
+    p[c] = p[c] + pp[c];
+  }
+}
+
+extern "C" int cans_updatep(const int n[3], const double dli[3], const double *dzci, const double *dzfi, double alpha,
+                            int is_impdiff, const double *pp, double *p, void *stream) {
+  if (!n || !dli || !dzci || !dzfi || !pp || !p || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  Dims d{n[0], n[1], n[2]};
+  k_updatep<<<blocks_for((long)n[0] * n[1] * n[2]), kTB, 0, as_stream(stream)>>>(d, dli[0], dli[1], alpha,
+                                                                                  is_impdiff ? 1 : 0, dzci, dzfi, pp, p);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ momentum
+// mom_xyz_ad (src/mom.f90:771-1019) fused with the RK update of src/rk.f90:155-186 and the
+// dudtrko = dudtrk copy (rk.f90:266-276).  The new velocity goes to `unew` (halo-free) because
+// neighbouring threads still read the old one; dudtrko is updated in place (cell-local).
+// When impdiff, the implicit part dudtd is written to `dtd` (halo-free, 3 fields).
+__global__ void __launch_bounds__(kTB) k_mom_rk(Dims d, double dxi, double dyi, double visc, double f1, double f2,
+                                                double f12, double bfx, double bfy, double bfz, int impdiff,
+                                                const double *__restrict__ dzci, const double *__restrict__ dzfi,
+                                                const double *__restrict__ u, const double *__restrict__ v,
+                                                const double *__restrict__ w, const double *__restrict__ p,
+                                                double *__restrict__ dudtrko, double *__restrict__ dvdtrko,
+                                                double *__restrict__ dwdtrko, double *__restrict__ unew,
+                                                double *__restrict__ dtd) {
+  int i, j, k;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!cell3(t, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t np = (size_t)d.n1 * d.n2 * d.n3;
+  const size_t sx = 1, sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
+  const size_t c = hidx(i, j, k, n1, n2);
+  const double dzci_k = dzci[k], dzci_km = dzci[k - 1], dzfi_k = dzfi[k], dzfi_kp = dzfi[k + 1];
+  const double rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
+  const double u_ccm = u[c - sz], u_cmc = u[c - sy], u_mcc = u[c - sx], u_ccc = u[c], u_pcc = u[c + sx],
+               u_mpc = u[c - sx + sy], u_cpc = u[c + sy], u_cmp = u[c - sy + sz], u_mcp = u[c - sx + sz],
+               u_ccp = u[c + sz];
+  const double v_ccm = v[c - sz], v_pcm = v[c + sx - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx],
+               v_ccc = v[c], v_pcc = v[c + sx], v_cpc = v[c + sy], v_ccp = v[c + sz], v_cmp = v[c - sy + sz];
+  const double w_ccm = w[c - sz], w_pcm = w[c + sx - sz], w_cpm = w[c + sy - sz], w_cmc = w[c - sy], w_mcc = w[c - sx],
+               w_ccc = w[c], w_pcc = w[c + sx], w_cpc = w[c + sy], w_ccp = w[c + sz];
+  // x
+  const double dudxp = (u_pcc - u_ccc) * dxi, dudxm = (u_ccc - u_mcc) * dxi;
+  const double dudyp = (u_cpc - u_ccc) * dyi, dudym = (u_ccc - u_cmc) * dyi;
+  const double dudzp = (u_ccp - u_ccc) * dzci_k, dudzm = (u_ccc - u_ccm) * dzci_km;
+  const double uuip = 0.25 * (u_ccc + u_pcc) * u_pcc, uuim = 0.25 * (u_ccc + u_mcc) * u_mcc;
+  const double vujp = 0.25 * (v_ccc + v_pcc) * u_cpc, vujm = 0.25 * (v_cmc + v_pmc) * u_cmc;
+  const double wukp = 0.25 * (w_ccc + w_pcc) * u_ccp, wukm = 0.25 * (w_ccm + w_pcm) * u_ccm;
+  const double dudtd_xy = visc * (dudxp - dudxm) * dxi + visc * (dudyp - dudym) * dyi;
+  const double dudtd_z = visc * (dudzp - dudzm) * dzfi_k;
+  double dudt = -(uuip - uuim) * dxi - (vujp - vujm) * dyi - (wukp - wukm) * dzfi_k;
+  // y
+  const double dvdxp = (v_pcc - v_ccc) * dxi, dvdxm = (v_ccc - v_mcc) * dxi;
+  const double dvdyp = (v_cpc - v_ccc) * dyi, dvdym = (v_ccc - v_cmc) * dyi;
+  const double dvdzp = (v_ccp - v_ccc) * dzci_k, dvdzm = (v_ccc - v_ccm) * dzci_km;
+  const double uvip = 0.25 * (u_ccc + u_cpc) * v_pcc, uvim = 0.25 * (u_mcc + u_mpc) * v_mcc;
+  const double vvjp = 0.25 * (v_ccc + v_cpc) * v_cpc, vvjm = 0.25 * (v_ccc + v_cmc) * v_cmc;
+  const double wvkp = 0.25 * (w_ccc + w_cpc) * v_ccp, wvkm = 0.25 * (w_ccm + w_cpm) * v_ccm;
+  const double dvdtd_xy = visc * (dvdxp - dvdxm) * dxi + visc * (dvdyp - dvdym) * dyi;
+  const double dvdtd_z = visc * (dvdzp - dvdzm) * dzfi_k;
+  double dvdt = -(uvip - uvim) * dxi - (vvjp - vvjm) * dyi - (wvkp - wvkm) * dzfi_k;
+  // z
+  const double dwdxp = (w_pcc - w_ccc) * dxi, dwdxm = (w_ccc - w_mcc) * dxi;
+  const double dwdyp = (w_cpc - w_ccc) * dyi, dwdym = (w_ccc - w_cmc) * dyi;
+  const double dwdzp = (w_ccp - w_ccc) * dzfi_kp, dwdzm = (w_ccc - w_ccm) * dzfi_k;
+  const double uwip = 0.25 * (rdzm * u_ccc + rdzp * u_ccp) * w_pcc, uwim = 0.25 * (rdzm * u_mcc + rdzp * u_mcp) * w_mcc;
+  const double vwjp = 0.25 * (rdzm * v_ccc + rdzp * v_ccp) * w_cpc, vwjm = 0.25 * (rdzm * v_cmc + rdzp * v_cmp) * w_cmc;
+  const double wwkp = 0.25 * (w_ccc + w_ccp) * w_ccp, wwkm = 0.25 * (w_ccc + w_ccm) * w_ccm;
+  const double dwdtd_xy = visc * (dwdxp - dwdxm) * dxi + visc * (dwdyp - dwdym) * dyi;
+  const double dwdtd_z = visc * (dwdzp - dwdzm) * dzci_k;
+  double dwdt = -(uwip - uwim) * dxi - (vwjp - vwjm) * dyi - (wwkp - wwkm) * dzci_k;
+  double dud = 0., dvd = 0., dwd = 0.;
+  if (impdiff) {
+    dud = dudtd_xy + dudtd_z; dvd = dvdtd_xy + dvdtd_z; dwd = dwdtd_xy + dwdtd_z;
+  } else {
+    dudt = dudt + dudtd_xy + dudtd_z;
+    dvdt = dvdt + dvdtd_xy + dvdtd_z;
+    dwdt = dwdt + dwdtd_xy + dwdtd_z;
+  }
+  const size_t h = (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
+  const double pc = p[c];
+  double un = u_ccc + f1 * dudt + f2 * dudtrko[h] + f12 * (bfx - dxi * (p[c + sx] - pc));
+  double vn = v_ccc + f1 * dvdt + f2 * dvdtrko[h] + f12 * (bfy - dyi * (p[c + sy] - pc));
+  double wn = w_ccc + f1 * dwdt + f2 * dwdtrko[h] + f12 * (bfz - dzci_k * (p[c + sz] - pc));
+  if (impdiff) {
+    un = un + f12 * dud; vn = vn + f12 * dvd; wn = wn + f12 * dwd;
+    dtd[h] = dud; dtd[h + np] = dvd; dtd[h + 2 * np] = dwd;
+  }
+  dudtrko[h] = dudt; dvdtrko[h] = dvdt; dwdtrko[h] = dwdt;
+  unew[h] = un; unew[h + np] = vn; unew[h + 2 * np] = wn;
+}
+
+// copy-back of the new velocity with the per-block partial sums of the bulk means
+// (grid_vol_ratio weighted, src/utils.f90:15-42); partials[blk*3 + c]
+__global__ void __launch_bounds__(kTB) k_rk_writeback(Dims d, const double *__restrict__ unew,
+                                                      const double *__restrict__ gvr_c,
+                                                      const double *__restrict__ gvr_f, double *__restrict__ u,
+                                                      double *__restrict__ v, double *__restrict__ w,
+                                                      double *__restrict__ partials) {
+  __shared__ double red[3][kTB / 32];
+  int i, j, k;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  double s0 = 0., s1 = 0., s2 = 0.;
+  if (cell3(t, d, i, j, k)) {
+    const size_t np = (size_t)d.n1 * d.n2 * d.n3;
+    const size_t c = hidx(i, j, k, d.n1, d.n2);
+    const double un = unew[t], vn = unew[t + np], wn = unew[t + 2 * np];
+    u[c] = un; v[c] = vn; w[c] = wn;
+    s0 = un * gvr_f[k]; s1 = vn * gvr_f[k]; s2 = wn * gvr_c[k];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+  }
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { red[0][wid] = s0; red[1][wid] = s1; red[2][wid] = s2; }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double s = 0.;
+    for (int q = 0; q < kTB / 32; q++) s += red[threadIdx.x][q];
+    partials[(size_t)blockIdx.x * 3 + threadIdx.x] = s;
+  }
+}
+
+// deterministic final sum of per-block partials: out[c] = sum_b partials[b*stride + c]
+__global__ void k_sum_partials(const double *__restrict__ partials, long nblk, int stride, int ncomp,
+                               double *__restrict__ out) {
+  __shared__ double red[kTB];
+  for (int c = 0; c < ncomp; c++) {
+    double s = 0.;
+    for (long b = threadIdx.x; b < nblk; b += blockDim.x) s += partials[(size_t)b * stride + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[c] = red[0];
+    __syncthreads();
+  }
+}
+
+// deterministic max of per-block partials
+__global__ void k_max_partials(const double *__restrict__ partials, long nblk, double *__restrict__ out) {
+  __shared__ double red[kTB];
+  double s = 0.;
+  for (long b = threadIdx.x; b < nblk; b += blockDim.x) s = fmax(s, partials[b]);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
+}
+
+// forcing: f_c = velf_c - mean_c on the device, then u += f (explicit) or
+// u = (u - .5*f12*dudtd) + f (implicit diffusion, rk.f90:310-326)
+__global__ void __launch_bounds__(kTB) k_rk_forcing(Dims d, const double *__restrict__ means, double vfx, double vfy,
+                                                    double vfz, int fx, int fy, int fz, int impdiff, double f12,
+                                                    const double *__restrict__ dtd, double *__restrict__ u,
+                                                    double *__restrict__ v, double *__restrict__ w,
+                                                    double *__restrict__ fout) {
+  int i, j, k;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const double f0 = fx ? vfx - means[0] : 0., f1 = fy ? vfy - means[1] : 0., f2 = fz ? vfz - means[2] : 0.;
+  if (t == 0 && fout) { fout[0] = f0; fout[1] = f1; fout[2] = f2; }
+  if (!cell3(t, d, i, j, k)) return;
+  const size_t c = hidx(i, j, k, d.n1, d.n2);
+  if (impdiff) {
+    const size_t np = (size_t)d.n1 * d.n2 * d.n3;
+    u[c] = (u[c] - .5 * f12 * dtd[t]) + f0;
+    v[c] = (v[c] - .5 * f12 * dtd[t + np]) + f1;
+    w[c] = (w[c] - .5 * f12 * dtd[t + 2 * np]) + f2;
+  } else {
+    if (fx) u[c] = u[c] + f0;
+    if (fy) v[c] = v[c] + f1;
+    if (fz) w[c] = w[c] + f2;
+  }
+}
+
+namespace {
+struct RkScratch {
+  double *buf = nullptr;
+  size_t bytes = 0;
+  int dev = -1;
+} g_rk;
+
+int rk_scratch(size_t bytes, double **out) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (g_rk.bytes < bytes || g_rk.dev != dev) {
+    if (g_rk.buf) cudaFree(g_rk.buf);
+    g_rk.buf = nullptr;
+    g_rk.bytes = 0;
+    CANS_CUDA_TRY(cudaMalloc(&g_rk.buf, bytes));
+    g_rk.bytes = bytes;
+    g_rk.dev = dev;
+  }
+  *out = g_rk.buf;
+  return CANS_OK;
+}
+}  // namespace
+
+extern "C" size_t cans_rk_work_doubles(const int n[3], int is_impdiff) {
+  if (!n) return 0;
+  const long np = (long)n[0] * n[1] * n[2];
+  return (size_t)3 * np + (is_impdiff ? 3 * (size_t)np : 0) + 3 * (size_t)blocks_for(np) + 8;
+}
+
+extern "C" int cans_rk(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                       const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
+                       const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
+                       int is_impdiff, double *dudtrko, double *dvdtrko, double *dwdtrko, double *u, double *v,
+                       double *w, double f[3], double *work, void *stream) {
+  if (!rkpar || !n || !dli || !dzci || !dzfi || !gvr_c || !gvr_f || !p || !is_forced || !velf || !bforce ||
+      !dudtrko || !dvdtrko || !dwdtrko || !u || !v || !w)
+    return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const long np = (long)n[0] * n[1] * n[2];
+  const unsigned nblk = blocks_for(np);
+  // scratch: unew (3 np) + dtd (3 np, impdiff) + partials (3 nblk) + means (3) + f (3)
+  const size_t need = sizeof(double) * cans_rk_work_doubles(n, is_impdiff);
+  double *s = work;
+  if (!s) {
+    int rc = rk_scratch(need, &s);
+    if (rc) return rc;
+  }
+  double *unew = s, *dtd = s + 3 * np, *partials = dtd + (is_impdiff ? 3 * np : 0), *means = partials + 3 * (size_t)nblk,
+         *fdev = means + 3;
+  const double f1 = rkpar[0] * dt, f2 = rkpar[1] * dt, f12 = f1 + f2;
+  k_mom_rk<<<nblk, kTB, 0, st>>>(d, dli[0], dli[1], visc, f1, f2, f12, bforce[0], bforce[1], bforce[2],
+                                  is_impdiff ? 1 : 0, dzci, dzfi, u, v, w, p, dudtrko, dvdtrko, dwdtrko, unew, dtd);
+  CANS_LAUNCH_CHECK();
+  k_rk_writeback<<<nblk, kTB, 0, st>>>(d, unew, gvr_c, gvr_f, u, v, w, partials);
+  CANS_LAUNCH_CHECK();
+  const bool forced = is_forced[0] || is_forced[1] || is_forced[2];
+  if (forced || is_impdiff) {
+    k_sum_partials<<<1, kTB, 0, st>>>(partials, nblk, 3, 3, means);
+    CANS_LAUNCH_CHECK();
+    k_rk_forcing<<<nblk, kTB, 0, st>>>(d, means, velf[0], velf[1], velf[2], is_forced[0], is_forced[1], is_forced[2],
+                                       is_impdiff ? 1 : 0, f12, dtd, u, v, w, fdev);
+    CANS_LAUNCH_CHECK();
+  }
+  if (f) {
+    f[0] = f[1] = f[2] = 0.;
+    if (forced) {
+      CANS_CUDA_TRY(cudaMemcpyAsync(f, fdev, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CANS_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+  }
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ boundaries
+// periodic self-exchange (one GPU) along dir 1 (y) or 2 (z): full extent of the other dims
+__global__ void k_halo_copy(double *p, int n1, int n2, int n3, int dir, int up, int lo) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int e1 = n1 + 2, e2 = dir == 1 ? n3 + 2 : n2 + 2;
+  if (t >= (long)e1 * e2) return;
+  const int a = (int)(t % e1), b = (int)(t / e1);
+  if (dir == 1) {
+    if (up) p[hidx(a, n2 + 1, b, n1, n2)] = p[hidx(a, 1, b, n1, n2)];
+    if (lo) p[hidx(a, 0, b, n1, n2)] = p[hidx(a, n2, b, n1, n2)];
+  } else {
+    if (up) p[hidx(a, b, n3 + 1, n1, n2)] = p[hidx(a, b, 1, n1, n2)];
+    if (lo) p[hidx(a, b, 0, n1, n2)] = p[hidx(a, b, n3, n1, n2)];
+  }
+}
+
+// set_bc (src/bound.f90:182-463), nh = 1
+__global__ void k_set_bc(double *p, int n1, int n2, int n3, char ctype, int ib, int dir, int centered, double factor,
+                         double sgn) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int e1 = (dir == 0 ? n2 : n1) + 2, e2 = (dir == 2 ? n2 : n3) + 2;
+  if (t >= (long)e1 * e2) return;
+  const int b1 = (int)(t % e1), b2 = (int)(t / e1);
+  const int nn = dir == 0 ? n1 : (dir == 1 ? n2 : n3);
+  auto at = [&](int m) -> double & {
+    return dir == 0 ? p[hidx(m, b1, b2, n1, n2)] : (dir == 1 ? p[hidx(b1, m, b2, n1, n2)] : p[hidx(b1, b2, m, n1, n2)]);
+  };
+  if (ctype == 'P') {
+    if (ib == 0) at(0) = at(nn); else at(nn + 1) = at(1);
+  } else if (centered) {
+    if (ib == 0) at(0) = factor + sgn * at(1); else at(nn + 1) = factor + sgn * at(nn);
+  } else if (ctype == 'D') {
+    if (ib == 0) at(0) = factor;
+    else { at(nn + 1) = at(nn - 1); at(nn) = factor; }
+  } else {
+    if (ib == 0) at(0) = 1. * factor + at(1);
+    else { at(nn + 1) = at(nn); at(nn) = 1. * factor + at(nn - 1); }
+  }
+}
+
+static int launch_set_bc(double *p, const int n[3], char ctype, int ib, int dir, int centered, double rvalue, double dr,
+                         cudaStream_t st) {
+  double factor = rvalue, sgn = 0.;
+  if (ctype == 'D' && centered) { factor = 2. * factor; sgn = -1.; }
+  if (ctype == 'N') { factor = ib == 0 ? -dr * factor : dr * factor; sgn = 1.; }
+  const long cnt = (long)((dir == 0 ? n[1] : n[0]) + 2) * ((dir == 2 ? n[1] : n[2]) + 2);
+  k_set_bc<<<blocks_for(cnt), kTB, 0, st>>>(p, n[0], n[1], n[2], ctype, ib, dir, centered, factor, sgn);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+static int launch_halo(double *p, const int n[3], int dir, int side, cudaStream_t st) {
+  const int up = side == 2 || side == 1, lo = side == 2 || side == -1;
+  if (!(up || lo)) return CANS_OK;
+  const long cnt = (long)(n[0] + 2) * ((dir == 1 ? n[2] : n[1]) + 2);
+  k_halo_copy<<<blocks_for(cnt), kTB, 0, st>>>(p, n[0], n[1], n[2], dir, up, lo);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+static bool bc_char_ok(char c) { return c == 'P' || c == 'D' || c == 'N'; }
+
+// bounduvw, one GPU with x-aligned pencils (is_bound in x always true; periodic y/z
+// ghosts are local copies): CPU-path order of src/bound.f90:17-122
+extern "C" int cans_bounduvw(const char cbc[18], const int n[3], const double bc[18], const int is_bound[6],
+                             const double dl[3], const double *dzc, const double *dzf, double *u, double *v,
+                             double *w, int keep_norm, int halos_norm, int halos_tang, void *stream) {
+  if (!cbc || !n || !bc || !is_bound || !dl || !dzc || !dzf || !u || !v || !w) return CANS_EINVAL;
+  for (int e = 0; e < 18; e++) if (!bc_char_ok(cbc[e])) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  int updt_norm[2] = {1, 1};
+  if (halos_norm == -1) updt_norm[1] = 0;
+  else if (halos_norm == 0) updt_norm[0] = updt_norm[1] = 0;
+  else if (halos_norm == 1) updt_norm[0] = 0;
+  double *f[3] = {u, v, w};
+  int rc;
+  for (int dd = 1; dd < 3; dd++)
+    for (int c = 0; c < 3; c++) {
+      const bool pp = cbc[2 * dd + 6 * c] == 'P' && cbc[1 + 2 * dd + 6 * c] == 'P';
+      if (!pp || is_bound[2 * dd] || is_bound[2 * dd + 1]) continue;
+      if ((rc = launch_halo(f[c], n, dd, c == dd ? halos_norm : halos_tang, st))) return rc;
+    }
+  for (int dd = 0; dd < 3; dd++)
+    for (int ib = 0; ib < 2; ib++) {
+      if (!is_bound[ib + 2 * dd]) continue;
+      const bool pp = cbc[2 * dd + 6 * dd] == 'P' && cbc[1 + 2 * dd + 6 * dd] == 'P';
+      const bool apply_norm = !keep_norm || (pp && updt_norm[ib]);
+      for (int c = 0; c < 3; c++) {
+        double dr;
+        if (dd < 2) dr = dl[dd];
+        else if (c == 2) dr = ib == 0 ? dzf[0] : dzf[n[2]];
+        else dr = ib == 0 ? dzc[0] : dzc[n[2]];
+        const char ct = cbc[ib + 2 * dd + 6 * c];
+        const double bv = bc[ib + 2 * dd + 6 * c];
+        if (c == dd) {
+          if (apply_norm && (rc = launch_set_bc(f[c], n, ct, ib, dd, 0, bv, dr, st))) return rc;
+        } else if ((rc = launch_set_bc(f[c], n, ct, ib, dd, 1, bv, dr, st))) {
+          return rc;
+        }
+      }
+    }
+  return CANS_OK;
+}
+
+// boundp (src/bound.f90:124-180)
+extern "C" int cans_boundp(const char cbc[6], const int n[3], const double bc[6], const int is_bound[6],
+                           const double dl[3], const double *dzc, double *p, int halo_side, void *stream) {
+  if (!cbc || !n || !bc || !is_bound || !dl || !dzc || !p) return CANS_EINVAL;
+  for (int e = 0; e < 6; e++) if (!bc_char_ok(cbc[e])) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  int upd[2] = {1, 1};
+  if (halo_side == -1) upd[1] = 0;
+  else if (halo_side == 0) upd[0] = upd[1] = 0;
+  else if (halo_side == 1) upd[0] = 0;
+  int rc;
+  for (int dd = 1; dd < 3; dd++) {
+    const bool pp = cbc[2 * dd] == 'P' && cbc[2 * dd + 1] == 'P';
+    if (!pp || is_bound[2 * dd] || is_bound[2 * dd + 1]) continue;
+    if ((rc = launch_halo(p, n, dd, halo_side, st))) return rc;
+  }
+  for (int dd = 0; dd < 3; dd++)
+    for (int ib = 0; ib < 2; ib++) {
+      if (!is_bound[ib + 2 * dd] || !upd[ib]) continue;
+      const double dr = dd < 2 ? dl[dd] : (ib == 0 ? dzc[0] : dzc[n[2]]);
+      if ((rc = launch_set_bc(p, n, cbc[ib + 2 * dd], ib, dd, 1, bc[ib + 2 * dd], dr, st))) return rc;
+    }
+  return CANS_OK;
+}
+
+int cans_rhsb_add(const char c_or_f[3], const char cbc[6], const int n[3], const int is_bound[6],
+                  const double rhsb[6], double *p, double norm, cudaStream_t st);
+
+// updt_rhs_b (src/bound.f90:514-598)
+extern "C" int cans_updt_rhs_b(const char c_or_f[3], const char cbc[6], const int n[3], const int is_bound[6],
+                               const double rhsb[6], double *p, double alpha, int has_alpha, void *stream) {
+  if (!c_or_f || !cbc || !n || !is_bound || !rhsb || !p) return CANS_EINVAL;
+  return cans_rhsb_add(c_or_f, cbc, n, is_bound, rhsb, p, has_alpha ? alpha : 1., as_stream(stream));
+}
+
+// ------------------------------------------------------------------------------ reductions
+__global__ void __launch_bounds__(kTB) k_chkdiv(Dims d, double dxi, double dyi, const double *__restrict__ dzfi,
+                                                const double *__restrict__ u, const double *__restrict__ v,
+                                                const double *__restrict__ w, double *__restrict__ part_sum,
+                                                double *__restrict__ part_max) {
+  __shared__ double rs[kTB / 32], rm[kTB / 32];
+  int i, j, k;
+  double s = 0., mx = 0.;
+  if (cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) {
+    const int n1 = d.n1, n2 = d.n2;
+    const size_t c = hidx(i, j, k, n1, n2);
+    const double div = ((w[c] - w[hidx(i, j, k - 1, n1, n2)]) * dzfi[k] + (v[c] - v[hidx(i, j - 1, k, n1, n2)]) * dyi) +
+                       (u[c] - u[c - 1]) * dxi;
+    mx = fabs(div);
+    s = fabs(div) / (dxi * dyi * dzfi[k]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, o);
+    mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0) { rs[threadIdx.x >> 5] = s; rm[threadIdx.x >> 5] = mx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0., b = 0.;
+    for (int q = 0; q < kTB / 32; q++) { a += rs[q]; b = fmax(b, rm[q]); }
+    part_sum[blockIdx.x] = a;
+    part_max[blockIdx.x] = b;
+  }
+}
+
+namespace {
+struct RedScratch {
+  double *buf = nullptr;
+  size_t n = 0;
+  int dev = -1;
+} g_red;
+int red_scratch(size_t count, double **out) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (g_red.n < count || g_red.dev != dev) {
+    if (g_red.buf) cudaFree(g_red.buf);
+    g_red.buf = nullptr;
+    g_red.n = 0;
+    CANS_CUDA_TRY(cudaMalloc(&g_red.buf, count * sizeof(double)));
+    g_red.n = count;
+    g_red.dev = dev;
+  }
+  *out = g_red.buf;
+  return CANS_OK;
+}
+}  // namespace
+
+extern "C" int cans_chkdiv(const int n[3], const double l[3], const double dli[3], const double *dzfi, const double *u,
+                           const double *v, const double *w, double *divtot, double *divmax, void *stream) {
+  if (!n || !l || !dli || !dzfi || !u || !v || !w || !divtot || !divmax) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const long np = (long)n[0] * n[1] * n[2];
+  const unsigned nblk = blocks_for(np);
+  double *s;
+  int rc = red_scratch(2 * (size_t)nblk + 4, &s);
+  if (rc) return rc;
+  k_chkdiv<<<nblk, kTB, 0, st>>>(d, dli[0], dli[1], dzfi, u, v, w, s, s + nblk);
+  CANS_LAUNCH_CHECK();
+  k_sum_partials<<<1, kTB, 0, st>>>(s, nblk, 1, 1, s + 2 * nblk);
+  CANS_LAUNCH_CHECK();
+  k_max_partials<<<1, kTB, 0, st>>>(s + nblk, nblk, s + 2 * nblk + 1);
+  CANS_LAUNCH_CHECK();
+  double h[2];
+  CANS_CUDA_TRY(cudaMemcpyAsync(h, s + 2 * nblk, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaStreamSynchronize(st));
+  *divtot = h[0] / (l[0] * l[1] * l[2]);
+  *divmax = h[1];
+  return CANS_OK;
+}
+
+__global__ void __launch_bounds__(kTB) k_chkdt(Dims d, double dxi, double dyi, const double *__restrict__ dzci,
+                                               const double *__restrict__ dzfi, const double *__restrict__ u,
+                                               const double *__restrict__ v, const double *__restrict__ w,
+                                               double *__restrict__ part) {
+  __shared__ double rm[kTB / 32];
+  int i, j, k;
+  double mx = 0.;
+  if (cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) {
+    const int n1 = d.n1, n2 = d.n2;
+    auto U = [&](int a, int b, int cc) { return u[hidx(a, b, cc, n1, n2)]; };
+    auto V = [&](int a, int b, int cc) { return v[hidx(a, b, cc, n1, n2)]; };
+    auto W = [&](int a, int b, int cc) { return w[hidx(a, b, cc, n1, n2)]; };
+    const double ux = fabs(U(i, j, k));
+    const double vx = 0.25 * fabs(V(i, j, k) + V(i, j - 1, k) + V(i + 1, j, k) + V(i + 1, j - 1, k));
+    const double wx = 0.25 * fabs(W(i, j, k) + W(i, j, k - 1) + W(i + 1, j, k) + W(i + 1, j, k - 1));
+    const double dtix = ux * dxi + vx * dyi + wx * dzfi[k];
+    const double uy = 0.25 * fabs(U(i, j, k) + U(i, j + 1, k) + U(i - 1, j + 1, k) + U(i - 1, j, k));
+    const double vy = fabs(V(i, j, k));
+    const double wy = 0.25 * fabs(W(i, j, k) + W(i, j + 1, k) + W(i, j + 1, k - 1) + W(i, j, k - 1));
+    const double dtiy = uy * dxi + vy * dyi + wy * dzfi[k];
+    const double uz = 0.25 * fabs(U(i, j, k) + U(i - 1, j, k) + U(i - 1, j, k + 1) + U(i, j, k + 1));
+    const double vz = 0.25 * fabs(V(i, j, k) + V(i, j - 1, k) + V(i, j - 1, k + 1) + V(i, j, k + 1));
+    const double wz = fabs(W(i, j, k));
+    const double dtiz = uz * dxi + vz * dyi + wz * dzci[k];
+    mx = fmax(fmax(dtix, dtiy), dtiz);
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) rm[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.;
+    for (int q = 0; q < kTB / 32; q++) b = fmax(b, rm[q]);
+    part[blockIdx.x] = b;
+  }
+}
+
+extern "C" int cans_chkdt(const int n[3], const double dl[3], const double *dzci, const double *dzfi, double visc,
+                          double alpha, int is_impdiff, int is_impdiff_1d, const double *u, const double *v,
+                          const double *w, double *dtmax, void *stream) {
+  if (!n || !dl || !dzci || !dzfi || !u || !v || !w || !dtmax) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const long np = (long)n[0] * n[1] * n[2];
+  const unsigned nblk = blocks_for(np);
+  double *s;
+  int rc = red_scratch((size_t)nblk + 4, &s);
+  if (rc) return rc;
+  k_chkdt<<<nblk, kTB, 0, st>>>(d, 1. / dl[0], 1. / dl[1], dzci, dzfi, u, v, w, s);
+  CANS_LAUNCH_CHECK();
+  k_max_partials<<<1, kTB, 0, st>>>(s, nblk, s + nblk);
+  CANS_LAUNCH_CHECK();
+  double dti = 0.;
+  std::vector<double> hz((size_t)n[2] + 2);
+  CANS_CUDA_TRY(cudaMemcpyAsync(&dti, s + nblk, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaMemcpyAsync(hz.data(), dzfi, hz.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaStreamSynchronize(st));
+  double dlmin = fmin(dl[0], dl[1]);
+  if (!is_impdiff_1d)
+    for (double z : hz) dlmin = fmin(dlmin, 1. / z);
+  if (dti < DBL_EPSILON) dti = 1.;
+  const double sq3 = (double)sqrtf(3.0f);       // the reference's single-precision literal sqrt(3.)
+  const double c165 = (double)(1.65f / 12.0f);  // and 1.65/12.
+  if (is_impdiff && !is_impdiff_1d) *dtmax = sq3 / dti;
+  else *dtmax = fmin(c165 / fmax(visc, alpha) * (dlmin * dlmin), sq3 / dti);
+  return CANS_OK;
+}
+
+__global__ void __launch_bounds__(kTB) k_bulk_mean(Dims d, const double *__restrict__ gvr, const double *__restrict__ p,
+                                                   double *__restrict__ part) {
+  __shared__ double rs[kTB / 32];
+  int i, j, k;
+  double s = 0.;
+  if (cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) s = p[hidx(i, j, k, d.n1, d.n2)] * gvr[k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) rs[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.;
+    for (int q = 0; q < kTB / 32; q++) a += rs[q];
+    part[blockIdx.x] = a;
+  }
+}
+
+extern "C" int cans_bulk_mean(const int n[3], const double *gvr, const double *p, double *mean, void *stream) {
+  if (!n || !gvr || !p || !mean) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const unsigned nblk = blocks_for((long)n[0] * n[1] * n[2]);
+  double *s;
+  int rc = red_scratch((size_t)nblk + 2, &s);
+  if (rc) return rc;
+  k_bulk_mean<<<nblk, kTB, 0, st>>>(d, gvr, p, s);
+  CANS_LAUNCH_CHECK();
+  k_sum_partials<<<1, kTB, 0, st>>>(s, nblk, 1, 1, s + nblk);
+  CANS_LAUNCH_CHECK();
+  CANS_CUDA_TRY(cudaMemcpyAsync(mean, s + nblk, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaStreamSynchronize(st));
+  return CANS_OK;
+}

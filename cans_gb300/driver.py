@@ -1,0 +1,139 @@
+"""Single-GPU time loop over the C ABI, mirroring src/main.f90:144-520.
+
+`Simulation(case)` performs the set-up of src/main.f90:158-418 (grid, solver
+plans, initial condition, boundary conditions, first dt) and `step()` one time
+step of src/main.f90:437-510 (three RK3 substeps of rk / bounduvw / fillps /
+updt_rhs_b / solver / boundp / correc / bounduvw / updatep / boundp, then the
+dt and divergence checks every `icheck` steps).  All arithmetic runs in the
+library's CUDA kernels; this module only orders the calls, exactly as the
+Fortran host would.
+
+`case` keys follow input.nml (&dns, &numerics): ng, l, gtype, gr, cfl, dtmax,
+dt_f, visci, icheck, cbcvel (18 chars, cbcvel(0:1,3,3) order), bcvel (18),
+cbcpre (6 chars), bcpre (6), bforce, is_forced, velf, is_impdiff, inivel.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import cans
+
+RKCOEFF = ((32. / 60., 0. / 60.), (25. / 60., -17. / 60.), (45. / 60., -25. / 60.))  # src/param.f90:20-22
+DBL_MAX = np.finfo(np.float64).max
+
+
+def initgrid(gtype, n, gr, lz, is_periodic):
+    """src/initgrid.f90:14-99 through the library's cans_initgrid."""
+    arrs = [np.zeros(n + 2) for _ in range(4)]
+    rc = cans.lib().cans_initgrid(int(gtype), int(n), float(gr), float(lz), int(is_periodic),
+                                  *[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs])
+    if rc != 0:
+        raise cans.CansError(rc, "cans_initgrid")
+    return arrs  # dzc, dzf, zc, zf
+
+
+class Simulation:
+    def __init__(self, case, device="cuda"):
+        import torch
+        self.case = case
+        self.device = device
+        n = [int(x) for x in case["ng"]]
+        self.n = n
+        self.l = [float(x) for x in case["l"]]
+        self.dl = [self.l[d] / n[d] for d in range(3)]
+        self.dli = [1. / x for x in self.dl]
+        self.visc = 1. / case["visci"]
+        self.cbcvel, self.cbcpre = case["cbcvel"], case["cbcpre"]
+        self.bcvel = list(case.get("bcvel", [0.] * 18))
+        self.bcpre = list(case.get("bcpre", [0.] * 6))
+        self.bforce = list(case.get("bforce", [0.] * 3))
+        self.is_forced = [int(x) for x in case.get("is_forced", [0] * 3)]
+        self.velf = list(case.get("velf", [0.] * 3))
+        self.is_impdiff = int(case.get("is_impdiff", 0))
+        self.icheck = int(case.get("icheck", 10))
+        self.cfl, self.dtmax, self.dt_f = case.get("cfl", 0.95), case.get("dtmax", 1e5), case.get("dt_f", -1.)
+        zper = self.cbcpre[4:6] == "PP"
+        dzc, dzf, zc, zf = initgrid(case.get("gtype", 1), n[2], case.get("gr", 0.), self.l[2], zper)
+        self.dzc, self.dzf, self.zc, self.zf = dzc, dzf, zc, zf
+        self.dzci_h, self.dzfi_h = 1. / dzc, 1. / dzf
+        vol = self.l[0] * self.l[1] * self.l[2]
+        gvr_c = self.dl[0] * self.dl[1] * dzc / vol
+        gvr_f = self.dl[0] * self.dl[1] * dzf / vol
+        t = lambda a: torch.tensor(a, dtype=torch.float64, device=device)
+        self.dzci, self.dzfi, self.gvr_c, self.gvr_f = t(self.dzci_h), t(self.dzfi_h), t(gvr_c), t(gvr_f)
+        # is_bound on one GPU with x-aligned pencils (src/initmpi.f90:193-267)
+        self.is_bound = [1, 1] + [0 if self.cbcpre[2 * d:2 * d + 2] == "PP" else 1 for d in (1, 2) for _ in (0, 1)]
+        self.plan_p = cans.Plan(n, self.dli, self.dzci_h, self.dzfi_h, self.cbcpre, self.bcpre, "ccc")
+        self.plans_v = []
+        if self.is_impdiff:
+            for c in range(3):
+                cf = ["c", "c", "c"]
+                cf[c] = "f"
+                self.plans_v.append(cans.Plan(n, self.dli, self.dzci_h, self.dzfi_h, self.cbcvel[6 * c:6 * c + 6],
+                                              self.bcvel[6 * c:6 * c + 6], "".join(cf)))
+        self.u, self.v, self.w, self.p, self.pp = [cans.field(n, device) for _ in range(5)]
+        self.dudtrko, self.dvdtrko, self.dwdtrko = [torch.zeros((n[2], n[1], n[0]), dtype=torch.float64,
+                                                                device=device) for _ in range(3)]
+        self.time, self.istep, self.dt, self.dti = 0., 0, 0., 0.
+        self.divtot = self.divmax = 0.
+        self.dpdl = np.zeros(3)
+
+    # ------------------------------------------------------------------ initial conditions
+    def set_fields(self, u=None, v=None, w=None, p=None):
+        """Fortran-indexed host arrays (n1+2, n2+2, n3+2) -> device fields."""
+        for name, a in (("u", u), ("v", v), ("w", w), ("p", p)):
+            if a is not None:
+                getattr(self, name).copy_(cans.to_device(a, self.device))
+
+    def start(self):
+        """src/main.f90:388-418: BCs on the initial fields and the first dt."""
+        n = self.n
+        cans.bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
+                      self.w, False)
+        cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
+        self._new_dt()
+        self.istep, self.time = 0, 0.
+
+    def _new_dt(self):
+        dt_cfl = cans.chkdt(self.n, self.dl, self.dzci, self.dzfi, self.visc, 1. / DBL_MAX, self.is_impdiff, 0,
+                            self.u, self.v, self.w)
+        self.dt = self.dt_f if self.dt_f > 0. else min(self.cfl * dt_cfl, self.dtmax)
+        self.dti = 1. / self.dt
+        return dt_cfl
+
+    def substep(self, irk):
+        n = self.n
+        dtrk = (RKCOEFF[irk][0] + RKCOEFF[irk][1]) * self.dt
+        dtrki = 1. / dtrk
+        f = cans.rk(RKCOEFF[irk], n, self.dli, self.dzci, self.dzfi, self.gvr_c, self.gvr_f, self.dt, self.visc,
+                    self.p, self.is_forced, self.velf, self.bforce, self.is_impdiff, self.dudtrko, self.dvdtrko,
+                    self.dwdtrko, self.u, self.v, self.w)
+        self.dpdl += f
+        alpha = 0.
+        if self.is_impdiff:
+            alpha = -.5 * self.visc * dtrk
+            for c, fld in enumerate((self.u, self.v, self.w)):
+                self.plans_v[c].solve_helmholtz(alpha, self.is_bound, fld)
+        cans.bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
+                      self.w, False, cans.HALO_LOWER)
+        cans.fillps(n, self.dli, self.dzfi, dtrki, self.u, self.v, self.w, self.pp)
+        cans.updt_rhs_b("ccc", self.cbcpre, n, self.is_bound, self.plan_p.rhsb, self.pp)
+        self.plan_p.solve(self.pp)
+        cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.pp)
+        cans.correc(n, self.dli, self.dzci, dtrk, self.pp, self.u, self.v, self.w)
+        cans.bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
+                      self.w, True, cans.HALO_UPPER, cans.HALO_NONE)
+        cans.updatep(n, self.dli, self.dzci, self.dzfi, alpha, self.is_impdiff, self.pp, self.p)
+        cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
+
+    def step(self, nsteps=1):
+        for _ in range(nsteps):
+            self.istep += 1
+            self.time += self.dt
+            self.dpdl[:] = 0.
+            for irk in range(3):
+                self.substep(irk)
+            self.dpdl = -self.dpdl * self.dti
+            if self.icheck > 0 and self.istep % self.icheck == 0:
+                self._new_dt()
+                self.divtot, self.divmax = cans.chkdiv(self.n, self.l, self.dli, self.dzfi, self.u, self.v, self.w)

@@ -1,0 +1,150 @@
+/*
+ * cans_gb300 -- C ABI of the GB300 (sm_103a) pressure-correction path of CaNS.
+ *
+ * Every entry point mirrors one routine of the reference Fortran code
+ * (file:line cited per declaration) with the same argument meaning, so a
+ * Fortran host binds it with an iso_c_binding interface block and passes the
+ * device addresses of its `!$acc enter data` arrays (host_data use_device).
+ *
+ * Conventions
+ *   - Fields u, v, w, p, pp are caller-owned DEVICE arrays in Fortran order
+ *     with one ghost layer: extents (n1+2, n2+2, n3+2), element (i,j,k),
+ *     0 <= i <= n1+1, at offset i + (n1+2)*(j + (n2+2)*k).
+ *   - 1D grid arrays dzc, dzf, dzci, dzfi are DEVICE arrays indexed 0..n3+1;
+ *     the `_g` arrays passed to cans_initsolver are HOST arrays 0..ng3+1.
+ *   - Boundary conditions cbc(0:1,3) are 6 chars in Fortran order
+ *     cbc[ibound + 2*idir] ('P','D','N'); velocity cbcvel(0:1,3,3) are 18
+ *     chars cbcvel[ibound + 2*idir + 6*icomp]; values bc/bcvel likewise.
+ *   - is_bound(0:1,3) is 6 ints, is_bound[ibound + 2*idir].
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  All calls
+ *     are asynchronous on it unless documented otherwise; nothing aborts;
+ *     every call returns a status code below.
+ *   - A plan is not thread-safe; use one plan per host thread.
+ */
+#ifndef CANS_GB300_H
+#define CANS_GB300_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference ignores istat and uses `error stop`) */
+#define CANS_OK 0
+#define CANS_EINVAL 1      /* bad argument (sizes, BC characters, NULL pointers) */
+#define CANS_ENOMEM 2      /* device allocation failed */
+#define CANS_ECUDA 3       /* a CUDA call or kernel launch failed */
+#define CANS_ENOTSUP 4     /* transform length or BC combination not supported */
+#define CANS_ETIMEOUT 5    /* a bounded device wait expired */
+#define CANS_ENONFINITE 6  /* non-finite value detected in a checked result */
+
+/* arithmetic of a plan */
+#define CANS_FP64 0        /* all transforms/eliminations in FP64 */
+#define CANS_FP32 1        /* FP32 transforms, FP64 tridiagonal elimination */
+
+typedef struct cans_plan cans_plan; /* arrplan + lambdaxy + a,b,c + normfft + work space */
+
+const char *cans_strerror(int status);
+/* library build identification (e.g. "cans_gb300 sm_103a") */
+const char *cans_version(void);
+
+/* ---- set-up ------------------------------------------------------------------------------ */
+/* initgrid (src/initgrid.f90:14-99): HOST arrays dzc, dzf, zc, zf (0..n+1); gtype 1..4
+ * (two-end, one-end, one-end reversed, middle clustering) */
+int cans_initgrid(int gtype, int n, double gr, double lz, int is_periodic, double *dzc, double *dzf,
+                  double *zc, double *zf);
+/* initsolver (src/initsolver.f90:15-16) + fftini (src/fft.f90:25-209).
+ * Builds the eigenvalues, the z tridiagonal coefficients, the boundary RHS
+ * values and the transform plans on the device.  Optional HOST outputs (NULL
+ * to skip) return what the reference returns:
+ *   lambdaxy[ng1*ng2] (Fortran order), a,b,c[ng3], *normfft,
+ *   rhsb[6] = the constant face values of rhsb{x,y,z}(:,:,0:1), rhsb[ibound+2*idir]. */
+int cans_initsolver(const int ng[3], const double dli[3], const double *dzci_g, const double *dzfi_g,
+                    const char cbc[6], const double bc[6], const char c_or_f[3], int precision,
+                    void *stream, cans_plan **plan,
+                    double *lambdaxy, double *a, double *b, double *c, double *normfft, double rhsb[6]);
+/* fftend (src/fft.f90:210-246): releases the plan and its device memory */
+int cans_plan_destroy(cans_plan *plan);
+/* device bytes held by the plan (work space + factorisations) */
+long long cans_plan_device_bytes(const cans_plan *plan);
+/* profiling aid (the reference's src/timer.f90 role): when enabled, CUDA events are
+ * recorded on the plan's stream between the five passes of every solve (x-forward,
+ * y-forward, z-elimination, y-backward, x-backward); cans_plan_get_timing synchronises
+ * the stream and returns the mean milliseconds per pass over the recorded solves
+ * (at most 256 since the last call) and clears them. */
+int cans_plan_set_timing(cans_plan *plan, int enable);
+int cans_plan_get_timing(cans_plan *plan, double ms[5], int *nsolves);
+/* running total of CUDA kernel launches issued by this library in this process */
+long long cans_launch_count(void);
+
+/* ---- the Poisson / Helmholtz solve ------------------------------------------------------- */
+/* solver / solver_gpu (src/solver.f90:17, src/solver_gpu.f90:34): in-place solve on
+ * the interior of the haloed device field p (FP64).  Ghost cells are not touched. */
+int cans_solver(cans_plan *plan, double *p);
+/* same solve on an FP32 field (plan created with CANS_FP32) */
+int cans_solver_f32(cans_plan *plan, float *p);
+/* FP64 solve on an FP32-arithmetic plan recovered to FP64 accuracy by iterative
+ * refinement: r = rhs - L p in FP64, correction solved in FP32, p += e (FP64).
+ * Stops when ||r||_2 <= rtol*||rhs||_2 or after max_iter corrections; returns the
+ * number of corrections in *iters and the final relative residual in *relres
+ * (both may be NULL).  dzci/dzfi: device grid arrays (0..n3+1). */
+int cans_solver_refined(cans_plan *plan, double *p, const double dli[3], const double *dzci,
+                        const double *dzfi, double rtol, int max_iter, int *iters, double *relres);
+/* solve_helmholtz (src/solve_helmholtz.f90:28): p/alpha + lap(p) = rhs, 3D variant.
+ * Adds the boundary RHS (updt_rhs_b with alpha) then solves with b+1/alpha and
+ * normfft/alpha.  Factorisations for recent alpha values are cached in the plan. */
+int cans_solve_helmholtz(cans_plan *plan, double alpha, const int is_bound[6], double *p);
+
+/* ---- projection and momentum kernels (FP64) ---------------------------------------------- */
+/* fillps (src/fillps.f90:13) */
+int cans_fillps(const int n[3], const double dli[3], const double *dzfi, double dti,
+                const double *u, const double *v, const double *w, double *p, void *stream);
+/* correc (src/correc.f90:13) */
+int cans_correc(const int n[3], const double dli[3], const double *dzci, double dt,
+                const double *p, double *u, double *v, double *w, void *stream);
+/* updatep (src/updatep.f90:14); is_impdiff selects p += pp + alpha*lap(pp) */
+int cans_updatep(const int n[3], const double dli[3], const double *dzci, const double *dzfi,
+                 double alpha, int is_impdiff, const double *pp, double *p, void *stream);
+/* rk (src/rk.f90:24) with mom_xyz_ad (src/mom.f90:771): one low-storage RK3 substep of
+ * the momentum equations (explicit pressure gradient, constant-flow-rate forcing).
+ * dudtrko..: halo-free (n1,n2,n3) device arrays (previous substep RHS, updated).
+ * work: device scratch of at least cans_rk_work_doubles(n, is_impdiff) doubles, or NULL
+ * to use a scratch buffer the library allocates on first use and keeps.
+ * f[3] (host out): the bulk-velocity forcing applied (velf - mean).  The forcing
+ * reduction is done on the device; the call synchronises `stream` once when any
+ * is_forced is set. */
+int cans_rk(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+            const double *dzfi, const double *grid_vol_ratio_c, const double *grid_vol_ratio_f,
+            double dt, double visc, const double *p, const int is_forced[3], const double velf[3],
+            const double bforce[3], int is_impdiff, double *dudtrko, double *dvdtrko, double *dwdtrko,
+            double *u, double *v, double *w, double f[3], double *work, void *stream);
+size_t cans_rk_work_doubles(const int n[3], int is_impdiff);
+/* bounduvw (src/bound.f90:17), one GPU: halos_* are -1 lower, 0 none, 1 upper, 2 both
+ * (argument absent in the reference).  dl: host; dzc, dzf: HOST arrays 0..n3+1
+ * (only dzc(0), dzc(n3), dzf(0), dzf(n3) are read). */
+int cans_bounduvw(const char cbc[18], const int n[3], const double bc[18], const int is_bound[6],
+                  const double dl[3], const double *dzc, const double *dzf, double *u, double *v,
+                  double *w, int keep_norm, int halos_norm, int halos_tang, void *stream);
+/* boundp (src/bound.f90:124) */
+int cans_boundp(const char cbc[6], const int n[3], const double bc[6], const int is_bound[6],
+                const double dl[3], const double *dzc, double *p, int halo_side, void *stream);
+/* updt_rhs_b (src/bound.f90:514): rhsb[6] constant face values (from cans_initsolver);
+ * has_alpha = 0 when the reference's optional alpha is absent */
+int cans_updt_rhs_b(const char c_or_f[3], const char cbc[6], const int n[3], const int is_bound[6],
+                    const double rhsb[6], double *p, double alpha, int has_alpha, void *stream);
+/* chkdiv (src/chkdiv.f90:15): device FP64 reduction, synchronises `stream` */
+int cans_chkdiv(const int n[3], const double l[3], const double dli[3], const double *dzfi,
+                const double *u, const double *v, const double *w, double *divtot, double *divmax,
+                void *stream);
+/* chkdt (src/chkdt.f90:16): device reduction, synchronises `stream`.  dlmin is computed
+ * from dl and the device dzfi as the reference does. */
+int cans_chkdt(const int n[3], const double dl[3], const double *dzci, const double *dzfi,
+               double visc, double alpha, int is_impdiff, int is_impdiff_1d, const double *u,
+               const double *v, const double *w, double *dtmax, void *stream);
+/* bulk_mean (src/utils.f90:15): device FP64 reduction, synchronises `stream` */
+int cans_bulk_mean(const int n[3], const double *grid_vol_ratio, const double *p, double *mean,
+                   void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,31 @@
+"""Shared set-up for the -m gpu parity tests: build a case on the oracle and the library."""
+import numpy as np
+
+from oracle import oracle as O
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.linalg.norm(b.ravel())
+    return np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0)
+
+
+def is_bound_for(cbcpre):
+    return [1, 1] + [0 if cbcpre[2 * d:2 * d + 2] == "PP" else 1 for d in (1, 2) for _ in (0, 1)]
+
+
+def grid_for(n, l, cbc, gr):
+    zper = cbc[4:6] == "PP"
+    dzc, dzf, zc, zf = O.initgrid(1, n[2], 0.0 if zper else gr, l[2], zper)
+    return dzc, dzf, 1.0 / dzc, 1.0 / dzf
+
+
+def random_field(n, seed, zero_mean=False, dzf=None):
+    rng = np.random.default_rng(seed)
+    p = O.field(n)
+    p[1:-1, 1:-1, 1:-1] = rng.standard_normal(n)
+    if zero_mean:
+        wts = dzf[1:-1][None, None, :] * np.ones(n)
+        p[1:-1, 1:-1, 1:-1] -= (p[1:-1, 1:-1, 1:-1] * wts).sum() / wts.sum()
+    return p

@@ -1,0 +1,108 @@
+"""Poisson / Helmholtz solve on the GPU against the CPU oracle (FP64, rel. L2 <= 1e-12)."""
+import numpy as np
+import pytest
+
+from gpu_common import grid_for, is_bound_for, random_field, rel_l2
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12  # relative L2 on the Poisson solution (FP64 path)
+
+CASES = [
+    # (n, l, cbc, c_or_f, gr)
+    ((16, 12, 10), (1.0, 0.8, 2.0), "PPPPNN", "ccc", 1.4),     # channel-like
+    ((12, 10, 9), (1.3, 0.7, 2.0), "PPNNNN", "ccc", 1.2),      # duct-like
+    ((2, 64, 64), (0.03125, 1.0, 1.0), "PPNNNN", "ccc", 0.0),  # the lid-driven-cavity case
+    ((8, 6, 5), (1.0, 1.0, 1.0), "NNDDPP", "ccc", 0.0),        # periodic z (Sherman-Morrison)
+    ((16, 16, 16), (6.2831853, 6.2831853, 6.2831853), "PPPPPP", "ccc", 0.0),  # triperiodic
+    ((10, 14, 12), (1.0, 2.0, 1.5), "DDNNDD", "ccc", 1.1),
+    ((15, 9, 7), (1.0, 1.0, 1.0), "NNPPNN", "ccc", 0.0),       # odd sizes (radix 3, 5)
+    ((48, 80, 33), (1.0, 2.0, 2.0), "PPDDNN", "ccc", 1.4),     # mixed radix
+    ((112, 96, 40), (2.0, 2.0, 2.0), "NNNNNN", "ccc", 1.3),    # radix 7
+    ((12, 10, 9), (1.0, 1.0, 1.0), "NDDNNN", "ccc", 0.0),      # DCT-IV / DST-IV kinds
+    ((12, 10, 9), (1.0, 1.0, 1.0), "DDDDDD", "fcc", 1.2),      # face-centred DD in x (RODFT00, n-1)
+    ((12, 10, 9), (1.0, 1.0, 1.0), "DDDDDD", "cfc", 1.2),      # face-centred DD in y
+    ((12, 10, 9), (1.0, 1.0, 1.0), "DDDDDD", "ccf", 1.2),      # face-centred Dirichlet top in z
+    ((9, 10, 8), (1.0, 1.0, 1.0), "NNNNDD", "fcc", 0.0),       # face-centred NN (REDFT00)
+    ((64, 48, 32), (4.0, 2.0, 2.0), "PPPPNN", "ccc", 1.4),
+]
+
+
+def _solve_pair(n, l, cbc, c_or_f, gr, seed=1):
+    from cans_gb300 import cans
+    dl = [l[d] / n[d] for d in range(3)]
+    dli = [1 / x for x in dl]
+    dzc, dzf, dzci, dzfi = grid_for(n, l, cbc, gr)
+    ref = O.initsolver(n, dli, dzci, dzfi, cbc, [0.] * 6, c_or_f)
+    plan = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, c_or_f)
+    # set-up outputs identical to the oracle's initsolver
+    assert np.array_equal(plan.lambdaxy, ref["lambdaxy"])
+    assert np.array_equal(plan.a, ref["a"]) and np.array_equal(plan.b, ref["b"]) and np.array_equal(plan.c, ref["c"])
+    assert plan.normfft == ref["normfft"]
+    assert np.array_equal(plan.rhsb, ref["rhsb"])
+    p = random_field(n, seed, zero_mean="D" not in cbc, dzf=dzf)
+    d = cans.to_device(p)
+    O.solver(n, ref["normfft"], ref["lambdaxy"], ref["a"], ref["b"], ref["c"], cbc, c_or_f, p)
+    plan.solve(d)
+    return cans.fview(d), p, plan, ref
+
+
+@pytest.mark.parametrize("n,l,cbc,c_or_f,gr", CASES)
+def test_solver_matches_oracle(require_gpu, n, l, cbc, c_or_f, gr):
+    got, want, _, _ = _solve_pair(n, l, cbc, c_or_f, gr)
+    err = rel_l2(got[1:-1, 1:-1, 1:-1], want[1:-1, 1:-1, 1:-1])
+    assert err <= TOL, err
+    # ghost cells are not touched by the solve
+    assert np.array_equal(got[0], np.zeros_like(got[0])) and np.array_equal(got[:, :, -1], np.zeros_like(got[:, :, -1]))
+
+
+def test_solver_repeatable_and_linear(require_gpu):
+    """Same input -> same bits; solve(a*x + y) = a*solve(x) + solve(y) to rounding."""
+    from cans_gb300 import cans
+    n, l, cbc = (32, 24, 20), (2.0, 1.0, 2.0), "PPPPNN"
+    dl = [l[d] / n[d] for d in range(3)]
+    dzc, dzf, dzci, dzfi = grid_for(n, l, cbc, 1.4)
+    plan = cans.Plan(n, [1 / x for x in dl], dzci, dzfi, cbc, [0.] * 6, "ccc")
+    x = random_field(n, 3, True, dzf)
+    y = random_field(n, 4, True, dzf)
+    outs = []
+    for f in (x, x, y, 2.5 * x + y):
+        d = cans.to_device(f)
+        plan.solve(d)
+        outs.append(cans.fview(d))
+    assert np.array_equal(outs[0], outs[1])
+    assert rel_l2(outs[3], 2.5 * outs[0] + outs[2]) < 1e-13
+
+
+@pytest.mark.parametrize("cbc,c_or_f", [("PPNNNN", "ccc"), ("DDDDDD", "fcc"), ("DDDDDD", "ccf"), ("PPDDDD", "cfc")])
+def test_helmholtz_matches_oracle(require_gpu, cbc, c_or_f):
+    """solve_helmholtz (src/solve_helmholtz.f90:28) incl. the boundary RHS and alpha cache."""
+    from cans_gb300 import cans
+    n, l = (12, 10, 14), (1.0, 1.0, 1.0)
+    dl = [l[d] / n[d] for d in range(3)]
+    dli = [1 / x for x in dl]
+    dzc, dzf, dzci, dzfi = grid_for(n, l, cbc, 1.2)
+    bc = [0.3, -0.2, 0.5, 1.0, -0.7, 0.25]
+    ref = O.initsolver(n, dli, dzci, dzfi, cbc, bc, c_or_f)
+    plan = cans.Plan(n, dli, dzci, dzfi, cbc, bc, c_or_f)
+    is_bound = is_bound_for(cbc)
+    for alpha in (-0.013, -0.021, -0.013):
+        p = random_field(n, 7)
+        d = cans.to_device(p)
+        O.solve_helmholtz(n, ref["normfft"], alpha, ref["lambdaxy"], ref["a"], ref["b"], ref["c"], ref["rhsb"],
+                          is_bound, cbc, c_or_f, p)
+        plan.solve_helmholtz(alpha, is_bound, d)
+        got = cans.fview(d)
+        assert rel_l2(got[1:-1, 1:-1, 1:-1], p[1:-1, 1:-1, 1:-1]) <= TOL
+
+
+def test_invalid_arguments_raise(require_gpu):
+    from cans_gb300 import cans
+    n = (8, 8, 8)
+    dzc, dzf, dzci, dzfi = grid_for(n, (1, 1, 1), "PPPPNN", 0.0)
+    with pytest.raises(cans.CansError) as e:
+        cans.Plan(n, [8, 8, 8], dzci, dzfi, "PXPPNN", [0.] * 6, "ccc")
+    assert e.value.status == cans.EINVAL
+    with pytest.raises(cans.CansError) as e:
+        cans.Plan((11, 8, 8), [8, 8, 8], dzci, dzfi, "PPPPNN", [0.] * 6, "ccc")  # length 11: prime radix
+    assert e.value.status == cans.ENOTSUP
