@@ -30,6 +30,12 @@ struct DirParams {
   const void *pre;   // T2[nt] exp(-i pi j/(2n)) (kinds 11)
 };
 
+// FFT sign a kind is defined with: the "backward" kinds (HC2R, REDFT01, RODFT01) use
+// exp(+i...), every other kind exp(-i...) -- whichever pass (forward/backward) uses it
+__host__ __device__ __forceinline__ int kind_sign(int kind) {
+  return (kind == K_HC2R || kind == K_REDFT01 || kind == K_RODFT01) ? +1 : -1;
+}
+
 // ---------------------------------------------------------------------------------- DFT_R
 template <int R> struct RootTab;  // cos/sin(2 pi e / R), e = 0..R-1
 template <> struct RootTab<3> {

@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(256) k_xfwd(const TF *__restrict__ p, T *__res
   __syncthreads();
   r2r_pre<T>(P, stg, A);
   __syncthreads();
-  const T2 *Z = fft_lines<-1>(A, B, P);
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_lines<+1>(A, B, P) : fft_lines<-1>(A, B, P);
   T *Sk = S + (size_t)k * n1 * n2;
   for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
     const int i = e / lpb, r = e - i * lpb, j = j0 + r;
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(256) k_xfwd(const TF *__restrict__ p, T *__res
 }
 
 // 2./4. y pass, in place on contiguous lines S[l*n2 .. l*n2+n2-1], l = k*n1 + i
-template <typename T, int SIGN>
+template <typename T>
 __global__ void __launch_bounds__(256) k_ylines(T *__restrict__ S, long nlines, int n2, DirParams P) {
   using T2 = cplx_t<T>;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(256) k_ylines(T *__restrict__ S, long nlines, 
   __syncthreads();
   r2r_pre<T>(P, stg, A);
   __syncthreads();
-  const T2 *Z = fft_lines<SIGN>(A, B, P);
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_lines<+1>(A, B, P) : fft_lines<-1>(A, B, P);
   for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
     const int r = e / nt, j = e - r * nt;
     if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T>(P, Z, r, j);
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__res
   __syncthreads();
   r2r_pre<T>(P, stg, A);
   __syncthreads();
-  const T2 *Z = fft_lines<+1>(A, B, P);
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_lines<+1>(A, B, P) : fft_lines<-1>(A, B, P);
   for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
     const int r = e / n1, i = e - r * n1, j = j0 + r;
     if (j >= n2) continue;
@@ -359,26 +359,40 @@ __global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__res
 // z factorisation per spectral column (src/solver.f90:114-307 with the RHS-independent
 // part hoisted): zinv_k = 1/den_k (0 where the singular mode is pinned), dd_k = c_k/den_k;
 // periodic z: the auxiliary Sherman-Morrison solution p2 and the closure denominator.
+// Every operation that feeds the pivot test is rounded exactly as the reference's
+// (no FMA contraction: __dadd_rn/__dmul_rn are never fused), so the singular zero
+// mode is pinned in exactly the columns where the reference pins it.
+__device__ __forceinline__ double uadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double usub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double umul(double a, double b) { return __dmul_rn(a, b); }
+
+// `sing`: the z operator of this Poisson plan is singular for lambda_xy == 0 (Neumann or
+// periodic at both z ends).  The reference's relative pivot test alone misses that column
+// on stretched grids (|den| of a few 1e-11 against a tolerance of a few 1e-11 at 512 rows);
+// pinning it whenever lambda_xy is exactly zero keeps every column the reference pins
+// pinned and fixes the gauge of the others to the reference's intended p_hat(0,0,nn) = 0.
 __global__ void k_zfactor(const double *__restrict__ lamcol, const double *__restrict__ a,
                           const double *__restrict__ b, const double *__restrict__ c, long ncol, int nn,
-                          int zper, double *__restrict__ zinv, double *__restrict__ dd, double *__restrict__ p2,
-                          double *__restrict__ dcl) {
+                          int zper, int sing, double *__restrict__ zinv, double *__restrict__ dd,
+                          double *__restrict__ p2, double *__restrict__ dcl) {
   const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   const double lam = lamcol[col];
-  double z = 1. / (b[0] + lam);
-  double dprev = c[0] * z;
+  const bool structural = sing && lam == 0.;
+  double z = 1. / uadd(b[0], lam);
+  double dprev = umul(c[0], z);
   zinv[col] = z;
   dd[col] = dprev;
   for (int k = 1; k < nn; k++) {
-    const double den = b[k] + lam - a[k] * dprev;
-    const double pt = DBL_EPSILON * fmax(fabs(b[k] + lam), fabs(a[k] * dprev));
+    const double bl = uadd(b[k], lam), ad = umul(a[k], dprev);
+    const double den = usub(bl, ad);
+    const double pt = umul(DBL_EPSILON, fmax(fabs(bl), fabs(ad)));
     const size_t idx = (size_t)k * ncol + col;
-    if (k == nn - 1 && fabs(den) <= pt) {
+    if (k == nn - 1 && (fabs(den) <= pt || (structural && !zper))) {
       zinv[idx] = 0.; dd[idx] = 0.; dprev = 0.;
     } else {
       z = 1. / den;
-      dprev = c[k] * z;
+      dprev = umul(c[k], z);
       zinv[idx] = z; dd[idx] = dprev;
     }
   }
@@ -388,23 +402,23 @@ __global__ void k_zfactor(const double *__restrict__ lamcol, const double *__res
   for (int k = 0; k < nn; k++) {
     double r = 0.;
     if (k == 0) r = -a[0];
-    if (k == nn - 1) r = r - c[nn - 1];
-    const double zz = 1. / (k == 0 ? b[0] + lam : b[k] + lam - a[k] * dq);
-    dq = c[k] * zz;
-    y = (k == 0) ? r * zz : (r - a[k] * y) * zz;
+    if (k == nn - 1) r = usub(r, c[nn - 1]);
+    const double zz = 1. / (k == 0 ? uadd(b[0], lam) : usub(uadd(b[k], lam), umul(a[k], dq)));
+    dq = umul(c[k], zz);
+    y = (k == 0) ? umul(r, zz) : umul(usub(r, umul(a[k], y)), zz);
     p2[(size_t)k * ncol + col] = y;
   }
   for (int k = nn - 2; k >= 0; k--) {
     const size_t idx = (size_t)k * ncol + col;
-    // recompute d_k of the auxiliary recursion = dd unless the main one was pinned at nn-1
-    const double dk = dd[idx];
-    y = p2[idx] - dk * y;
+    // d_k of the auxiliary recursion equals dd_k for k < nn-1 (pinning only touches nn-1)
+    y = usub(p2[idx], umul(dd[idx], y));
     p2[idx] = y;
   }
   const double q1 = p2[col], qn = p2[(size_t)(nn - 1) * ncol + col];
-  const double den = b[nn] + lam + c[nn] * q1 + a[nn] * qn;
-  const double pt = DBL_EPSILON * fmax(fabs(b[nn] + lam), fabs(c[nn] * q1 + a[nn] * qn));
-  dcl[col] = fabs(den) <= pt ? 0. : den;
+  const double bl = uadd(b[nn], lam), cq = umul(c[nn], q1), aq = umul(a[nn], qn);
+  const double den = uadd(uadd(bl, cq), aq);
+  const double pt = umul(DBL_EPSILON, fmax(fabs(bl), fabs(uadd(cq, aq))));
+  dcl[col] = (fabs(den) <= pt || structural) ? 0. : den;
 }
 
 // z solve, FP64 spectral data, in place
@@ -555,9 +569,11 @@ static int get_factor(cans_plan *P, double key, bool helm, Factor **out) {
     b = P->bb_d;
   }
   const int tpb = 128;
+  // the Poisson operator is singular for lambda_xy = 0 when z is periodic or Neumann at both ends
+  const bool zsing = !helm && (P->zper || (P->cbc[4] == 'N' && P->cbc[5] == 'N'));
   k_zfactor<<<(unsigned)((ncol + tpb - 1) / tpb), tpb, 0, P->stream>>>(P->lamcol, P->a_d, b, P->c_d, ncol, nn,
-                                                                       P->zper, slot->zinv, slot->dd, slot->p2,
-                                                                       slot->dcl);
+                                                                       P->zper, zsing ? 1 : 0, slot->zinv, slot->dd,
+                                                                       slot->p2, slot->dcl);
   CANS_LAUNCH_CHECK();
   slot->key = key;
   slot->valid = true;
@@ -596,15 +612,9 @@ template <typename T> static int launch_y(cans_plan *P, int fwd) {
   const size_t sm = smem_bytes<T>(q);
   const long nlines = (long)P->n[0] * P->n[2];
   const unsigned grid = (unsigned)((nlines + q.lpb - 1) / q.lpb);
-  if (fwd) {
-    int rc = set_smem<T>((const void *)k_ylines<T, -1>, sm);
-    if (rc) return rc;
-    k_ylines<T, -1><<<grid, 256, sm, P->stream>>>((T *)P->S, nlines, P->n[1], q);
-  } else {
-    int rc = set_smem<T>((const void *)k_ylines<T, +1>, sm);
-    if (rc) return rc;
-    k_ylines<T, +1><<<grid, 256, sm, P->stream>>>((T *)P->S, nlines, P->n[1], q);
-  }
+  int rc = set_smem<T>((const void *)k_ylines<T>, sm);
+  if (rc) return rc;
+  k_ylines<T><<<grid, 256, sm, P->stream>>>((T *)P->S, nlines, P->n[1], q);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }

@@ -29,3 +29,20 @@ def random_field(n, seed, zero_mean=False, dzf=None):
         wts = dzf[1:-1][None, None, :] * np.ones(n)
         p[1:-1, 1:-1, 1:-1] -= (p[1:-1, 1:-1, 1:-1] * wts).sum() / wts.sum()
     return p
+
+
+def singular(cbc, c_or_f="ccc"):
+    """True when the discrete Poisson operator has the constant null mode (no Dirichlet side)."""
+    return "D" not in cbc
+
+
+def demean(f, dzf):
+    """subtract the cell-volume-weighted mean (dz-weighted; x, y uniform) of an interior array"""
+    w = np.asarray(dzf)[1:-1][None, None, :] * np.ones(f.shape)
+    return f - (f * w).sum() / w.sum()
+
+
+def gauge_rel_l2(got, want, dzf):
+    """relative L2 after removing each field's mean: the comparison that is independent of the
+    additive constant of a singular (all Neumann/periodic) Poisson problem"""
+    return rel_l2(demean(got, dzf), demean(want, dzf))

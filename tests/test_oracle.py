@@ -145,3 +145,21 @@ def test_lid_driven_cavity_golden():
     prof = r.v[1, n[1] // 2 + 1, 1:n[2] + 1]
     np.testing.assert_allclose(r.grid()["zc"][1:n[2] + 1], ref[:, 0], rtol=1e-7)
     np.testing.assert_allclose(prof, ref[:, 1], rtol=1e-7, atol=0)
+
+
+def test_reference_pivot_rule_misses_stretched_zero_mode():
+    """Documents a property of the reference's pin (src/solver.f90:137-147): on the 512-row
+    tanh grid (gr = 1.4) of the channel case the last pivot of the lambda = 0 column is
+    |den| = O(1e-11) above its tolerance eps*max(|b+lam|,|a*d|), so the constant pressure mode
+    is not pinned and its value is set by rounding."""
+    dzc, dzf, zc, zf = O.initgrid(1, 512, 1.4, 2.0, False)
+    a, b, c = O.tridmatrix("NN", 512, 1 / dzc, 1 / dzf, "c")
+    d = c[0] / b[0]
+    for k in range(1, 512):
+        bl, ad = b[k], a[k] * d
+        den = bl - ad
+        if k < 511:
+            d = c[k] / den
+    pt = np.finfo(float).eps * max(abs(bl), abs(ad))
+    assert abs(den) > pt  # not pinned by the reference's test
+    assert abs(den) < 1e-9 * abs(bl)  # yet numerically singular
