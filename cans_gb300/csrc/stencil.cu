@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <cfloat>
+#include <mutex>
 #include <vector>
 
 #include "cans_internal.cuh"
@@ -566,6 +567,58 @@ extern "C" int cans_chkdiv(const int n[3], const double l[3], const double dli[3
   int rc = red_scratch(2 * (size_t)nblk + 4, &s);
   if (rc) return rc;
   k_chkdiv<<<nblk, kTB, 0, st>>>(d, dli[0], dli[1], dzfi, u, v, w, s, s + nblk);
+  CANS_LAUNCH_CHECK();
+  k_sum_partials<<<1, kTB, 0, st>>>(s, nblk, 1, 1, s + 2 * nblk);
+  CANS_LAUNCH_CHECK();
+  k_max_partials<<<1, kTB, 0, st>>>(s + nblk, nblk, s + 2 * nblk + 1);
+  CANS_LAUNCH_CHECK();
+  double h[2];
+  CANS_CUDA_TRY(cudaMemcpyAsync(h, s + 2 * nblk, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaStreamSynchronize(st));
+  *divtot = h[0] / (l[0] * l[1] * l[2]);
+  *divmax = h[1];
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ chkdiv, no allocation
+// Variant of cans_chkdiv for callers that must not allocate device memory.  Its scratch (the
+// per-block partial sums and maxima plus the two final values) is a fixed file-scope device
+// array, sized for at most kNoAllocMaxBlocks blocks of kTB threads.  Host code cannot use the
+// array's name as a device address, so its address is looked up with cudaGetSymbolAddress once
+// per device, on the first call made with that device current, and cached.
+namespace {
+constexpr long kNoAllocMaxBlocks = 65536;  // 65536 x 256 = 16,777,216 interior cells
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[kNoAllocMaxDevices] = {};
+}  // namespace
+static __device__ __align__(256) double g_chkdiv_scratch[2 * kNoAllocMaxBlocks + 8];
+
+extern "C" int cans_chkdiv_noalloc(const int n[3], const double l[3], const double dli[3], const double *dzfi,
+                                   const double *u, const double *v, const double *w, double *divtot,
+                                   double *divmax, void *stream) {
+  if (!n || !l || !dli || !dzfi || !u || !v || !w || !divtot || !divmax) return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  const long np = (long)n[0] * n[1] * n[2];
+  const long nblk = (np + kTB - 1) / kTB;
+  if (nblk > kNoAllocMaxBlocks) return CANS_EINVAL;  // beyond the fixed scratch: rejected, nothing launched
+  int dev = 0;
+  CANS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return CANS_EINVAL;
+  double *s = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void *ptr = nullptr;
+      CANS_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_chkdiv_scratch));
+      g_noalloc_addr[dev] = static_cast<double *>(ptr);
+    }
+    s = g_noalloc_addr[dev];
+  }
+  // every slot read below is written earlier in this call, so nothing needs clearing
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  k_chkdiv<<<(unsigned)nblk, kTB, 0, st>>>(d, dli[0], dli[1], dzfi, u, v, w, s, s + nblk);
   CANS_LAUNCH_CHECK();
   k_sum_partials<<<1, kTB, 0, st>>>(s, nblk, 1, 1, s + 2 * nblk);
   CANS_LAUNCH_CHECK();

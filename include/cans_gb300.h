@@ -135,6 +135,22 @@ int cans_updt_rhs_b(const char c_or_f[3], const char cbc[6], const int n[3], con
 int cans_chkdiv(const int n[3], const double l[3], const double dli[3], const double *dzfi,
                 const double *u, const double *v, const double *w, double *divtot, double *divmax,
                 void *stream);
+/* Divergence check that allocates nothing.  No counterpart in the reference: it is
+ * cans_chkdiv with its scratch moved into a fixed device array inside the library, for
+ * callers that cannot call cudaMalloc -- e.g. a host whose device memory is owned by the
+ * OpenACC runtime's pool, a host that is capturing the stream into a CUDA graph (cudaMalloc
+ * is not allowed during capture), or a long run that fixes its memory budget up front.
+ * Limit: n1*n2*n3 <= 16,777,216 interior cells (65,536 blocks of 256 threads); larger sizes
+ * return CANS_EINVAL and launch nothing.  The array (1 MiB) is held on every device that
+ * loads the library until the process exits.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the one array and it keeps the last
+ * call's contents (each call writes every slot it reads), so calls that overlap on the GPU
+ * (different streams or host threads at the same time) race: serialise them.  Results,
+ * arguments and the stream synchronisation are those of cans_chkdiv. */
+int cans_chkdiv_noalloc(const int n[3], const double l[3], const double dli[3], const double *dzfi,
+                        const double *u, const double *v, const double *w, double *divtot,
+                        double *divmax, void *stream);
 /* chkdt (src/chkdt.f90:16): device reduction, synchronises `stream`.  dlmin is computed
  * from dl and the device dzfi as the reference does. */
 int cans_chkdt(const int n[3], const double dl[3], const double *dzci, const double *dzfi,
