@@ -227,7 +227,9 @@ struct cans_plan {
   double *a_d = nullptr, *b_d = nullptr, *c_d = nullptr, *bb_d = nullptr;
   void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)
   double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
-  float *R32 = nullptr;
+  float *R32 = nullptr;        // refinement: FP32 haloed residual / correction field
+  double *rhs64 = nullptr;     // refinement: FP64 copy of the right-hand side
+  double *rpart = nullptr;     // refinement: per-block partial norms
   Factor fac[4];
   unsigned long long clock = 0;
   long long bytes = 0;
@@ -328,7 +330,8 @@ __global__ void __launch_bounds__(256) k_ylines(T *__restrict__ S, long nlines, 
 
 // 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k)
 template <typename T, typename TF>
-__global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2, DirParams P) {
+__global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2, DirParams P,
+                                              int acc) {
   using T2 = cplx_t<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   T2 *A = reinterpret_cast<T2 *>(smem);
@@ -352,7 +355,9 @@ __global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__res
   for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
     const int r = e / n1, i = e - r * n1, j = j0 + r;
     if (j >= n2) continue;
-    p[hidx(i + 1, j + 1, k + 1, n1, n2)] = (TF)((i < nt) ? r2r_post<T>(P, Z, r, i) : pass[r]);
+    const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+    const T val = (i < nt) ? r2r_post<T>(P, Z, r, i) : pass[r];
+    p[idx] = acc ? (TF)(p[idx] + (TF)val) : (TF)val;
   }
 }
 
@@ -529,7 +534,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
   cudaFree(P->lamcol); cudaFree(P->a_d); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
-  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red);
+  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->rhs64); cudaFree(P->rpart);
   for (auto &e : P->ev) cudaEventDestroy(e);
   delete P;
   return CANS_OK;
@@ -597,13 +602,13 @@ template <typename T, typename TF> static int launch_xfwd(cans_plan *P, const TF
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
-template <typename T, typename TF> static int launch_xbwd(cans_plan *P, TF *p) {
+template <typename T, typename TF> static int launch_xbwd(cans_plan *P, TF *p, int acc = 0) {
   DirParams q = make_params<T>(P, 0, 0);
   const size_t sm = smem_bytes<T>(q);
   int rc = set_smem<T>((const void *)k_xbwd<T, TF>, sm);
   if (rc) return rc;
   dim3 grid((P->n[1] + q.lpb - 1) / q.lpb, P->n[2]);
-  k_xbwd<T, TF><<<grid, 256, sm, P->stream>>>((const T *)P->S, p, P->n[0], P->n[1], q);
+  k_xbwd<T, TF><<<grid, 256, sm, P->stream>>>((const T *)P->S, p, P->n[0], P->n[1], q, acc);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
@@ -838,4 +843,50 @@ extern "C" int cans_solve_helmholtz(cans_plan *P, double alpha, const int is_bou
   const double alphai = 1. / alpha;
   if (P->precision != CANS_FP64) return solve_impl<float, double>(P, p, alphai, true, P->normfft * alphai);
   return solve_impl<double, double>(P, p, alphai, true, P->normfft * alphai);
+}
+
+// ------------------------------------------------------------------ refinement support
+int cans_plan_refine_buffers(cans_plan *P, double **rhs64, float **e32, double **partials, int *n, char *cbc,
+                             char *c_or_f, const double **a, const double **b, const double **c, cudaStream_t *st) {
+  if (P->precision != CANS_FP32) return CANS_EINVAL;
+  const size_t np = (size_t)P->n[0] * P->n[1] * P->n[2];
+  const size_t nh = (size_t)(P->n[0] + 2) * (P->n[1] + 2) * (P->n[2] + 2);
+  const size_t nblk = (np + 255) / 256;
+  if (!P->rhs64) {
+    CANS_CUDA_TRY(cudaMalloc(&P->rhs64, np * sizeof(double)));
+    CANS_CUDA_TRY(cudaMalloc(&P->R32, nh * sizeof(float)));
+    CANS_CUDA_TRY(cudaMemsetAsync(P->R32, 0, nh * sizeof(float), P->stream));
+    CANS_CUDA_TRY(cudaMalloc(&P->rpart, (2 * nblk + 8) * sizeof(double)));
+    P->bytes += (long long)(np * sizeof(double) + nh * sizeof(float) + (2 * nblk + 8) * sizeof(double));
+  }
+  *rhs64 = P->rhs64;
+  *e32 = P->R32;
+  *partials = P->rpart;
+  for (int d = 0; d < 3; d++) n[d] = P->n[d];
+  memcpy(cbc, P->cbc, 6);
+  memcpy(c_or_f, P->c_or_f, 3);
+  *a = P->a_d; *b = P->b_d; *c = P->c_d;
+  *st = P->stream;
+  return CANS_OK;
+}
+
+// FP32 solve of the haloed FP32 field `in`; the result is written (accumulate = 0) or
+// added (accumulate = 1) to the interior of the haloed FP64 field `out`
+int cans_plan_solve_mixed(cans_plan *P, const float *in, double *out, int accumulate) {
+  if (P->precision != CANS_FP32) return CANS_EINVAL;
+  Factor *F = nullptr;
+  int rc;
+  if ((rc = get_factor(P, 0., false, &F))) return rc;
+  mark(P, 0);
+  if ((rc = launch_xfwd<float, float>(P, in))) return rc;
+  mark(P, 1);
+  if ((rc = launch_y<float>(P, 1))) return rc;
+  mark(P, 2);
+  if ((rc = launch_z(P, F, P->normfft, true))) return rc;
+  mark(P, 3);
+  if ((rc = launch_y<float>(P, 0))) return rc;
+  mark(P, 4);
+  if ((rc = launch_xbwd<float, double>(P, out, accumulate))) return rc;
+  mark(P, 5);
+  return CANS_OK;
 }

@@ -1,0 +1,77 @@
+"""FP32 transforms + FP64 refinement against the FP64 oracle (the benchmark spec precision form)."""
+import numpy as np
+import pytest
+
+from gpu_common import gauge_rel_l2, grid_for, random_field, rel_l2, singular
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ((64, 48, 32), (4.0, 2.0, 2.0), "PPPPNN", 1.4),
+    ((32, 40, 24), (1.0, 2.0, 1.0), "PPNNNN", 1.2),
+    ((30, 20, 16), (1.0, 1.0, 1.0), "DDNNDD", 1.1),
+    ((16, 16, 16), (6.2831853, 6.2831853, 6.2831853), "PPPPPP", 0.0),
+    ((24, 16, 20), (1.0, 1.0, 2.0), "NNDDNN", 1.3),
+]
+
+
+def _setup(n, l, cbc, gr, seed=2):
+    from cans_gb300 import cans
+    dl = [l[d] / n[d] for d in range(3)]
+    dli = [1 / x for x in dl]
+    dzc, dzf, dzci, dzfi = grid_for(n, l, cbc, gr)
+    ref = O.initsolver(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc")
+    p = random_field(n, seed, zero_mean=singular(cbc), dzf=dzf)
+    want = p.copy()
+    O.solver(n, ref["normfft"], ref["lambdaxy"], ref["a"], ref["b"], ref["c"], cbc, "ccc", want)
+    return dl, dli, dzc, dzf, dzci, dzfi, p, want
+
+
+@pytest.mark.parametrize("n,l,cbc,gr", CASES)
+def test_fp32_solve_is_fp32_accurate(require_gpu, n, l, cbc, gr):
+    import torch
+    from cans_gb300 import cans
+    dl, dli, dzc, dzf, dzci, dzfi, p, want = _setup(n, l, cbc, gr)
+    plan = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc", precision=cans.FP32)
+    d = cans.to_device(p, dtype=torch.float32)
+    plan.solve(d)
+    got = cans.fview(d).astype(np.float64)[1:-1, 1:-1, 1:-1]
+    w = want[1:-1, 1:-1, 1:-1]
+    err = gauge_rel_l2(got, w, dzf) if singular(cbc) else rel_l2(got, w)
+    assert err < 1e-4, err
+
+
+@pytest.mark.parametrize("n,l,cbc,gr", CASES)
+def test_refined_reaches_fp64_accuracy(require_gpu, n, l, cbc, gr):
+    import torch
+    from cans_gb300 import cans
+    dl, dli, dzc, dzf, dzci, dzfi, p, want = _setup(n, l, cbc, gr)
+    plan = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc", precision=cans.FP32)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
+    d = cans.to_device(p)
+    it, rr = plan.solve_refined(d, dli, T(dzci), T(dzfi), rtol=1e-14, max_iter=8)
+    got = cans.fview(d)[1:-1, 1:-1, 1:-1]
+    w = want[1:-1, 1:-1, 1:-1]
+    err = gauge_rel_l2(got, w, dzf) if singular(cbc) else rel_l2(got, w)
+    assert err <= 1e-12, (err, it, rr)
+    assert it <= 4 and rr <= 1e-14, (it, rr)
+    # ghost cells untouched
+    g = cans.fview(d)
+    assert np.all(g[0] == 0) and np.all(g[:, :, -1] == 0)
+
+
+def test_refined_matches_fp64_gpu_path(require_gpu):
+    """Same RHS through the FP64 plan and the FP32+refinement plan: same gauge, 1e-12."""
+    import torch
+    from cans_gb300 import cans
+    n, l, cbc, gr = (64, 48, 40), (4.0, 2.0, 2.0), "PPPPNN", 1.4
+    dl, dli, dzc, dzf, dzci, dzfi, p, want = _setup(n, l, cbc, gr, seed=9)
+    p64 = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc")
+    p32 = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc", precision=cans.FP32)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
+    a, b = cans.to_device(p), cans.to_device(p)
+    p64.solve(a)
+    p32.solve_refined(b, dli, T(dzci), T(dzfi), rtol=1e-14, max_iter=8)
+    ga, gb = cans.fview(a)[1:-1, 1:-1, 1:-1], cans.fview(b)[1:-1, 1:-1, 1:-1]
+    assert rel_l2(gb, ga) <= 1e-12
