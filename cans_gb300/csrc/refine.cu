@@ -9,7 +9,7 @@
 // src/debug.f90:91-132.
 //
 //   x_0 = solve32(rhs)
-//   repeat:  r = rhs - L x      (FP64 arithmetic; relative residual reduced on the device)
+//   repeat:  r = rhs - L x      (FP64, flux form; relative residual reduced on the device)
 //            stop when ||r|| <= rtol ||rhs||
 //            x += solve32(r)    (FP32 transforms, FP64 z elimination; the update of x is
 //                                fused into the last transform pass)
@@ -22,7 +22,7 @@
 // solver.cu internals used here
 struct cans_plan;
 int cans_plan_refine_buffers(cans_plan *P, double **rhs64, float **e32, double **partials, int *n, char *cbc,
-                             char *c_or_f, const double **a, const double **b, const double **c, cudaStream_t *st);
+                             char *c_or_f, const double **a, const double **sres, const double **c, cudaStream_t *st);
 int cans_plan_solve_mixed(cans_plan *P, const float *in, double *out, int accumulate);
 
 namespace {
@@ -49,10 +49,16 @@ __global__ void __launch_bounds__(kTB) k_split_rhs(const double *__restrict__ p,
   e32[c] = (float)v;
 }
 
-// r = rhs - L x in FP64; r stored as FP32 in the haloed e32; per-block partial sums of r^2, rhs^2
+// r = rhs - L x in FP64 and in flux form: every second difference is formed from first
+// differences of x (x_nb - x_c), and the z diagonal b_k enters only through the exact residue
+// s_k = a_k + b_k + c_k of the reference's rounded coefficients (host-computed in extended
+// precision).  The plain form a x_{k-1} + b x_k + c x_{k+1} cancels terms of size |b| |x|
+// (|b| ~ 2.4e5 at the walls of a 512-row tanh grid), which caps refinement at ~cond*eps;
+// the flux form's rounding scales with |x_nb - x_c| instead.  r is stored as FP32 in the
+// haloed e32; per-block partial sums of r^2 and rhs^2 go to `part`.
 __global__ void __launch_bounds__(kTB) k_residual64(const double *__restrict__ x, const double *__restrict__ rhs64,
                                                     float *__restrict__ e32, const double *__restrict__ a,
-                                                    const double *__restrict__ b, const double *__restrict__ c,
+                                                    const double *__restrict__ sres, const double *__restrict__ c,
                                                     OpParams o, double *__restrict__ part) {
   __shared__ double red[2][kTB / 32];
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -63,17 +69,20 @@ __global__ void __launch_bounds__(kTB) k_residual64(const double *__restrict__ x
     const size_t sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
     const size_t cc = hidx(i, j, k, n1, n2);
     const double xc = x[cc];
-    const double xw = i > 1 ? x[cc - 1] : (o.gx0 == 0 ? x[cc + (n1 - 1)] : o.gx0 * xc);
-    const double xe = i < n1 ? x[cc + 1] : (o.gx1 == 0 ? x[cc - (n1 - 1)] : o.gx1 * xc);
-    const double xs = j > 1 ? x[cc - sy] : (o.gy0 == 0 ? x[cc + (size_t)(n2 - 1) * sy] : o.gy0 * xc);
-    const double xn = j < n2 ? x[cc + sy] : (o.gy1 == 0 ? x[cc - (size_t)(n2 - 1) * sy] : o.gy1 * xc);
+    // first differences toward each neighbour; ghost rule: periodic wrap, Neumann 0, Dirichlet -2 x_c
+    const double dw = i > 1 ? x[cc - 1] - xc : (o.gx0 == 0 ? x[cc + (n1 - 1)] - xc : (o.gx0 > 0 ? 0. : -2. * xc));
+    const double de = i < n1 ? x[cc + 1] - xc : (o.gx1 == 0 ? x[cc - (n1 - 1)] - xc : (o.gx1 > 0 ? 0. : -2. * xc));
+    const double ds = j > 1 ? x[cc - sy] - xc
+                            : (o.gy0 == 0 ? x[cc + (size_t)(n2 - 1) * sy] - xc : (o.gy0 > 0 ? 0. : -2. * xc));
+    const double dn = j < n2 ? x[cc + sy] - xc
+                             : (o.gy1 == 0 ? x[cc - (size_t)(n2 - 1) * sy] - xc : (o.gy1 > 0 ? 0. : -2. * xc));
     const int kk = k - 1;
-    double lz = b[kk] * xc;
-    if (k > 1) lz += a[kk] * x[cc - sz];
-    else if (o.zper) lz += a[kk] * x[cc + (size_t)(n3 - 1) * sz];
-    if (k < n3) lz += c[kk] * x[cc + sz];
-    else if (o.zper) lz += c[kk] * x[cc - (size_t)(n3 - 1) * sz];
-    const double lap = (xe - 2. * xc + xw) * o.cx + (xn - 2. * xc + xs) * o.cy + lz;
+    double lz = sres[kk] * xc;
+    if (k > 1) lz += a[kk] * (x[cc - sz] - xc);
+    else if (o.zper) lz += a[kk] * (x[cc + (size_t)(n3 - 1) * sz] - xc);
+    if (k < n3) lz += c[kk] * (x[cc + sz] - xc);
+    else if (o.zper) lz += c[kk] * (x[cc - (size_t)(n3 - 1) * sz] - xc);
+    const double lap = (de + dw) * o.cx + (dn + ds) * o.cy + lz;
     const double rhs = rhs64[t];
     const double r = rhs - lap;
     e32[cc] = (float)r;
@@ -118,9 +127,9 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   float *e32 = nullptr;
   int n[3];
   char cbc[6], cof[3];
-  const double *a, *b, *c;
+  const double *a, *sres, *c;
   cudaStream_t st;
-  int rc = cans_plan_refine_buffers(P, &rhs64, &e32, &part, n, cbc, cof, &a, &b, &c, &st);
+  int rc = cans_plan_refine_buffers(P, &rhs64, &e32, &part, n, cbc, cof, &a, &sres, &c, &st);
   if (rc) return rc;
   if (cof[0] != 'c' || cof[1] != 'c' || cof[2] != 'c') return CANS_ENOTSUP;
   OpParams o;
@@ -140,7 +149,7 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   double rel = 1.;
   double *sums = part + 2 * (size_t)nblk;
   for (;;) {
-    k_residual64<<<nblk, kTB, 0, st>>>(p, rhs64, e32, a, b, c, o, part);
+    k_residual64<<<nblk, kTB, 0, st>>>(p, rhs64, e32, a, sres, c, o, part);
     CANS_LAUNCH_CHECK();
     k_sum2<<<1, kTB, 0, st>>>(part, nblk, sums);
     CANS_LAUNCH_CHECK();

@@ -230,6 +230,7 @@ struct cans_plan {
   float *R32 = nullptr;        // refinement: FP32 haloed residual / correction field
   double *rhs64 = nullptr;     // refinement: FP64 copy of the right-hand side
   double *rpart = nullptr;     // refinement: per-block partial norms
+  double *sres = nullptr;      // refinement: exact residues a_k + b_k + c_k of the z rows
   Factor fac[4];
   unsigned long long clock = 0;
   long long bytes = 0;
@@ -534,7 +535,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
   cudaFree(P->lamcol); cudaFree(P->a_d); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
-  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->rhs64); cudaFree(P->rpart);
+  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->rhs64); cudaFree(P->rpart); cudaFree(P->sres);
   for (auto &e : P->ev) cudaEventDestroy(e);
   delete P;
   return CANS_OK;
@@ -847,7 +848,7 @@ extern "C" int cans_solve_helmholtz(cans_plan *P, double alpha, const int is_bou
 
 // ------------------------------------------------------------------ refinement support
 int cans_plan_refine_buffers(cans_plan *P, double **rhs64, float **e32, double **partials, int *n, char *cbc,
-                             char *c_or_f, const double **a, const double **b, const double **c, cudaStream_t *st) {
+                             char *c_or_f, const double **a, const double **sres, const double **c, cudaStream_t *st) {
   if (P->precision != CANS_FP32) return CANS_EINVAL;
   const size_t np = (size_t)P->n[0] * P->n[1] * P->n[2];
   const size_t nh = (size_t)(P->n[0] + 2) * (P->n[1] + 2) * (P->n[2] + 2);
@@ -857,7 +858,19 @@ int cans_plan_refine_buffers(cans_plan *P, double **rhs64, float **e32, double *
     CANS_CUDA_TRY(cudaMalloc(&P->R32, nh * sizeof(float)));
     CANS_CUDA_TRY(cudaMemsetAsync(P->R32, 0, nh * sizeof(float), P->stream));
     CANS_CUDA_TRY(cudaMalloc(&P->rpart, (2 * nblk + 8) * sizeof(double)));
-    P->bytes += (long long)(np * sizeof(double) + nh * sizeof(float) + (2 * nblk + 8) * sizeof(double));
+    // residue of each z row of the operator the solver inverts, exact in extended precision:
+    // interior rows a+b+c; wall rows without the absent neighbour's coefficient
+    const int n3 = P->n[2];
+    std::vector<double> sr(n3);
+    for (int k = 0; k < n3; k++) {
+      long double acc = (long double)P->b_h[k];
+      if (k > 0 || P->zper) acc += (long double)P->a_h[k];
+      if (k < n3 - 1 || P->zper) acc += (long double)P->c_h[k];
+      sr[k] = (double)acc;
+    }
+    CANS_CUDA_TRY(cudaMalloc(&P->sres, n3 * sizeof(double)));
+    CANS_CUDA_TRY(cudaMemcpy(P->sres, sr.data(), n3 * sizeof(double), cudaMemcpyHostToDevice));
+    P->bytes += (long long)(np * sizeof(double) + nh * sizeof(float) + (2 * nblk + 8 + n3) * sizeof(double));
   }
   *rhs64 = P->rhs64;
   *e32 = P->R32;
@@ -865,7 +878,7 @@ int cans_plan_refine_buffers(cans_plan *P, double **rhs64, float **e32, double *
   for (int d = 0; d < 3; d++) n[d] = P->n[d];
   memcpy(cbc, P->cbc, 6);
   memcpy(c_or_f, P->c_or_f, 3);
-  *a = P->a_d; *b = P->b_d; *c = P->c_d;
+  *a = P->a_d; *sres = P->sres; *c = P->c_d;
   *st = P->stream;
   return CANS_OK;
 }
