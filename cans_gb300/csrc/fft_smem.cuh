@@ -165,17 +165,69 @@ __device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P) {
   return src;
 }
 
+// ---------------------------------------------------------------- compile-time lengths
+// For power-of-two lengths the stage geometry is a compile-time constant: the butterfly and
+// output indices become shifts and masks instead of runtime divisions (which dominate the
+// instruction count of the generic path once the arithmetic is FP32).
+template <int R, int SIGN, int M, int NS, typename T2>
+__device__ __forceinline__ void fft_stage_ct(const T2 *__restrict__ src, T2 *__restrict__ dst, int nlines,
+                                             const T2 *__restrict__ tw) {
+  constexpr int NB = M / R, LD = M + 1, TWS = M / (NS * R);
+  const unsigned total = (unsigned)(NB * nlines);
+  for (unsigned b = threadIdx.x; b < total; b += blockDim.x) {
+    const unsigned line = b / NB, jb = b % NB;
+    const T2 *s = src + line * LD;
+    T2 *d = dst + line * LD;
+    const unsigned k = jb % NS;
+    T2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      v[r] = s[jb + r * NB];
+      if (NS > 1 && r > 0) {
+        T2 w = __ldg(&tw[r * k * TWS]);
+        if (SIGN > 0) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    dft<R, SIGN>(v);
+    const unsigned idxD = (jb / NS) * (NS * R) + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[idxD + r * NS] = v[r];
+  }
+}
+
+template <int M, int NS, int SIGN, typename T2>
+__device__ __forceinline__ T2 *fft_ct(T2 *src, T2 *dst, int nlines, const T2 *tw) {
+  if constexpr (NS >= M) {
+    return src;
+  } else {
+    constexpr int REM = M / NS;
+    constexpr int R = (REM % 8 == 0 && REM != 16) ? 8 : (REM % 4 == 0 ? 4 : 2);
+    fft_stage_ct<R, SIGN, M, NS>(src, dst, nlines, tw);
+    __syncthreads();
+    return fft_ct<M, NS * R, SIGN>(dst, src, nlines, tw);
+  }
+}
+
+// batched FFT: compile-time length M (power of two) or the generic runtime path (M == 0)
+template <int M, int SIGN, typename T2>
+__device__ __forceinline__ T2 *fft_any(T2 *A, T2 *B, const DirParams &P) {
+  if constexpr (M > 0) return fft_ct<M, 1, SIGN>(A, B, P.ncx, reinterpret_cast<const T2 *>(P.tw));
+  else return fft_lines<SIGN>(A, B, P);
+}
+
 // ------------------------------------------------------------------------ r2r pre-processing
 // staging: real line r at stg[r*sld + i], i < nt.  Fills the complex sequences A[q*ld + k], k < m.
-template <typename T>
-__device__ void r2r_pre(const DirParams &P, const T *__restrict__ stg, cplx_t<T> *__restrict__ A) {
+template <typename T, int M = 0>
+__device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict__ stg, cplx_t<T> *__restrict__ A) {
   using T2 = cplx_t<T>;
-  const int m = P.m, nt = P.nt, n = P.nt, sld = P.sld, ld = P.ld;
+  // with a compile-time M the kinds handled have nt == n == m (no extension)
+  const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? M + 1 : P.sld, ld = M ? M + 1 : P.ld;
   const T2 *tab = reinterpret_cast<const T2 *>(P.post);
   const T2 *pre = reinterpret_cast<const T2 *>(P.pre);
   const int total = P.ncx * m;
   for (int e = threadIdx.x; e < total; e += blockDim.x) {
-    const int q = e / m, k = e - q * m;
+    const int q = M ? (int)((unsigned)e / (unsigned)m) : e / m, k = e - q * m;
     const T *x0 = stg + (2 * q) * sld, *x1 = x0 + sld;
     T2 z;
     switch (P.kind) {
@@ -228,28 +280,28 @@ __device__ void r2r_pre(const DirParams &P, const T *__restrict__ stg, cplx_t<T>
 
 // ----------------------------------------------------------------------- r2r post-processing
 // value of output index k (< nt) of real line r from the FFT result Z
-template <typename T>
+template <typename T, int M = 0>
 __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__restrict__ Z, int r, int k) {
   using T2 = cplx_t<T>;
-  const int m = P.m, n = P.nt;
+  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? M + 1 : P.ld;
   const T2 *tab = reinterpret_cast<const T2 *>(P.post);
   if (!P.pairs) {  // kinds 11
-    const T2 z = Z[r * P.ld + k], w = tab[k];
+    const T2 z = Z[r * ldz + k], w = tab[k];
     const T re = w.x * z.x - w.y * z.y, im = w.x * z.y + w.y * z.x;
     return P.kind == K_REDFT11 ? T(2) * re : T(-2) * im;
   }
   const int q = r >> 1, wsel = r & 1;
-  const T2 *L = Z + q * P.ld;
+  const T2 *L = Z + q * ldz;
   switch (P.kind) {
     case K_R2HC: {
-      const T2 a = L[k], b = L[(m - k) % m];
+      const T2 a = L[k], b = L[M ? ((m - k) & (M - 1)) : ((m - k) % m)];
       if (2 * k <= n) return wsel == 0 ? T(0.5) * (a.x + b.x) : T(0.5) * (a.y + b.y);
       return wsel == 0 ? T(0.5) * (b.y - a.y) : T(0.5) * (a.x - b.x);
     }
     case K_REDFT10:
     case K_RODFT10: {
       const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
-      const T2 a = L[kk], b = L[(m - kk) % m], t = tab[kk];
+      const T2 a = L[kk], b = L[M ? ((m - kk) & (M - 1)) : ((m - kk) % m)], t = tab[kk];
       const T c = t.x, s = -t.y;
       return wsel == 0 ? c * (a.x + b.x) + s * (a.y - b.y) : c * (a.y + b.y) - s * (a.x - b.x);
     }

@@ -242,6 +242,16 @@ struct cans_plan {
 };
 static const int kPasses = 5, kTimedSolves = 256;
 
+// complex sequences per CTA: the largest power of two (<= 16) keeping the two FFT buffers
+// within 96 KB, so three CTAs fit an SM and the transposed x stores are >= 32-byte runs
+__host__ __device__ constexpr int ncx_for(int m, int cbytes) {
+  return (96 * 1024) / (2 * (m + 1) * cbytes) >= 16  ? 16
+         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 8 ? 8
+         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 4 ? 4
+         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 2 ? 2
+                                                      : 1;
+}
+
 template <typename T> DirParams make_params(const cans_plan *P, int d, int fwd) {
   DirParams q;
   memset(&q, 0, sizeof(q));
@@ -257,13 +267,16 @@ template <typename T> DirParams make_params(const cans_plan *P, int d, int fwd) 
   q.tw = P->tab[d].tw;
   q.post = P->tab[d].post;
   q.pre = P->tab[d].pre;
-  // complex sequences per CTA: keep the two FFT buffers near 96 KB
-  const size_t per = (size_t)q.ld * sizeof(cplx_t<T>) * 2;
-  int ncx = (int)std::max<size_t>(1, (96 * 1024) / per);
-  ncx = std::min(ncx, 16);
-  q.ncx = ncx;
-  q.lpb = q.pairs ? 2 * ncx : ncx;
+  q.ncx = ncx_for(q.m, (int)sizeof(cplx_t<T>));
+  q.lpb = q.pairs ? 2 * q.ncx : q.ncx;
   return q;
+}
+
+// compile-time length used for a pass (0 = generic runtime path): power-of-two lengths of
+// the kinds that transform all n points with no extension
+static int spec_len(const DirParams &q) {
+  const bool pow2 = q.m >= 32 && q.m <= 1024 && (q.m & (q.m - 1)) == 0;
+  return (pow2 && q.pairs && q.nt == q.m && q.n == q.nt) ? q.m : 0;
 }
 
 template <typename T> size_t smem_bytes(const DirParams &q) {
@@ -275,89 +288,107 @@ template <typename T> size_t smem_bytes(const DirParams &q) {
 // ====================================================================================
 // kernels
 // ====================================================================================
+// Geometry of a pass: compile-time when M > 0 (then nt == n == m and the kind is a "pairs"
+// kind), from DirParams otherwise.
+template <typename T, int M> struct PassGeo {
+  static constexpr int NCX = M ? ncx_for(M, (int)sizeof(cplx_t<T>)) : 0;
+  static constexpr int LPB = 2 * NCX;
+  static constexpr int LD = M + 1;
+};
+
 // 1. x-forward: haloed rows -> S[k][i][j]
-template <typename T, typename TF>
+template <typename T, typename TF, int M>
 __global__ void __launch_bounds__(256) k_xfwd(const TF *__restrict__ p, T *__restrict__ S, int n1, int n2, DirParams P) {
   using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
   extern __shared__ __align__(16) unsigned char smem[];
+  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
   T2 *A = reinterpret_cast<T2 *>(smem);
-  T2 *B = A + (size_t)P.ncx * P.ld;
+  T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
-  const size_t bbytes = std::max((size_t)P.ncx * P.ld * sizeof(T2), (size_t)P.lpb * P.sld * sizeof(T));
+  const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
+                                                                                      : (size_t)lpb * sld * sizeof(T);
   T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
-  const int k = blockIdx.y, j0 = blockIdx.x * P.lpb, lpb = P.lpb, nt = P.nt;
+  const int k = blockIdx.y, j0 = blockIdx.x * lpb;
   for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-    const int r = e / nt, i = e - r * nt, j = j0 + r;
-    stg[r * P.sld + i] = (j < n2) ? (T)p[hidx(i + 1, j + 1, k + 1, n1, n2)] : T(0);
+    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, i = e - r * nt, j = j0 + r;
+    stg[r * sld + i] = (j < n2) ? (T)p[hidx(i + 1, j + 1, k + 1, n1, n2)] : T(0);
   }
-  if (nt < n1)
+  if (!M && nt < n1)
     for (int r = threadIdx.x; r < lpb; r += blockDim.x)
       pass[r] = (j0 + r < n2) ? (T)p[hidx(n1, j0 + r + 1, k + 1, n1, n2)] : T(0);
   __syncthreads();
-  r2r_pre<T>(P, stg, A);
+  r2r_pre<T, M>(P, stg, A);
   __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_lines<+1>(A, B, P) : fft_lines<-1>(A, B, P);
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
   T *Sk = S + (size_t)k * n1 * n2;
   for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
-    const int i = e / lpb, r = e - i * lpb, j = j0 + r;
+    const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
     if (j >= n2) continue;
-    Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T>(P, Z, r, i) : pass[r];
+    Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M>(P, Z, r, i) : pass[r];
   }
 }
 
 // 2./4. y pass, in place on contiguous lines S[l*n2 .. l*n2+n2-1], l = k*n1 + i
-template <typename T>
+template <typename T, int M>
 __global__ void __launch_bounds__(256) k_ylines(T *__restrict__ S, long nlines, int n2, DirParams P) {
   using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
   extern __shared__ __align__(16) unsigned char smem[];
+  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
   T2 *A = reinterpret_cast<T2 *>(smem);
-  T2 *B = A + (size_t)P.ncx * P.ld;
+  T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
-  const long l0 = (long)blockIdx.x * P.lpb;
-  const int lpb = P.lpb, nt = P.nt;
+  const long l0 = (long)blockIdx.x * lpb;
   for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-    const int r = e / nt, j = e - r * nt;
-    stg[r * P.sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
+    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
+    stg[r * sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
   }
   __syncthreads();
-  r2r_pre<T>(P, stg, A);
+  r2r_pre<T, M>(P, stg, A);
   __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_lines<+1>(A, B, P) : fft_lines<-1>(A, B, P);
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
   for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-    const int r = e / nt, j = e - r * nt;
-    if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T>(P, Z, r, j);
+    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
+    if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M>(P, Z, r, j);
   }
 }
 
-// 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k)
-template <typename T, typename TF>
+// 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k) (written, or added when acc)
+template <typename T, typename TF, int M>
 __global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2, DirParams P,
                                               int acc) {
   using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
   extern __shared__ __align__(16) unsigned char smem[];
+  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
   T2 *A = reinterpret_cast<T2 *>(smem);
-  T2 *B = A + (size_t)P.ncx * P.ld;
+  T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
-  const size_t bbytes = std::max((size_t)P.ncx * P.ld * sizeof(T2), (size_t)P.lpb * P.sld * sizeof(T));
+  const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
+                                                                                      : (size_t)lpb * sld * sizeof(T);
   T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
-  const int k = blockIdx.y, j0 = blockIdx.x * P.lpb, lpb = P.lpb, nt = P.nt;
+  const int k = blockIdx.y, j0 = blockIdx.x * lpb;
   const T *Sk = S + (size_t)k * n1 * n2;
   for (int e = threadIdx.x; e < nt * lpb; e += blockDim.x) {
-    const int i = e / lpb, r = e - i * lpb, j = j0 + r;
-    stg[r * P.sld + i] = (j < n2) ? Sk[(size_t)i * n2 + j] : T(0);
+    const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
+    stg[r * sld + i] = (j < n2) ? Sk[(size_t)i * n2 + j] : T(0);
   }
-  if (nt < n1)
+  if (!M && nt < n1)
     for (int r = threadIdx.x; r < lpb; r += blockDim.x)
       pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
   __syncthreads();
-  r2r_pre<T>(P, stg, A);
+  r2r_pre<T, M>(P, stg, A);
   __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_lines<+1>(A, B, P) : fft_lines<-1>(A, B, P);
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
   for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
-    const int r = e / n1, i = e - r * n1, j = j0 + r;
+    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / n1, i = e - r * n1, j = j0 + r;
     if (j >= n2) continue;
     const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-    const T val = (i < nt) ? r2r_post<T>(P, Z, r, i) : pass[r];
+    const T val = (i < nt) ? r2r_post<T, M>(P, Z, r, i) : pass[r];
     p[idx] = acc ? (TF)(p[idx] + (TF)val) : (TF)val;
   }
 }
@@ -593,34 +624,64 @@ template <typename T> static int set_smem(const void *fn, size_t bytes) {
   return CANS_OK;
 }
 
+// run F.template operator()<M>() for the compile-time length of the pass (or M = 0)
+#define CANS_DISPATCH_M(mlen, CALL) \
+  switch (mlen) {                   \
+    case 32: CALL(32); break;       \
+    case 64: CALL(64); break;       \
+    case 128: CALL(128); break;     \
+    case 256: CALL(256); break;     \
+    case 512: CALL(512); break;     \
+    case 1024: CALL(1024); break;   \
+    default: CALL(0); break;        \
+  }
+
 template <typename T, typename TF> static int launch_xfwd(cans_plan *P, const TF *p) {
   DirParams q = make_params<T>(P, 0, 1);
   const size_t sm = smem_bytes<T>(q);
-  int rc = set_smem<T>((const void *)k_xfwd<T, TF>, sm);
-  if (rc) return rc;
+  const int M = spec_len(q);
   dim3 grid((P->n[1] + q.lpb - 1) / q.lpb, P->n[2]);
-  k_xfwd<T, TF><<<grid, 256, sm, P->stream>>>(p, (T *)P->S, P->n[0], P->n[1], q);
+  int rc = CANS_OK;
+#define CALL_XF(MM)                                                                        \
+  do {                                                                                     \
+    if ((rc = set_smem<T>((const void *)k_xfwd<T, TF, MM>, sm))) return rc;                \
+    k_xfwd<T, TF, MM><<<grid, 256, sm, P->stream>>>(p, (T *)P->S, P->n[0], P->n[1], q);    \
+  } while (0)
+  CANS_DISPATCH_M(M, CALL_XF)
+#undef CALL_XF
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
 template <typename T, typename TF> static int launch_xbwd(cans_plan *P, TF *p, int acc = 0) {
   DirParams q = make_params<T>(P, 0, 0);
   const size_t sm = smem_bytes<T>(q);
-  int rc = set_smem<T>((const void *)k_xbwd<T, TF>, sm);
-  if (rc) return rc;
+  const int M = spec_len(q);
   dim3 grid((P->n[1] + q.lpb - 1) / q.lpb, P->n[2]);
-  k_xbwd<T, TF><<<grid, 256, sm, P->stream>>>((const T *)P->S, p, P->n[0], P->n[1], q, acc);
+  int rc = CANS_OK;
+#define CALL_XB(MM)                                                                               \
+  do {                                                                                            \
+    if ((rc = set_smem<T>((const void *)k_xbwd<T, TF, MM>, sm))) return rc;                       \
+    k_xbwd<T, TF, MM><<<grid, 256, sm, P->stream>>>((const T *)P->S, p, P->n[0], P->n[1], q, acc); \
+  } while (0)
+  CANS_DISPATCH_M(M, CALL_XB)
+#undef CALL_XB
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
 template <typename T> static int launch_y(cans_plan *P, int fwd) {
   DirParams q = make_params<T>(P, 1, fwd);
   const size_t sm = smem_bytes<T>(q);
+  const int M = spec_len(q);
   const long nlines = (long)P->n[0] * P->n[2];
   const unsigned grid = (unsigned)((nlines + q.lpb - 1) / q.lpb);
-  int rc = set_smem<T>((const void *)k_ylines<T>, sm);
-  if (rc) return rc;
-  k_ylines<T><<<grid, 256, sm, P->stream>>>((T *)P->S, nlines, P->n[1], q);
+  int rc = CANS_OK;
+#define CALL_Y(MM)                                                                       \
+  do {                                                                                   \
+    if ((rc = set_smem<T>((const void *)k_ylines<T, MM>, sm))) return rc;                \
+    k_ylines<T, MM><<<grid, 256, sm, P->stream>>>((T *)P->S, nlines, P->n[1], q);        \
+  } while (0)
+  CANS_DISPATCH_M(M, CALL_Y)
+#undef CALL_Y
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
