@@ -126,6 +126,8 @@ def bench_ours(args, rank, world):
     dl = [L_CH[d] / n[d] for d in range(3)]
     dli = [1. / x for x in dl]
     dzc, dzf, zc, zf = initgrid(1, n[2], 1.4, L_CH[2], False)
+    if args.skip_fp64:  # profiling aid: only the FP32 + refinement leg
+        return {"fp32_refined": bench_refined(args, n, dli, dzc, dzf, None, None, dev, world)}
     plan = cans.Plan(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc")
     p = make_rhs(n, dzf, dev)
     ncell = n[0] * n[1] * n[2]
@@ -219,17 +221,20 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world):
     dzci, dzfi = T(1. / dzc), T(1. / dzf)
     rtol = args.rtol
     # accuracy at equal input: one fresh RHS through both paths
-    a = make_rhs(n, dzf, dev, seed=11)
-    b = a.clone()
-    plan64.solve(a)
-    it0, rr0 = plan.solve_refined(b, dli, dzci, dzfi, rtol=rtol, max_iter=8)
-    diff = (b - a)[1:-1, 1:-1, 1:-1]
-    ref = a[1:-1, 1:-1, 1:-1]
-    err = float(torch.linalg.vector_norm(diff) / torch.linalg.vector_norm(ref))
-    wz = torch.tensor(dzf[1:-1], device=dev, dtype=torch.float64)[:, None, None]
-    dm = lambda f: f - (f * wz).sum() / (wz.sum() * n[0] * n[1])
-    err_gauge = float(torch.linalg.vector_norm(dm(diff)) / torch.linalg.vector_norm(dm(ref)))
-    del a, b
+    err = err_gauge = None
+    it0 = rr0 = None
+    if plan64 is not None:
+        a = make_rhs(n, dzf, dev, seed=11)
+        b = a.clone()
+        plan64.solve(a)
+        it0, rr0 = plan.solve_refined(b, dli, dzci, dzfi, rtol=rtol, max_iter=8)
+        diff = (b - a)[1:-1, 1:-1, 1:-1]
+        ref = a[1:-1, 1:-1, 1:-1]
+        err = float(torch.linalg.vector_norm(diff) / torch.linalg.vector_norm(ref))
+        wz = torch.tensor(dzf[1:-1], device=dev, dtype=torch.float64)[:, None, None]
+        dm = lambda f: f - (f * wz).sum() / (wz.sum() * n[0] * n[1])
+        err_gauge = float(torch.linalg.vector_norm(dm(diff)) / torch.linalg.vector_norm(dm(ref)))
+        del a, b
     src = make_rhs(n, dzf, dev)
     p = src.clone()
     for _ in range(args.warmup):
@@ -329,6 +334,7 @@ def main():
     ap.add_argument("--skip-rk3", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-refine", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--rtol", type=float, default=1e-13)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

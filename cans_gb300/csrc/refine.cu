@@ -5,116 +5,205 @@
 // solver inverts (src/solver.f90:17-112 with src/initsolver.f90): second differences in x
 // and y with the homogeneous ghost rule of each boundary (periodic wrap, Neumann x0 = x1,
 // Dirichlet x0 = -x1, cell-centred) and the tridiagonal a, b, c of tridmatrix in z (the
-// ghost rule already folded into b at the walls) -- i.e. the 7-point operator of
+// ghost rule already folded into b at the walls) -- the 7-point operator of
 // src/debug.f90:91-132.
 //
-//   x_0 = solve32(rhs)
-//   repeat:  r = rhs - L x      (FP64, flux form; relative residual reduced on the device)
-//            stop when ||r|| <= rtol ||rhs||
-//            x += solve32(r)    (FP32 transforms, FP64 z elimination; the update of x is
-//                                fused into the last transform pass)
+// GB300 executes FP64 at 1/58 of its FP32 rate, while FP64<->FP32 conversions run at the
+// FP32 rate.  The refinement therefore keeps the residual on the FP32 pipes in double-float
+// arithmetic (value = hi + lo, two FP32 numbers, ~48-bit significand):
+//
+//   rhs -> (R, Rlo)             split of the FP64 right-hand side (one FP64 add per cell)
+//   e_0 = solve32(R)
+//   loop:  (R, Rlo) -= L e_k    double-float, in flux form: every second difference is built
+//                               from exact first differences of the FP32 values e_k, and the
+//                               z diagonal enters through the exact residue s = a + b + c
+//          x += e_k             FP64 (x lives in the caller's field)
+//          stop when ||R|| <= rtol ||rhs||
+//          e_{k+1} = solve32(R)
+//
+// The corrections e_k are exact FP32 numbers, so L e_k is evaluated without representation
+// error; the residual's rounding is relative to the flux terms (~2^-48 |a (e_nb - e_c)|), not
+// to |b| |x| as in a plain FP64 evaluation a x_{k-1} + b x_k + c x_{k+1}, whose cancellation
+// at the walls of a stretched grid (|b| ~ 2.4e5 at 512 rows) would cap the accuracy near
+// cond * eps.
 #include <math.h>
 
 #include <vector>
 
 #include "cans_internal.cuh"
 
+struct RefineBufs {
+  float *R;        // haloed FP32: residual, high part (input of the FP32 solve)
+  float *E;        // haloed FP32: correction (output of the FP32 solve)
+  float *Rlo;      // halo-free FP32: residual, low part
+  double *part;    // per-block partial norms
+  const float2 *a2, *c2, *s2;  // double-float z coefficients: a_k, c_k, residue s_k
+  int n[3];
+  char cbc[6], c_or_f[3];
+  cudaStream_t st;
+};
 // solver.cu internals used here
-struct cans_plan;
-int cans_plan_refine_buffers(cans_plan *P, double **rhs64, float **e32, double **partials, int *n, char *cbc,
-                             char *c_or_f, const double **a, const double **sres, const double **c, cudaStream_t *st);
-int cans_plan_solve_mixed(cans_plan *P, const float *in, double *out, int accumulate);
+int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b);
+int cans_plan_solve_f32io(cans_plan *P, const float *in, float *out);
 
 namespace {
 constexpr int kTB = 256;
 
+struct df {
+  float h, l;
+};
+// error-free transformations (Knuth two-sum, Dekker fast-two-sum, FMA two-product)
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df df_add(df x, df y) {
+  df s = two_sum(x.h, y.h);
+  const df t = two_sum(x.l, y.l);
+  s.l = __fadd_rn(s.l, t.h);
+  s = fast_two_sum(s.h, s.l);
+  s.l = __fadd_rn(s.l, t.l);
+  return fast_two_sum(s.h, s.l);
+}
+__device__ __forceinline__ df df_neg(df x) { return {-x.h, -x.l}; }
+__device__ __forceinline__ df df_mul(df x, df y) {
+  const float p = __fmul_rn(x.h, y.h);
+  float e = __fmaf_rn(x.h, y.h, -p);
+  e = __fmaf_rn(x.h, y.l, e);
+  e = __fmaf_rn(x.l, y.h, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df df_mul_f(df x, float y) {
+  const float p = __fmul_rn(x.h, y);
+  float e = __fmaf_rn(x.h, y, -p);
+  e = __fmaf_rn(x.l, y, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df dfv(float2 v) { return {v.x, v.y}; }
+
 struct OpParams {
   int n1, n2, n3;
-  double cx, cy;            // dxi^2, dyi^2
+  float2 cx, cy;            // dxi^2, dyi^2 as double-float
   int gx0, gx1, gy0, gy1;   // ghost rule: 0 periodic, +1 Neumann, -1 Dirichlet
   int zper;
 };
 
-__device__ __forceinline__ int ghost_rule(char b) { return b == 'P' ? 0 : (b == 'N' ? 1 : -1); }
-
-// copy the interior of the FP64 field into rhs64 (halo-free) and into the FP32 haloed field
-__global__ void __launch_bounds__(kTB) k_split_rhs(const double *__restrict__ p, double *__restrict__ rhs64,
-                                                   float *__restrict__ e32, int n1, int n2, int n3) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long)n1 * n2 * n3) return;
-  const int i = (int)(t % n1) + 1, j = (int)((t / n1) % n2) + 1, k = (int)(t / ((long)n1 * n2)) + 1;
-  const size_t c = hidx(i, j, k, n1, n2);
-  const double v = p[c];
-  rhs64[t] = v;
-  e32[c] = (float)v;
+// exact difference e_nb - e_c of two FP32 values; at a boundary the ghost rule applies:
+// periodic (enb is the wrapped value), Neumann (ghost = e_c: 0), Dirichlet (ghost = -e_c)
+__device__ __forceinline__ df diff_nb(bool inside, int rule, float enb, float ec) {
+  if (inside || rule == 0) return two_sum(enb, -ec);
+  if (rule > 0) return {0.f, 0.f};
+  return {-2.f * ec, 0.f};  // exact
 }
 
-// r = rhs - L x in FP64 and in flux form: every second difference is formed from first
-// differences of x (x_nb - x_c), and the z diagonal b_k enters only through the exact residue
-// s_k = a_k + b_k + c_k of the reference's rounded coefficients (host-computed in extended
-// precision).  The plain form a x_{k-1} + b x_k + c x_{k+1} cancels terms of size |b| |x|
-// (|b| ~ 2.4e5 at the walls of a 512-row tanh grid), which caps refinement at ~cond*eps;
-// the flux form's rounding scales with |x_nb - x_c| instead.  r is stored as FP32 in the
-// haloed e32; per-block partial sums of r^2 and rhs^2 go to `part`.
-__global__ void __launch_bounds__(kTB) k_residual64(const double *__restrict__ x, const double *__restrict__ rhs64,
-                                                    float *__restrict__ e32, const double *__restrict__ a,
-                                                    const double *__restrict__ sres, const double *__restrict__ c,
-                                                    OpParams o, double *__restrict__ part) {
-  __shared__ double red[2][kTB / 32];
+// block sum of a per-thread FP32 value: warp shuffles in FP32 (the FP64 pipe is 58x slower),
+// per-warp partials accumulated in FP64 by one thread
+__device__ __forceinline__ void block_reduce_to(float v, double *out) {
+  __shared__ float red[kTB / 32];
+  for (int s = 16; s > 0; s >>= 1) v += __shfl_down_sync(0xffffffffu, v, s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.;
+    for (int q = 0; q < kTB / 32; q++) a += (double)red[q];
+    *out = a;
+  }
+}
+
+// rhs (FP64, interior of p) -> (R hi, Rlo lo) and ||rhs||^2 partials
+__global__ void __launch_bounds__(kTB) k_split_df(const double *__restrict__ p, float *__restrict__ R,
+                                                  float *__restrict__ Rlo, int n1, int n2, int n3,
+                                                  double *__restrict__ part) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  float sq = 0.f;
+  if (t < (long)n1 * n2 * n3) {
+    const int i = (int)(t % n1) + 1, j = (int)((t / n1) % n2) + 1, k = (int)(t / ((long)n1 * n2)) + 1;
+    const size_t c = hidx(i, j, k, n1, n2);
+    const double v = p[c];
+    const float hi = __double2float_rn(v);
+    R[c] = hi;
+    Rlo[t] = __double2float_rn(v - (double)hi);
+    sq = hi * hi;
+  }
+  block_reduce_to(sq, &part[blockIdx.x]);
+}
+
+// (R, Rlo) -= L e ;  x += e (x = e when first) ;  ||R||^2 partials
+__global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, float *__restrict__ R,
+                                               float *__restrict__ Rlo, double *__restrict__ x, int first,
+                                               const float2 *__restrict__ a2, const float2 *__restrict__ c2,
+                                               const float2 *__restrict__ s2, OpParams o,
+                                               double *__restrict__ part) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int n1 = o.n1, n2 = o.n2, n3 = o.n3;
-  double rr = 0., bb = 0.;
+  float sq = 0.f;
   if (t < (long)n1 * n2 * n3) {
     const int i = (int)(t % n1) + 1, j = (int)((t / n1) % n2) + 1, k = (int)(t / ((long)n1 * n2)) + 1;
     const size_t sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
     const size_t cc = hidx(i, j, k, n1, n2);
-    const double xc = x[cc];
-    // first differences toward each neighbour; ghost rule: periodic wrap, Neumann 0, Dirichlet -2 x_c
-    const double dw = i > 1 ? x[cc - 1] - xc : (o.gx0 == 0 ? x[cc + (n1 - 1)] - xc : (o.gx0 > 0 ? 0. : -2. * xc));
-    const double de = i < n1 ? x[cc + 1] - xc : (o.gx1 == 0 ? x[cc - (n1 - 1)] - xc : (o.gx1 > 0 ? 0. : -2. * xc));
-    const double ds = j > 1 ? x[cc - sy] - xc
-                            : (o.gy0 == 0 ? x[cc + (size_t)(n2 - 1) * sy] - xc : (o.gy0 > 0 ? 0. : -2. * xc));
-    const double dn = j < n2 ? x[cc + sy] - xc
-                             : (o.gy1 == 0 ? x[cc - (size_t)(n2 - 1) * sy] - xc : (o.gy1 > 0 ? 0. : -2. * xc));
+    const float ec = E[cc];
+    // neighbour values: the periodic wrap is loaded only on the boundary cell that needs it
+    const float ew = i > 1 ? E[cc - 1] : (o.gx0 == 0 ? E[cc + (n1 - 1)] : 0.f);
+    const float ee = i < n1 ? E[cc + 1] : (o.gx1 == 0 ? E[cc - (n1 - 1)] : 0.f);
+    const float es = j > 1 ? E[cc - sy] : (o.gy0 == 0 ? E[cc + (size_t)(n2 - 1) * sy] : 0.f);
+    const float en = j < n2 ? E[cc + sy] : (o.gy1 == 0 ? E[cc - (size_t)(n2 - 1) * sy] : 0.f);
+    const df dw = diff_nb(i > 1, o.gx0, ew, ec);
+    const df de = diff_nb(i < n1, o.gx1, ee, ec);
+    const df ds = diff_nb(j > 1, o.gy0, es, ec);
+    const df dn = diff_nb(j < n2, o.gy1, en, ec);
     const int kk = k - 1;
-    double lz = sres[kk] * xc;
-    if (k > 1) lz += a[kk] * (x[cc - sz] - xc);
-    else if (o.zper) lz += a[kk] * (x[cc + (size_t)(n3 - 1) * sz] - xc);
-    if (k < n3) lz += c[kk] * (x[cc + sz] - xc);
-    else if (o.zper) lz += c[kk] * (x[cc - (size_t)(n3 - 1) * sz] - xc);
-    const double lap = (de + dw) * o.cx + (dn + ds) * o.cy + lz;
-    const double rhs = rhs64[t];
-    const double r = rhs - lap;
-    e32[cc] = (float)r;
-    rr = r * r;
-    bb = rhs * rhs;
+    df lz = df_mul_f(dfv(s2[kk]), ec);
+    if (k > 1 || o.zper) {
+      const float eb = k > 1 ? E[cc - sz] : E[cc + (size_t)(n3 - 1) * sz];
+      lz = df_add(lz, df_mul(dfv(a2[kk]), two_sum(eb, -ec)));
+    }
+    if (k < n3 || o.zper) {
+      const float et = k < n3 ? E[cc + sz] : E[cc - (size_t)(n3 - 1) * sz];
+      lz = df_add(lz, df_mul(dfv(c2[kk]), two_sum(et, -ec)));
+    }
+    const df lx = df_mul(df_add(de, dw), dfv(o.cx));
+    const df ly = df_mul(df_add(dn, ds), dfv(o.cy));
+    const df lap = df_add(df_add(lx, ly), lz);
+    const df r = df_add({R[cc], Rlo[t]}, df_neg(lap));
+    R[cc] = r.h;
+    Rlo[t] = r.l;
+    x[cc] = first ? (double)ec : x[cc] + (double)ec;
+    sq = r.h * r.h;
   }
-  for (int s = 16; s > 0; s >>= 1) {
-    rr += __shfl_down_sync(0xffffffffu, rr, s);
-    bb += __shfl_down_sync(0xffffffffu, bb, s);
-  }
-  if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = rr; red[1][threadIdx.x >> 5] = bb; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s0 = 0., s1 = 0.;
-    for (int q = 0; q < kTB / 32; q++) { s0 += red[0][q]; s1 += red[1][q]; }
-    part[2 * (size_t)blockIdx.x] = s0;
-    part[2 * (size_t)blockIdx.x + 1] = s1;
-  }
+  block_reduce_to(sq, &part[blockIdx.x]);
 }
 
-__global__ void k_sum2(const double *__restrict__ part, long nblk, double *__restrict__ out) {
-  __shared__ double r0[kTB], r1[kTB];
-  double s0 = 0., s1 = 0.;
-  for (long q = threadIdx.x; q < nblk; q += blockDim.x) { s0 += part[2 * q]; s1 += part[2 * q + 1]; }
+__global__ void k_sum1(const double *__restrict__ part, long nblk, double *__restrict__ out) {
+  __shared__ double r0[kTB];
+  double s0 = 0.;
+  for (long q = threadIdx.x; q < nblk; q += blockDim.x) s0 += part[q];
   r0[threadIdx.x] = s0;
-  r1[threadIdx.x] = s1;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) { r0[threadIdx.x] += r0[threadIdx.x + o]; r1[threadIdx.x] += r1[threadIdx.x + o]; }
+    if (threadIdx.x < o) r0[threadIdx.x] += r0[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) { out[0] = r0[0]; out[1] = r1[0]; }
+  if (threadIdx.x == 0) out[0] = r0[0];
+}
+
+float2 to_df(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
+int read_norm(double *part, unsigned nblk, cudaStream_t st, double *out) {
+  double *sum = part + nblk;
+  k_sum1<<<1, kTB, 0, st>>>(part, nblk, sum);
+  CANS_LAUNCH_CHECK();
+  CANS_CUDA_TRY(cudaMemcpyAsync(out, sum, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaStreamSynchronize(st));
+  return CANS_OK;
 }
 }  // namespace
 
@@ -123,43 +212,36 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   (void)dzci;
   (void)dzfi;
   if (!P || !p || !dli || max_iter < 0) return CANS_EINVAL;
-  double *rhs64 = nullptr, *part = nullptr;
-  float *e32 = nullptr;
-  int n[3];
-  char cbc[6], cof[3];
-  const double *a, *sres, *c;
-  cudaStream_t st;
-  int rc = cans_plan_refine_buffers(P, &rhs64, &e32, &part, n, cbc, cof, &a, &sres, &c, &st);
+  RefineBufs b;
+  int rc = cans_plan_refine_buffers(P, &b);
   if (rc) return rc;
-  if (cof[0] != 'c' || cof[1] != 'c' || cof[2] != 'c') return CANS_ENOTSUP;
+  if (b.c_or_f[0] != 'c' || b.c_or_f[1] != 'c' || b.c_or_f[2] != 'c') return CANS_ENOTSUP;
   OpParams o;
-  o.n1 = n[0]; o.n2 = n[1]; o.n3 = n[2];
-  o.cx = dli[0] * dli[0];
-  o.cy = dli[1] * dli[1];
+  o.n1 = b.n[0]; o.n2 = b.n[1]; o.n3 = b.n[2];
+  o.cx = to_df(dli[0] * dli[0]);
+  o.cy = to_df(dli[1] * dli[1]);
   auto rule = [](char ch) { return ch == 'P' ? 0 : (ch == 'N' ? 1 : -1); };
-  o.gx0 = rule(cbc[0]); o.gx1 = rule(cbc[1]); o.gy0 = rule(cbc[2]); o.gy1 = rule(cbc[3]);
-  o.zper = cbc[4] == 'P' && cbc[5] == 'P';
-  const long np = (long)n[0] * n[1] * n[2];
+  o.gx0 = rule(b.cbc[0]); o.gx1 = rule(b.cbc[1]); o.gy0 = rule(b.cbc[2]); o.gy1 = rule(b.cbc[3]);
+  o.zper = b.cbc[4] == 'P' && b.cbc[5] == 'P';
+  const long np = (long)o.n1 * o.n2 * o.n3;
   const unsigned nblk = (unsigned)((np + kTB - 1) / kTB);
-  k_split_rhs<<<nblk, kTB, 0, st>>>(p, rhs64, e32, n[0], n[1], n[2]);
+  cudaStream_t st = b.st;
+  k_split_df<<<nblk, kTB, 0, st>>>(p, b.R, b.Rlo, o.n1, o.n2, o.n3, b.part);
   CANS_LAUNCH_CHECK();
-  // x_0 = solve32(rhs)
-  if ((rc = cans_plan_solve_mixed(P, e32, p, 0))) return rc;
-  int it = 0;
+  double nrhs = 0., nr = 0.;
+  if ((rc = read_norm(b.part, nblk, st, &nrhs))) return rc;
+  if ((rc = cans_plan_solve_f32io(P, b.R, b.E))) return rc;  // e_0
+  int it = 0, first = 1;
   double rel = 1.;
-  double *sums = part + 2 * (size_t)nblk;
   for (;;) {
-    k_residual64<<<nblk, kTB, 0, st>>>(p, rhs64, e32, a, sres, c, o, part);
+    k_dfres<<<nblk, kTB, 0, st>>>(b.E, b.R, b.Rlo, p, first, b.a2, b.c2, b.s2, o, b.part);
     CANS_LAUNCH_CHECK();
-    k_sum2<<<1, kTB, 0, st>>>(part, nblk, sums);
-    CANS_LAUNCH_CHECK();
-    double h[2];
-    CANS_CUDA_TRY(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, st));
-    CANS_CUDA_TRY(cudaStreamSynchronize(st));
-    if (!(h[0] == h[0]) || !(h[1] == h[1])) return CANS_ENONFINITE;
-    rel = h[1] > 0. ? sqrt(h[0] / h[1]) : sqrt(h[0]);
+    first = 0;
+    if ((rc = read_norm(b.part, nblk, st, &nr))) return rc;
+    if (!(nr == nr)) return CANS_ENONFINITE;
+    rel = nrhs > 0. ? sqrt(nr / nrhs) : sqrt(nr);
     if (rel <= rtol || it >= max_iter) break;
-    if ((rc = cans_plan_solve_mixed(P, e32, p, 1))) return rc;  // x += solve32(r)
+    if ((rc = cans_plan_solve_f32io(P, b.R, b.E))) return rc;  // e_{k+1} = solve32(r)
     it++;
   }
   if (iters) *iters = it;

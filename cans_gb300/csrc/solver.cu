@@ -204,7 +204,8 @@ struct DirTables {
 struct Factor {
   double key = 0.;       // 1/alpha for Helmholtz, NaN-free sentinel 0 for Poisson
   bool valid = false;
-  double *zinv = nullptr, *dd = nullptr, *p2 = nullptr, *dcl = nullptr;  // device
+  double *zinv = nullptr, *dd = nullptr, *p2 = nullptr, *dcl = nullptr;  // device, FP64
+  float *zinv32 = nullptr, *dd32 = nullptr, *p232 = nullptr;             // FP32 copies (FP32 plans)
   unsigned long long stamp = 0;
 };
 
@@ -222,15 +223,17 @@ struct cans_plan {
   int q;             // 1 when the last z row is a Dirichlet face (not solved)
   int nn;            // rows of the z system (n3 - q)
   int zper;          // periodic z
+  double lam32 = 0.; // FP32 plans: columns with |lambda_xy| >= lam32 eliminate in FP32
   std::vector<double> lam_h, a_h, b_h, c_h;
   double *lamcol = nullptr;   // device lambda in spectral column order (i*n2 + j)
   double *a_d = nullptr, *b_d = nullptr, *c_d = nullptr, *bb_d = nullptr;
   void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)
   double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
-  float *R32 = nullptr;        // refinement: FP32 haloed residual / correction field
-  double *rhs64 = nullptr;     // refinement: FP64 copy of the right-hand side
+  float *R32 = nullptr;        // refinement: FP32 haloed residual (high part)
+  float *E32 = nullptr;        // refinement: FP32 haloed correction
+  float *Rlo = nullptr;        // refinement: residual low part (halo-free)
   double *rpart = nullptr;     // refinement: per-block partial norms
-  double *sres = nullptr;      // refinement: exact residues a_k + b_k + c_k of the z rows
+  float2 *coef2 = nullptr;     // refinement: double-float a_k, c_k and residues s_k
   Factor fac[4];
   unsigned long long clock = 0;
   long long bytes = 0;
@@ -458,6 +461,81 @@ __global__ void k_zfactor(const double *__restrict__ lamcol, const double *__res
   dcl[col] = (fabs(den) <= pt || structural) ? 0. : den;
 }
 
+__global__ void k_factor_to_f32(const double *__restrict__ a, float *__restrict__ b, size_t n) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) b[t] = (float)a[t];
+}
+
+// z solve on FP32 spectral data (FP32 plans).  Columns with |lambda_xy| >= lam32 are
+// eliminated in FP32 with the FP32-rounded factors (their system has condition number below
+// ~300, so FP32 gives ~1e-5 or better and the refinement contracts by that per step); the
+// columns below (the low wavenumbers, incl. the singular mode) run the FP64 elimination with
+// the FP64 factors and an FP64 scratch for the forward sweep.  Both overwrite S in place.
+__global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, double *__restrict__ W,
+                                                    const double *__restrict__ lamcol, double lam32,
+                                                    const double *__restrict__ zinv, const double *__restrict__ dd,
+                                                    const double *__restrict__ p2, const double *__restrict__ dcl,
+                                                    const float *__restrict__ zinv32, const float *__restrict__ dd32,
+                                                    const float *__restrict__ p232, const double *__restrict__ a,
+                                                    const double *__restrict__ c, long ncol, int nn, int zper,
+                                                    double norm) {
+  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  if (fabs(lamcol[col]) >= lam32) {
+    const float normf = (float)norm;
+    float y = 0.f;
+    for (int k = 0; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      y = (S[idx] * normf - (float)a[k] * y) * zinv32[idx];
+      S[idx] = y;
+    }
+    const float sn = y;
+    for (int k = nn - 2; k >= 0; k--) {
+      const size_t idx = (size_t)k * ncol + col;
+      y = S[idx] - dd32[idx] * y;
+      S[idx] = y;
+    }
+    if (zper) {
+      const size_t iN = (size_t)nn * ncol + col;
+      const double den = dcl[col];
+      const float pN = den == 0. ? 0.f : (float)(((double)S[iN] * norm - c[nn] * (double)y - a[nn] * (double)sn) / den);
+      S[iN] = pN;
+      for (int k = 0; k < nn; k++) {
+        const size_t idx = (size_t)k * ncol + col;
+        S[idx] = S[idx] + p232[idx] * pN;
+      }
+    }
+    return;
+  }
+  double y = 0.;
+  for (int k = 0; k < nn; k++) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = ((double)S[idx] * norm - a[k] * y) * zinv[idx];
+    W[idx] = y;
+  }
+  const double sn = y;
+  for (int k = nn - 2; k >= 0; k--) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = W[idx] - dd[idx] * y;
+    W[idx] = y;
+  }
+  if (zper) {
+    const size_t iN = (size_t)nn * ncol + col;
+    const double den = dcl[col];
+    const double pN = den == 0. ? 0. : ((double)S[iN] * norm - c[nn] * y - a[nn] * sn) / den;
+    S[iN] = (float)pN;
+    for (int k = 0; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      S[idx] = (float)(W[idx] + p2[idx] * pN);
+    }
+  } else {
+    for (int k = 0; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      S[idx] = (float)W[idx];
+    }
+  }
+}
+
 // z solve, FP64 spectral data, in place
 __global__ void __launch_bounds__(128) k_zsolve64(double *__restrict__ S, const double *__restrict__ zinv,
                                                   const double *__restrict__ dd, const double *__restrict__ p2,
@@ -558,6 +636,7 @@ template <typename T> static int upload_tables(cans_plan *P, int d) {
 
 static void free_factor(Factor &f) {
   cudaFree(f.zinv); cudaFree(f.dd); cudaFree(f.p2); cudaFree(f.dcl);
+  cudaFree(f.zinv32); cudaFree(f.dd32); cudaFree(f.p232);
   f = Factor();
 }
 
@@ -566,7 +645,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
   cudaFree(P->lamcol); cudaFree(P->a_d); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
-  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->rhs64); cudaFree(P->rpart); cudaFree(P->sres);
+  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
   delete P;
   return CANS_OK;
@@ -612,6 +691,27 @@ static int get_factor(cans_plan *P, double key, bool helm, Factor **out) {
                                                                        P->zper, zsing ? 1 : 0, slot->zinv, slot->dd,
                                                                        slot->p2, slot->dcl);
   CANS_LAUNCH_CHECK();
+  if (P->precision == CANS_FP32) {
+    const size_t cells = (size_t)ncol * std::max(nn, 1);
+    if (!slot->zinv32) {
+      CANS_CUDA_TRY(cudaMalloc(&slot->zinv32, cells * sizeof(float)));
+      CANS_CUDA_TRY(cudaMalloc(&slot->dd32, cells * sizeof(float)));
+      P->bytes += (long long)(2 * cells * sizeof(float));
+      if (P->zper) {
+        CANS_CUDA_TRY(cudaMalloc(&slot->p232, cells * sizeof(float)));
+        P->bytes += (long long)(cells * sizeof(float));
+      }
+    }
+    const unsigned g = (unsigned)((cells + 255) / 256);
+    k_factor_to_f32<<<g, 256, 0, P->stream>>>(slot->zinv, slot->zinv32, cells);
+    CANS_LAUNCH_CHECK();
+    k_factor_to_f32<<<g, 256, 0, P->stream>>>(slot->dd, slot->dd32, cells);
+    CANS_LAUNCH_CHECK();
+    if (P->zper) {
+      k_factor_to_f32<<<g, 256, 0, P->stream>>>(slot->p2, slot->p232, cells);
+      CANS_LAUNCH_CHECK();
+    }
+  }
   slot->key = key;
   slot->valid = true;
   slot->stamp = ++P->clock;
@@ -695,8 +795,9 @@ static int launch_z(cans_plan *P, const Factor *F, double norm, bool f32) {
     k_zsolve64<<<grid, tpb, 0, P->stream>>>((double *)P->S, F->zinv, F->dd, F->p2, F->dcl, P->a_d, P->c_d, ncol,
                                             nn, P->zper, norm);
   else
-    k_zsolve32<<<grid, tpb, 0, P->stream>>>((float *)P->S, P->R64, F->zinv, F->dd, F->p2, F->dcl, P->a_d, P->c_d,
-                                            ncol, nn, P->zper, norm);
+    k_zsolve_hyb<<<grid, tpb, 0, P->stream>>>((float *)P->S, P->R64, P->lamcol, P->lam32, F->zinv, F->dd, F->p2,
+                                              F->dcl, F->zinv32, F->dd32, F->p232, P->a_d, P->c_d, ncol, nn, P->zper,
+                                              norm);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
@@ -810,6 +911,12 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
   P->q = (c_or_f[2] == 'f' && cbc[5] == 'D') ? 1 : 0;
   P->nn = n3 - P->q;
   P->zper = cbc[4] == 'P' && cbc[5] == 'P';
+  {
+    // FP32 elimination only where the column's condition number (max|b| + |lam|)/|lam| < ~300
+    double bmax = 0.;
+    for (int k = 0; k < n3; k++) bmax = fmax(bmax, fabs(P->b_h[k]) + fabs(P->a_h[k]) + fabs(P->c_h[k]));
+    P->lam32 = bmax / 300.;
+  }
   if (P->zper && P->nn < 2) { delete P; return CANS_ENOTSUP; }
   // host outputs
   if (lambdaxy) memcpy(lambdaxy, P->lam_h.data(), sizeof(double) * P->lam_h.size());
@@ -908,45 +1015,66 @@ extern "C" int cans_solve_helmholtz(cans_plan *P, double alpha, const int is_bou
 }
 
 // ------------------------------------------------------------------ refinement support
-int cans_plan_refine_buffers(cans_plan *P, double **rhs64, float **e32, double **partials, int *n, char *cbc,
-                             char *c_or_f, const double **a, const double **sres, const double **c, cudaStream_t *st) {
+struct RefineBufs {
+  float *R;
+  float *E;
+  float *Rlo;
+  double *part;
+  const float2 *a2, *c2, *s2;
+  int n[3];
+  char cbc[6], c_or_f[3];
+  cudaStream_t st;
+};
+
+int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
   if (P->precision != CANS_FP32) return CANS_EINVAL;
   const size_t np = (size_t)P->n[0] * P->n[1] * P->n[2];
   const size_t nh = (size_t)(P->n[0] + 2) * (P->n[1] + 2) * (P->n[2] + 2);
   const size_t nblk = (np + 255) / 256;
-  if (!P->rhs64) {
-    CANS_CUDA_TRY(cudaMalloc(&P->rhs64, np * sizeof(double)));
+  const int n3 = P->n[2];
+  if (!P->R32) {
     CANS_CUDA_TRY(cudaMalloc(&P->R32, nh * sizeof(float)));
+    CANS_CUDA_TRY(cudaMalloc(&P->E32, nh * sizeof(float)));
     CANS_CUDA_TRY(cudaMemsetAsync(P->R32, 0, nh * sizeof(float), P->stream));
-    CANS_CUDA_TRY(cudaMalloc(&P->rpart, (2 * nblk + 8) * sizeof(double)));
-    // residue of each z row of the operator the solver inverts, exact in extended precision:
-    // interior rows a+b+c; wall rows without the absent neighbour's coefficient
-    const int n3 = P->n[2];
-    std::vector<double> sr(n3);
+    CANS_CUDA_TRY(cudaMemsetAsync(P->E32, 0, nh * sizeof(float), P->stream));
+    CANS_CUDA_TRY(cudaMalloc(&P->Rlo, np * sizeof(float)));
+    CANS_CUDA_TRY(cudaMalloc(&P->rpart, (nblk + 8) * sizeof(double)));
+    // double-float z coefficients; the residue of each row of the operator the solver inverts
+    // (interior rows a+b+c, wall rows without the absent neighbour) exact in extended precision
+    std::vector<float2> h(3 * (size_t)n3);
+    auto df = [](long double v) {
+      const float hi = (float)v;
+      return make_float2(hi, (float)(v - (long double)hi));
+    };
     for (int k = 0; k < n3; k++) {
       long double acc = (long double)P->b_h[k];
       if (k > 0 || P->zper) acc += (long double)P->a_h[k];
       if (k < n3 - 1 || P->zper) acc += (long double)P->c_h[k];
-      sr[k] = (double)acc;
+      h[k] = df(P->a_h[k]);
+      h[n3 + k] = df(P->c_h[k]);
+      h[2 * n3 + k] = df(acc);
     }
-    CANS_CUDA_TRY(cudaMalloc(&P->sres, n3 * sizeof(double)));
-    CANS_CUDA_TRY(cudaMemcpy(P->sres, sr.data(), n3 * sizeof(double), cudaMemcpyHostToDevice));
-    P->bytes += (long long)(np * sizeof(double) + nh * sizeof(float) + (2 * nblk + 8 + n3) * sizeof(double));
+    CANS_CUDA_TRY(cudaMalloc(&P->coef2, h.size() * sizeof(float2)));
+    CANS_CUDA_TRY(cudaMemcpy(P->coef2, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    P->bytes += (long long)(2 * nh * sizeof(float) + np * sizeof(float) + (nblk + 8) * sizeof(double) +
+                            h.size() * sizeof(float2));
   }
-  *rhs64 = P->rhs64;
-  *e32 = P->R32;
-  *partials = P->rpart;
-  for (int d = 0; d < 3; d++) n[d] = P->n[d];
-  memcpy(cbc, P->cbc, 6);
-  memcpy(c_or_f, P->c_or_f, 3);
-  *a = P->a_d; *sres = P->sres; *c = P->c_d;
-  *st = P->stream;
+  b->R = P->R32;
+  b->E = P->E32;
+  b->Rlo = P->Rlo;
+  b->part = P->rpart;
+  b->a2 = P->coef2;
+  b->c2 = P->coef2 + n3;
+  b->s2 = P->coef2 + 2 * n3;
+  for (int d = 0; d < 3; d++) b->n[d] = P->n[d];
+  memcpy(b->cbc, P->cbc, 6);
+  memcpy(b->c_or_f, P->c_or_f, 3);
+  b->st = P->stream;
   return CANS_OK;
 }
 
-// FP32 solve of the haloed FP32 field `in`; the result is written (accumulate = 0) or
-// added (accumulate = 1) to the interior of the haloed FP64 field `out`
-int cans_plan_solve_mixed(cans_plan *P, const float *in, double *out, int accumulate) {
+// FP32 solve of the haloed FP32 field `in`, result into the interior of the haloed FP32 `out`
+int cans_plan_solve_f32io(cans_plan *P, const float *in, float *out) {
   if (P->precision != CANS_FP32) return CANS_EINVAL;
   Factor *F = nullptr;
   int rc;
@@ -960,7 +1088,7 @@ int cans_plan_solve_mixed(cans_plan *P, const float *in, double *out, int accumu
   mark(P, 3);
   if ((rc = launch_y<float>(P, 0))) return rc;
   mark(P, 4);
-  if ((rc = launch_xbwd<float, double>(P, out, accumulate))) return rc;
+  if ((rc = launch_xbwd<float, float>(P, out, 0))) return rc;
   mark(P, 5);
   return CANS_OK;
 }
