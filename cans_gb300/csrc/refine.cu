@@ -28,6 +28,7 @@
 // cond * eps.
 #include <math.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "cans_internal.cuh"
@@ -111,70 +112,134 @@ __device__ __forceinline__ void block_reduce_to(float v, double *out) {
   __syncthreads();
   if (threadIdx.x == 0) {
     double a = 0.;
-    for (int q = 0; q < kTB / 32; q++) a += (double)red[q];
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) a += (double)red[q];
     *out = a;
   }
 }
 
-// rhs (FP64, interior of p) -> (R hi, Rlo lo) and ||rhs||^2 partials
+// rhs (FP64, interior of p) -> (R hi, Rlo lo) and ||rhs||^2 partials.  Grid-stride over the
+// (j, k) rows so the partials number gridDim.x, not the cell count.
 __global__ void __launch_bounds__(kTB) k_split_df(const double *__restrict__ p, float *__restrict__ R,
                                                   float *__restrict__ Rlo, int n1, int n2, int n3,
                                                   double *__restrict__ part) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   float sq = 0.f;
-  if (t < (long)n1 * n2 * n3) {
-    const int i = (int)(t % n1) + 1, j = (int)((t / n1) % n2) + 1, k = (int)(t / ((long)n1 * n2)) + 1;
-    const size_t c = hidx(i, j, k, n1, n2);
-    const double v = p[c];
-    const float hi = __double2float_rn(v);
-    R[c] = hi;
-    Rlo[t] = __double2float_rn(v - (double)hi);
-    sq = hi * hi;
+  const long nrows = (long)n2 * n3;
+  for (long row = blockIdx.x; row < nrows; row += gridDim.x) {
+    const int j = (int)(row % n2) + 1, k = (int)(row / n2) + 1;
+    for (int i = threadIdx.x + 1; i <= n1; i += blockDim.x) {
+      const size_t c = hidx(i, j, k, n1, n2);
+      const size_t t = (size_t)(i - 1) + (size_t)n1 * (size_t)row;
+      const double v = p[c];
+      const float hi = __double2float_rn(v);
+      R[c] = hi;
+      Rlo[t] = __double2float_rn(v - (double)hi);
+      sq = __fmaf_rn(hi, hi, sq);
+    }
   }
   block_reduce_to(sq, &part[blockIdx.x]);
 }
 
-// (R, Rlo) -= L e ;  x += e (x = e when first) ;  ||R||^2 partials
+// Compensated accumulation (Ogita-Rump-Oishi "Dot2"): the running sum's high part goes
+// through two-sum, every error term (two-sum residues, two-product residues, cross products
+// with the coefficients' low parts) into one FP32 accumulator.  Accuracy is that of
+// double-float evaluation (~2^-48 of the sum of |terms|) at about a quarter of the flops
+// of chained double-float additions.
+struct Dot2 {
+  float s, err;
+  __device__ __forceinline__ void add(float v) {
+    const df t = two_sum(s, v);
+    s = t.h;
+    err = __fadd_rn(err, t.l);
+  }
+  // += c * d with c double-float and d = (dh, dl) double-float
+  __device__ __forceinline__ void add_prod(float2 c, float dh, float dl) {
+    const float pr = __fmul_rn(c.x, dh);
+    float e = __fmaf_rn(c.x, dh, -pr);
+    e = __fmaf_rn(c.x, dl, e);
+    e = __fmaf_rn(c.y, dh, e);
+    add(pr);
+    err = __fadd_rn(err, e);
+  }
+};
+
+// (R, Rlo) -= L e ;  x += e (x = e when first) ;  ||R||^2 partials.
+// Work unit: JB = 4 consecutive j rows of one k plane; the CTA strides over these units and
+// its threads run along i.  Every load of a unit is issued before the arithmetic (the
+// j-1..j+JB column of e is a sliding window in registers), so the memory latency of one unit
+// overlaps its ~100 FP32 operations per cell instead of stalling each cell.
+constexpr int JB = 4;
 __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, float *__restrict__ R,
                                                float *__restrict__ Rlo, double *__restrict__ x, int first,
                                                const float2 *__restrict__ a2, const float2 *__restrict__ c2,
                                                const float2 *__restrict__ s2, OpParams o,
                                                double *__restrict__ part) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int n1 = o.n1, n2 = o.n2, n3 = o.n3;
+  const size_t sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
+  const int nub = (n2 + JB - 1) / JB;
+  const long nunits = (long)nub * n3;
   float sq = 0.f;
-  if (t < (long)n1 * n2 * n3) {
-    const int i = (int)(t % n1) + 1, j = (int)((t / n1) % n2) + 1, k = (int)(t / ((long)n1 * n2)) + 1;
-    const size_t sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
-    const size_t cc = hidx(i, j, k, n1, n2);
-    const float ec = E[cc];
-    // neighbour values: the periodic wrap is loaded only on the boundary cell that needs it
-    const float ew = i > 1 ? E[cc - 1] : (o.gx0 == 0 ? E[cc + (n1 - 1)] : 0.f);
-    const float ee = i < n1 ? E[cc + 1] : (o.gx1 == 0 ? E[cc - (n1 - 1)] : 0.f);
-    const float es = j > 1 ? E[cc - sy] : (o.gy0 == 0 ? E[cc + (size_t)(n2 - 1) * sy] : 0.f);
-    const float en = j < n2 ? E[cc + sy] : (o.gy1 == 0 ? E[cc - (size_t)(n2 - 1) * sy] : 0.f);
-    const df dw = diff_nb(i > 1, o.gx0, ew, ec);
-    const df de = diff_nb(i < n1, o.gx1, ee, ec);
-    const df ds = diff_nb(j > 1, o.gy0, es, ec);
-    const df dn = diff_nb(j < n2, o.gy1, en, ec);
+  for (long u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const int j0 = (int)(u % nub) * JB + 1, k = (int)(u / nub) + 1;
     const int kk = k - 1;
-    df lz = df_mul_f(dfv(s2[kk]), ec);
-    if (k > 1 || o.zper) {
-      const float eb = k > 1 ? E[cc - sz] : E[cc + (size_t)(n3 - 1) * sz];
-      lz = df_add(lz, df_mul(dfv(a2[kk]), two_sum(eb, -ec)));
+    const float2 av = a2[kk], cv = c2[kk], sv = s2[kk];
+    const bool hasb = k > 1 || o.zper, hast = k < n3 || o.zper;
+    for (int i = threadIdx.x + 1; i <= n1; i += blockDim.x) {
+      // column e(i, j0-1 .. j0+JB, k) with the y ghost rule at the ends
+      float col[JB + 2], ew[JB], ee[JB], eb[JB], et[JB], rh[JB], rl[JB];
+      const size_t c0 = hidx(i, j0, k, n1, n2);
+#pragma unroll
+      for (int q = 0; q < JB; q++) {
+        const int j = j0 + q;
+        if (j > n2) { col[q + 1] = 0.f; continue; }
+        const size_t cc = c0 + (size_t)q * sy;
+        col[q + 1] = E[cc];
+        ew[q] = i > 1 ? E[cc - 1] : (o.gx0 == 0 ? E[cc + (n1 - 1)] : 0.f);
+        ee[q] = i < n1 ? E[cc + 1] : (o.gx1 == 0 ? E[cc - (n1 - 1)] : 0.f);
+        eb[q] = hasb ? (k > 1 ? E[cc - sz] : E[cc + (size_t)(n3 - 1) * sz]) : 0.f;
+        et[q] = hast ? (k < n3 ? E[cc + sz] : E[cc - (size_t)(n3 - 1) * sz]) : 0.f;
+        rh[q] = R[cc];
+        rl[q] = Rlo[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * kk)];
+      }
+      col[0] = j0 > 1 ? E[c0 - sy] : (o.gy0 == 0 ? E[c0 + (size_t)(n2 - 1) * sy] : 0.f);
+      {
+        const int jl = j0 + JB;  // row after the unit
+        col[JB + 1] = jl <= n2 ? E[c0 + (size_t)JB * sy] : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < JB; q++) {
+        const int j = j0 + q;
+        if (j > n2) continue;
+        const float ec = col[q + 1];
+        // y neighbours from the window; the upper end of the domain uses the ghost rule
+        const float es = col[q];
+        const float en = j < n2 ? col[q + 2] : (o.gy1 == 0 ? E[c0 + (size_t)q * sy - (size_t)(n2 - 1) * sy] : 0.f);
+        const df dw = diff_nb(i > 1, o.gx0, ew[q], ec);
+        const df de = diff_nb(i < n1, o.gx1, ee[q], ec);
+        const df ds = diff_nb(j > 1, o.gy0, es, ec);
+        const df dn = diff_nb(j < n2, o.gy1, en, ec);
+        Dot2 acc{rh[q], rl[q]};
+        const float2 mcx = make_float2(-o.cx.x, -o.cx.y), mcy = make_float2(-o.cy.x, -o.cy.y);
+        acc.add_prod(mcx, de.h, de.l);
+        acc.add_prod(mcx, dw.h, dw.l);
+        acc.add_prod(mcy, dn.h, dn.l);
+        acc.add_prod(mcy, ds.h, ds.l);
+        if (hasb) {
+          const df db = two_sum(eb[q], -ec);
+          acc.add_prod(make_float2(-av.x, -av.y), db.h, db.l);
+        }
+        if (hast) {
+          const df dt = two_sum(et[q], -ec);
+          acc.add_prod(make_float2(-cv.x, -cv.y), dt.h, dt.l);
+        }
+        acc.add_prod(make_float2(-sv.x, -sv.y), ec, 0.f);
+        const df r = two_sum(acc.s, acc.err);  // |err| may exceed |s| after cancellation
+        const size_t cc = c0 + (size_t)q * sy;
+        R[cc] = r.h;
+        Rlo[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * kk)] = r.l;
+        x[cc] = first ? (double)ec : x[cc] + (double)ec;
+        sq = __fmaf_rn(r.h, r.h, sq);
+      }
     }
-    if (k < n3 || o.zper) {
-      const float et = k < n3 ? E[cc + sz] : E[cc - (size_t)(n3 - 1) * sz];
-      lz = df_add(lz, df_mul(dfv(c2[kk]), two_sum(et, -ec)));
-    }
-    const df lx = df_mul(df_add(de, dw), dfv(o.cx));
-    const df ly = df_mul(df_add(dn, ds), dfv(o.cy));
-    const df lap = df_add(df_add(lx, ly), lz);
-    const df r = df_add({R[cc], Rlo[t]}, df_neg(lap));
-    R[cc] = r.h;
-    Rlo[t] = r.l;
-    x[cc] = first ? (double)ec : x[cc] + (double)ec;
-    sq = r.h * r.h;
   }
   block_reduce_to(sq, &part[blockIdx.x]);
 }
@@ -223,10 +288,16 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   auto rule = [](char ch) { return ch == 'P' ? 0 : (ch == 'N' ? 1 : -1); };
   o.gx0 = rule(b.cbc[0]); o.gx1 = rule(b.cbc[1]); o.gy0 = rule(b.cbc[2]); o.gy1 = rule(b.cbc[3]);
   o.zper = b.cbc[4] == 'P' && b.cbc[5] == 'P';
-  const long np = (long)o.n1 * o.n2 * o.n3;
-  const unsigned nblk = (unsigned)((np + kTB - 1) / kTB);
+  // fixed grid (8 CTAs per SM) striding over the rows: gridDim.x partial sums
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long nrows = (long)o.n2 * o.n3;
+  const unsigned nblk = (unsigned)std::min<long>(nrows, 8L * nsm);
+  const unsigned nblk_r = (unsigned)std::min<long>((long)((o.n2 + JB - 1) / JB) * o.n3, 8L * nsm);
+  const int tpb = o.n1 >= 256 ? 256 : (o.n1 >= 128 ? 128 : 64);
   cudaStream_t st = b.st;
-  k_split_df<<<nblk, kTB, 0, st>>>(p, b.R, b.Rlo, o.n1, o.n2, o.n3, b.part);
+  k_split_df<<<nblk, tpb, 0, st>>>(p, b.R, b.Rlo, o.n1, o.n2, o.n3, b.part);
   CANS_LAUNCH_CHECK();
   double nrhs = 0., nr = 0.;
   if ((rc = read_norm(b.part, nblk, st, &nrhs))) return rc;
@@ -234,10 +305,10 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   int it = 0, first = 1;
   double rel = 1.;
   for (;;) {
-    k_dfres<<<nblk, kTB, 0, st>>>(b.E, b.R, b.Rlo, p, first, b.a2, b.c2, b.s2, o, b.part);
+    k_dfres<<<nblk_r, tpb, 0, st>>>(b.E, b.R, b.Rlo, p, first, b.a2, b.c2, b.s2, o, b.part);
     CANS_LAUNCH_CHECK();
     first = 0;
-    if ((rc = read_norm(b.part, nblk, st, &nr))) return rc;
+    if ((rc = read_norm(b.part, nblk_r, st, &nr))) return rc;
     if (!(nr == nr)) return CANS_ENONFINITE;
     rel = nrhs > 0. ? sqrt(nr / nrhs) : sqrt(nr);
     if (rel <= rtol || it >= max_iter) break;

@@ -482,15 +482,47 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
   const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   if (fabs(lamcol[col]) >= lam32) {
+    // the loads do not depend on the recurrence: fetch 8 rows ahead so they overlap it
+    constexpr int U = 8;
     const float normf = (float)norm;
     float y = 0.f;
-    for (int k = 0; k < nn; k++) {
+    int k = 0;
+    for (; k + U <= nn; k += U) {
+      float sv[U], zv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const size_t idx = (size_t)(k + u) * ncol + col;
+        sv[u] = S[idx];
+        zv[u] = zinv32[idx];
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        y = (sv[u] * normf - (float)a[k + u] * y) * zv[u];
+        S[(size_t)(k + u) * ncol + col] = y;
+      }
+    }
+    for (; k < nn; k++) {
       const size_t idx = (size_t)k * ncol + col;
       y = (S[idx] * normf - (float)a[k] * y) * zinv32[idx];
       S[idx] = y;
     }
     const float sn = y;
-    for (int k = nn - 2; k >= 0; k--) {
+    k = nn - 2;
+    for (; k - U + 1 >= 0; k -= U) {
+      float sv[U], dv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const size_t idx = (size_t)(k - u) * ncol + col;
+        sv[u] = S[idx];
+        dv[u] = dd32[idx];
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        y = sv[u] - dv[u] * y;
+        S[(size_t)(k - u) * ncol + col] = y;
+      }
+    }
+    for (; k >= 0; k--) {
       const size_t idx = (size_t)k * ncol + col;
       y = S[idx] - dd32[idx] * y;
       S[idx] = y;
@@ -507,14 +539,47 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
     }
     return;
   }
+  // FP64 columns: same prefetch structure
+  constexpr int U = 8;
   double y = 0.;
-  for (int k = 0; k < nn; k++) {
+  int k = 0;
+  for (; k + U <= nn; k += U) {
+    float sv[U];
+    double zv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const size_t idx = (size_t)(k + u) * ncol + col;
+      sv[u] = S[idx];
+      zv[u] = zinv[idx];
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      y = ((double)sv[u] * norm - a[k + u] * y) * zv[u];
+      W[(size_t)(k + u) * ncol + col] = y;
+    }
+  }
+  for (; k < nn; k++) {
     const size_t idx = (size_t)k * ncol + col;
     y = ((double)S[idx] * norm - a[k] * y) * zinv[idx];
     W[idx] = y;
   }
   const double sn = y;
-  for (int k = nn - 2; k >= 0; k--) {
+  k = nn - 2;
+  for (; k - U + 1 >= 0; k -= U) {
+    double wv[U], dv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const size_t idx = (size_t)(k - u) * ncol + col;
+      wv[u] = W[idx];
+      dv[u] = dd[idx];
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      y = wv[u] - dv[u] * y;
+      W[(size_t)(k - u) * ncol + col] = y;
+    }
+  }
+  for (; k >= 0; k--) {
     const size_t idx = (size_t)k * ncol + col;
     y = W[idx] - dd[idx] * y;
     W[idx] = y;
@@ -529,7 +594,14 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
       S[idx] = (float)(W[idx] + p2[idx] * pN);
     }
   } else {
-    for (int k = 0; k < nn; k++) {
+    for (k = 0; k + U <= nn; k += U) {
+      double wv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) wv[u] = W[(size_t)(k + u) * ncol + col];
+#pragma unroll
+      for (int u = 0; u < U; u++) S[(size_t)(k + u) * ncol + col] = (float)wv[u];
+    }
+    for (; k < nn; k++) {
       const size_t idx = (size_t)k * ncol + col;
       S[idx] = (float)W[idx];
     }
@@ -564,45 +636,6 @@ __global__ void __launch_bounds__(128) k_zsolve64(double *__restrict__ S, const 
     for (int k = 0; k < nn; k++) {
       const size_t idx = (size_t)k * ncol + col;
       S[idx] = S[idx] + p2[idx] * pN;
-    }
-  }
-}
-
-// z solve on FP32 spectral data: elimination in FP64, forward sweep kept in FP64 in the
-// FP64 scratch W (same layout), result rounded to FP32 on the backward sweep
-__global__ void __launch_bounds__(128) k_zsolve32(float *__restrict__ S, double *__restrict__ W,
-                                                  const double *__restrict__ zinv, const double *__restrict__ dd,
-                                                  const double *__restrict__ p2, const double *__restrict__ dcl,
-                                                  const double *__restrict__ a, const double *__restrict__ c,
-                                                  long ncol, int nn, int zper, double norm) {
-  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
-  double y = 0.;
-  for (int k = 0; k < nn; k++) {
-    const size_t idx = (size_t)k * ncol + col;
-    y = ((double)S[idx] * norm - a[k] * y) * zinv[idx];
-    W[idx] = y;
-  }
-  double s1 = 0., sn = y;
-  for (int k = nn - 2; k >= 0; k--) {
-    const size_t idx = (size_t)k * ncol + col;
-    y = W[idx] - dd[idx] * y;
-    W[idx] = y;
-  }
-  s1 = nn > 1 ? y : sn;
-  if (zper) {
-    const size_t iN = (size_t)nn * ncol + col;
-    const double den = dcl[col];
-    const double pN = den == 0. ? 0. : ((double)S[iN] * norm - c[nn] * s1 - a[nn] * sn) / den;
-    S[iN] = (float)pN;
-    for (int k = 0; k < nn; k++) {
-      const size_t idx = (size_t)k * ncol + col;
-      S[idx] = (float)(W[idx] + p2[idx] * pN);
-    }
-  } else {
-    for (int k = 0; k < nn; k++) {
-      const size_t idx = (size_t)k * ncol + col;
-      S[idx] = (float)W[idx];
     }
   }
 }
@@ -1038,7 +1071,8 @@ int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
     CANS_CUDA_TRY(cudaMemsetAsync(P->R32, 0, nh * sizeof(float), P->stream));
     CANS_CUDA_TRY(cudaMemsetAsync(P->E32, 0, nh * sizeof(float), P->stream));
     CANS_CUDA_TRY(cudaMalloc(&P->Rlo, np * sizeof(float)));
-    CANS_CUDA_TRY(cudaMalloc(&P->rpart, (nblk + 8) * sizeof(double)));
+    const size_t nrblk = 8 * 1024;  // the refinement kernels use at most 8 CTAs per SM
+    CANS_CUDA_TRY(cudaMalloc(&P->rpart, (std::max(nblk, nrblk) + 8) * sizeof(double)));
     // double-float z coefficients; the residue of each row of the operator the solver inverts
     // (interior rows a+b+c, wall rows without the absent neighbour) exact in extended precision
     std::vector<float2> h(3 * (size_t)n3);
@@ -1056,7 +1090,7 @@ int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
     }
     CANS_CUDA_TRY(cudaMalloc(&P->coef2, h.size() * sizeof(float2)));
     CANS_CUDA_TRY(cudaMemcpy(P->coef2, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice));
-    P->bytes += (long long)(2 * nh * sizeof(float) + np * sizeof(float) + (nblk + 8) * sizeof(double) +
+    P->bytes += (long long)(2 * nh * sizeof(float) + np * sizeof(float) + (std::max(nblk, nrblk) + 8) * sizeof(double) +
                             h.size() * sizeof(float2));
   }
   b->R = P->R32;
