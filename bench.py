@@ -207,6 +207,10 @@ def bench_ours(args, rank, world):
            "e2e": e2e, "roofline": roof, "clocks": clk.summary(), "gpu_launches": launches}
     if rk3:
         out["rk3_step"] = rk3
+    if args.boxes > 0:
+        torch.cuda.empty_cache()
+        out["batched_boxes"] = bench_boxes(args.boxes, dev, max(1, min(args.steps, 5)),
+                                           unbatched_boxes=min(args.boxes, 32))
     if ref:
         out["fp32_refined"] = ref
     return out
@@ -301,6 +305,88 @@ def bench_rk3(size, dev, steps):
             "ms_per_step": round(ms, 3), "steps": steps, "gpu_launches_per_step": (cans.launch_count() - l0) // steps}
 
 
+def bx_cases(nbox, seed=7):
+    """The batched closed-box workload: lid-driven cavities with nx, ny, nz drawn from
+    {32, 48, ..., 128}, Re from U[100, 1000], lid u = 1 at the top, Dirichlet velocity and
+    Neumann pressure walls, uniform unit cube grid, implicit diffusion, fixed dt (CFL 0.5 at
+    the lid velocity)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.arange(32, 129, 16)
+    cases = []
+    for _ in range(nbox):
+        n = [int(x) for x in rng.choice(sizes, 3)]
+        re = float(rng.uniform(100., 1000.))
+        bcvel = [0.] * 18
+        bcvel[5] = 1.0
+        dlmin = min(1. / n[0], 1. / n[1], 1. / n[2])
+        cases.append(dict(ng=n, l=[1., 1., 1.], gtype=1, gr=0., visci=re, dt_f=0.5 * dlmin, icheck=0,
+                          cbcvel="DDDDDD" * 3, bcvel=bcvel, cbcpre="NNNNNN", bcpre=[0.] * 6, is_impdiff=1))
+    return cases
+
+
+def bench_boxes(nbox, dev, steps, autotune=True, unbatched_boxes=0):
+    """Batched boxes: one persistent launch per stage over all boxes, a captured CUDA graph
+    per time step; Mcell-steps/s over all boxes.  unbatched_boxes > 0 also times the
+    single-box call sequence on that many boxes (a host-driven loop, for contrast)."""
+    import torch
+    from cans_gb300 import cans
+    from cans_gb300.driver import Boxes, Simulation
+    cases = bx_cases(nbox)
+    cells = sum(c["ng"][0] * c["ng"][1] * c["ng"][2] for c in cases)
+    t0 = time.perf_counter()
+    bx = Boxes(cases, autotune=autotune, device=dev)
+    setup_s = time.perf_counter() - t0
+    bx.start()
+    st = bx.stream
+    out = {"workload": f"bx_{nbox}_lid_cavities_32-128_impdiff_fp64", "boxes": nbox, "cells": cells,
+           "autotune": bool(autotune), "setup_s": round(setup_s, 2)}
+    # graph: first call runs + captures, then replays
+    bx.step(2, use_graph=True)
+    bx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = cans.launch_count()
+    e0.record(st)
+    bx.step(steps, use_graph=True)
+    e1.record(st)
+    bx.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    out["graph"] = {"Mcell_steps_per_s": round(cells / (ms * 1e-3) / 1e6, 2), "ms_per_step": round(ms, 3),
+                    "graph_launches_per_step": (cans.launch_count() - l0) // steps,
+                    "kernel_nodes_per_step": bx.graph_nodes}
+    # the same stages launched eagerly (no graph)
+    e0.record(st)
+    l0 = cans.launch_count()
+    bx.step(steps, use_graph=False)
+    e1.record(st)
+    bx.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    out["eager"] = {"Mcell_steps_per_s": round(cells / (ms * 1e-3) / 1e6, 2), "ms_per_step": round(ms, 3),
+                    "gpu_launches_per_step": (cans.launch_count() - l0) // steps}
+    del bx
+    torch.cuda.empty_cache()
+    if unbatched_boxes:
+        sims = []
+        for c in cases[:unbatched_boxes]:
+            s = Simulation(c, device=dev)
+            s.start()
+            sims.append(s)
+        for s in sims:
+            s.step(1)
+        torch.cuda.synchronize()
+        ub_cells = sum(c["ng"][0] * c["ng"][1] * c["ng"][2] for c in cases[:unbatched_boxes])
+        t0 = time.perf_counter()
+        for s in sims:
+            s.step(1)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        out["unbatched"] = {"boxes": unbatched_boxes, "Mcell_steps_per_s": round(ub_cells / sec / 1e6, 2),
+                            "ms_per_step": round(sec * 1e3, 3),
+                            "note": "single-box call sequence per box from Python (host clock)"}
+        del sims
+        torch.cuda.empty_cache()
+    return out
+
+
 def bench_cpu(size, steps, warmup, threads=None):
     """The oracle (CPU restatement of src/solver.f90 with FFTW r2r semantics), all host cores."""
     from oracle import oracle as O
@@ -336,6 +422,7 @@ def main():
     ap.add_argument("--skip-refine", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--rtol", type=float, default=1e-13)
+    ap.add_argument("--boxes", type=int, default=256, help="batched closed-box leg (0: skip)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

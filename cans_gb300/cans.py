@@ -51,6 +51,15 @@ def lib():
     return _lib
 
 
+class CBox(C.Structure):
+    """struct cans_box of include/cans_gb300.h"""
+    _fields_ = [("n", C.c_int * 3), ("l", C.c_double * 3), ("visc", C.c_double), ("dt", C.c_double),
+                ("cbcvel", C.c_char * 18), ("cbcpre", C.c_char * 6), ("bcvel", C.c_double * 18),
+                ("bcpre", C.c_double * 6), ("bforce", C.c_double * 3), ("dzc_g", _D), ("dzf_g", _D),
+                ("dzci", _V), ("dzfi", _V), ("u", _V), ("v", _V), ("w", _V), ("p", _V), ("pp", _V),
+                ("dudtrko", _V), ("dvdtrko", _V), ("dwdtrko", _V)]
+
+
 def _setup(L):
     L.cans_strerror.restype = C.c_char_p
     L.cans_strerror.argtypes = [C.c_int]
@@ -79,6 +88,29 @@ def _setup(L):
     L.cans_chkdiv.argtypes = [_I, _D, _D, _V, _V, _V, _V, _D, _D, _V]
     L.cans_chkdt.argtypes = [_I, _D, _V, _V, C.c_double, C.c_double, C.c_int, C.c_int, _V, _V, _V, _D, _V]
     L.cans_bulk_mean.argtypes = [_I, _V, _V, _D, _V]
+    L.cans_batch_create.argtypes = [C.c_int, C.POINTER(_V), _V, C.POINTER(_V)]
+    L.cans_batch_destroy.argtypes = [_V]
+    L.cans_batch_solve.argtypes = [_V, C.POINTER(_V), _D, _I]
+    L.cans_boxes_create.argtypes = [C.c_int, C.POINTER(CBox), C.c_int, C.c_int, _V, C.POINTER(_V)]
+    L.cans_plan_autotune.argtypes = [_V, C.c_int, _D]
+    L.cans_solver_adjoint.argtypes = [_V, _V]
+    L.cans_solve_helmholtz_adjoint.argtypes = [_V, C.c_double, _V]
+    L.cans_fillps_adjoint.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
+    L.cans_correc_adjoint.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
+    L.cans_updatep_adjoint.argtypes = [_I, C.c_int, _V, _V, _V]
+    L.cans_bounduvw_adjoint.argtypes = [C.c_char_p, _I, _D, _I, _D, _D, _D, _V, _V, _V, C.c_int, C.c_int, C.c_int, _V]
+    L.cans_boundp_adjoint.argtypes = [C.c_char_p, _I, _D, _I, _D, _D, _V, C.c_int, _V]
+    L.cans_rk_adjoint.argtypes = [_D, _I, _D, _V, _V, C.c_double, C.c_double, _V, _V, _V, _V, _V, _V, _V, _V, _V,
+                                  _V, _D, _V, _V]
+    L.cans_rk_adjoint_work_doubles.argtypes = [_I]
+    L.cans_rk_adjoint_work_doubles.restype = C.c_size_t
+    L.cans_plan_get_shape.argtypes = [_V, C.c_int, _I, _I, _I, _I]
+    L.cans_boxes_destroy.argtypes = [_V]
+    L.cans_boxes_start.argtypes = [_V]
+    L.cans_boxes_substep.argtypes = [_V, C.c_int]
+    L.cans_boxes_step.argtypes = [_V, C.c_int]
+    L.cans_boxes_graph_nodes.argtypes = [_V]
+    L.cans_boxes_graph_nodes.restype = C.c_longlong
 
 
 def _check(rc, where):
@@ -191,10 +223,64 @@ class Plan:
                                          C.byref(it), C.byref(rr)), "cans_solver_refined")
         return it.value, rr.value
 
+    def autotune(self, force=False):
+        """cans_plan_autotune: fastest x/y transform shapes; returns the chosen pass times (ms)"""
+        ms = (C.c_double * 2)()
+        _check(lib().cans_plan_autotune(self._h, int(force), ms), "cans_plan_autotune")
+        return list(ms)
+
+    def shape(self, d):
+        """(radix order, lines per CTA, compile-time length or 0) of direction d"""
+        r = (C.c_int * 12)()
+        ns, ncx, spec = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().cans_plan_get_shape(self._h, int(d), r, C.byref(ns), C.byref(ncx), C.byref(spec)),
+               "cans_plan_get_shape")
+        return list(r)[:ns.value], ncx.value, spec.value
+
+    def solve_adjoint(self, g):
+        """S^T g in place (cans_solver_adjoint)"""
+        _check(lib().cans_solver_adjoint(self._h, _ptr(g)), "cans_solver_adjoint")
+        return g
+
+    def solve_helmholtz_adjoint(self, alpha, g):
+        _check(lib().cans_solve_helmholtz_adjoint(self._h, float(alpha), _ptr(g)), "cans_solve_helmholtz_adjoint")
+        return g
+
     def solve_helmholtz(self, alpha, is_bound, p):
         """solve_helmholtz (src/solve_helmholtz.f90:28), 3D variant."""
         _check(lib().cans_solve_helmholtz(self._h, float(alpha), _ints(is_bound), _ptr(p)), "cans_solve_helmholtz")
         return p
+
+
+class Batch:
+    """Independent solves of many plans in one persistent launch per pass (cans_batch_*).
+
+    `solve(fields, alpha=None, is_bound=None)`: system s is the Helmholtz solve of
+    `plans[s].solve_helmholtz(alpha[s], is_bound[s], fields[s])` when alpha[s] != 0, else
+    `updt_rhs_b` (when is_bound is given) followed by `plans[s].solve(fields[s])`."""
+
+    def __init__(self, plans, stream=None):
+        self.plans = list(plans)
+        hs = (_V * len(self.plans))(*[pl._h.value for pl in self.plans])
+        h = C.c_void_p()
+        _check(lib().cans_batch_create(len(self.plans), hs, _stream(stream), C.byref(h)), "cans_batch_create")
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.cans_batch_destroy(h)
+            self._h = None
+
+    def solve(self, fields, alpha=None, is_bound=None):
+        ns = len(self.plans)
+        if len(fields) != ns:
+            raise ValueError("one field per system")
+        ps = (_V * ns)(*[f.data_ptr() for f in fields])
+        al = None if alpha is None else _dbls(alpha)
+        ib = None if is_bound is None else _ints([int(x) for b in is_bound for x in b])
+        _check(lib().cans_batch_solve(self._h, ps, al, ib), "cans_batch_solve")
+        return fields
 
 
 # ------------------------------------------------------------------------------ kernels
@@ -266,3 +352,50 @@ def bulk_mean(n, gvr, p, stream=None):
     r = C.c_double()
     _check(lib().cans_bulk_mean(_ints(n), _ptr(gvr), _ptr(p), C.byref(r), _stream(stream)), "cans_bulk_mean")
     return r.value
+
+
+# ------------------------------------------------------------------------------ adjoints
+def fillps_adjoint(n, dli, dzfi, dti, gp, gu, gv, gw, stream=None):
+    _check(lib().cans_fillps_adjoint(_ints(n), _dbls(dli), _ptr(dzfi), float(dti), _ptr(gp), _ptr(gu), _ptr(gv),
+                                     _ptr(gw), _stream(stream)), "cans_fillps_adjoint")
+
+
+def correc_adjoint(n, dli, dzci, dt, gu, gv, gw, gp, stream=None):
+    _check(lib().cans_correc_adjoint(_ints(n), _dbls(dli), _ptr(dzci), float(dt), _ptr(gu), _ptr(gv), _ptr(gw),
+                                     _ptr(gp), _stream(stream)), "cans_correc_adjoint")
+
+
+def updatep_adjoint(n, is_impdiff, gp, gpp, stream=None):
+    _check(lib().cans_updatep_adjoint(_ints(n), int(is_impdiff), _ptr(gp), _ptr(gpp), _stream(stream)),
+           "cans_updatep_adjoint")
+
+
+def bounduvw_adjoint(cbc, n, bc, is_bound, dl, dzc_h, dzf_h, gu, gv, gw, keep_norm=False, halos_norm=HALO_BOTH,
+                     halos_tang=HALO_BOTH, stream=None):
+    dzc_h, pzc = _hp(dzc_h)
+    dzf_h, pzf = _hp(dzf_h)
+    _check(lib().cans_bounduvw_adjoint(_chars(cbc), _ints(n), _dbls(bc), _ints(is_bound), _dbls(dl), pzc, pzf,
+                                       _ptr(gu), _ptr(gv), _ptr(gw), int(keep_norm), int(halos_norm),
+                                       int(halos_tang), _stream(stream)), "cans_bounduvw_adjoint")
+
+
+def boundp_adjoint(cbc, n, bc, is_bound, dl, dzc_h, gp, halo_side=HALO_BOTH, stream=None):
+    dzc_h, pzc = _hp(dzc_h)
+    _check(lib().cans_boundp_adjoint(_chars(cbc), _ints(n), _dbls(bc), _ints(is_bound), _dbls(dl), pzc, _ptr(gp),
+                                     int(halo_side), _stream(stream)), "cans_boundp_adjoint")
+
+
+def rk_adjoint_work(n, device="cuda"):
+    import torch
+    return torch.empty(int(lib().cans_rk_adjoint_work_doubles(_ints(n))), dtype=torch.float64, device=device)
+
+
+def rk_adjoint(rkpar, n, dli, dzci, dzfi, dt, visc, u, v, w, gu, gv, gw, gdu, gdv, gdw, gp, work, want_gbf=True,
+               stream=None):
+    """returns the body-force adjoint increment (3,) when want_gbf"""
+    gbf = (C.c_double * 3)()
+    _check(lib().cans_rk_adjoint(_dbls(rkpar), _ints(n), _dbls(dli), _ptr(dzci), _ptr(dzfi), float(dt), float(visc),
+                                 _ptr(u), _ptr(v), _ptr(w), _ptr(gu), _ptr(gv), _ptr(gw), _ptr(gdu), _ptr(gdv),
+                                 _ptr(gdw), _ptr(gp), gbf if want_gbf else None, _ptr(work), _stream(stream)),
+           "cans_rk_adjoint")
+    return np.array(list(gbf))

@@ -24,6 +24,7 @@ struct DirParams {
   int ld;        // complex line stride in shared memory (m + 1)
   int sld;       // real staging line stride (nt + 1)
   int nstages;
+  int spec;      // compile-time length of the pass kernel (0: generic runtime path)
   int radix[12];
   const void *tw;    // T2[m]  exp(-2 pi i e / m)
   const void *post;  // T2[nt] exp(-i pi k/(2 nt)) (Makhoul) | exp(-i pi (2k+1)/(4n)) (kinds 11)

@@ -1,0 +1,264 @@
+// Plan state and the per-tile bodies of the five solve passes, shared by the
+// single-system kernels (solver.cu) and the batched persistent kernels (batch.cu).
+#pragma once
+#include <cfloat>
+#include <vector>
+
+#include "cans_internal.cuh"
+#include "fft_smem.cuh"
+
+struct DirTables {
+  void *tw = nullptr, *post = nullptr, *pre = nullptr;  // device, precision of the plan
+};
+
+struct Factor {
+  double key = 0.;       // 1/alpha for Helmholtz, NaN-free sentinel 0 for Poisson
+  bool valid = false;
+  double *zinv = nullptr, *dd = nullptr, *p2 = nullptr, *dcl = nullptr;  // device, FP64
+  float *zinv32 = nullptr, *dd32 = nullptr, *p232 = nullptr;             // FP32 copies (FP32 plans)
+  unsigned long long stamp = 0;
+};
+
+struct cans_plan {
+  int n[3];
+  char cbc[6];
+  char c_or_f[3];
+  int precision;
+  cudaStream_t stream;
+  int kf[2], kb[2], nt[2], m[2];
+  int radix[2][12], nstages[2];
+  int ncx_tuned[2] = {0, 0};  // lines-per-CTA choice of the autotuner (0: default rule)
+  int nospec[2] = {0, 0};     // 1: the autotuner chose the generic kernel over the compile-time one
+  DirTables tab[2];
+  double normfft;
+  double rhsb[6];
+  int q;             // 1 when the last z row is a Dirichlet face (not solved)
+  int nn;            // rows of the z system (n3 - q)
+  int zper;          // periodic z
+  double lam32 = 0.; // FP32 plans: columns with |lambda_xy| >= lam32 eliminate in FP32
+  std::vector<double> lam_h, a_h, b_h, c_h;
+  double *lamcol = nullptr;   // device lambda in spectral column order (i*n2 + j)
+  double *zw = nullptr;       // device diagonal D of the z operator T = D M, M symmetric (0:n3+1)
+  double *a_d = nullptr, *b_d = nullptr, *c_d = nullptr, *bb_d = nullptr;
+  void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)
+  double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
+  float *R32 = nullptr;        // refinement: FP32 haloed residual (high part)
+  float *E32 = nullptr;        // refinement: FP32 haloed correction
+  float *Rlo = nullptr;        // refinement: residual low part (halo-free)
+  double *rpart = nullptr;     // refinement: per-block partial norms
+  float2 *coef2 = nullptr;     // refinement: double-float a_k, c_k and residues s_k
+  Factor fac[4];
+  unsigned long long clock = 0;
+  long long bytes = 0;
+  void *red = nullptr;        // reduction scratch
+  // optional per-pass timing: events recorded between the passes of each solve
+  bool timing = false;
+  std::vector<cudaEvent_t> ev;  // kTimedSolves x (kPasses + 1)
+  int nrec = 0;
+};
+static const int kPasses = 5, kTimedSolves = 256;
+
+// complex sequences per CTA: the largest power of two (<= 16) keeping the two FFT buffers
+// within 96 KB, so three CTAs fit an SM and the transposed x stores are >= 32-byte runs
+__host__ __device__ constexpr int ncx_for(int m, int cbytes) {
+  return (96 * 1024) / (2 * (m + 1) * cbytes) >= 16  ? 16
+         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 8 ? 8
+         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 4 ? 4
+         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 2 ? 2
+                                                      : 1;
+}
+
+template <typename T> inline DirParams make_params(const cans_plan *P, int d, int fwd) {
+  DirParams q;
+  memset(&q, 0, sizeof(q));
+  q.n = P->n[d];
+  q.nt = P->nt[d];
+  q.m = P->m[d];
+  q.kind = fwd ? P->kf[d] : P->kb[d];
+  q.pairs = (q.kind == K_REDFT11 || q.kind == K_RODFT11) ? 0 : 1;
+  q.ld = q.m + 1;
+  q.sld = q.nt + 1;
+  q.nstages = P->nstages[d];
+  for (int s = 0; s < 12; s++) q.radix[s] = P->radix[d][s];
+  q.tw = P->tab[d].tw;
+  q.post = P->tab[d].post;
+  q.pre = P->tab[d].pre;
+  const int ncx0 = ncx_for(q.m, (int)sizeof(cplx_t<T>));
+  q.ncx = P->ncx_tuned[d] > 0 ? P->ncx_tuned[d] : ncx0;
+  q.lpb = q.pairs ? 2 * q.ncx : q.ncx;
+  // compile-time length (power-of-two lengths of the kinds that transform all n points with
+  // no extension, at the default lines per CTA); 0 = generic runtime path
+  const bool pow2 = q.m >= 32 && q.m <= 1024 && (q.m & (q.m - 1)) == 0;
+  q.spec = (pow2 && q.pairs && q.nt == q.m && q.n == q.nt && q.ncx == ncx0 && !P->nospec[d]) ? q.m : 0;
+  return q;
+}
+
+static inline int spec_len(const DirParams &q) { return q.spec; }
+
+// boundary terms of updt_rhs_b (src/bound.f90:514-598) fused into the x-forward load:
+// face (ib, dir) adds v[ib + 2*dir] on interior plane `plane[ib + 2*dir]` (-1: none), in
+// the reference's order x-lower, x-upper, y-lower, ..., z-upper
+struct FaceAdd {
+  int plane[6];
+  double v[6];
+};
+__device__ __forceinline__ double face_add(double x, int i, int j, int k, const FaceAdd &F) {
+  if (i == F.plane[0]) x = x + F.v[0];
+  if (i == F.plane[1]) x = x + F.v[1];
+  if (j == F.plane[2]) x = x + F.v[2];
+  if (j == F.plane[3]) x = x + F.v[3];
+  if (k == F.plane[4]) x = x + F.v[4];
+  if (k == F.plane[5]) x = x + F.v[5];
+  return x;
+}
+
+template <typename T> inline size_t smem_bytes(const DirParams &q) {
+  const size_t a = (size_t)q.ncx * q.ld * sizeof(cplx_t<T>);
+  const size_t b = std::max(a, (size_t)q.lpb * q.sld * sizeof(T));
+  return a + b + (size_t)q.lpb * sizeof(T) + 64;
+}
+
+// get (or build) the z factorisation of plan P for the diagonal shift `key`
+int get_factor(cans_plan *P, double key, bool helm, Factor **out);
+
+// Geometry of a pass: compile-time when M > 0 (then nt == n == m and the kind is a "pairs"
+// kind), from DirParams otherwise.
+template <typename T, int M> struct PassGeo {
+  static constexpr int NCX = M ? ncx_for(M, (int)sizeof(cplx_t<T>)) : 0;
+  static constexpr int LPB = 2 * NCX;
+  static constexpr int LD = M + 1;
+};
+
+// 1. x-forward: haloed rows -> S[k][i][j] (FACES: boundary terms added as the rows load)
+template <typename T, typename TF, int M, bool FACES = false>
+__device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restrict__ S, int n1, int n2,
+                                          const DirParams &P, int tile, int k, unsigned char *smem,
+                                          const FaceAdd *fa = nullptr) {
+  using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
+  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)ncx * ld;
+  T *stg = reinterpret_cast<T *>(B);
+  const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
+                                                                                      : (size_t)lpb * sld * sizeof(T);
+  T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
+  const int j0 = tile * lpb;
+  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, i = e - r * nt, j = j0 + r;
+    if constexpr (FACES)
+      stg[r * sld + i] = (j < n2) ? (T)face_add(p[hidx(i + 1, j + 1, k + 1, n1, n2)], i + 1, j + 1, k + 1, *fa) : T(0);
+    else
+      stg[r * sld + i] = (j < n2) ? (T)p[hidx(i + 1, j + 1, k + 1, n1, n2)] : T(0);
+  }
+  if (!M && nt < n1)
+    for (int r = threadIdx.x; r < lpb; r += blockDim.x) {
+      if constexpr (FACES)
+        pass[r] = (j0 + r < n2) ? (T)face_add(p[hidx(n1, j0 + r + 1, k + 1, n1, n2)], n1, j0 + r + 1, k + 1, *fa) : T(0);
+      else
+        pass[r] = (j0 + r < n2) ? (T)p[hidx(n1, j0 + r + 1, k + 1, n1, n2)] : T(0);
+    }
+  __syncthreads();
+  r2r_pre<T, M>(P, stg, A);
+  __syncthreads();
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
+  T *Sk = S + (size_t)k * n1 * n2;
+  for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
+    const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
+    if (j >= n2) continue;
+    Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M>(P, Z, r, i) : pass[r];
+  }
+}
+
+// 2./4. y pass, in place on contiguous lines S[l*n2 .. l*n2+n2-1], l = k*n1 + i
+template <typename T, int M>
+__device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int n2, const DirParams &P, long tile,
+                                            unsigned char *smem) {
+  using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
+  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)ncx * ld;
+  T *stg = reinterpret_cast<T *>(B);
+  const long l0 = tile * lpb;
+  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
+    stg[r * sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
+  }
+  __syncthreads();
+  r2r_pre<T, M>(P, stg, A);
+  __syncthreads();
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
+  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
+    if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M>(P, Z, r, j);
+  }
+}
+
+// 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k) (written, or added when acc)
+template <typename T, typename TF, int M>
+__device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2,
+                                          const DirParams &P, int acc, int tile, int k, unsigned char *smem) {
+  using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
+  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)ncx * ld;
+  T *stg = reinterpret_cast<T *>(B);
+  const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
+                                                                                      : (size_t)lpb * sld * sizeof(T);
+  T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
+  const int j0 = tile * lpb;
+  const T *Sk = S + (size_t)k * n1 * n2;
+  for (int e = threadIdx.x; e < nt * lpb; e += blockDim.x) {
+    const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
+    stg[r * sld + i] = (j < n2) ? Sk[(size_t)i * n2 + j] : T(0);
+  }
+  if (!M && nt < n1)
+    for (int r = threadIdx.x; r < lpb; r += blockDim.x)
+      pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
+  __syncthreads();
+  r2r_pre<T, M>(P, stg, A);
+  __syncthreads();
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
+  for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
+    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / n1, i = e - r * n1, j = j0 + r;
+    if (j >= n2) continue;
+    const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+    const T val = (i < nt) ? r2r_post<T, M>(P, Z, r, i) : pass[r];
+    p[idx] = acc ? (TF)(p[idx] + (TF)val) : (TF)val;
+  }
+}
+
+// z solve, FP64 spectral data, in place (one spectral column)
+__device__ __forceinline__ void zsolve64_col(double *__restrict__ S, const double *__restrict__ zinv,
+                                             const double *__restrict__ dd, const double *__restrict__ p2,
+                                             const double *__restrict__ dcl, const double *__restrict__ a,
+                                             const double *__restrict__ c, long ncol, int nn, int zper, double norm,
+                                             long col) {
+  double y = 0.;
+  for (int k = 0; k < nn; k++) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = (S[idx] * norm - a[k] * y) * zinv[idx];
+    S[idx] = y;
+  }
+  for (int k = nn - 2; k >= 0; k--) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = S[idx] - dd[idx] * y;
+    S[idx] = y;
+  }
+  if (zper) {
+    const size_t iN = (size_t)nn * ncol + col;
+    const double den = dcl[col];
+    const double s1 = S[col], sn = S[(size_t)(nn - 1) * ncol + col];
+    const double pN = den == 0. ? 0. : (S[iN] * norm - c[nn] * s1 - a[nn] * sn) / den;
+    S[iN] = pN;
+    for (int k = 0; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      S[idx] = S[idx] + p2[idx] * pN;
+    }
+  }
+}

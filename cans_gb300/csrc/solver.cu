@@ -21,11 +21,15 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cfloat>
 #include <vector>
 
 #include "cans_internal.cuh"
 #include "fft_smem.cuh"
+#include "plan.cuh"
 
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 void cans_set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
@@ -195,205 +199,26 @@ extern "C" int cans_initgrid(int gtype, int n, double gr, double lz, int is_peri
 }
 
 // ====================================================================================
-// plan
+// kernels (plan state and tile bodies: plan.cuh)
 // ====================================================================================
-struct DirTables {
-  void *tw = nullptr, *post = nullptr, *pre = nullptr;  // device, precision of the plan
-};
-
-struct Factor {
-  double key = 0.;       // 1/alpha for Helmholtz, NaN-free sentinel 0 for Poisson
-  bool valid = false;
-  double *zinv = nullptr, *dd = nullptr, *p2 = nullptr, *dcl = nullptr;  // device, FP64
-  float *zinv32 = nullptr, *dd32 = nullptr, *p232 = nullptr;             // FP32 copies (FP32 plans)
-  unsigned long long stamp = 0;
-};
-
-struct cans_plan {
-  int n[3];
-  char cbc[6];
-  char c_or_f[3];
-  int precision;
-  cudaStream_t stream;
-  int kf[2], kb[2], nt[2], m[2];
-  int radix[2][12], nstages[2];
-  DirTables tab[2];
-  double normfft;
-  double rhsb[6];
-  int q;             // 1 when the last z row is a Dirichlet face (not solved)
-  int nn;            // rows of the z system (n3 - q)
-  int zper;          // periodic z
-  double lam32 = 0.; // FP32 plans: columns with |lambda_xy| >= lam32 eliminate in FP32
-  std::vector<double> lam_h, a_h, b_h, c_h;
-  double *lamcol = nullptr;   // device lambda in spectral column order (i*n2 + j)
-  double *a_d = nullptr, *b_d = nullptr, *c_d = nullptr, *bb_d = nullptr;
-  void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)
-  double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
-  float *R32 = nullptr;        // refinement: FP32 haloed residual (high part)
-  float *E32 = nullptr;        // refinement: FP32 haloed correction
-  float *Rlo = nullptr;        // refinement: residual low part (halo-free)
-  double *rpart = nullptr;     // refinement: per-block partial norms
-  float2 *coef2 = nullptr;     // refinement: double-float a_k, c_k and residues s_k
-  Factor fac[4];
-  unsigned long long clock = 0;
-  long long bytes = 0;
-  void *red = nullptr;        // reduction scratch
-  // optional per-pass timing: events recorded between the passes of each solve
-  bool timing = false;
-  std::vector<cudaEvent_t> ev;  // kTimedSolves x (kPasses + 1)
-  int nrec = 0;
-};
-static const int kPasses = 5, kTimedSolves = 256;
-
-// complex sequences per CTA: the largest power of two (<= 16) keeping the two FFT buffers
-// within 96 KB, so three CTAs fit an SM and the transposed x stores are >= 32-byte runs
-__host__ __device__ constexpr int ncx_for(int m, int cbytes) {
-  return (96 * 1024) / (2 * (m + 1) * cbytes) >= 16  ? 16
-         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 8 ? 8
-         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 4 ? 4
-         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 2 ? 2
-                                                      : 1;
-}
-
-template <typename T> DirParams make_params(const cans_plan *P, int d, int fwd) {
-  DirParams q;
-  memset(&q, 0, sizeof(q));
-  q.n = P->n[d];
-  q.nt = P->nt[d];
-  q.m = P->m[d];
-  q.kind = fwd ? P->kf[d] : P->kb[d];
-  q.pairs = (q.kind == K_REDFT11 || q.kind == K_RODFT11) ? 0 : 1;
-  q.ld = q.m + 1;
-  q.sld = q.nt + 1;
-  q.nstages = P->nstages[d];
-  for (int s = 0; s < 12; s++) q.radix[s] = P->radix[d][s];
-  q.tw = P->tab[d].tw;
-  q.post = P->tab[d].post;
-  q.pre = P->tab[d].pre;
-  q.ncx = ncx_for(q.m, (int)sizeof(cplx_t<T>));
-  q.lpb = q.pairs ? 2 * q.ncx : q.ncx;
-  return q;
-}
-
-// compile-time length used for a pass (0 = generic runtime path): power-of-two lengths of
-// the kinds that transform all n points with no extension
-static int spec_len(const DirParams &q) {
-  const bool pow2 = q.m >= 32 && q.m <= 1024 && (q.m & (q.m - 1)) == 0;
-  return (pow2 && q.pairs && q.nt == q.m && q.n == q.nt) ? q.m : 0;
-}
-
-template <typename T> size_t smem_bytes(const DirParams &q) {
-  const size_t a = (size_t)q.ncx * q.ld * sizeof(cplx_t<T>);
-  const size_t b = std::max(a, (size_t)q.lpb * q.sld * sizeof(T));
-  return a + b + (size_t)q.lpb * sizeof(T) + 64;
-}
-
-// ====================================================================================
-// kernels
-// ====================================================================================
-// Geometry of a pass: compile-time when M > 0 (then nt == n == m and the kind is a "pairs"
-// kind), from DirParams otherwise.
-template <typename T, int M> struct PassGeo {
-  static constexpr int NCX = M ? ncx_for(M, (int)sizeof(cplx_t<T>)) : 0;
-  static constexpr int LPB = 2 * NCX;
-  static constexpr int LD = M + 1;
-};
-
-// 1. x-forward: haloed rows -> S[k][i][j]
+// single-system pass kernels: one tile per CTA
 template <typename T, typename TF, int M>
 __global__ void __launch_bounds__(256) k_xfwd(const TF *__restrict__ p, T *__restrict__ S, int n1, int n2, DirParams P) {
-  using T2 = cplx_t<T>;
-  using G = PassGeo<T, M>;
   extern __shared__ __align__(16) unsigned char smem[];
-  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
-  T2 *A = reinterpret_cast<T2 *>(smem);
-  T2 *B = A + (size_t)ncx * ld;
-  T *stg = reinterpret_cast<T *>(B);
-  const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
-                                                                                      : (size_t)lpb * sld * sizeof(T);
-  T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
-  const int k = blockIdx.y, j0 = blockIdx.x * lpb;
-  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, i = e - r * nt, j = j0 + r;
-    stg[r * sld + i] = (j < n2) ? (T)p[hidx(i + 1, j + 1, k + 1, n1, n2)] : T(0);
-  }
-  if (!M && nt < n1)
-    for (int r = threadIdx.x; r < lpb; r += blockDim.x)
-      pass[r] = (j0 + r < n2) ? (T)p[hidx(n1, j0 + r + 1, k + 1, n1, n2)] : T(0);
-  __syncthreads();
-  r2r_pre<T, M>(P, stg, A);
-  __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
-  T *Sk = S + (size_t)k * n1 * n2;
-  for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
-    const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
-    if (j >= n2) continue;
-    Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M>(P, Z, r, i) : pass[r];
-  }
+  xfwd_tile<T, TF, M>(p, S, n1, n2, P, blockIdx.x, blockIdx.y, smem);
 }
 
-// 2./4. y pass, in place on contiguous lines S[l*n2 .. l*n2+n2-1], l = k*n1 + i
 template <typename T, int M>
 __global__ void __launch_bounds__(256) k_ylines(T *__restrict__ S, long nlines, int n2, DirParams P) {
-  using T2 = cplx_t<T>;
-  using G = PassGeo<T, M>;
   extern __shared__ __align__(16) unsigned char smem[];
-  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
-  T2 *A = reinterpret_cast<T2 *>(smem);
-  T2 *B = A + (size_t)ncx * ld;
-  T *stg = reinterpret_cast<T *>(B);
-  const long l0 = (long)blockIdx.x * lpb;
-  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
-    stg[r * sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
-  }
-  __syncthreads();
-  r2r_pre<T, M>(P, stg, A);
-  __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
-  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
-    if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M>(P, Z, r, j);
-  }
+  ylines_tile<T, M>(S, nlines, n2, P, blockIdx.x, smem);
 }
 
-// 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k) (written, or added when acc)
 template <typename T, typename TF, int M>
 __global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2, DirParams P,
                                               int acc) {
-  using T2 = cplx_t<T>;
-  using G = PassGeo<T, M>;
   extern __shared__ __align__(16) unsigned char smem[];
-  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
-  T2 *A = reinterpret_cast<T2 *>(smem);
-  T2 *B = A + (size_t)ncx * ld;
-  T *stg = reinterpret_cast<T *>(B);
-  const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
-                                                                                      : (size_t)lpb * sld * sizeof(T);
-  T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
-  const int k = blockIdx.y, j0 = blockIdx.x * lpb;
-  const T *Sk = S + (size_t)k * n1 * n2;
-  for (int e = threadIdx.x; e < nt * lpb; e += blockDim.x) {
-    const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
-    stg[r * sld + i] = (j < n2) ? Sk[(size_t)i * n2 + j] : T(0);
-  }
-  if (!M && nt < n1)
-    for (int r = threadIdx.x; r < lpb; r += blockDim.x)
-      pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
-  __syncthreads();
-  r2r_pre<T, M>(P, stg, A);
-  __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
-  for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
-    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / n1, i = e - r * n1, j = j0 + r;
-    if (j >= n2) continue;
-    const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-    const T val = (i < nt) ? r2r_post<T, M>(P, Z, r, i) : pass[r];
-    p[idx] = acc ? (TF)(p[idx] + (TF)val) : (TF)val;
-  }
+  xbwd_tile<T, TF, M>(S, p, n1, n2, P, acc, blockIdx.x, blockIdx.y, smem);
 }
 
 // z factorisation per spectral column (src/solver.f90:114-307 with the RHS-independent
@@ -608,7 +433,6 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
   }
 }
 
-// z solve, FP64 spectral data, in place
 __global__ void __launch_bounds__(128) k_zsolve64(double *__restrict__ S, const double *__restrict__ zinv,
                                                   const double *__restrict__ dd, const double *__restrict__ p2,
                                                   const double *__restrict__ dcl, const double *__restrict__ a,
@@ -616,28 +440,7 @@ __global__ void __launch_bounds__(128) k_zsolve64(double *__restrict__ S, const 
                                                   double norm) {
   const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
-  double y = 0.;
-  for (int k = 0; k < nn; k++) {
-    const size_t idx = (size_t)k * ncol + col;
-    y = (S[idx] * norm - a[k] * y) * zinv[idx];
-    S[idx] = y;
-  }
-  for (int k = nn - 2; k >= 0; k--) {
-    const size_t idx = (size_t)k * ncol + col;
-    y = S[idx] - dd[idx] * y;
-    S[idx] = y;
-  }
-  if (zper) {
-    const size_t iN = (size_t)nn * ncol + col;
-    const double den = dcl[col];
-    const double s1 = S[col], sn = S[(size_t)(nn - 1) * ncol + col];
-    const double pN = den == 0. ? 0. : (S[iN] * norm - c[nn] * s1 - a[nn] * sn) / den;
-    S[iN] = pN;
-    for (int k = 0; k < nn; k++) {
-      const size_t idx = (size_t)k * ncol + col;
-      S[idx] = S[idx] + p2[idx] * pN;
-    }
-  }
+  zsolve64_col(S, zinv, dd, p2, dcl, a, c, ncol, nn, zper, norm, col);
 }
 
 // ====================================================================================
@@ -677,7 +480,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   if (!P) return CANS_OK;
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
-  cudaFree(P->lamcol); cudaFree(P->a_d); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
+  cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
   cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
   delete P;
@@ -687,7 +490,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
 extern "C" long long cans_plan_device_bytes(const cans_plan *P) { return P ? P->bytes : 0; }
 
 // get (or build) the factorisation for the diagonal shift `key` (0 = Poisson: b as is)
-static int get_factor(cans_plan *P, double key, bool helm, Factor **out) {
+int get_factor(cans_plan *P, double key, bool helm, Factor **out) {
   const long ncol = (long)P->n[0] * P->n[1];
   const int nn = P->zper ? P->nn - 1 : P->nn;
   for (auto &f : P->fac)
@@ -968,6 +771,7 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
   const size_t esz = precision == CANS_FP64 ? sizeof(double) : sizeof(float);
   cudaError_t e;
   if ((e = cudaMalloc(&P->lamcol, lamcol.size() * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&P->zw, (n3 + 2) * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->a_d, n3 * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->b_d, n3 * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->c_d, n3 * sizeof(double))) != cudaSuccess ||
@@ -985,7 +789,10 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
     }
     P->bytes += (long long)(ncell * sizeof(double));
   }
-  if (cudaMemcpy(P->lamcol, lamcol.data(), lamcol.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+  // tridmatrix rows are D_k * (symmetric second difference): D = dzfi (centred) or dzci (faces)
+  const double *zw_h = c_or_f[2] == 'c' ? dzfi_g : dzci_g;
+  if (cudaMemcpy(P->zw, zw_h, (n3 + 2) * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(P->lamcol, lamcol.data(), lamcol.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(P->a_d, P->a_h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(P->b_d, P->b_h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(P->c_d, P->c_h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -997,6 +804,183 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
   Factor *F;
   if ((rc = get_factor(P, 0., false, &F))) return fail(rc);
   *plan = P;
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------ autotuner
+// Per direction of a plan, the tuner times the forward pass kernel of the plan on its own
+// spectral buffer for each candidate shape and keeps the fastest:
+//   - the compile-time kernel (power-of-two lengths) at its fixed lines per CTA;
+//   - the generic kernel with every distinct ordering of a few radix factorisations
+//     (radix-8 first, radix-4 first, small radices first, odd radices first) and lines per
+//     CTA from 1 to 32 that fit two CTAs per SM.
+// The choice changes only the order of the floating-point operations of the transform.
+// Results are kept per (precision, direction, n, nt, kinds) in a process-wide table, so
+// plans with the same transform (e.g. many boxes sharing a size along x or y) are measured
+// once, on the first of them tuned.
+namespace {
+struct TuneKey {
+  int prec, d, n, nt, kf, kb;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(prec, d, n, nt, kf, kb) < std::tie(o.prec, o.d, o.n, o.nt, o.kf, o.kb);
+  }
+};
+struct TuneVal {
+  int radix[12], nstages, ncx, nospec;
+  float ms;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune;
+
+std::vector<std::vector<int>> radix_orders(int m) {
+  std::vector<std::vector<int>> out;
+  auto add = [&](std::vector<int> v) {
+    if (v.empty() || v.size() > 12) return;
+    if (std::find(out.begin(), out.end(), v) == out.end()) out.push_back(v);
+  };
+  int r[12], ns = 0;
+  if (!factor_radices(m, r, &ns)) return out;
+  std::vector<int> base(r, r + ns);
+  add(base);
+  std::vector<int> rev(base.rbegin(), base.rend());
+  add(rev);
+  // radix-4 first: split the power of two into 4s (and one 2)
+  int mm = m, p2 = 0;
+  while (mm % 2 == 0) { mm /= 2; p2++; }
+  std::vector<int> f4;
+  for (int e = 0; e + 1 < p2; e += 2) f4.push_back(4);
+  if (p2 % 2) f4.push_back(2);
+  for (int q : {3, 5, 7}) while (mm % q == 0) { f4.push_back(q); mm /= q; }
+  add(f4);
+  // odd radices first, then the base's powers of two
+  std::vector<int> odd, even;
+  for (int x : base) (x % 2 ? odd : even).push_back(x);
+  std::vector<int> oe = odd;
+  oe.insert(oe.end(), even.begin(), even.end());
+  add(oe);
+  std::vector<int> f4o;
+  for (int x : f4) if (x % 2) f4o.push_back(x);
+  for (int x : f4) if (!(x % 2)) f4o.push_back(x);
+  add(f4o);
+  return out;
+}
+
+template <typename T> int time_pass(cans_plan *P, int d, const void *pin, float *ms) {
+  cudaEvent_t a, b;
+  CANS_CUDA_TRY(cudaEventCreate(&a));
+  CANS_CUDA_TRY(cudaEventCreate(&b));
+  const int reps = 4;
+  int rc = CANS_OK;
+  for (int it = 0; it < reps + 1 && !rc; it++) {
+    if (it == 1) cudaEventRecord(a, P->stream);
+    rc = d == 0 ? launch_xfwd<T, T>(P, (const T *)pin) : launch_y<T>(P, 1);
+  }
+  cudaEventRecord(b, P->stream);
+  cudaError_t e = cudaEventSynchronize(b);
+  float t = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  if (e != cudaSuccess) { cans_set_last_cuda_error(e); return CANS_ECUDA; }
+  *ms = t / reps;
+  return CANS_OK;
+}
+
+template <typename T> int tune_dir(cans_plan *P, int d, const void *pin, int force) {
+  const TuneKey key{P->precision, d, P->n[d], P->nt[d], P->kf[d], P->kb[d]};
+  if (!force) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      const TuneVal &v = it->second;
+      memcpy(P->radix[d], v.radix, sizeof(v.radix));
+      P->nstages[d] = v.nstages; P->ncx_tuned[d] = v.ncx; P->nospec[d] = v.nospec;
+      return CANS_OK;
+    }
+  }
+  const int m = P->m[d];
+  const size_t cb = sizeof(cplx_t<T>);
+  TuneVal best;
+  best.ms = FLT_MAX;
+  auto consider = [&](const std::vector<int> &order, int ncx, int nospec) -> int {
+    for (size_t e = 0; e < 12; e++) P->radix[d][e] = e < order.size() ? order[e] : 0;
+    P->nstages[d] = (int)order.size();
+    P->ncx_tuned[d] = ncx;
+    P->nospec[d] = nospec;
+    const DirParams q = make_params<T>(P, d, 1);
+    if (smem_bytes<T>(q) > 113 * 1024) return CANS_OK;  // keep two CTAs per SM
+    float ms = 0.f;
+    int rc = time_pass<T>(P, d, pin, &ms);
+    if (rc) return rc;
+    if (ms < best.ms) {
+      memcpy(best.radix, P->radix[d], sizeof(best.radix));
+      best.nstages = P->nstages[d]; best.ncx = ncx; best.nospec = nospec; best.ms = ms;
+    }
+    return CANS_OK;
+  };
+  const std::vector<std::vector<int>> orders = radix_orders(m);
+  if (orders.empty()) return CANS_ENOTSUP;
+  int rc;
+  // the compile-time kernel, when the length has one (default lines per CTA)
+  {
+    P->ncx_tuned[d] = 0;
+    P->nospec[d] = 0;
+    for (size_t e = 0; e < 12; e++) P->radix[d][e] = e < orders[0].size() ? orders[0][e] : 0;
+    P->nstages[d] = (int)orders[0].size();
+    if (make_params<T>(P, d, 1).spec && (rc = consider(orders[0], 0, 0))) return rc;
+  }
+  for (const auto &o : orders)
+    for (int ncx = 1; ncx <= 32; ncx *= 2) {
+      if ((size_t)2 * ncx * (m + 1) * cb > 112 * 1024) break;
+      if ((rc = consider(o, ncx, 1))) return rc;
+    }
+  memcpy(P->radix[d], best.radix, sizeof(best.radix));
+  P->nstages[d] = best.nstages; P->ncx_tuned[d] = best.ncx; P->nospec[d] = best.nospec;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tune[key] = best;
+  return CANS_OK;
+}
+}  // namespace
+
+extern "C" int cans_plan_autotune(cans_plan *P, int force, double ms_out[2]) {
+  if (!P) return CANS_EINVAL;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CANS_CUDA_TRY(cudaStreamIsCapturing(P->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return CANS_ENOTSUP;
+  const size_t esz = P->precision == CANS_FP64 ? sizeof(double) : sizeof(float);
+  const size_t cells = (size_t)(P->n[0] + 2) * (P->n[1] + 2) * (P->n[2] + 2);
+  void *pin = nullptr;
+  CANS_CUDA_TRY(cudaMalloc(&pin, cells * esz));
+  const size_t ncell = (size_t)P->n[0] * P->n[1] * P->n[2];
+  int rc = (cudaMemsetAsync(pin, 0, cells * esz, P->stream) == cudaSuccess &&
+            cudaMemsetAsync(P->S, 0, ncell * esz, P->stream) == cudaSuccess)
+               ? CANS_OK
+               : CANS_ECUDA;
+  for (int d = 0; d < 2 && !rc; d++)
+    rc = P->precision == CANS_FP64 ? tune_dir<double>(P, d, pin, force) : tune_dir<float>(P, d, pin, force);
+  cudaStreamSynchronize(P->stream);
+  cudaFree(pin);
+  if (rc) return rc;
+  if (ms_out) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    for (int d = 0; d < 2; d++) {
+      auto it = g_tune.find(TuneKey{P->precision, d, P->n[d], P->nt[d], P->kf[d], P->kb[d]});
+      ms_out[d] = it != g_tune.end() ? it->second.ms : 0.;
+    }
+  }
+  return CANS_OK;
+}
+
+// current shape choice of direction d: radix order (nstages entries), lines per CTA and
+// whether the compile-time kernel is used
+extern "C" int cans_plan_get_shape(const cans_plan *P, int d, int radix[12], int *nstages, int *ncx, int *spec) {
+  if (!P || d < 0 || d > 1) return CANS_EINVAL;
+  const DirParams q = P->precision == CANS_FP64 ? make_params<double>(P, d, 1) : make_params<float>(P, d, 1);
+  if (radix) memcpy(radix, q.radix, sizeof(q.radix));
+  if (nstages) *nstages = q.nstages;
+  if (ncx) *ncx = q.ncx;
+  if (spec) *spec = q.spec;
   return CANS_OK;
 }
 
@@ -1045,6 +1029,51 @@ extern "C" int cans_solve_helmholtz(cans_plan *P, double alpha, const int is_bou
   const double alphai = 1. / alpha;
   if (P->precision != CANS_FP64) return solve_impl<float, double>(P, p, alphai, true, P->normfft * alphai);
   return solve_impl<double, double>(P, p, alphai, true, P->normfft * alphai);
+}
+
+// ------------------------------------------------------------------ adjoint solves
+// The plan's solve is S = V_b T^-1 V_f (x/y transforms V, z tridiagonal T per spectral
+// column).  Every r2r pair on a uniform x/y grid is orthogonal up to a diagonal scaling in
+// mode space, which commutes with the column-wise T^-1, so V_b T^-1 V_f transposes to
+// V_b T^-T V_f.  T = D M with D diagonal (plan->zw) and M symmetric (also for the periodic
+// closure, and for the pinned zero mode, which solves the leading block and sets the last
+// row to zero), so T^-T = D^-1 T^-1 D and S^T = D^-1 S D: scale by D, solve, unscale.
+// Helmholtz: T + (1/alpha) I = D (M + (1/alpha) D^-1), the same relation.
+__global__ void k_zscale(double *p, int n1, int n2, int n3, const double *__restrict__ zw, int inv) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nx = n1, ny = n2;
+  if (t >= nx * ny * n3) return;
+  const int i = (int)(t % nx) + 1, j = (int)((t / nx) % ny) + 1, k = (int)(t / (nx * ny)) + 1;
+  const size_t c = hidx(i, j, k, n1, n2);
+  p[c] = inv ? p[c] / zw[k] : p[c] * zw[k];
+}
+
+static int zscale(cans_plan *P, double *p, int inv) {
+  const long cnt = (long)P->n[0] * P->n[1] * P->n[2];
+  k_zscale<<<(unsigned)((cnt + 255) / 256), 256, 0, P->stream>>>(p, P->n[0], P->n[1], P->n[2], P->zw, inv);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+extern "C" int cans_solver_adjoint(cans_plan *P, double *g) {
+  if (!P || !g) return CANS_EINVAL;
+  if (P->precision != CANS_FP64) return CANS_ENOTSUP;
+  int rc;
+  if ((rc = zscale(P, g, 0)) || (rc = solve_impl<double, double>(P, g, 0., false, P->normfft)) ||
+      (rc = zscale(P, g, 1)))
+    return rc;
+  return CANS_OK;
+}
+
+extern "C" int cans_solve_helmholtz_adjoint(cans_plan *P, double alpha, double *g) {
+  if (!P || !g || alpha == 0.) return CANS_EINVAL;
+  if (P->precision != CANS_FP64) return CANS_ENOTSUP;
+  const double alphai = 1. / alpha;
+  int rc;
+  if ((rc = zscale(P, g, 0)) || (rc = solve_impl<double, double>(P, g, alphai, true, P->normfft * alphai)) ||
+      (rc = zscale(P, g, 1)))
+    return rc;
+  return CANS_OK;
 }
 
 // ------------------------------------------------------------------ refinement support

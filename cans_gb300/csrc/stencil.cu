@@ -17,23 +17,12 @@
 #include <vector>
 
 #include "cans_internal.cuh"
+#include "bound_ops.h"
+#include "stencil_body.cuh"
 
 namespace {
 constexpr int kTB = 256;
 
-struct Dims {
-  int n1, n2, n3;
-};
-
-__device__ __forceinline__ bool cell3(long t, const Dims &d, int &i, int &j, int &k) {
-  const long nx = d.n1, ny = d.n2;
-  if (t >= nx * ny * d.n3) return false;
-  i = (int)(t % nx) + 1;
-  const long r = t / nx;
-  j = (int)(r % ny) + 1;
-  k = (int)(r / ny) + 1;
-  return true;
-}
 
 unsigned blocks_for(long count, int tb = kTB) { return (unsigned)((count + tb - 1) / tb); }
 }  // namespace
@@ -43,12 +32,7 @@ __global__ void __launch_bounds__(kTB) k_fillps(Dims d, double dti, double dtidx
                                                 const double *__restrict__ dzfi, const double *__restrict__ u,
                                                 const double *__restrict__ v, const double *__restrict__ w,
                                                 double *__restrict__ p) {
-  int i, j, k;
-  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
-  const int n1 = d.n1, n2 = d.n2;
-  const size_t c = hidx(i, j, k, n1, n2);
-  p[c] = ((w[c] - w[hidx(i, j, k - 1, n1, n2)]) * dti * dzfi[k] + (v[c] - v[hidx(i, j - 1, k, n1, n2)]) * dtidyi) +
-         (u[c] - u[hidx(i - 1, j, k, n1, n2)]) * dtidxi;
+  fillps_cell(d, dti, dtidxi, dtidyi, dzfi, u, v, w, p, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 extern "C" int cans_fillps(const int n[3], const double dli[3], const double *dzfi, double dti, const double *u,
@@ -67,16 +51,7 @@ __global__ void __launch_bounds__(kTB) k_correc(Dims d, double fi, double fj, do
                                                 const double *__restrict__ dzci, const double *__restrict__ p,
                                                 double *__restrict__ u, double *__restrict__ v,
                                                 double *__restrict__ w) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long nx = d.n1 + 2, ny = d.n2 + 2;
-  if (t >= nx * ny * (d.n3 + 2)) return;
-  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / (nx * ny));
-  const int n1 = d.n1, n2 = d.n2;
-  const size_t c = (size_t)t;
-  const double pc = p[c];
-  if (i <= d.n1) u[c] = u[c] - fi * (p[c + 1] - pc);
-  if (j <= d.n2) v[c] = v[c] - fj * (p[hidx(i, j + 1, k, n1, n2)] - pc);
-  if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * (p[hidx(i, j, k + 1, n1, n2)] - pc);
+  correc_cell(d, fi, fj, dt, dzci, p, u, v, w, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 extern "C" int cans_correc(const int n[3], const double dli[3], const double *dzci, double dt, const double *p,
@@ -93,21 +68,7 @@ extern "C" int cans_correc(const int n[3], const double dli[3], const double *dz
 __global__ void __launch_bounds__(kTB) k_updatep(Dims d, double dxi, double dyi, double alpha, int impl,
                                                  const double *__restrict__ dzci, const double *__restrict__ dzfi,
                                                  const double *__restrict__ pp, double *__restrict__ p) {
-  int i, j, k;
-  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
-  const int n1 = d.n1, n2 = d.n2;
-  const size_t c = hidx(i, j, k, n1, n2);
-  if (impl) {
-    const double ppc = pp[c];
-    double lap = 0.;
-    lap = lap + ((pp[c + 1] - 2. * ppc + pp[c - 1]) * (dxi * dxi) +
-                 (pp[hidx(i, j + 1, k, n1, n2)] - 2. * ppc + pp[hidx(i, j - 1, k, n1, n2)]) * (dyi * dyi));
-    lap = lap + ((pp[hidx(i, j, k + 1, n1, n2)] - ppc) * dzci[k] - (ppc - pp[hidx(i, j, k - 1, n1, n2)]) * dzci[k - 1]) *
-                    dzfi[k];
-    p[c] = p[c] + ppc + alpha * lap;
-  } else {
-    p[c] = p[c] + pp[c];
-  }
+  updatep_cell(d, dxi, dyi, alpha, impl, dzci, dzfi, pp, p, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 extern "C" int cans_updatep(const int n[3], const double dli[3], const double *dzci, const double *dzfi, double alpha,
@@ -133,71 +94,8 @@ __global__ void __launch_bounds__(kTB) k_mom_rk(Dims d, double dxi, double dyi, 
                                                 double *__restrict__ dudtrko, double *__restrict__ dvdtrko,
                                                 double *__restrict__ dwdtrko, double *__restrict__ unew,
                                                 double *__restrict__ dtd) {
-  int i, j, k;
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (!cell3(t, d, i, j, k)) return;
-  const int n1 = d.n1, n2 = d.n2;
-  const size_t np = (size_t)d.n1 * d.n2 * d.n3;
-  const size_t sx = 1, sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
-  const size_t c = hidx(i, j, k, n1, n2);
-  const double dzci_k = dzci[k], dzci_km = dzci[k - 1], dzfi_k = dzfi[k], dzfi_kp = dzfi[k + 1];
-  const double rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
-  const double u_ccm = u[c - sz], u_cmc = u[c - sy], u_mcc = u[c - sx], u_ccc = u[c], u_pcc = u[c + sx],
-               u_mpc = u[c - sx + sy], u_cpc = u[c + sy], u_cmp = u[c - sy + sz], u_mcp = u[c - sx + sz],
-               u_ccp = u[c + sz];
-  const double v_ccm = v[c - sz], v_pcm = v[c + sx - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx],
-               v_ccc = v[c], v_pcc = v[c + sx], v_cpc = v[c + sy], v_ccp = v[c + sz], v_cmp = v[c - sy + sz];
-  const double w_ccm = w[c - sz], w_pcm = w[c + sx - sz], w_cpm = w[c + sy - sz], w_cmc = w[c - sy], w_mcc = w[c - sx],
-               w_ccc = w[c], w_pcc = w[c + sx], w_cpc = w[c + sy], w_ccp = w[c + sz];
-  // x
-  const double dudxp = (u_pcc - u_ccc) * dxi, dudxm = (u_ccc - u_mcc) * dxi;
-  const double dudyp = (u_cpc - u_ccc) * dyi, dudym = (u_ccc - u_cmc) * dyi;
-  const double dudzp = (u_ccp - u_ccc) * dzci_k, dudzm = (u_ccc - u_ccm) * dzci_km;
-  const double uuip = 0.25 * (u_ccc + u_pcc) * u_pcc, uuim = 0.25 * (u_ccc + u_mcc) * u_mcc;
-  const double vujp = 0.25 * (v_ccc + v_pcc) * u_cpc, vujm = 0.25 * (v_cmc + v_pmc) * u_cmc;
-  const double wukp = 0.25 * (w_ccc + w_pcc) * u_ccp, wukm = 0.25 * (w_ccm + w_pcm) * u_ccm;
-  const double dudtd_xy = visc * (dudxp - dudxm) * dxi + visc * (dudyp - dudym) * dyi;
-  const double dudtd_z = visc * (dudzp - dudzm) * dzfi_k;
-  double dudt = -(uuip - uuim) * dxi - (vujp - vujm) * dyi - (wukp - wukm) * dzfi_k;
-  // y
-  const double dvdxp = (v_pcc - v_ccc) * dxi, dvdxm = (v_ccc - v_mcc) * dxi;
-  const double dvdyp = (v_cpc - v_ccc) * dyi, dvdym = (v_ccc - v_cmc) * dyi;
-  const double dvdzp = (v_ccp - v_ccc) * dzci_k, dvdzm = (v_ccc - v_ccm) * dzci_km;
-  const double uvip = 0.25 * (u_ccc + u_cpc) * v_pcc, uvim = 0.25 * (u_mcc + u_mpc) * v_mcc;
-  const double vvjp = 0.25 * (v_ccc + v_cpc) * v_cpc, vvjm = 0.25 * (v_ccc + v_cmc) * v_cmc;
-  const double wvkp = 0.25 * (w_ccc + w_cpc) * v_ccp, wvkm = 0.25 * (w_ccm + w_cpm) * v_ccm;
-  const double dvdtd_xy = visc * (dvdxp - dvdxm) * dxi + visc * (dvdyp - dvdym) * dyi;
-  const double dvdtd_z = visc * (dvdzp - dvdzm) * dzfi_k;
-  double dvdt = -(uvip - uvim) * dxi - (vvjp - vvjm) * dyi - (wvkp - wvkm) * dzfi_k;
-  // z
-  const double dwdxp = (w_pcc - w_ccc) * dxi, dwdxm = (w_ccc - w_mcc) * dxi;
-  const double dwdyp = (w_cpc - w_ccc) * dyi, dwdym = (w_ccc - w_cmc) * dyi;
-  const double dwdzp = (w_ccp - w_ccc) * dzfi_kp, dwdzm = (w_ccc - w_ccm) * dzfi_k;
-  const double uwip = 0.25 * (rdzm * u_ccc + rdzp * u_ccp) * w_pcc, uwim = 0.25 * (rdzm * u_mcc + rdzp * u_mcp) * w_mcc;
-  const double vwjp = 0.25 * (rdzm * v_ccc + rdzp * v_ccp) * w_cpc, vwjm = 0.25 * (rdzm * v_cmc + rdzp * v_cmp) * w_cmc;
-  const double wwkp = 0.25 * (w_ccc + w_ccp) * w_ccp, wwkm = 0.25 * (w_ccc + w_ccm) * w_ccm;
-  const double dwdtd_xy = visc * (dwdxp - dwdxm) * dxi + visc * (dwdyp - dwdym) * dyi;
-  const double dwdtd_z = visc * (dwdzp - dwdzm) * dzci_k;
-  double dwdt = -(uwip - uwim) * dxi - (vwjp - vwjm) * dyi - (wwkp - wwkm) * dzci_k;
-  double dud = 0., dvd = 0., dwd = 0.;
-  if (impdiff) {
-    dud = dudtd_xy + dudtd_z; dvd = dvdtd_xy + dvdtd_z; dwd = dwdtd_xy + dwdtd_z;
-  } else {
-    dudt = dudt + dudtd_xy + dudtd_z;
-    dvdt = dvdt + dvdtd_xy + dvdtd_z;
-    dwdt = dwdt + dwdtd_xy + dwdtd_z;
-  }
-  const size_t h = (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
-  const double pc = p[c];
-  double un = u_ccc + f1 * dudt + f2 * dudtrko[h] + f12 * (bfx - dxi * (p[c + sx] - pc));
-  double vn = v_ccc + f1 * dvdt + f2 * dvdtrko[h] + f12 * (bfy - dyi * (p[c + sy] - pc));
-  double wn = w_ccc + f1 * dwdt + f2 * dwdtrko[h] + f12 * (bfz - dzci_k * (p[c + sz] - pc));
-  if (impdiff) {
-    un = un + f12 * dud; vn = vn + f12 * dvd; wn = wn + f12 * dwd;
-    dtd[h] = dud; dtd[h + np] = dvd; dtd[h + 2 * np] = dwd;
-  }
-  dudtrko[h] = dudt; dvdtrko[h] = dvdt; dwdtrko[h] = dwdt;
-  unew[h] = un; unew[h + np] = vn; unew[h + 2 * np] = wn;
+  mom_rk_cell(d, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, impdiff, dzci, dzfi, u, v, w, p, dudtrko, dvdtrko, dwdtrko,
+              unew, dtd, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // copy-back of the new velocity with the per-block partial sums of the bulk means
@@ -368,59 +266,21 @@ extern "C" int cans_rk(const double rkpar[2], const int n[3], const double dli[3
 // ------------------------------------------------------------------------------ boundaries
 // periodic self-exchange (one GPU) along dir 1 (y) or 2 (z): full extent of the other dims
 __global__ void k_halo_copy(double *p, int n1, int n2, int n3, int dir, int up, int lo) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int e1 = n1 + 2, e2 = dir == 1 ? n3 + 2 : n2 + 2;
-  if (t >= (long)e1 * e2) return;
-  const int a = (int)(t % e1), b = (int)(t / e1);
-  if (dir == 1) {
-    if (up) p[hidx(a, n2 + 1, b, n1, n2)] = p[hidx(a, 1, b, n1, n2)];
-    if (lo) p[hidx(a, 0, b, n1, n2)] = p[hidx(a, n2, b, n1, n2)];
-  } else {
-    if (up) p[hidx(a, b, n3 + 1, n1, n2)] = p[hidx(a, b, 1, n1, n2)];
-    if (lo) p[hidx(a, b, 0, n1, n2)] = p[hidx(a, b, n3, n1, n2)];
-  }
+  halo_copy_cell(p, n1, n2, n3, dir, up, lo, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // set_bc (src/bound.f90:182-463), nh = 1
 __global__ void k_set_bc(double *p, int n1, int n2, int n3, char ctype, int ib, int dir, int centered, double factor,
                          double sgn) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int e1 = (dir == 0 ? n2 : n1) + 2, e2 = (dir == 2 ? n2 : n3) + 2;
-  if (t >= (long)e1 * e2) return;
-  const int b1 = (int)(t % e1), b2 = (int)(t / e1);
-  const int nn = dir == 0 ? n1 : (dir == 1 ? n2 : n3);
-  auto at = [&](int m) -> double & {
-    return dir == 0 ? p[hidx(m, b1, b2, n1, n2)] : (dir == 1 ? p[hidx(b1, m, b2, n1, n2)] : p[hidx(b1, b2, m, n1, n2)]);
-  };
-  if (ctype == 'P') {
-    if (ib == 0) at(0) = at(nn); else at(nn + 1) = at(1);
-  } else if (centered) {
-    if (ib == 0) at(0) = factor + sgn * at(1); else at(nn + 1) = factor + sgn * at(nn);
-  } else if (ctype == 'D') {
-    if (ib == 0) at(0) = factor;
-    else { at(nn + 1) = at(nn - 1); at(nn) = factor; }
-  } else {
-    if (ib == 0) at(0) = 1. * factor + at(1);
-    else { at(nn + 1) = at(nn); at(nn) = 1. * factor + at(nn - 1); }
-  }
+  set_bc_cell(p, n1, n2, n3, ctype, ib, dir, centered, factor, sgn, (long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-static int launch_set_bc(double *p, const int n[3], char ctype, int ib, int dir, int centered, double rvalue, double dr,
-                         cudaStream_t st) {
-  double factor = rvalue, sgn = 0.;
-  if (ctype == 'D' && centered) { factor = 2. * factor; sgn = -1.; }
-  if (ctype == 'N') { factor = ib == 0 ? -dr * factor : dr * factor; sgn = 1.; }
-  const long cnt = (long)((dir == 0 ? n[1] : n[0]) + 2) * ((dir == 2 ? n[1] : n[2]) + 2);
-  k_set_bc<<<blocks_for(cnt), kTB, 0, st>>>(p, n[0], n[1], n[2], ctype, ib, dir, centered, factor, sgn);
-  CANS_LAUNCH_CHECK();
-  return CANS_OK;
-}
-
-static int launch_halo(double *p, const int n[3], int dir, int side, cudaStream_t st) {
-  const int up = side == 2 || side == 1, lo = side == 2 || side == -1;
-  if (!(up || lo)) return CANS_OK;
-  const long cnt = (long)(n[0] + 2) * ((dir == 1 ? n[2] : n[1]) + 2);
-  k_halo_copy<<<blocks_for(cnt), kTB, 0, st>>>(p, n[0], n[1], n[2], dir, up, lo);
+static int launch_op(double *p, const int n[3], const BcOp &o, cudaStream_t st) {
+  const unsigned g = blocks_for(bc_op_cells(o, n));
+  if (o.op == 0)
+    k_set_bc<<<g, kTB, 0, st>>>(p, n[0], n[1], n[2], o.ctype, o.ib, o.dir, o.centered, o.factor, o.sgn);
+  else
+    k_halo_copy<<<g, kTB, 0, st>>>(p, n[0], n[1], n[2], o.dir, o.up, o.lo);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
@@ -434,38 +294,13 @@ extern "C" int cans_bounduvw(const char cbc[18], const int n[3], const double bc
                              double *w, int keep_norm, int halos_norm, int halos_tang, void *stream) {
   if (!cbc || !n || !bc || !is_bound || !dl || !dzc || !dzf || !u || !v || !w) return CANS_EINVAL;
   for (int e = 0; e < 18; e++) if (!bc_char_ok(cbc[e])) return CANS_EINVAL;
-  cudaStream_t st = as_stream(stream);
-  int updt_norm[2] = {1, 1};
-  if (halos_norm == -1) updt_norm[1] = 0;
-  else if (halos_norm == 0) updt_norm[0] = updt_norm[1] = 0;
-  else if (halos_norm == 1) updt_norm[0] = 0;
+  std::vector<BcOp> ops;
+  bounduvw_ops(cbc, n, bc, is_bound, dl, dzc, dzf, keep_norm, halos_norm, halos_tang, ops);
   double *f[3] = {u, v, w};
-  int rc;
-  for (int dd = 1; dd < 3; dd++)
-    for (int c = 0; c < 3; c++) {
-      const bool pp = cbc[2 * dd + 6 * c] == 'P' && cbc[1 + 2 * dd + 6 * c] == 'P';
-      if (!pp || is_bound[2 * dd] || is_bound[2 * dd + 1]) continue;
-      if ((rc = launch_halo(f[c], n, dd, c == dd ? halos_norm : halos_tang, st))) return rc;
-    }
-  for (int dd = 0; dd < 3; dd++)
-    for (int ib = 0; ib < 2; ib++) {
-      if (!is_bound[ib + 2 * dd]) continue;
-      const bool pp = cbc[2 * dd + 6 * dd] == 'P' && cbc[1 + 2 * dd + 6 * dd] == 'P';
-      const bool apply_norm = !keep_norm || (pp && updt_norm[ib]);
-      for (int c = 0; c < 3; c++) {
-        double dr;
-        if (dd < 2) dr = dl[dd];
-        else if (c == 2) dr = ib == 0 ? dzf[0] : dzf[n[2]];
-        else dr = ib == 0 ? dzc[0] : dzc[n[2]];
-        const char ct = cbc[ib + 2 * dd + 6 * c];
-        const double bv = bc[ib + 2 * dd + 6 * c];
-        if (c == dd) {
-          if (apply_norm && (rc = launch_set_bc(f[c], n, ct, ib, dd, 0, bv, dr, st))) return rc;
-        } else if ((rc = launch_set_bc(f[c], n, ct, ib, dd, 1, bv, dr, st))) {
-          return rc;
-        }
-      }
-    }
+  for (const BcOp &o : ops) {
+    const int rc = launch_op(f[o.field], n, o, as_stream(stream));
+    if (rc) return rc;
+  }
   return CANS_OK;
 }
 
@@ -474,23 +309,12 @@ extern "C" int cans_boundp(const char cbc[6], const int n[3], const double bc[6]
                            const double dl[3], const double *dzc, double *p, int halo_side, void *stream) {
   if (!cbc || !n || !bc || !is_bound || !dl || !dzc || !p) return CANS_EINVAL;
   for (int e = 0; e < 6; e++) if (!bc_char_ok(cbc[e])) return CANS_EINVAL;
-  cudaStream_t st = as_stream(stream);
-  int upd[2] = {1, 1};
-  if (halo_side == -1) upd[1] = 0;
-  else if (halo_side == 0) upd[0] = upd[1] = 0;
-  else if (halo_side == 1) upd[0] = 0;
-  int rc;
-  for (int dd = 1; dd < 3; dd++) {
-    const bool pp = cbc[2 * dd] == 'P' && cbc[2 * dd + 1] == 'P';
-    if (!pp || is_bound[2 * dd] || is_bound[2 * dd + 1]) continue;
-    if ((rc = launch_halo(p, n, dd, halo_side, st))) return rc;
+  std::vector<BcOp> ops;
+  boundp_ops(cbc, n, bc, is_bound, dl, dzc, halo_side, ops);
+  for (const BcOp &o : ops) {
+    const int rc = launch_op(p, n, o, as_stream(stream));
+    if (rc) return rc;
   }
-  for (int dd = 0; dd < 3; dd++)
-    for (int ib = 0; ib < 2; ib++) {
-      if (!is_bound[ib + 2 * dd] || !upd[ib]) continue;
-      const double dr = dd < 2 ? dl[dd] : (ib == 0 ? dzc[0] : dzc[n[2]]);
-      if ((rc = launch_set_bc(p, n, cbc[ib + 2 * dd], ib, dd, 1, bc[ib + 2 * dd], dr, st))) return rc;
-    }
   return CANS_OK;
 }
 

@@ -1,0 +1,183 @@
+// Per-cell bodies of the projection, momentum and boundary kernels, shared by the
+// single-box kernels (stencil.cu) and the batched box kernels (boxes.cu) so both run
+// the same arithmetic in the same order.
+#pragma once
+#include "cans_internal.cuh"
+
+struct Dims {
+  int n1, n2, n3;
+};
+
+// interior cell (i, j, k), 1-based, of flat index t (i fastest); false past the end
+__device__ __forceinline__ bool cell3(long t, const Dims &d, int &i, int &j, int &k) {
+  const long nx = d.n1, ny = d.n2;
+  if (t >= nx * ny * d.n3) return false;
+  i = (int)(t % nx) + 1;
+  const long r = t / nx;
+  j = (int)(r % ny) + 1;
+  k = (int)(r / ny) + 1;
+  return true;
+}
+
+// fillps (src/fillps.f90:13-51) at interior cell t
+__device__ __forceinline__ void fillps_cell(const Dims &d, double dti, double dtidxi, double dtidyi,
+                                            const double *__restrict__ dzfi, const double *__restrict__ u,
+                                            const double *__restrict__ v, const double *__restrict__ w,
+                                            double *__restrict__ p, long t) {
+  int i, j, k;
+  if (!cell3(t, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t c = hidx(i, j, k, n1, n2);
+  p[c] = ((w[c] - w[hidx(i, j, k - 1, n1, n2)]) * dti * dzfi[k] + (v[c] - v[hidx(i, j - 1, k, n1, n2)]) * dtidyi) +
+         (u[c] - u[hidx(i - 1, j, k, n1, n2)]) * dtidxi;
+}
+
+// correc (src/correc.f90:13-60) at haloed cell t
+__device__ __forceinline__ void correc_cell(const Dims &d, double fi, double fj, double dt,
+                                                const double *__restrict__ dzci, const double *__restrict__ p,
+                                                double *__restrict__ u, double *__restrict__ v,
+                                                double *__restrict__ w, long t) {
+  const long nx = d.n1 + 2, ny = d.n2 + 2;
+  if (t >= nx * ny * (d.n3 + 2)) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / (nx * ny));
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t c = (size_t)t;
+  const double pc = p[c];
+  if (i <= d.n1) u[c] = u[c] - fi * (p[c + 1] - pc);
+  if (j <= d.n2) v[c] = v[c] - fj * (p[hidx(i, j + 1, k, n1, n2)] - pc);
+  if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * (p[hidx(i, j, k + 1, n1, n2)] - pc);
+}
+
+// updatep (src/updatep.f90:14-88) at interior cell t
+__device__ __forceinline__ void updatep_cell(const Dims &d, double dxi, double dyi, double alpha, int impl,
+                                                 const double *__restrict__ dzci, const double *__restrict__ dzfi,
+                                                 const double *__restrict__ pp, double *__restrict__ p, long t) {
+  int i, j, k;
+  if (!cell3(t, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t c = hidx(i, j, k, n1, n2);
+  if (impl) {
+    const double ppc = pp[c];
+    double lap = 0.;
+    lap = lap + ((pp[c + 1] - 2. * ppc + pp[c - 1]) * (dxi * dxi) +
+                 (pp[hidx(i, j + 1, k, n1, n2)] - 2. * ppc + pp[hidx(i, j - 1, k, n1, n2)]) * (dyi * dyi));
+    lap = lap + ((pp[hidx(i, j, k + 1, n1, n2)] - ppc) * dzci[k] - (ppc - pp[hidx(i, j, k - 1, n1, n2)]) * dzci[k - 1]) *
+                    dzfi[k];
+    p[c] = p[c] + ppc + alpha * lap;
+  } else {
+    p[c] = p[c] + pp[c];
+  }
+}
+
+// mom_xyz_ad (src/mom.f90:771-1019) fused with the RK update of src/rk.f90:155-186 at
+// interior cell t: new velocity to unew (halo-free), dudtrko in place, dudtd to dtd (impdiff)
+__device__ __forceinline__ void mom_rk_cell(const Dims &d, double dxi, double dyi, double visc, double f1, double f2,
+                                                double f12, double bfx, double bfy, double bfz, int impdiff,
+                                                const double *__restrict__ dzci, const double *__restrict__ dzfi,
+                                                const double *__restrict__ u, const double *__restrict__ v,
+                                                const double *__restrict__ w, const double *__restrict__ p,
+                                                double *__restrict__ dudtrko, double *__restrict__ dvdtrko,
+                                                double *__restrict__ dwdtrko, double *__restrict__ unew,
+                                                double *__restrict__ dtd, long t) {
+  int i, j, k;
+  if (!cell3(t, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t np = (size_t)d.n1 * d.n2 * d.n3;
+  const size_t sx = 1, sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
+  const size_t c = hidx(i, j, k, n1, n2);
+  const double dzci_k = dzci[k], dzci_km = dzci[k - 1], dzfi_k = dzfi[k], dzfi_kp = dzfi[k + 1];
+  const double rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
+  const double u_ccm = u[c - sz], u_cmc = u[c - sy], u_mcc = u[c - sx], u_ccc = u[c], u_pcc = u[c + sx],
+               u_mpc = u[c - sx + sy], u_cpc = u[c + sy], u_cmp = u[c - sy + sz], u_mcp = u[c - sx + sz],
+               u_ccp = u[c + sz];
+  const double v_ccm = v[c - sz], v_pcm = v[c + sx - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx],
+               v_ccc = v[c], v_pcc = v[c + sx], v_cpc = v[c + sy], v_ccp = v[c + sz], v_cmp = v[c - sy + sz];
+  const double w_ccm = w[c - sz], w_pcm = w[c + sx - sz], w_cpm = w[c + sy - sz], w_cmc = w[c - sy], w_mcc = w[c - sx],
+               w_ccc = w[c], w_pcc = w[c + sx], w_cpc = w[c + sy], w_ccp = w[c + sz];
+  // x
+  const double dudxp = (u_pcc - u_ccc) * dxi, dudxm = (u_ccc - u_mcc) * dxi;
+  const double dudyp = (u_cpc - u_ccc) * dyi, dudym = (u_ccc - u_cmc) * dyi;
+  const double dudzp = (u_ccp - u_ccc) * dzci_k, dudzm = (u_ccc - u_ccm) * dzci_km;
+  const double uuip = 0.25 * (u_ccc + u_pcc) * u_pcc, uuim = 0.25 * (u_ccc + u_mcc) * u_mcc;
+  const double vujp = 0.25 * (v_ccc + v_pcc) * u_cpc, vujm = 0.25 * (v_cmc + v_pmc) * u_cmc;
+  const double wukp = 0.25 * (w_ccc + w_pcc) * u_ccp, wukm = 0.25 * (w_ccm + w_pcm) * u_ccm;
+  const double dudtd_xy = visc * (dudxp - dudxm) * dxi + visc * (dudyp - dudym) * dyi;
+  const double dudtd_z = visc * (dudzp - dudzm) * dzfi_k;
+  double dudt = -(uuip - uuim) * dxi - (vujp - vujm) * dyi - (wukp - wukm) * dzfi_k;
+  // y
+  const double dvdxp = (v_pcc - v_ccc) * dxi, dvdxm = (v_ccc - v_mcc) * dxi;
+  const double dvdyp = (v_cpc - v_ccc) * dyi, dvdym = (v_ccc - v_cmc) * dyi;
+  const double dvdzp = (v_ccp - v_ccc) * dzci_k, dvdzm = (v_ccc - v_ccm) * dzci_km;
+  const double uvip = 0.25 * (u_ccc + u_cpc) * v_pcc, uvim = 0.25 * (u_mcc + u_mpc) * v_mcc;
+  const double vvjp = 0.25 * (v_ccc + v_cpc) * v_cpc, vvjm = 0.25 * (v_ccc + v_cmc) * v_cmc;
+  const double wvkp = 0.25 * (w_ccc + w_cpc) * v_ccp, wvkm = 0.25 * (w_ccm + w_cpm) * v_ccm;
+  const double dvdtd_xy = visc * (dvdxp - dvdxm) * dxi + visc * (dvdyp - dvdym) * dyi;
+  const double dvdtd_z = visc * (dvdzp - dvdzm) * dzfi_k;
+  double dvdt = -(uvip - uvim) * dxi - (vvjp - vvjm) * dyi - (wvkp - wvkm) * dzfi_k;
+  // z
+  const double dwdxp = (w_pcc - w_ccc) * dxi, dwdxm = (w_ccc - w_mcc) * dxi;
+  const double dwdyp = (w_cpc - w_ccc) * dyi, dwdym = (w_ccc - w_cmc) * dyi;
+  const double dwdzp = (w_ccp - w_ccc) * dzfi_kp, dwdzm = (w_ccc - w_ccm) * dzfi_k;
+  const double uwip = 0.25 * (rdzm * u_ccc + rdzp * u_ccp) * w_pcc, uwim = 0.25 * (rdzm * u_mcc + rdzp * u_mcp) * w_mcc;
+  const double vwjp = 0.25 * (rdzm * v_ccc + rdzp * v_ccp) * w_cpc, vwjm = 0.25 * (rdzm * v_cmc + rdzp * v_cmp) * w_cmc;
+  const double wwkp = 0.25 * (w_ccc + w_ccp) * w_ccp, wwkm = 0.25 * (w_ccc + w_ccm) * w_ccm;
+  const double dwdtd_xy = visc * (dwdxp - dwdxm) * dxi + visc * (dwdyp - dwdym) * dyi;
+  const double dwdtd_z = visc * (dwdzp - dwdzm) * dzci_k;
+  double dwdt = -(uwip - uwim) * dxi - (vwjp - vwjm) * dyi - (wwkp - wwkm) * dzci_k;
+  double dud = 0., dvd = 0., dwd = 0.;
+  if (impdiff) {
+    dud = dudtd_xy + dudtd_z; dvd = dvdtd_xy + dvdtd_z; dwd = dwdtd_xy + dwdtd_z;
+  } else {
+    dudt = dudt + dudtd_xy + dudtd_z;
+    dvdt = dvdt + dvdtd_xy + dvdtd_z;
+    dwdt = dwdt + dwdtd_xy + dwdtd_z;
+  }
+  const size_t h = (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
+  const double pc = p[c];
+  double un = u_ccc + f1 * dudt + f2 * dudtrko[h] + f12 * (bfx - dxi * (p[c + sx] - pc));
+  double vn = v_ccc + f1 * dvdt + f2 * dvdtrko[h] + f12 * (bfy - dyi * (p[c + sy] - pc));
+  double wn = w_ccc + f1 * dwdt + f2 * dwdtrko[h] + f12 * (bfz - dzci_k * (p[c + sz] - pc));
+  if (impdiff) {
+    un = un + f12 * dud; vn = vn + f12 * dvd; wn = wn + f12 * dwd;
+    dtd[h] = dud; dtd[h + np] = dvd; dtd[h + 2 * np] = dwd;
+  }
+  dudtrko[h] = dudt; dvdtrko[h] = dvdt; dwdtrko[h] = dwdt;
+  unew[h] = un; unew[h + np] = vn; unew[h + 2 * np] = wn;
+}
+
+// periodic self-exchange along dir 1 (y) or 2 (z) at face cell t
+__device__ __forceinline__ void halo_copy_cell(double *p, int n1, int n2, int n3, int dir, int up, int lo, long t) {
+  const int e1 = n1 + 2, e2 = dir == 1 ? n3 + 2 : n2 + 2;
+  if (t >= (long)e1 * e2) return;
+  const int a = (int)(t % e1), b = (int)(t / e1);
+  if (dir == 1) {
+    if (up) p[hidx(a, n2 + 1, b, n1, n2)] = p[hidx(a, 1, b, n1, n2)];
+    if (lo) p[hidx(a, 0, b, n1, n2)] = p[hidx(a, n2, b, n1, n2)];
+  } else {
+    if (up) p[hidx(a, b, n3 + 1, n1, n2)] = p[hidx(a, b, 1, n1, n2)];
+    if (lo) p[hidx(a, b, 0, n1, n2)] = p[hidx(a, b, n3, n1, n2)];
+  }
+}
+
+// set_bc (src/bound.f90:182-463), nh = 1, at face cell t
+__device__ __forceinline__ void set_bc_cell(double *p, int n1, int n2, int n3, char ctype, int ib, int dir,
+                                            int centered, double factor, double sgn, long t) {
+  const int e1 = (dir == 0 ? n2 : n1) + 2, e2 = (dir == 2 ? n2 : n3) + 2;
+  if (t >= (long)e1 * e2) return;
+  const int b1 = (int)(t % e1), b2 = (int)(t / e1);
+  const int nn = dir == 0 ? n1 : (dir == 1 ? n2 : n3);
+  auto at = [&](int m) -> double & {
+    return dir == 0 ? p[hidx(m, b1, b2, n1, n2)] : (dir == 1 ? p[hidx(b1, m, b2, n1, n2)] : p[hidx(b1, b2, m, n1, n2)]);
+  };
+  if (ctype == 'P') {
+    if (ib == 0) at(0) = at(nn); else at(nn + 1) = at(1);
+  } else if (centered) {
+    if (ib == 0) at(0) = factor + sgn * at(1); else at(nn + 1) = factor + sgn * at(nn);
+  } else if (ctype == 'D') {
+    if (ib == 0) at(0) = factor;
+    else { at(nn + 1) = at(nn - 1); at(nn) = factor; }
+  } else {
+    if (ib == 0) at(0) = 1. * factor + at(1);
+    else { at(nn + 1) = at(nn); at(nn) = 1. * factor + at(nn - 1); }
+  }
+}

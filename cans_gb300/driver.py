@@ -137,3 +137,85 @@ class Simulation:
             if self.icheck > 0 and self.istep % self.icheck == 0:
                 self._new_dt()
                 self.divtot, self.divmax = cans.chkdiv(self.n, self.l, self.dli, self.dzfi, self.u, self.v, self.w)
+
+
+class Boxes:
+    """Many independent boxes advanced together (cans_boxes_*): the batched form of
+    `Simulation` for closed boxes with a fixed time step and implicit diffusion.
+
+    `cases`: list of dicts with the `Simulation` keys ng, l, gtype, gr, visci, dt_f, cbcvel,
+    bcvel, cbcpre, bcpre (and bforce).  Every box runs the call sequence of
+    `Simulation.substep` and evolves bit-identically to it; one stage of a substep is one
+    persistent launch over all boxes, and `step(use_graph=True)` replays one CUDA graph per
+    time step.  The boxes run on their own CUDA stream (`self.stream`)."""
+
+    def __init__(self, cases, is_impdiff=1, autotune=False, device="cuda"):
+        import torch
+        self.device = device
+        self.stream = torch.cuda.Stream(device=device)
+        self.boxes = []
+        self._keep = []
+        structs = (cans.CBox * len(cases))()
+        for b, case in enumerate(cases):
+            n = [int(x) for x in case["ng"]]
+            l = [float(x) for x in case["l"]]
+            zper = case["cbcpre"][4:6] == "PP"
+            dzc, dzf, zc, zf = initgrid(case.get("gtype", 1), n[2], case.get("gr", 0.), l[2], zper)
+            t = lambda a: torch.tensor(a, dtype=torch.float64, device=device)
+            box = dict(n=n, l=l, dzc=dzc, dzf=dzf, dzci=t(1. / dzc), dzfi=t(1. / dzf),
+                       u=cans.field(n, device), v=cans.field(n, device), w=cans.field(n, device),
+                       p=cans.field(n, device), pp=cans.field(n, device),
+                       dudtrko=torch.zeros((n[2], n[1], n[0]), dtype=torch.float64, device=device),
+                       dvdtrko=torch.zeros((n[2], n[1], n[0]), dtype=torch.float64, device=device),
+                       dwdtrko=torch.zeros((n[2], n[1], n[0]), dtype=torch.float64, device=device))
+            s = structs[b]
+            s.n[:] = n
+            s.l[:] = l
+            s.visc = 1. / case["visci"]
+            s.dt = float(case["dt_f"])
+            s.cbcvel = case["cbcvel"].encode()
+            s.cbcpre = case["cbcpre"].encode()
+            s.bcvel[:] = list(case.get("bcvel", [0.] * 18))
+            s.bcpre[:] = list(case.get("bcpre", [0.] * 6))
+            s.bforce[:] = list(case.get("bforce", [0.] * 3))
+            s.dzc_g = dzc.ctypes.data_as(cans._D)
+            s.dzf_g = dzf.ctypes.data_as(cans._D)
+            for name in ("dzci", "dzfi", "u", "v", "w", "p", "pp", "dudtrko", "dvdtrko", "dwdtrko"):
+                setattr(s, name, box[name].data_ptr())
+            self.boxes.append(box)
+        h = C.c_void_p()
+        rc = cans.lib().cans_boxes_create(len(cases), structs, int(is_impdiff), int(bool(autotune)),
+                                          C.c_void_p(self.stream.cuda_stream), C.byref(h))
+        if rc != 0:
+            raise cans.CansError(rc, "cans_boxes_create")
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and cans._lib is not None:
+            cans._lib.cans_boxes_destroy(h)
+            self._h = None
+
+    def _call(self, name, *args):
+        rc = getattr(cans.lib(), name)(self._h, *args)
+        if rc != 0:
+            raise cans.CansError(rc, name)
+
+    def start(self):
+        import torch
+        torch.cuda.synchronize()
+        self._call("cans_boxes_start")
+
+    def substep(self, irk):
+        self._call("cans_boxes_substep", int(irk))
+
+    def step(self, nsteps=1, use_graph=False):
+        for _ in range(nsteps):
+            self._call("cans_boxes_step", int(bool(use_graph)))
+
+    @property
+    def graph_nodes(self):
+        return cans.lib().cans_boxes_graph_nodes(self._h)
+
+    def synchronize(self):
+        self.stream.synchronize()

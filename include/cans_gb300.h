@@ -160,6 +160,125 @@ int cans_chkdt(const int n[3], const double dl[3], const double *dzci, const dou
 int cans_bulk_mean(const int n[3], const double *grid_vol_ratio, const double *p, double *mean,
                    void *stream);
 
+/* ---------------------------------------------------------------- adjoints
+ * No counterpart in the reference.  Transposed (vector-Jacobian) products of the FP64
+ * substep routines with explicit diffusion and no flow-rate forcing, for reverse-mode
+ * gradients.  Every adjoint argument g* is a device array laid out like the forward
+ * quantity it belongs to; "+=" arguments accumulate. */
+/* S^T g for the plan's solve S (cans_solver): g <- D^-1 S D g with D the diagonal of the
+ * z operator's symmetric factorisation (dzfi, or dzci for face-centred z); in place */
+int cans_solver_adjoint(cans_plan *plan, double *g);
+/* the same for the linear part of cans_solve_helmholtz (no boundary terms) */
+int cans_solve_helmholtz_adjoint(cans_plan *plan, double alpha, double *g);
+/* fillps^T: gu, gv, gw (haloed) += D^T gp (gp interior) */
+int cans_fillps_adjoint(const int n[3], const double dli[3], const double *dzfi, double dti,
+                        const double *gp, double *gu, double *gv, double *gw, void *stream);
+/* correc^T: gp (haloed) += G^T (gu, gv, gw); the velocity adjoints pass through */
+int cans_correc_adjoint(const int n[3], const double dli[3], const double *dzci, double dt,
+                        const double *gu, const double *gv, const double *gw, double *gp,
+                        void *stream);
+/* updatep^T (explicit: p += pp): gpp += gp on the interior; is_impdiff != 0: CANS_ENOTSUP */
+int cans_updatep_adjoint(const int n[3], int is_impdiff, const double *gp, double *gpp,
+                         void *stream);
+/* transposes of bounduvw / boundp (same arguments): ghost adjoints go back to the
+ * interior cells the ghosts were filled from, in reverse order, and are zeroed */
+int cans_bounduvw_adjoint(const char cbc[18], const int n[3], const double bc[18],
+                          const int is_bound[6], const double dl[3], const double *dzc,
+                          const double *dzf, double *gu, double *gv, double *gw, int keep_norm,
+                          int halos_norm, int halos_tang, void *stream);
+int cans_boundp_adjoint(const char cbc[6], const int n[3], const double bc[6],
+                        const int is_bound[6], const double dl[3], const double *dzc, double *gp,
+                        int halo_side, void *stream);
+/* rk^T (src/rk.f90:24 with mom_xyz_ad, explicit diffusion, is_forced = 0).  u, v, w: the
+ * velocity rk read (haloed).  In: gu, gv, gw = adjoint of the velocity after rk (haloed),
+ * gdu, gdv, gdw = adjoint of the dudtrko rk wrote.  Out, in place: the adjoints of the
+ * input velocity and of the input dudtrko; gp (haloed) += the pressure's; gbf[3] (host,
+ * may be NULL) += the uniform body force's (synchronises the stream).  work: device
+ * scratch of cans_rk_adjoint_work_doubles(n) doubles. */
+int cans_rk_adjoint(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                    const double *dzfi, double dt, double visc, const double *u, const double *v,
+                    const double *w, double *gu, double *gv, double *gw, double *gdu, double *gdv,
+                    double *gdw, double *gp, double gbf[3], double *work, void *stream);
+size_t cans_rk_adjoint_work_doubles(const int n[3]);
+
+/* ---------------------------------------------------------------- batched solves
+ * No counterpart in the reference (one box per run there).  A batch groups FP64 plans of
+ * independent systems -- boxes of uneven size, and per box e.g. the three velocity
+ * Helmholtz plans or the pressure plan -- and solves all of them with one persistent
+ * launch per pass (x-forward, y-forward, z, y-backward, x-backward) over the
+ * concatenated work of every system.  Each system uses its own plan's spectral buffer
+ * and factorisations, so a plan may appear in one batch once and must not be used on
+ * another stream while the batch runs. */
+typedef struct cans_batch cans_batch;
+
+/* Autotuner (no counterpart in the reference; cuFFT/FFTW choose their own plans there):
+ * times the plan's x and y transform kernels for each candidate shape -- the compile-time
+ * kernel of power-of-two lengths, and the generic kernel over radix orders x lines per CTA
+ * -- and keeps the fastest in the plan.  Results are remembered per (precision, direction,
+ * length, kinds) for the process, so plans sharing a transform are measured once, on the
+ * first one tuned (force != 0 measures again).  Only the order of the transform's floating-point operations changes.
+ * ms[2] (optional): the chosen x and y forward-pass times.  Synchronises the plan's
+ * stream; not allowed during stream capture. */
+int cans_plan_autotune(cans_plan *plan, int force, double ms[2]);
+/* current shape of direction d (0 x, 1 y): radix order, lines per CTA, compile-time length
+ * (0: generic kernel) */
+int cans_plan_get_shape(const cans_plan *plan, int d, int radix[12], int *nstages, int *ncx,
+                        int *spec);
+int cans_batch_create(int nsys, cans_plan *const *plans, void *stream, cans_batch **batch);
+int cans_batch_destroy(cans_batch *batch);
+/* System s, on the field p[s] (device, haloed):
+ *   alpha[s] != 0: cans_solve_helmholtz(plans[s], alpha[s], is_bound + 6*s, p[s])
+ *                  (src/solve_helmholtz.f90:28-75);
+ *   alpha[s] == 0: cans_updt_rhs_b(c_or_f, cbc, n, is_bound + 6*s, rhsb, p[s], 1, 0)
+ *                  followed by cans_solver(plans[s], p[s]) (src/bound.f90:514,
+ *                  src/solver_gpu.f90:34).
+ * alpha == NULL: every system is a Poisson solve; is_bound == NULL: no boundary terms.
+ * Results are bit-identical to those single calls.  The boundary terms are added while
+ * the x-forward pass loads the field (p itself is then overwritten by the solution).
+ * The first call with a given (p, alpha, is_bound) builds and caches a device work table
+ * (and the factorisations for new alphas); later calls with the same arguments launch
+ * the five pass kernels only, and may be captured into a CUDA graph.  A call during
+ * stream capture whose table is not cached returns CANS_ENOTSUP. */
+int cans_batch_solve(cans_batch *batch, double *const *p, const double *alpha,
+                     const int *is_bound);
+
+/* ---------------------------------------------------------------- batched boxes
+ * No counterpart in the reference.  Many independent boxes (e.g. closed boxes / lid-driven
+ * cavities of uneven size), each with its own grid, BCs, viscosity and fixed time step,
+ * advanced together: every stage of an RK3 substep (rk + mom, the velocity Helmholtz
+ * solves, bounduvw, fillps, updt_rhs_b + pressure solve, boundp, correc, updatep) is one
+ * persistent launch over all boxes, and a time step can be captured once as a CUDA graph.
+ * Each box evolves bit-identically to the single-box call sequence of src/main.f90:452-472
+ * with a fixed dt (dt_f) and no flow-rate forcing.  The caller owns the fields. */
+typedef struct cans_box {
+  int n[3];              /* interior cells */
+  double l[3];           /* domain lengths: dl = l/n, dli = 1/dl */
+  double visc, dt;       /* 1/Re and the fixed time step */
+  char cbcvel[18];       /* cbcvel(0:1,3,3) order */
+  char cbcpre[6];
+  double bcvel[18], bcpre[6], bforce[3];
+  const double *dzc_g, *dzf_g;  /* host z grid (0:n3+1), as cans_initgrid returns */
+  const double *dzci, *dzfi;    /* device 1/dzc, 1/dzf (0:n3+1) */
+  double *u, *v, *w, *p, *pp;   /* device haloed fields (n1+2)(n2+2)(n3+2) */
+  double *dudtrko, *dvdtrko, *dwdtrko;  /* device n1*n2*n3 */
+} cans_box;
+typedef struct cans_boxes cans_boxes;
+/* builds per box the pressure plan (and, when is_impdiff, the three velocity Helmholtz
+ * plans: c_or_f 'f' along the component), the device work lists of every stage and two
+ * solve batches; allocates 3 (6 with is_impdiff) doubles per cell of scratch */
+int cans_boxes_create(int nbox, const cans_box *boxes, int is_impdiff, int autotune,
+                      void *stream, cans_boxes **out);
+int cans_boxes_destroy(cans_boxes *boxes);
+/* bounduvw + boundp on the initial fields (src/main.f90:388-418) */
+int cans_boxes_start(cans_boxes *boxes);
+/* RK3 substep irk (0, 1, 2) of every box, asynchronous on the stream */
+int cans_boxes_substep(cans_boxes *boxes, int irk);
+/* one time step (three substeps).  use_graph != 0: the first call runs the step and
+ * captures it as a CUDA graph (needs a non-default stream); later calls replay the graph */
+int cans_boxes_step(cans_boxes *boxes, int use_graph);
+/* kernel nodes of the captured step graph (0 before capture) */
+long long cans_boxes_graph_nodes(const cans_boxes *boxes);
+
 #ifdef __cplusplus
 }
 #endif
