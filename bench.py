@@ -207,6 +207,9 @@ def bench_ours(args, rank, world):
            "e2e": e2e, "roofline": roof, "clocks": clk.summary(), "gpu_launches": launches}
     if rk3:
         out["rk3_step"] = rk3
+    if not args.skip_adjoint:
+        torch.cuda.empty_cache()
+        out["adjoint_duct"] = bench_adjoint(dev)
     if args.boxes > 0:
         torch.cuda.empty_cache()
         out["batched_boxes"] = bench_boxes(args.boxes, dev, max(1, min(args.steps, 5)),
@@ -387,6 +390,66 @@ def bench_boxes(nbox, dev, steps, autotune=True, unbatched_boxes=0):
     return out
 
 
+def bench_adjoint(dev, n=(256, 128, 128), nsteps=50, ckpt=10, ndir=8, seed=11):
+    """Square-duct differentiation workload: J = volume-integrated kinetic energy after
+    `nsteps` RK3 steps (explicit diffusion, fixed dt), dJ/d(initial velocity) and
+    dJ/d(uniform body force) by the hand-written adjoint with checkpoints every `ckpt`
+    steps, checked against central differences of the same model along `ndir` seeded
+    random directions (and the three body-force components)."""
+    import torch
+    from cans_gb300.adjoint import AdjointRun
+    l = (6.0, 2.0, 2.0)
+    dlmin = min(l[0] / n[0], l[1] / n[1], l[2] / n[2])
+    case = dict(ng=list(n), l=list(l), gtype=1, gr=0.0, cfl=0.5, dt_f=0.5 * dlmin / 2.35, visci=4410.0, icheck=0,
+                cbcvel="PPDDDD" * 3, bcvel=[0.0] * 18, cbcpre="PPNNNN", bcpre=[0.0] * 6, is_impdiff=0,
+                is_forced=[0, 0, 0])
+    y = (np.arange(n[1]) + 0.5) / n[1] * 2 - 1
+    z = (np.arange(n[2]) + 0.5) / n[2] * 2 - 1
+    rng = np.random.default_rng(seed)
+    prof = 2.25 * np.outer(1 - z ** 2, 1 - y ** 2)[:, :, None] * np.ones(n[0])[None, None, :]
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+    u0 = T(prof + 0.1 * rng.uniform(-1, 1, prof.shape))
+    v0 = T(0.1 * rng.uniform(-1, 1, prof.shape))
+    w0 = T(0.1 * rng.uniform(-1, 1, prof.shape))
+    bf = [0.01, 0.0, 0.0]
+    run = AdjointRun(case, device=dev, ckpt_every=ckpt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J = run.forward(u0, v0, w0, bf, nsteps)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    du, dv, dw, dbf = run.backward()
+    torch.cuda.synchronize()
+    t_bwd = time.perf_counter() - t0
+    errs = []
+    eps = 1e-5
+    for _ in range(ndir):
+        d = [T(rng.standard_normal(prof.shape)) for _ in range(3)]
+        ad = float(sum((g * di).sum() for g, di in zip((du, dv, dw), d)))
+        jp = run.forward(*[a + eps * di for a, di in zip((u0, v0, w0), d)], bf, nsteps)
+        jm = run.forward(*[a - eps * di for a, di in zip((u0, v0, w0), d)], bf, nsteps)
+        fd = (jp - jm) / (2 * eps)
+        errs.append(abs(fd - ad) / max(abs(fd), 1e-300))
+    bchk = {}
+    for c in range(3):
+        b = list(bf)
+        b[c] += eps
+        jp = run.forward(u0, v0, w0, b, nsteps)
+        b[c] -= 2 * eps
+        jm = run.forward(u0, v0, w0, b, nsteps)
+        fd = (jp - jm) / (2 * eps)
+        # y, z: a uniform force across walls is a gradient the projection absorbs (dJ = 0)
+        bchk["xyz"[c]] = {"fd": float(fd), "adjoint": float(dbf[c]),
+                          "rel_err": float(abs(fd - dbf[c]) / max(abs(fd), 1e-300)) if c == 0 else None}
+    return {"workload": f"duct_{n[0]}x{n[1]}x{n[2]}_ke_after_{nsteps}_rk3_steps_fp64", "J": J,
+            "forward_ms_per_step": round(t_fwd / nsteps * 1e3, 3),
+            "adjoint_ms_per_step": round(t_bwd / nsteps * 1e3, 3),
+            "adjoint_over_forward": round(t_bwd / t_fwd, 2), "checkpoint_every": ckpt,
+            "fd_directions": ndir, "fd_eps": eps, "max_rel_err_velocity": float(max(errs)),
+            "bforce_check": bchk, "clock": "host, synchronised"}
+
+
 def bench_cpu(size, steps, warmup, threads=None):
     """The oracle (CPU restatement of src/solver.f90 with FFTW r2r semantics), all host cores."""
     from oracle import oracle as O
@@ -423,6 +486,7 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--rtol", type=float, default=1e-13)
     ap.add_argument("--boxes", type=int, default=256, help="batched closed-box leg (0: skip)")
+    ap.add_argument("--skip-adjoint", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

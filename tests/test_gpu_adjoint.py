@@ -228,7 +228,14 @@ def test_energy_gradient_vs_finite_differences_and_oracle(require_gpu):
         eps = 1e-5
         jp = run.forward(u0, v0, w0, (bf.numpy() + eps * db).tolist(), nsteps)
         jm = run.forward(u0, v0, w0, (bf.numpy() - eps * db).tolist(), nsteps)
-        assert _close((jp - jm) / (2 * eps), gbf[c], 1e-6), (c, (jp - jm) / (2 * eps), gbf[c])
+        fd = (jp - jm) / (2 * eps)
+        if c == 0:
+            assert _close(fd, gbf[c], 1e-6), (c, fd, gbf[c])
+        else:
+            # a uniform force across the walled directions is a pure gradient, which the
+            # projection absorbs: dJ/dbf is zero there, the difference quotient is rounding
+            noise = 1e-15 * abs(float(J)) / eps * 100
+            assert abs(fd) <= noise and abs(gbf[c]) <= noise, (c, fd, gbf[c])
     # FP64 reference: central differences of the oracle's whole-run driver, one direction
     d = [torch.tensor(rng.standard_normal((n[2], n[1], n[0])), device="cuda") for _ in range(3)]
     ad = sum(_dot(g, di) for g, di in zip(grads, d))

@@ -143,9 +143,12 @@ def test_autotuned_plans_stay_exact_and_batched_matches(require_gpu):
             radix, ncx, spec = pl.shape(d)
             assert ncx >= 1 and (spec == 0 or spec in (32, 64, 128, 256, 512, 1024))
             assert int(np.prod(radix)) > 0
-    # pressure plan against the oracle (gauge-free comparison: singular NN problem)
+    # pressure plan against the oracle (consistent right-hand side of the singular NN
+    # problem, gauge-free comparison)
     ref = O.initsolver(n, bx["dli"], bx["dzci"], bx["dzfi"], CBCPRE, [0.0] * 6, "ccc")
     p = bx["fields"][3].copy(order="F")
+    wz = (1.0 / bx["dzfi"])[1:-1][None, None, :] * np.ones(n)
+    p[1:-1, 1:-1, 1:-1] -= (p[1:-1, 1:-1, 1:-1] * wz).sum() / wz.sum()
     rhs = p.copy(order="F")
     d = cans.to_device(rhs)
     O.solver(n, ref["normfft"], ref["lambdaxy"], ref["a"], ref["b"], ref["c"], CBCPRE, "ccc", p)
