@@ -126,8 +126,15 @@ def bench_ours(args, rank, world):
     dl = [L_CH[d] / n[d] for d in range(3)]
     dli = [1. / x for x in dl]
     dzc, dzf, zc, zf = initgrid(1, n[2], 1.4, L_CH[2], False)
-    if args.skip_fp64:  # profiling aid: only the FP32 + refinement leg
+    if args.skip_fp64 or args.only == "refined":  # profiling aid: only the FP32 + refinement leg
         return {"fp32_refined": bench_refined(args, n, dli, dzc, dzf, None, None, dev, world)}
+    if args.only == "rk3":
+        return {"rk3_step": bench_rk3(args.size, dev, max(1, min(args.steps, 5)))}
+    if args.only == "adjoint":
+        return {"adjoint_duct": bench_adjoint(dev, nsteps=args.adjoint_steps, ndir=args.adjoint_dirs)}
+    if args.only == "boxes":
+        return {"batched_boxes": bench_boxes(max(args.boxes, 1), dev, max(1, min(args.steps, 5)),
+                                             unbatched_boxes=0)}
     plan = cans.Plan(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc")
     p = make_rhs(n, dzf, dev)
     ncell = n[0] * n[1] * n[2]
@@ -209,7 +216,7 @@ def bench_ours(args, rank, world):
         out["rk3_step"] = rk3
     if not args.skip_adjoint:
         torch.cuda.empty_cache()
-        out["adjoint_duct"] = bench_adjoint(dev)
+        out["adjoint_duct"] = bench_adjoint(dev, nsteps=args.adjoint_steps, ndir=args.adjoint_dirs)
     if args.boxes > 0:
         torch.cuda.empty_cache()
         out["batched_boxes"] = bench_boxes(args.boxes, dev, max(1, min(args.steps, 5)),
@@ -487,6 +494,10 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-13)
     ap.add_argument("--boxes", type=int, default=256, help="batched closed-box leg (0: skip)")
     ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=50)
+    ap.add_argument("--adjoint-dirs", type=int, default=8)
+    ap.add_argument("--only", choices=["refined", "rk3", "adjoint", "boxes"], default=None,
+                    help="profiling aid: run one secondary leg and print its JSON")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

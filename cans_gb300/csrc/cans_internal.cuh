@@ -3,7 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/cans_gb300.h"
+#include "cans_gb300.h"
 
 #define CANS_CUDA_TRY(expr)                                  \
   do {                                                       \

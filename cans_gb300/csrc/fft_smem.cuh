@@ -131,7 +131,7 @@ __device__ __forceinline__ void fft_stage(const T2 *__restrict__ src, T2 *__rest
     for (int r = 0; r < R; ++r) {
       v[r] = s[jb + r * nb];
       if (r > 0 && Ns > 1) {
-        T2 w = __ldg(&tw[r * k * tws]);
+        T2 w = tw[r * k * tws];
         if (SIGN > 0) w.y = -w.y;
         v[r] = cmul(v[r], w);
       }
@@ -145,8 +145,7 @@ __device__ __forceinline__ void fft_stage(const T2 *__restrict__ src, T2 *__rest
 
 // batched complex FFT of the CTA's lines; data starts in A; returns the buffer holding the result
 template <int SIGN, typename T2>
-__device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P) {
-  const T2 *tw = reinterpret_cast<const T2 *>(P.tw);
+__device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P, const T2 *__restrict__ tw) {
   T2 *src = A, *dst = B;
   int Ns = 1;
   for (int s = 0; s < P.nstages; ++s) {
@@ -185,7 +184,7 @@ __device__ __forceinline__ void fft_stage_ct(const T2 *__restrict__ src, T2 *__r
     for (int r = 0; r < R; ++r) {
       v[r] = s[jb + r * NB];
       if (NS > 1 && r > 0) {
-        T2 w = __ldg(&tw[r * k * TWS]);
+        T2 w = tw[r * k * TWS];
         if (SIGN > 0) w.y = -w.y;
         v[r] = cmul(v[r], w);
       }
@@ -211,21 +210,22 @@ __device__ __forceinline__ T2 *fft_ct(T2 *src, T2 *dst, int nlines, const T2 *tw
 }
 
 // batched FFT: compile-time length M (power of two) or the generic runtime path (M == 0)
+// tw: the m twiddles exp(-2 pi i e/m) (the CTA's shared-memory copy)
 template <int M, int SIGN, typename T2>
-__device__ __forceinline__ T2 *fft_any(T2 *A, T2 *B, const DirParams &P) {
-  if constexpr (M > 0) return fft_ct<M, 1, SIGN>(A, B, P.ncx, reinterpret_cast<const T2 *>(P.tw));
-  else return fft_lines<SIGN>(A, B, P);
+__device__ __forceinline__ T2 *fft_any(T2 *A, T2 *B, const DirParams &P, const T2 *__restrict__ tw) {
+  if constexpr (M > 0) return fft_ct<M, 1, SIGN>(A, B, P.ncx, tw);
+  else return fft_lines<SIGN>(A, B, P, tw);
 }
 
 // ------------------------------------------------------------------------ r2r pre-processing
 // staging: real line r at stg[r*sld + i], i < nt.  Fills the complex sequences A[q*ld + k], k < m.
+// tab, pre: the CTA's copies of the plan's post and pre tables
 template <typename T, int M = 0>
-__device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict__ stg, cplx_t<T> *__restrict__ A) {
+__device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict__ stg, cplx_t<T> *__restrict__ A,
+                                        const cplx_t<T> *__restrict__ tab, const cplx_t<T> *__restrict__ pre) {
   using T2 = cplx_t<T>;
   // with a compile-time M the kinds handled have nt == n == m (no extension)
   const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? M + 1 : P.sld, ld = M ? M + 1 : P.ld;
-  const T2 *tab = reinterpret_cast<const T2 *>(P.post);
-  const T2 *pre = reinterpret_cast<const T2 *>(P.pre);
   const int total = P.ncx * m;
   for (int e = threadIdx.x; e < total; e += blockDim.x) {
     const int q = M ? (int)((unsigned)e / (unsigned)m) : e / m, k = e - q * m;
@@ -282,10 +282,10 @@ __device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict_
 // ----------------------------------------------------------------------- r2r post-processing
 // value of output index k (< nt) of real line r from the FFT result Z
 template <typename T, int M = 0>
-__device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__restrict__ Z, int r, int k) {
+__device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__restrict__ Z, int r, int k,
+                                      const cplx_t<T> *__restrict__ tab) {
   using T2 = cplx_t<T>;
   const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? M + 1 : P.ld;
-  const T2 *tab = reinterpret_cast<const T2 *>(P.post);
   if (!P.pairs) {  // kinds 11
     const T2 z = Z[r * ldz + k], w = tab[k];
     const T re = w.x * z.x - w.y * z.y, im = w.x * z.y + w.y * z.x;
@@ -325,5 +325,48 @@ __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__res
       const T2 a = L[k];
       return wsel == 0 ? a.x : a.y;
     }
+  }
+}
+
+// both real outputs (lines 2q and 2q+1) of output index k of a "pairs" kind, sharing the
+// loads of r2r_post (same arithmetic as r2r_post with r = 2q and r = 2q + 1)
+template <typename T, int M = 0>
+__device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *__restrict__ Z, int q, int k,
+                                          const cplx_t<T> *__restrict__ tab, T &v0, T &v1) {
+  using T2 = cplx_t<T>;
+  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? M + 1 : P.ld;
+  const T2 *L = Z + q * ldz;
+  switch (P.kind) {
+    case K_R2HC: {
+      const T2 a = L[k], b = L[M ? ((m - k) & (M - 1)) : ((m - k) % m)];
+      if (2 * k <= n) { v0 = T(0.5) * (a.x + b.x); v1 = T(0.5) * (a.y + b.y); }
+      else { v0 = T(0.5) * (b.y - a.y); v1 = T(0.5) * (a.x - b.x); }
+    } break;
+    case K_REDFT10:
+    case K_RODFT10: {
+      const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
+      const T2 a = L[kk], b = L[M ? ((m - kk) & (M - 1)) : ((m - kk) % m)], t = tab[kk];
+      const T c = t.x, s = -t.y;
+      v0 = c * (a.x + b.x) + s * (a.y - b.y);
+      v1 = c * (a.y + b.y) - s * (a.x - b.x);
+    } break;
+    case K_REDFT01:
+    case K_RODFT01: {
+      const int pos = (k & 1) == 0 ? (k >> 1) : n - 1 - ((k - 1) >> 1);
+      const T2 a = L[pos];
+      const bool neg = P.kind == K_RODFT01 && (k & 1);
+      v0 = neg ? -a.x : a.x;
+      v1 = neg ? -a.y : a.y;
+    } break;
+    case K_RODFT00: {
+      const T2 a = L[k + 1];
+      v0 = -a.y;
+      v1 = a.x;
+    } break;
+    default: {  // K_HC2R, K_REDFT00
+      const T2 a = L[k];
+      v0 = a.x;
+      v1 = a.y;
+    } break;
   }
 }

@@ -59,13 +59,17 @@ struct cans_plan {
 static const int kPasses = 5, kTimedSolves = 256;
 
 // complex sequences per CTA: the largest power of two (<= 16) keeping the two FFT buffers
-// within 96 KB, so three CTAs fit an SM and the transposed x stores are >= 32-byte runs
+// within a budget, so several CTAs share an SM and the transposed x stores are runs of
+// >= 32 bytes.  FP32 passes are latency-bound (integer/addressing work, not FP32 or HBM):
+// a 48 KB budget gives six resident CTAs per SM and measured 20% faster passes than 96 KB
+// at 512^3; the FP64 passes are FP64-pipe bound and keep 96 KB (fewer, wider tiles).
+__host__ __device__ constexpr int ncx_budget(int cbytes) { return cbytes <= 8 ? 48 * 1024 : 96 * 1024; }
 __host__ __device__ constexpr int ncx_for(int m, int cbytes) {
-  return (96 * 1024) / (2 * (m + 1) * cbytes) >= 16  ? 16
-         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 8 ? 8
-         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 4 ? 4
-         : (96 * 1024) / (2 * (m + 1) * cbytes) >= 2 ? 2
-                                                      : 1;
+  return ncx_budget(cbytes) / (2 * (m + 1) * cbytes) >= 16  ? 16
+         : ncx_budget(cbytes) / (2 * (m + 1) * cbytes) >= 8 ? 8
+         : ncx_budget(cbytes) / (2 * (m + 1) * cbytes) >= 4 ? 4
+         : ncx_budget(cbytes) / (2 * (m + 1) * cbytes) >= 2 ? 2
+                                                            : 1;
 }
 
 template <typename T> inline DirParams make_params(const cans_plan *P, int d, int fwd) {
@@ -112,10 +116,36 @@ __device__ __forceinline__ double face_add(double x, int i, int j, int k, const 
   return x;
 }
 
+// shared memory of a pass tile: FFT buffers A and B (B doubles as the real staging
+// array), the pass-through row, then the CTA's copies of the twiddle tables (m twiddles,
+// nt post, nt pre entries) at a 16-byte aligned offset
+template <typename T>
+__host__ __device__ inline size_t tile_tables_offset(int ncx, int ld, int lpb, int sld) {
+  const size_t a = (size_t)ncx * ld * sizeof(cplx_t<T>);
+  const size_t b = a > (size_t)lpb * sld * sizeof(T) ? a : (size_t)lpb * sld * sizeof(T);
+  return (a + b + (size_t)lpb * sizeof(T) + 15) & ~(size_t)15;
+}
 template <typename T> inline size_t smem_bytes(const DirParams &q) {
-  const size_t a = (size_t)q.ncx * q.ld * sizeof(cplx_t<T>);
-  const size_t b = std::max(a, (size_t)q.lpb * q.sld * sizeof(T));
-  return a + b + (size_t)q.lpb * sizeof(T) + 64;
+  return tile_tables_offset<T>(q.ncx, q.ld, q.lpb, q.sld) + (size_t)(q.m + 2 * q.nt) * sizeof(cplx_t<T>) + 16;
+}
+
+// copy the twiddle tables a pass uses into shared memory (before the tile's first barrier)
+template <typename T>
+__device__ __forceinline__ void copy_tables(const DirParams &P, int m, int nt, cplx_t<T> *tw, cplx_t<T> *post,
+                                            cplx_t<T> *pre) {
+  using T2 = cplx_t<T>;
+  const T2 *gtw = reinterpret_cast<const T2 *>(P.tw);
+  for (int e = threadIdx.x; e < m; e += blockDim.x) tw[e] = gtw[e];
+  const int kd = P.kind;
+  if (kd == K_REDFT10 || kd == K_RODFT10 || kd == K_REDFT01 || kd == K_RODFT01 || kd == K_REDFT11 ||
+      kd == K_RODFT11) {
+    const T2 *gp = reinterpret_cast<const T2 *>(P.post);
+    for (int e = threadIdx.x; e < nt; e += blockDim.x) post[e] = gp[e];
+  }
+  if (kd == K_REDFT11 || kd == K_RODFT11) {
+    const T2 *gq = reinterpret_cast<const T2 *>(P.pre);
+    for (int e = threadIdx.x; e < nt; e += blockDim.x) pre[e] = gq[e];
+  }
 }
 
 // get (or build) the z factorisation of plan P for the diagonal shift `key`
@@ -137,13 +167,15 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld, m = M ? M : P.m;
   T2 *A = reinterpret_cast<T2 *>(smem);
   T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
   const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
                                                                                       : (size_t)lpb * sld * sizeof(T);
   T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
+  T2 *tw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
+  T2 *post = tw + m, *pre = post + nt;
   const int j0 = tile * lpb;
   for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
     const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, i = e - r * nt, j = j0 + r;
@@ -159,15 +191,30 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
       else
         pass[r] = (j0 + r < n2) ? (T)p[hidx(n1, j0 + r + 1, k + 1, n1, n2)] : T(0);
     }
+  copy_tables<T>(P, m, nt, tw, post, pre);
   __syncthreads();
-  r2r_pre<T, M>(P, stg, A);
+  r2r_pre<T, M>(P, stg, A, post, pre);
   __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P, tw) : fft_any<M, -1>(A, B, P, tw);
   T *Sk = S + (size_t)k * n1 * n2;
-  for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
-    const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
-    if (j >= n2) continue;
-    Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M>(P, Z, r, i) : pass[r];
+  if (P.pairs) {
+    // both lines of a complex sequence per thread: runs of 2*ncx values along j per row i
+    for (int e = threadIdx.x; e < n1 * ncx; e += blockDim.x) {
+      const int i = M ? (int)((unsigned)e / (unsigned)G::NCX) : e / ncx, q = e - i * ncx, j = j0 + 2 * q;
+      if (j >= n2) continue;
+      T v0, v1;
+      if (i < nt) r2r_post2<T, M>(P, Z, q, i, post, v0, v1);
+      else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
+      T *dst = Sk + (size_t)i * n2 + j;
+      dst[0] = v0;
+      if (j + 1 < n2) dst[1] = v1;
+    }
+  } else {
+    for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
+      const int i = e / lpb, r = e - i * lpb, j = j0 + r;
+      if (j >= n2) continue;
+      Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M>(P, Z, r, i, post) : pass[r];
+    }
   }
 }
 
@@ -178,22 +225,37 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld, m = M ? M : P.m;
   T2 *A = reinterpret_cast<T2 *>(smem);
   T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
+  T2 *tw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
+  T2 *post = tw + m, *pre = post + nt;
   const long l0 = tile * lpb;
   for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
     const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
     stg[r * sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
   }
+  copy_tables<T>(P, m, nt, tw, post, pre);
   __syncthreads();
-  r2r_pre<T, M>(P, stg, A);
+  r2r_pre<T, M>(P, stg, A, post, pre);
   __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
-  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
-    if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M>(P, Z, r, j);
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P, tw) : fft_any<M, -1>(A, B, P, tw);
+  if (P.pairs) {
+    for (int e = threadIdx.x; e < ncx * nt; e += blockDim.x) {
+      const int q = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - q * nt;
+      const long l = l0 + 2 * q;
+      if (l >= nlines) continue;
+      T v0, v1;
+      r2r_post2<T, M>(P, Z, q, j, post, v0, v1);
+      S[(size_t)l * n2 + j] = v0;
+      if (l + 1 < nlines) S[(size_t)(l + 1) * n2 + j] = v1;
+    }
+  } else {
+    for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+      const int r = e / nt, j = e - r * nt;
+      if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M>(P, Z, r, j, post);
+    }
   }
 }
 
@@ -204,13 +266,15 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld;
+  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld, m = M ? M : P.m;
   T2 *A = reinterpret_cast<T2 *>(smem);
   T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
   const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
                                                                                       : (size_t)lpb * sld * sizeof(T);
   T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
+  T2 *tw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
+  T2 *post = tw + m, *pre = post + nt;
   const int j0 = tile * lpb;
   const T *Sk = S + (size_t)k * n1 * n2;
   for (int e = threadIdx.x; e < nt * lpb; e += blockDim.x) {
@@ -220,16 +284,33 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
   if (!M && nt < n1)
     for (int r = threadIdx.x; r < lpb; r += blockDim.x)
       pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
+  copy_tables<T>(P, m, nt, tw, post, pre);
   __syncthreads();
-  r2r_pre<T, M>(P, stg, A);
+  r2r_pre<T, M>(P, stg, A, post, pre);
   __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P) : fft_any<M, -1>(A, B, P);
-  for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
-    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / n1, i = e - r * n1, j = j0 + r;
-    if (j >= n2) continue;
-    const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-    const T val = (i < nt) ? r2r_post<T, M>(P, Z, r, i) : pass[r];
-    p[idx] = acc ? (TF)(p[idx] + (TF)val) : (TF)val;
+  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P, tw) : fft_any<M, -1>(A, B, P, tw);
+  if (P.pairs) {
+    for (int e = threadIdx.x; e < ncx * n1; e += blockDim.x) {
+      const int q = M ? (int)((unsigned)e / (unsigned)M) : e / n1, i = e - q * n1, j = j0 + 2 * q;
+      if (j >= n2) continue;
+      T v0, v1;
+      if (i < nt) r2r_post2<T, M>(P, Z, q, i, post, v0, v1);
+      else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
+      const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+      p[idx] = acc ? (TF)(p[idx] + (TF)v0) : (TF)v0;
+      if (j + 1 < n2) {
+        const size_t idx1 = idx + (size_t)(n1 + 2);
+        p[idx1] = acc ? (TF)(p[idx1] + (TF)v1) : (TF)v1;
+      }
+    }
+  } else {
+    for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
+      const int r = e / n1, i = e - r * n1, j = j0 + r;
+      if (j >= n2) continue;
+      const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+      const T val = (i < nt) ? r2r_post<T, M>(P, Z, r, i, post) : pass[r];
+      p[idx] = acc ? (TF)(p[idx] + (TF)val) : (TF)val;
+    }
   }
 }
 
