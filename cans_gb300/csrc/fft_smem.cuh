@@ -165,6 +165,13 @@ __device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P, const T2 *__restrict_
   return src;
 }
 
+// Shared-memory position of complex element x of a line in the compile-time path: one
+// padding element every 16 breaks the power-of-two strides of the Stockham stores
+// (stride R between neighbouring threads in the first stage), which would otherwise put
+// 16 threads of a warp on the same bank pair.  Line stride: M + M/16 + 1.
+template <int M> __host__ __device__ constexpr int spad(int x) { return M > 0 ? x + (x >> 4) : x; }
+template <int M> __host__ __device__ constexpr int sline(int m) { return M > 0 ? M + M / 16 + 1 : m + 1; }
+
 // ---------------------------------------------------------------- compile-time lengths
 // For power-of-two lengths the stage geometry is a compile-time constant: the butterfly and
 // output indices become shifts and masks instead of runtime divisions (which dominate the
@@ -172,7 +179,7 @@ __device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P, const T2 *__restrict_
 template <int R, int SIGN, int M, int NS, typename T2>
 __device__ __forceinline__ void fft_stage_ct(const T2 *__restrict__ src, T2 *__restrict__ dst, int nlines,
                                              const T2 *__restrict__ tw) {
-  constexpr int NB = M / R, LD = M + 1, TWS = M / (NS * R);
+  constexpr int NB = M / R, LD = sline<M>(M), TWS = M / (NS * R);
   const unsigned total = (unsigned)(NB * nlines);
   for (unsigned b = threadIdx.x; b < total; b += blockDim.x) {
     const unsigned line = b / NB, jb = b % NB;
@@ -182,7 +189,7 @@ __device__ __forceinline__ void fft_stage_ct(const T2 *__restrict__ src, T2 *__r
     T2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      v[r] = s[jb + r * NB];
+      v[r] = s[spad<M>(jb + r * NB)];
       if (NS > 1 && r > 0) {
         T2 w = tw[r * k * TWS];
         if (SIGN > 0) w.y = -w.y;
@@ -192,7 +199,7 @@ __device__ __forceinline__ void fft_stage_ct(const T2 *__restrict__ src, T2 *__r
     dft<R, SIGN>(v);
     const unsigned idxD = (jb / NS) * (NS * R) + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[idxD + r * NS] = v[r];
+    for (int r = 0; r < R; ++r) d[spad<M>(idxD + r * NS)] = v[r];
   }
 }
 
@@ -225,7 +232,7 @@ __device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict_
                                         const cplx_t<T> *__restrict__ tab, const cplx_t<T> *__restrict__ pre) {
   using T2 = cplx_t<T>;
   // with a compile-time M the kinds handled have nt == n == m (no extension)
-  const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? M + 1 : P.sld, ld = M ? M + 1 : P.ld;
+  const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? M + 1 : P.sld, ld = M ? sline<M>(M) : P.ld;
   const int total = P.ncx * m;
   for (int e = threadIdx.x; e < total; e += blockDim.x) {
     const int q = M ? (int)((unsigned)e / (unsigned)m) : e / m, k = e - q * m;
@@ -275,7 +282,7 @@ __device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict_
         else z = cmk<T2>(T(0), T(0));
       } break;
     }
-    A[q * ld + k] = z;
+    A[q * ld + spad<M>(k)] = z;
   }
 }
 
@@ -285,7 +292,7 @@ template <typename T, int M = 0>
 __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__restrict__ Z, int r, int k,
                                       const cplx_t<T> *__restrict__ tab) {
   using T2 = cplx_t<T>;
-  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? M + 1 : P.ld;
+  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? sline<M>(M) : P.ld;
   if (!P.pairs) {  // kinds 11
     const T2 z = Z[r * ldz + k], w = tab[k];
     const T re = w.x * z.x - w.y * z.y, im = w.x * z.y + w.y * z.x;
@@ -295,34 +302,34 @@ __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__res
   const T2 *L = Z + q * ldz;
   switch (P.kind) {
     case K_R2HC: {
-      const T2 a = L[k], b = L[M ? ((m - k) & (M - 1)) : ((m - k) % m)];
+      const T2 a = L[spad<M>(k)], b = L[spad<M>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
       if (2 * k <= n) return wsel == 0 ? T(0.5) * (a.x + b.x) : T(0.5) * (a.y + b.y);
       return wsel == 0 ? T(0.5) * (b.y - a.y) : T(0.5) * (a.x - b.x);
     }
     case K_REDFT10:
     case K_RODFT10: {
       const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
-      const T2 a = L[kk], b = L[M ? ((m - kk) & (M - 1)) : ((m - kk) % m)], t = tab[kk];
+      const T2 a = L[spad<M>(kk)], b = L[spad<M>(M ? ((m - kk) & (M - 1)) : ((m - kk) % m))], t = tab[kk];
       const T c = t.x, s = -t.y;
       return wsel == 0 ? c * (a.x + b.x) + s * (a.y - b.y) : c * (a.y + b.y) - s * (a.x - b.x);
     }
     case K_HC2R: {
-      const T2 a = L[k];
+      const T2 a = L[spad<M>(k)];
       return wsel == 0 ? a.x : a.y;
     }
     case K_REDFT01:
     case K_RODFT01: {
       const int pos = (k & 1) == 0 ? (k >> 1) : n - 1 - ((k - 1) >> 1);
-      const T2 a = L[pos];
+      const T2 a = L[spad<M>(pos)];
       const T v = wsel == 0 ? a.x : a.y;
       return (P.kind == K_RODFT01 && (k & 1)) ? -v : v;
     }
     case K_RODFT00: {
-      const T2 a = L[k + 1];
+      const T2 a = L[spad<M>(k + 1)];
       return wsel == 0 ? -a.y : a.x;
     }
     default: {  // K_REDFT00
-      const T2 a = L[k];
+      const T2 a = L[spad<M>(k)];
       return wsel == 0 ? a.x : a.y;
     }
   }
@@ -334,18 +341,18 @@ template <typename T, int M = 0>
 __device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *__restrict__ Z, int q, int k,
                                           const cplx_t<T> *__restrict__ tab, T &v0, T &v1) {
   using T2 = cplx_t<T>;
-  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? M + 1 : P.ld;
+  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? sline<M>(M) : P.ld;
   const T2 *L = Z + q * ldz;
   switch (P.kind) {
     case K_R2HC: {
-      const T2 a = L[k], b = L[M ? ((m - k) & (M - 1)) : ((m - k) % m)];
+      const T2 a = L[spad<M>(k)], b = L[spad<M>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
       if (2 * k <= n) { v0 = T(0.5) * (a.x + b.x); v1 = T(0.5) * (a.y + b.y); }
       else { v0 = T(0.5) * (b.y - a.y); v1 = T(0.5) * (a.x - b.x); }
     } break;
     case K_REDFT10:
     case K_RODFT10: {
       const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
-      const T2 a = L[kk], b = L[M ? ((m - kk) & (M - 1)) : ((m - kk) % m)], t = tab[kk];
+      const T2 a = L[spad<M>(kk)], b = L[spad<M>(M ? ((m - kk) & (M - 1)) : ((m - kk) % m))], t = tab[kk];
       const T c = t.x, s = -t.y;
       v0 = c * (a.x + b.x) + s * (a.y - b.y);
       v1 = c * (a.y + b.y) - s * (a.x - b.x);
@@ -353,18 +360,18 @@ __device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *_
     case K_REDFT01:
     case K_RODFT01: {
       const int pos = (k & 1) == 0 ? (k >> 1) : n - 1 - ((k - 1) >> 1);
-      const T2 a = L[pos];
+      const T2 a = L[spad<M>(pos)];
       const bool neg = P.kind == K_RODFT01 && (k & 1);
       v0 = neg ? -a.x : a.x;
       v1 = neg ? -a.y : a.y;
     } break;
     case K_RODFT00: {
-      const T2 a = L[k + 1];
+      const T2 a = L[spad<M>(k + 1)];
       v0 = -a.y;
       v1 = a.x;
     } break;
     default: {  // K_HC2R, K_REDFT00
-      const T2 a = L[k];
+      const T2 a = L[spad<M>(k)];
       v0 = a.x;
       v1 = a.y;
     } break;

@@ -94,6 +94,7 @@ template <typename T> inline DirParams make_params(const cans_plan *P, int d, in
   // no extension, at the default lines per CTA); 0 = generic runtime path
   const bool pow2 = q.m >= 32 && q.m <= 1024 && (q.m & (q.m - 1)) == 0;
   q.spec = (pow2 && q.pairs && q.nt == q.m && q.n == q.nt && q.ncx == ncx0 && !P->nospec[d]) ? q.m : 0;
+  if (q.spec) q.ld = q.m + q.m / 16 + 1;  // padded complex lines of the compile-time path (sline)
   return q;
 }
 
@@ -156,7 +157,8 @@ int get_factor(cans_plan *P, double key, bool helm, Factor **out);
 template <typename T, int M> struct PassGeo {
   static constexpr int NCX = M ? ncx_for(M, (int)sizeof(cplx_t<T>)) : 0;
   static constexpr int LPB = 2 * NCX;
-  static constexpr int LD = M + 1;
+  static constexpr int LD = M ? sline<M>(M) : 0;  // complex line stride (padded)
+  static constexpr int SLD = M + 1;                 // real staging line stride
 };
 
 // 1. x-forward: haloed rows -> S[k][i][j] (FACES: boundary terms added as the rows load)
@@ -167,7 +169,7 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld, m = M ? M : P.m;
+  const int nt = M ? M : P.nt, sld = M ? G::SLD : P.sld, m = M ? M : P.m;
   T2 *A = reinterpret_cast<T2 *>(smem);
   T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
@@ -225,7 +227,7 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld, m = M ? M : P.m;
+  const int nt = M ? M : P.nt, sld = M ? G::SLD : P.sld, m = M ? M : P.m;
   T2 *A = reinterpret_cast<T2 *>(smem);
   T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
@@ -266,7 +268,7 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
-  const int nt = M ? M : P.nt, sld = M ? G::LD : P.sld, m = M ? M : P.m;
+  const int nt = M ? M : P.nt, sld = M ? G::SLD : P.sld, m = M ? M : P.m;
   T2 *A = reinterpret_cast<T2 *>(smem);
   T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);

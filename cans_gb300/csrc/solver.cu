@@ -1137,6 +1137,26 @@ int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
 }
 
 // FP32 solve of the haloed FP32 field `in`, result into the interior of the haloed FP32 `out`
+// FP32 solve of a haloed FP32 field into a haloed FP64 field (acc: added to it)
+int cans_plan_solve_f32_to64(cans_plan *P, const float *in, double *out, int acc) {
+  if (P->precision != CANS_FP32) return CANS_EINVAL;
+  Factor *F = nullptr;
+  int rc;
+  if ((rc = get_factor(P, 0., false, &F))) return rc;
+  mark(P, 0);
+  if ((rc = launch_xfwd<float, float>(P, in))) return rc;
+  mark(P, 1);
+  if ((rc = launch_y<float>(P, 1))) return rc;
+  mark(P, 2);
+  if ((rc = launch_z(P, F, P->normfft, true))) return rc;
+  mark(P, 3);
+  if ((rc = launch_y<float>(P, 0))) return rc;
+  mark(P, 4);
+  if ((rc = launch_xbwd<float, double>(P, out, acc))) return rc;
+  mark(P, 5);
+  return CANS_OK;
+}
+
 int cans_plan_solve_f32io(cans_plan *P, const float *in, float *out) {
   if (P->precision != CANS_FP32) return CANS_EINVAL;
   Factor *F = nullptr;

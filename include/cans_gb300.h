@@ -85,8 +85,11 @@ int cans_solver_f32(cans_plan *plan, float *p);
 /* FP64 solve on an FP32-arithmetic plan recovered to FP64 accuracy by iterative
  * refinement: r = rhs - L p in FP64, correction solved in FP32, p += e (FP64).
  * Stops when ||r||_2 <= rtol*||rhs||_2 or after max_iter corrections; returns the
- * number of corrections in *iters and the final relative residual in *relres
- * (both may be NULL).  dzci/dzfi: device grid arrays (0..n3+1). */
+ * number of corrections in *iters and the last evaluated relative residual in *relres
+ * (both may be NULL).  When the iteration ends at max_iter, the last correction is
+ * added to p by its own x-backward pass and its residual is not evaluated (saves one
+ * residual pass), so *relres is the residual before that correction; max_iter = 0 is one
+ * FP32 solve written to p (*relres = 1).  dzci/dzfi: device grid arrays (0..n3+1). */
 int cans_solver_refined(cans_plan *plan, double *p, const double dli[3], const double *dzci,
                         const double *dzfi, double rtol, int max_iter, int *iters, double *relres);
 /* solve_helmholtz (src/solve_helmholtz.f90:28): p/alpha + lap(p) = rhs, 3D variant.
