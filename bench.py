@@ -116,10 +116,51 @@ def make_rhs(n, dzf, device, seed=20260101):
     return p
 
 
+def bench_fp64(args, n, dli, dzc, dzf, dev, world):
+    """The plain FP64 path: K in-place solves of the channel RHS (inputs resident)."""
+    import torch
+    from cans_gb300 import cans
+    plan = cans.Plan(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc")
+    p = make_rhs(n, dzf, dev)
+    ncell = n[0] * n[1] * n[2]
+    for _ in range(args.warmup):
+        plan.solve(p)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    plan.set_timing(True)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(args.steps):
+        plan.solve(p)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    pass_ms, nrec = plan.get_timing()
+    plan.set_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    names = ["solve_xfwd", "solve_yfwd", "solve_zthomas", "solve_ybwd", "solve_xbwd"]
+    top = int(np.argmax(pass_ms))
+    hbm, kind = peaks()
+    achieved = BYTES_PER_CELL_PASS * ncell / (pass_ms[top] * 1e-3) / 1e9
+    workload = f"poisson_{n[0]}x{n[1]}x{n[2]}_PPPPNN_fp64"
+    roof = {"bound": "hbm", "kernel": names[top], "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "peak_source": kind, "traffic": traffic_for(names[top], workload),
+            "algorithmic_bytes_per_launch": BYTES_PER_CELL_PASS * ncell,
+            "note": "FP64-pipe bound on GB300 (1.2 TFLOP/s FP64): 72% FP64 pipe busy in the transform passes"}
+    return plan, p, {"value": round(world / (ms * 1e-3), 4), "unit": "solves/s", "ms_per_step": round(ms, 4),
+                     "pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)}, "roofline": roof}
+
+
 def bench_ours(args, rank, world):
     import torch
     from cans_gb300 import cans
-    from cans_gb300.driver import Simulation, initgrid
+    from cans_gb300.driver import initgrid
     dev = f"cuda:{rank % max(1, torch.cuda.device_count())}"
     torch.cuda.set_device(dev)
     n = [args.size] * 3
@@ -135,83 +176,40 @@ def bench_ours(args, rank, world):
     if args.only == "boxes":
         return {"batched_boxes": bench_boxes(max(args.boxes, 1), dev, max(1, min(args.steps, 5)),
                                              unbatched_boxes=0)}
-    plan = cans.Plan(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc")
-    p = make_rhs(n, dzf, dev)
     ncell = n[0] * n[1] * n[2]
-    for _ in range(args.warmup):
-        plan.solve(p)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    plan.set_timing(True)
-    st = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    l0 = cans.launch_count()
+    workload = f"poisson_{n[0]}x{n[1]}x{n[2]}_PPPPNN"
+    plan64, p64, fp64 = bench_fp64(args, n, dli, dzc, dzf, dev, world)
+    # headline: FP32 transforms + FP64 refinement at the FP64 path's accuracy
     with Clocks(torch.cuda.current_device()) as clk:
-        torch.cuda.synchronize()
-        e0.record(st)
-        for _ in range(args.steps):
-            plan.solve(p)
-        e1.record(st)
-        torch.cuda.synchronize()
-    launches = cans.launch_count() - l0
-    ms = e0.elapsed_time(e1) / args.steps
-    pass_ms, nrec = plan.get_timing()
-    plan.set_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world / (ms * 1e-3)
-    # roofline of the dominant pass
-    names = ["solve_xfwd", "solve_yfwd", "solve_zthomas", "solve_ybwd", "solve_xbwd"]
-    top = int(np.argmax(pass_ms))
+        ref = bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=True)
+    del p64, plan64
+    torch.cuda.empty_cache()
     hbm, kind = peaks()
-    achieved = BYTES_PER_CELL_PASS * ncell / (pass_ms[top] * 1e-3) / 1e9
-    workload = f"poisson_{n[0]}x{n[1]}x{n[2]}_PPPPNN_fp64"
-    roof = {"bound": "hbm", "kernel": names[top], "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "peak_source": kind,
-            "traffic": traffic_for(names[top], workload),
-            "algorithmic_bytes_per_launch": BYTES_PER_CELL_PASS * ncell,
-            "pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)},
-            "solve_achieved_gbs": round(5 * BYTES_PER_CELL_PASS * ncell / (ms * 1e-3) / 1e9, 1)}
-    # end-to-end through the C ABI with host buffers: H2D rhs, solve, D2H solution
-    host_in = torch.empty(p.shape, dtype=torch.float64, pin_memory=True)
-    host_in.copy_(make_rhs(n, dzf, dev, seed=7).cpu())
-    host_out = torch.empty_like(host_in, pin_memory=True)
-    torch.cuda.synchronize()
-    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ke2e = max(1, min(args.steps, 5))
-    e2.record(st)
-    for _ in range(ke2e):
-        p.copy_(host_in, non_blocking=True)
-        plan.solve(p)
-        host_out.copy_(p, non_blocking=True)
-    e3.record(st)
-    torch.cuda.synchronize()
-    ms_e2e = e2.elapsed_time(e3) / ke2e
-    nbytes = p.numel() * 8
-    e2e = {"value": round(world / (ms_e2e * 1e-3), 3), "unit": "solves/s", "h2d_bytes_per_step": nbytes,
-           "d2h_bytes_per_step": nbytes}
-    del host_in, host_out
-    # FP32 transforms + FP64 refinement at equal error (the benchmark spec precision form)
-    ref = None
-    if not args.skip_refine:
-        ref = bench_refined(args, n, dli, dzc, dzf, plan, p, dev, world)
-    # secondary: RK3 step of the 512^3 Taylor-Green vortex (all kernels of one time step)
+    # dominant kernel of the refined solve: the FP32 y pass (two launches per FP32 solve,
+    # the largest share of the launch list); 8 algorithmic bytes per cell (read + write FP32)
+    y_ms = 0.5 * (ref["fp32_pass_ms"]["solve_yfwd"] + ref["fp32_pass_ms"]["solve_ybwd"])
+    achieved = 8 * ncell / (y_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_ylines<float> (FP32 y transform, in place)", "achieved": round(achieved, 1),
+            "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_source": kind,
+            "traffic": traffic_for("solve_y_fp32", workload + "_fp32"), "algorithmic_bytes_per_launch": 8 * ncell,
+            "kernel_ms": round(y_ms, 4),
+            "solve_passes_ms": ref["fp32_pass_ms"]}
     rk3 = None
     if not args.skip_rk3:
-        del p, plan
         torch.cuda.empty_cache()
         rk3 = bench_rk3(args.size, dev, max(1, min(args.steps, 5)))
-    out = {"metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) RHS, mean removed)",
-           "config": {"workload": workload, "grid": n, "bc_pressure": "PP,PP,NN", "z_grid": "tanh gr=1.4",
-                      "domain": [round(x, 6) for x in L_CH], "precision": "fp64",
-                      "l2": "working set 4+ GB per solve >> 129 MB L2 (no flush needed)",
+    out = {"metric": METRIC, "value": ref["value"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ref["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64 (FP32 transforms, FP64 residual/z/reductions)",
+           "data": "synthetic (seeded N(0,1) RHS, mean removed)",
+           "config": {"workload": workload + "_fp32_refined_to_fp64_accuracy", "grid": n, "bc_pressure": "PP,PP,NN",
+                      "z_grid": "tanh gr=1.4", "domain": [round(x, 6) for x in L_CH],
+                      "precision": "FP32 solve + FP64 iterative refinement, accuracy <= FP64 path",
+                      "l2": "working set 2+ GB per solve >> 129 MB L2 (no flush needed)",
                       "parallelism": f"replicas x{world}"},
-           "e2e": e2e, "roofline": roof, "clocks": clk.summary(), "gpu_launches": launches}
+           "e2e": ref.pop("e2e"), "roofline": roof, "clocks": clk.summary(), "gpu_launches": ref["gpu_launches"],
+           "fp32_refined": ref, "fp64_path": fp64,
+           "speedup_refined_over_fp64": round(ref["value"] / fp64["value"], 3)}
     if rk3:
         out["rk3_step"] = rk3
     if not args.skip_adjoint:
@@ -221,12 +219,10 @@ def bench_ours(args, rank, world):
         torch.cuda.empty_cache()
         out["batched_boxes"] = bench_boxes(args.boxes, dev, max(1, min(args.steps, 5)),
                                            unbatched_boxes=min(args.boxes, 32))
-    if ref:
-        out["fp32_refined"] = ref
     return out
 
 
-def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world):
+def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
     """FP32 plan + cans_solver_refined at the accuracy of the FP64 path.
 
     The number of corrections K is calibrated once per operator by a verified run
@@ -280,6 +276,31 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world):
     torch.cuda.synchronize()
     ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / args.steps
     launches = cans.launch_count() - l0
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    e2e_out = None
+    if e2e:
+        # end to end through the C ABI with host buffers: H2D of the RHS, refined solve, D2H
+        host_in = torch.empty(p.shape, dtype=torch.float64, pin_memory=True)
+        host_in.copy_(src.cpu())
+        host_out = torch.empty_like(host_in, pin_memory=True)
+        torch.cuda.synchronize()
+        k2 = max(1, min(args.steps, 5))
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        for _ in range(k2):
+            p.copy_(host_in, non_blocking=True)
+            plan.solve_refined(p, dli, dzci, dzfi, rtol=0.0, max_iter=k_cal)
+            host_out.copy_(p, non_blocking=True)
+        a1.record(st)
+        torch.cuda.synchronize()
+        ms_e2e = a0.elapsed_time(a1) / k2
+        nbytes = p.numel() * 8
+        e2e_out = {"value": round(world / (ms_e2e * 1e-3), 3), "unit": "solves/s", "h2d_bytes_per_step": nbytes,
+                   "d2h_bytes_per_step": nbytes}
+        del host_in, host_out
     plan.set_timing(True)
     plan.solve_refined(p, dli, dzci, dzfi, rtol=0.0, max_iter=k_cal)
     pass_ms, nrec = plan.get_timing()
@@ -290,7 +311,7 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world):
     return {"value": round(world / (ms * 1e-3), 3), "unit": "solves/s", "ms_per_step": round(ms, 4),
             "rtol": rtol, "corrections_per_solve": k_cal, "fp32_solves_per_solve": k_cal + 1,
             "residual_passes_per_solve": k_cal, "accuracy": acc, "gpu_launches": launches,
-            "fp32_pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)}}
+            "fp32_pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)}, "e2e": e2e_out}
 
 
 def bench_rk3(size, dev, steps):

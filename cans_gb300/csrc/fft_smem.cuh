@@ -171,6 +171,8 @@ __device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P, const T2 *__restrict_
 // 16 threads of a warp on the same bank pair.  Line stride: M + M/16 + 1.
 template <int M> __host__ __device__ constexpr int spad(int x) { return M > 0 ? x + (x >> 4) : x; }
 template <int M> __host__ __device__ constexpr int sline(int m) { return M > 0 ? M + M / 16 + 1 : m + 1; }
+// real staging line stride: 16-byte aligned rows in the compile-time path (vector loads)
+template <int M> __host__ __device__ constexpr int sstage(int nt) { return M > 0 ? M + 4 : nt + 1; }
 
 // ---------------------------------------------------------------- compile-time lengths
 // For power-of-two lengths the stage geometry is a compile-time constant: the butterfly and
@@ -232,7 +234,7 @@ __device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict_
                                         const cplx_t<T> *__restrict__ tab, const cplx_t<T> *__restrict__ pre) {
   using T2 = cplx_t<T>;
   // with a compile-time M the kinds handled have nt == n == m (no extension)
-  const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? M + 1 : P.sld, ld = M ? sline<M>(M) : P.ld;
+  const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? sstage<M>(M) : P.sld, ld = M ? sline<M>(M) : P.ld;
   const int total = P.ncx * m;
   for (int e = threadIdx.x; e < total; e += blockDim.x) {
     const int q = M ? (int)((unsigned)e / (unsigned)m) : e / m, k = e - q * m;

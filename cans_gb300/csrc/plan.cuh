@@ -44,6 +44,7 @@ struct cans_plan {
   double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
   float *R32 = nullptr;        // refinement: FP32 haloed residual (high part)
   float *E32 = nullptr;        // refinement: FP32 haloed correction
+  float *E32b = nullptr;       // refinement: second pending FP32 correction
   float *Rlo = nullptr;        // refinement: residual low part (halo-free)
   double *rpart = nullptr;     // refinement: per-block partial norms
   float2 *coef2 = nullptr;     // refinement: double-float a_k, c_k and residues s_k
@@ -94,7 +95,10 @@ template <typename T> inline DirParams make_params(const cans_plan *P, int d, in
   // no extension, at the default lines per CTA); 0 = generic runtime path
   const bool pow2 = q.m >= 32 && q.m <= 1024 && (q.m & (q.m - 1)) == 0;
   q.spec = (pow2 && q.pairs && q.nt == q.m && q.n == q.nt && q.ncx == ncx0 && !P->nospec[d]) ? q.m : 0;
-  if (q.spec) q.ld = q.m + q.m / 16 + 1;  // padded complex lines of the compile-time path (sline)
+  if (q.spec) {
+    q.ld = q.m + q.m / 16 + 1;  // padded complex lines of the compile-time path (sline)
+    q.sld = q.nt + 4;           // 16-byte aligned staging rows (sstage)
+  }
   return q;
 }
 
@@ -149,6 +153,18 @@ __device__ __forceinline__ void copy_tables(const DirParams &P, int m, int nt, c
   }
 }
 
+// device buffers of the FP32 + FP64 refinement of an FP32 plan (solver.cu allocates, refine.cu uses)
+struct RefineBufs {
+  float *R;        // haloed FP32: residual, high part (input of the FP32 solve)
+  float *E, *E2;   // haloed FP32: pending corrections (outputs of the FP32 solves)
+  float *Rlo;      // halo-free FP32: residual, low part
+  double *part;    // per-block partial norms
+  const float2 *a2, *c2, *s2;  // double-float z coefficients: a_k, c_k, residue s_k
+  int n[3];
+  char cbc[6], c_or_f[3];
+  cudaStream_t st;
+};
+
 // get (or build) the z factorisation of plan P for the diagonal shift `key`
 int get_factor(cans_plan *P, double key, bool helm, Factor **out);
 
@@ -158,8 +174,13 @@ template <typename T, int M> struct PassGeo {
   static constexpr int NCX = M ? ncx_for(M, (int)sizeof(cplx_t<T>)) : 0;
   static constexpr int LPB = 2 * NCX;
   static constexpr int LD = M ? sline<M>(M) : 0;  // complex line stride (padded)
-  static constexpr int SLD = M + 1;                 // real staging line stride
+  static constexpr int SLD = sstage<M>(M);          // real staging line stride (16-byte rows)
 };
+
+// 16-byte vector of T (global loads of contiguous rows in the compile-time path)
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; };
+template <> struct Vec16<double> { using type = double2; };
 
 // 1. x-forward: haloed rows -> S[k][i][j] (FACES: boundary terms added as the rows load)
 template <typename T, typename TF, int M, bool FACES = false>
@@ -208,8 +229,8 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
       if (i < nt) r2r_post2<T, M>(P, Z, q, i, post, v0, v1);
       else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
       T *dst = Sk + (size_t)i * n2 + j;
-      dst[0] = v0;
-      if (j + 1 < n2) dst[1] = v1;
+      if (((n2 & 1) == 0)) *reinterpret_cast<T2 *>(dst) = cmk<T2>(v0, v1);  // j even, n2 even: aligned pair
+      else { dst[0] = v0; if (j + 1 < n2) dst[1] = v1; }
     }
   } else {
     for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
@@ -234,18 +255,44 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
   T2 *tw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
   T2 *post = tw + m, *pre = post + nt;
   const long l0 = tile * lpb;
-  for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-    const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - r * nt;
-    stg[r * sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
+  if constexpr (M > 0) {
+    // the tile's lines are one contiguous, 16-byte aligned run of LPB*M values (n2 == M)
+    using V = typename Vec16<T>::type;
+    constexpr int VW = 16 / (int)sizeof(T), VPL = M / VW;
+    const V *src = reinterpret_cast<const V *>(S + (size_t)l0 * M);
+    const long rows = nlines - l0;
+    for (int e = threadIdx.x; e < G::LPB * VPL; e += blockDim.x) {
+      const int r = e / VPL, c = e - r * VPL;
+      V v{};
+      if (r < rows) v = src[e];
+      *reinterpret_cast<V *>(stg + r * G::SLD + c * VW) = v;
+    }
+  } else {
+    for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+      const int r = e / nt, j = e - r * nt;
+      stg[r * sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
+    }
   }
   copy_tables<T>(P, m, nt, tw, post, pre);
   __syncthreads();
   r2r_pre<T, M>(P, stg, A, post, pre);
   __syncthreads();
   const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P, tw) : fft_any<M, -1>(A, B, P, tw);
-  if (P.pairs) {
+  if (M > 0) {
+    // two neighbouring outputs of both lines per thread: 2-element vector stores
+    for (int e = threadIdx.x; e < G::NCX * (M / 2); e += blockDim.x) {
+      const int q = e / (M / 2), j = 2 * (e - q * (M / 2));
+      const long l = l0 + 2 * q;
+      if (l >= nlines) continue;
+      T a0, a1, b0, b1;
+      r2r_post2<T, M>(P, Z, q, j, post, a0, a1);
+      r2r_post2<T, M>(P, Z, q, j + 1, post, b0, b1);
+      *reinterpret_cast<T2 *>(S + (size_t)l * M + j) = cmk<T2>(a0, b0);
+      if (l + 1 < nlines) *reinterpret_cast<T2 *>(S + (size_t)(l + 1) * M + j) = cmk<T2>(a1, b1);
+    }
+  } else if (P.pairs) {
     for (int e = threadIdx.x; e < ncx * nt; e += blockDim.x) {
-      const int q = M ? (int)((unsigned)e / (unsigned)M) : e / nt, j = e - q * nt;
+      const int q = e / nt, j = e - q * nt;
       const long l = l0 + 2 * q;
       if (l >= nlines) continue;
       T v0, v1;
@@ -261,10 +308,23 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
   }
 }
 
-// 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k) (written, or added when acc)
+// value stored by the x-backward pass: acc 0 writes v, 1 adds v to p, 2 writes the sum of
+// the pending refinement corrections add0 (+ add1) and v, in that order (haloed like p)
+template <typename T, typename TF>
+__device__ __forceinline__ TF xbwd_value(const TF *__restrict__ p, size_t idx, int acc, T v, const T *add0,
+                                         const T *add1) {
+  if (acc == 0) return (TF)v;
+  if (acc == 1) return (TF)(p[idx] + (TF)v);
+  TF x = (TF)add0[idx];
+  if (add1) x = x + (TF)add1[idx];
+  return x + (TF)v;
+}
+
+// 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k) (see xbwd_value)
 template <typename T, typename TF, int M>
 __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2,
-                                          const DirParams &P, int acc, int tile, int k, unsigned char *smem) {
+                                          const DirParams &P, int acc, int tile, int k, unsigned char *smem,
+                                          const T *add0 = nullptr, const T *add1 = nullptr) {
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
@@ -279,9 +339,24 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
   T2 *post = tw + m, *pre = post + nt;
   const int j0 = tile * lpb;
   const T *Sk = S + (size_t)k * n1 * n2;
-  for (int e = threadIdx.x; e < nt * lpb; e += blockDim.x) {
-    const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
-    stg[r * sld + i] = (j < n2) ? Sk[(size_t)i * n2 + j] : T(0);
+  constexpr int VW = 16 / (int)sizeof(T);
+  if (M > 0 && n2 % VW == 0 && G::LPB % VW == 0) {
+    // 16-byte loads of each row's run of LPB values, transposed into the staging rows
+    using V = typename Vec16<T>::type;
+    constexpr int VPR = M > 0 ? G::LPB / VW : 1;
+    for (int e = threadIdx.x; e < nt * VPR; e += blockDim.x) {
+      const int i = e / VPR, c = e - i * VPR, j = j0 + c * VW;
+      V v{};
+      if (j < n2) v = *reinterpret_cast<const V *>(Sk + (size_t)i * n2 + j);  // n2 % VW == 0: whole vector
+      const T *u = reinterpret_cast<const T *>(&v);
+#pragma unroll
+      for (int q = 0; q < VW; q++) stg[(c * VW + q) * sld + i] = u[q];
+    }
+  } else {
+    for (int e = threadIdx.x; e < nt * lpb; e += blockDim.x) {
+      const int i = M ? (int)((unsigned)e / (unsigned)G::LPB) : e / lpb, r = e - i * lpb, j = j0 + r;
+      stg[r * sld + i] = (j < n2) ? Sk[(size_t)i * n2 + j] : T(0);
+    }
   }
   if (!M && nt < n1)
     for (int r = threadIdx.x; r < lpb; r += blockDim.x)
@@ -299,10 +374,10 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
       if (i < nt) r2r_post2<T, M>(P, Z, q, i, post, v0, v1);
       else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
       const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-      p[idx] = acc ? (TF)(p[idx] + (TF)v0) : (TF)v0;
+      p[idx] = xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
       if (j + 1 < n2) {
         const size_t idx1 = idx + (size_t)(n1 + 2);
-        p[idx1] = acc ? (TF)(p[idx1] + (TF)v1) : (TF)v1;
+        p[idx1] = xbwd_value<T, TF>(p, idx1, acc, v1, add0, add1);
       }
     }
   } else {
@@ -311,7 +386,7 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
       if (j >= n2) continue;
       const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
       const T val = (i < nt) ? r2r_post<T, M>(P, Z, r, i, post) : pass[r];
-      p[idx] = acc ? (TF)(p[idx] + (TF)val) : (TF)val;
+      p[idx] = xbwd_value<T, TF>(p, idx, acc, val, add0, add1);
     }
   }
 }

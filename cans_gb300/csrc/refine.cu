@@ -32,21 +32,13 @@
 #include <vector>
 
 #include "cans_internal.cuh"
+#include "plan.cuh"
 
-struct RefineBufs {
-  float *R;        // haloed FP32: residual, high part (input of the FP32 solve)
-  float *E;        // haloed FP32: correction (output of the FP32 solve)
-  float *Rlo;      // halo-free FP32: residual, low part
-  double *part;    // per-block partial norms
-  const float2 *a2, *c2, *s2;  // double-float z coefficients: a_k, c_k, residue s_k
-  int n[3];
-  char cbc[6], c_or_f[3];
-  cudaStream_t st;
-};
 // solver.cu internals used here
 int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b);
 int cans_plan_solve_f32io(cans_plan *P, const float *in, float *out);
-int cans_plan_solve_f32_to64(cans_plan *P, const float *in, double *out, int acc);
+int cans_plan_solve_f32_to64(cans_plan *P, const float *in, double *out, int acc, const float *add0,
+                             const float *add1);
 
 namespace {
 constexpr int kTB = 256;
@@ -163,14 +155,15 @@ struct Dot2 {
   }
 };
 
-// (R, Rlo) -= L e ;  x += e (x = e when first) ;  ||R||^2 partials.
-// Work unit: JB = 4 consecutive j rows of one k plane; the CTA strides over these units and
+// (R, Rlo) -= L e ;  ||R||^2 partials.  (The corrections are summed into x later: k_flush or
+// the last FP32 solve's x-backward pass.)
+// Work unit: JB consecutive j rows of one k plane; the CTA strides over these units and
 // its threads run along i.  Every load of a unit is issued before the arithmetic (the
-// j-1..j+JB column of e is a sliding window in registers), so the memory latency of one unit
-// overlaps its ~100 FP32 operations per cell instead of stalling each cell.
-constexpr int JB = 4;
+// j-1..j+JB column of e is a window in registers).  JB = 1 measured fastest at 512^3 (fewer
+// registers, more resident warps) against JB = 2 and 4.
+constexpr int JB = 1;
 __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, float *__restrict__ R,
-                                               float *__restrict__ Rlo, double *__restrict__ x, int first,
+                                               float *__restrict__ Rlo,
                                                const float2 *__restrict__ a2, const float2 *__restrict__ c2,
                                                const float2 *__restrict__ s2, OpParams o,
                                                double *__restrict__ part) {
@@ -237,7 +230,6 @@ __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, floa
         const size_t cc = c0 + (size_t)q * sy;
         R[cc] = r.h;
         Rlo[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * kk)] = r.l;
-        x[cc] = first ? (double)ec : x[cc] + (double)ec;
         sq = __fmaf_rn(r.h, r.h, sq);
       }
     }
@@ -256,6 +248,19 @@ __global__ void k_sum1(const double *__restrict__ part, long nblk, double *__res
     __syncthreads();
   }
   if (threadIdx.x == 0) out[0] = r0[0];
+}
+
+// x = (x_flushed or nothing) + e0 (+ e1), summed in FP64 in that order, interior cells
+__global__ void __launch_bounds__(kTB) k_flush(double *__restrict__ x, const float *__restrict__ e0,
+                                               const float *__restrict__ e1, int has_x, int n1, int n2, int n3) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nx = n1, ny = n2;
+  if (t >= nx * ny * n3) return;
+  const int i = (int)(t % nx) + 1, j = (int)((t / nx) % ny) + 1, k = (int)(t / (nx * ny)) + 1;
+  const size_t c = hidx(i, j, k, n1, n2);
+  double v = has_x ? x[c] + (double)e0[c] : (double)e0[c];
+  if (e1) v = v + (double)e1[c];
+  x[c] = v;
 }
 
 float2 to_df(double v) {
@@ -302,29 +307,53 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   CANS_LAUNCH_CHECK();
   double nrhs = 0., nr = 0.;
   if ((rc = read_norm(b.part, nblk, st, &nrhs))) return rc;
-  int it = 0, first = 1;
+  // Corrections are kept as FP32 fields (at most two pending) and summed into x in FP64 in
+  // the order x = e0 + e1 + ... : by k_flush, or by the last FP32 solve's x-backward pass.
+  int it = 0;
   double rel = 1.;
   if (max_iter == 0) {
     // one FP32 solve written straight into p; no residual is evaluated
-    if ((rc = cans_plan_solve_f32_to64(P, b.R, p, 0))) return rc;
+    if ((rc = cans_plan_solve_f32_to64(P, b.R, p, 0, nullptr, nullptr))) return rc;
   } else {
-    if ((rc = cans_plan_solve_f32io(P, b.R, b.E))) return rc;  // e_0
-    for (;;) {
-      k_dfres<<<nblk_r, tpb, 0, st>>>(b.E, b.R, b.Rlo, p, first, b.a2, b.c2, b.s2, o, b.part);
+    float *pend[2] = {b.E, b.E2};
+    int npend = 0, has_x = 0;  // has_x: p holds flushed corrections (else still the rhs)
+    auto flush = [&]() -> int {
+      const long np = (long)o.n1 * o.n2 * o.n3;
+      k_flush<<<(unsigned)((np + kTB - 1) / kTB), kTB, 0, st>>>(p, pend[0], npend > 1 ? pend[1] : nullptr, has_x,
+                                                               o.n1, o.n2, o.n3);
       CANS_LAUNCH_CHECK();
-      first = 0;
+      has_x = 1;
+      npend = 0;
+      return CANS_OK;
+    };
+    if ((rc = cans_plan_solve_f32io(P, b.R, pend[0]))) return rc;  // e_0
+    npend = 1;
+    for (;;) {
+      k_dfres<<<nblk_r, tpb, 0, st>>>(pend[npend - 1], b.R, b.Rlo, b.a2, b.c2, b.s2, o, b.part);
+      CANS_LAUNCH_CHECK();
       if ((rc = read_norm(b.part, nblk_r, st, &nr))) return rc;
       if (!(nr == nr)) return CANS_ENONFINITE;
       rel = nrhs > 0. ? sqrt(nr / nrhs) : sqrt(nr);
-      if (rel <= rtol) break;
+      if (rel <= rtol) {
+        if ((rc = flush())) return rc;
+        break;
+      }
       if (it + 1 >= max_iter) {
-        // the last correction allowed: its x-backward pass adds it to p in FP64, and its
-        // residual is not evaluated (rel stays the one measured before it)
-        if ((rc = cans_plan_solve_f32_to64(P, b.R, p, 1))) return rc;
+        // the last correction allowed: its x-backward pass writes x = pending + e in FP64,
+        // and its residual is not evaluated (rel stays the one measured before it)
+        if (has_x && (rc = flush())) return rc;
+        if (has_x) {
+          rc = cans_plan_solve_f32_to64(P, b.R, p, 1, nullptr, nullptr);
+        } else {
+          rc = cans_plan_solve_f32_to64(P, b.R, p, 2, pend[0], npend > 1 ? pend[1] : nullptr);
+        }
+        if (rc) return rc;
         it++;
         break;
       }
-      if ((rc = cans_plan_solve_f32io(P, b.R, b.E))) return rc;  // e_{k+1} = solve32(r)
+      if (npend == 2 && (rc = flush())) return rc;
+      if ((rc = cans_plan_solve_f32io(P, b.R, pend[npend]))) return rc;  // e_{k+1} = solve32(r)
+      npend++;
       it++;
     }
   }

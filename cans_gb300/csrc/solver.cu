@@ -216,9 +216,9 @@ __global__ void __launch_bounds__(256) k_ylines(T *__restrict__ S, long nlines, 
 
 template <typename T, typename TF, int M>
 __global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2, DirParams P,
-                                              int acc) {
+                                              int acc, const T *add0, const T *add1) {
   extern __shared__ __align__(16) unsigned char smem[];
-  xbwd_tile<T, TF, M>(S, p, n1, n2, P, acc, blockIdx.x, blockIdx.y, smem);
+  xbwd_tile<T, TF, M>(S, p, n1, n2, P, acc, blockIdx.x, blockIdx.y, smem, add0, add1);
 }
 
 // z factorisation per spectral column (src/solver.f90:114-307 with the RHS-independent
@@ -307,8 +307,9 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
   const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   if (fabs(lamcol[col]) >= lam32) {
-    // the loads do not depend on the recurrence: fetch 8 rows ahead so they overlap it
-    constexpr int U = 8;
+    // the loads do not depend on the recurrence: fetch 16 rows ahead so they overlap it
+    // (16 measured 10% faster than 8 at 512^3, 4 slower)
+    constexpr int U = 16;
     const float normf = (float)norm;
     float y = 0.f;
     int k = 0;
@@ -481,7 +482,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
   cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
-  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
+  cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->E32b); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
   delete P;
   return CANS_OK;
@@ -588,7 +589,8 @@ template <typename T, typename TF> static int launch_xfwd(cans_plan *P, const TF
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
-template <typename T, typename TF> static int launch_xbwd(cans_plan *P, TF *p, int acc = 0) {
+template <typename T, typename TF>
+static int launch_xbwd(cans_plan *P, TF *p, int acc = 0, const T *add0 = nullptr, const T *add1 = nullptr) {
   DirParams q = make_params<T>(P, 0, 0);
   const size_t sm = smem_bytes<T>(q);
   const int M = spec_len(q);
@@ -597,7 +599,7 @@ template <typename T, typename TF> static int launch_xbwd(cans_plan *P, TF *p, i
 #define CALL_XB(MM)                                                                               \
   do {                                                                                            \
     if ((rc = set_smem<T>((const void *)k_xbwd<T, TF, MM>, sm))) return rc;                       \
-    k_xbwd<T, TF, MM><<<grid, 256, sm, P->stream>>>((const T *)P->S, p, P->n[0], P->n[1], q, acc); \
+    k_xbwd<T, TF, MM><<<grid, 256, sm, P->stream>>>((const T *)P->S, p, P->n[0], P->n[1], q, acc, add0, add1); \
   } while (0)
   CANS_DISPATCH_M(M, CALL_XB)
 #undef CALL_XB
@@ -1077,16 +1079,6 @@ extern "C" int cans_solve_helmholtz_adjoint(cans_plan *P, double alpha, double *
 }
 
 // ------------------------------------------------------------------ refinement support
-struct RefineBufs {
-  float *R;
-  float *E;
-  float *Rlo;
-  double *part;
-  const float2 *a2, *c2, *s2;
-  int n[3];
-  char cbc[6], c_or_f[3];
-  cudaStream_t st;
-};
 
 int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
   if (P->precision != CANS_FP32) return CANS_EINVAL;
@@ -1097,6 +1089,8 @@ int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
   if (!P->R32) {
     CANS_CUDA_TRY(cudaMalloc(&P->R32, nh * sizeof(float)));
     CANS_CUDA_TRY(cudaMalloc(&P->E32, nh * sizeof(float)));
+    CANS_CUDA_TRY(cudaMalloc(&P->E32b, nh * sizeof(float)));
+    CANS_CUDA_TRY(cudaMemsetAsync(P->E32b, 0, nh * sizeof(float), P->stream));
     CANS_CUDA_TRY(cudaMemsetAsync(P->R32, 0, nh * sizeof(float), P->stream));
     CANS_CUDA_TRY(cudaMemsetAsync(P->E32, 0, nh * sizeof(float), P->stream));
     CANS_CUDA_TRY(cudaMalloc(&P->Rlo, np * sizeof(float)));
@@ -1119,11 +1113,12 @@ int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
     }
     CANS_CUDA_TRY(cudaMalloc(&P->coef2, h.size() * sizeof(float2)));
     CANS_CUDA_TRY(cudaMemcpy(P->coef2, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice));
-    P->bytes += (long long)(2 * nh * sizeof(float) + np * sizeof(float) + (std::max(nblk, nrblk) + 8) * sizeof(double) +
+    P->bytes += (long long)(3 * nh * sizeof(float) + np * sizeof(float) + (std::max(nblk, nrblk) + 8) * sizeof(double) +
                             h.size() * sizeof(float2));
   }
   b->R = P->R32;
   b->E = P->E32;
+  b->E2 = P->E32b;
   b->Rlo = P->Rlo;
   b->part = P->rpart;
   b->a2 = P->coef2;
@@ -1137,8 +1132,10 @@ int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
 }
 
 // FP32 solve of the haloed FP32 field `in`, result into the interior of the haloed FP32 `out`
-// FP32 solve of a haloed FP32 field into a haloed FP64 field (acc: added to it)
-int cans_plan_solve_f32_to64(cans_plan *P, const float *in, double *out, int acc) {
+// FP32 solve of a haloed FP32 field into a haloed FP64 field: acc 0 written, 1 added to it,
+// 2 written as add0 (+ add1) + solution (pending refinement corrections)
+int cans_plan_solve_f32_to64(cans_plan *P, const float *in, double *out, int acc, const float *add0,
+                             const float *add1) {
   if (P->precision != CANS_FP32) return CANS_EINVAL;
   Factor *F = nullptr;
   int rc;
@@ -1152,7 +1149,7 @@ int cans_plan_solve_f32_to64(cans_plan *P, const float *in, double *out, int acc
   mark(P, 3);
   if ((rc = launch_y<float>(P, 0))) return rc;
   mark(P, 4);
-  if ((rc = launch_xbwd<float, double>(P, out, acc))) return rc;
+  if ((rc = launch_xbwd<float, double>(P, out, acc, add0, add1))) return rc;
   mark(P, 5);
   return CANS_OK;
 }
