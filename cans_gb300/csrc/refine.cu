@@ -39,6 +39,8 @@ int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b);
 int cans_plan_solve_f32io(cans_plan *P, const float *in, float *out);
 int cans_plan_solve_f32_to64(cans_plan *P, const float *in, double *out, int acc, const float *add0,
                              const float *add1);
+int cans_plan_solve_f64in_f32out(cans_plan *P, const double *in, float *out);
+int cans_plan_solve_f64io(cans_plan *P, const double *in, double *out);
 
 namespace {
 constexpr int kTB = 256;
@@ -110,28 +112,6 @@ __device__ __forceinline__ void block_reduce_to(float v, double *out) {
   }
 }
 
-// rhs (FP64, interior of p) -> (R hi, Rlo lo) and ||rhs||^2 partials.  Grid-stride over the
-// (j, k) rows so the partials number gridDim.x, not the cell count.
-__global__ void __launch_bounds__(kTB) k_split_df(const double *__restrict__ p, float *__restrict__ R,
-                                                  float *__restrict__ Rlo, int n1, int n2, int n3,
-                                                  double *__restrict__ part) {
-  float sq = 0.f;
-  const long nrows = (long)n2 * n3;
-  for (long row = blockIdx.x; row < nrows; row += gridDim.x) {
-    const int j = (int)(row % n2) + 1, k = (int)(row / n2) + 1;
-    for (int i = threadIdx.x + 1; i <= n1; i += blockDim.x) {
-      const size_t c = hidx(i, j, k, n1, n2);
-      const size_t t = (size_t)(i - 1) + (size_t)n1 * (size_t)row;
-      const double v = p[c];
-      const float hi = __double2float_rn(v);
-      R[c] = hi;
-      Rlo[t] = __double2float_rn(v - (double)hi);
-      sq = __fmaf_rn(hi, hi, sq);
-    }
-  }
-  block_reduce_to(sq, &part[blockIdx.x]);
-}
-
 // Compensated accumulation (Ogita-Rump-Oishi "Dot2"): the running sum's high part goes
 // through two-sum, every error term (two-sum residues, two-product residues, cross products
 // with the coefficients' low parts) into one FP32 accumulator.  Accuracy is that of
@@ -155,23 +135,27 @@ struct Dot2 {
   }
 };
 
-// (R, Rlo) -= L e ;  ||R||^2 partials.  (The corrections are summed into x later: k_flush or
-// the last FP32 solve's x-backward pass.)
+// (R, Rlo) -= L e ;  ||R||^2 partials ;  folding of pending corrections into x (FP64), in the
+// order x = e0 + e1 + ... : xmode 0 none, 1 x = eprev + e, 2 x = (x + eprev) + e.
 // Work unit: JB consecutive j rows of one k plane; the CTA strides over these units and
 // its threads run along i.  Every load of a unit is issued before the arithmetic (the
 // j-1..j+JB column of e is a window in registers).  JB = 1 measured fastest at 512^3 (fewer
 // registers, more resident warps) against JB = 2 and 4.
 constexpr int JB = 1;
 __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, float *__restrict__ R,
-                                               float *__restrict__ Rlo,
+                                               float *__restrict__ Rlo, const float *__restrict__ Eprev,
+                                               double *__restrict__ x, int xmode,
                                                const float2 *__restrict__ a2, const float2 *__restrict__ c2,
                                                const float2 *__restrict__ s2, OpParams o,
-                                               double *__restrict__ part) {
+                                               double *__restrict__ part, const double *__restrict__ rhs,
+                                               double *__restrict__ part0) {
+  // rhs != nullptr (first residual): the current residual is the FP64 right-hand side itself,
+  // split into (hi, lo) here, and part0 receives the partial sums of ||rhs||^2
   const int n1 = o.n1, n2 = o.n2, n3 = o.n3;
   const size_t sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
   const int nub = (n2 + JB - 1) / JB;
   const long nunits = (long)nub * n3;
-  float sq = 0.f;
+  float sq = 0.f, sq0 = 0.f;
   for (long u = blockIdx.x; u < nunits; u += gridDim.x) {
     const int j0 = (int)(u % nub) * JB + 1, k = (int)(u / nub) + 1;
     const int kk = k - 1;
@@ -191,8 +175,15 @@ __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, floa
         ee[q] = i < n1 ? E[cc + 1] : (o.gx1 == 0 ? E[cc - (n1 - 1)] : 0.f);
         eb[q] = hasb ? (k > 1 ? E[cc - sz] : E[cc + (size_t)(n3 - 1) * sz]) : 0.f;
         et[q] = hast ? (k < n3 ? E[cc + sz] : E[cc - (size_t)(n3 - 1) * sz]) : 0.f;
-        rh[q] = R[cc];
-        rl[q] = Rlo[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * kk)];
+        if (rhs) {
+          const double v = rhs[cc];
+          rh[q] = __double2float_rn(v);
+          rl[q] = __double2float_rn(v - (double)rh[q]);
+          sq0 = __fmaf_rn(rh[q], rh[q], sq0);
+        } else {
+          rh[q] = R[cc];
+          rl[q] = Rlo[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * kk)];
+        }
       }
       col[0] = j0 > 1 ? E[c0 - sy] : (o.gy0 == 0 ? E[c0 + (size_t)(n2 - 1) * sy] : 0.f);
       {
@@ -230,11 +221,17 @@ __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, floa
         const size_t cc = c0 + (size_t)q * sy;
         R[cc] = r.h;
         Rlo[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * kk)] = r.l;
+        if (xmode == 1) x[cc] = (double)Eprev[cc] + (double)ec;
+        else if (xmode == 2) x[cc] = (x[cc] + (double)Eprev[cc]) + (double)ec;
         sq = __fmaf_rn(r.h, r.h, sq);
       }
     }
   }
   block_reduce_to(sq, &part[blockIdx.x]);
+  if (rhs) {
+    __syncthreads();  // block_reduce_to's shared array is reused
+    block_reduce_to(sq0, &part0[blockIdx.x]);
+  }
 }
 
 __global__ void k_sum1(const double *__restrict__ part, long nblk, double *__restrict__ out) {
@@ -298,22 +295,19 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const long nrows = (long)o.n2 * o.n3;
-  const unsigned nblk = (unsigned)std::min<long>(nrows, 8L * nsm);
   const unsigned nblk_r = (unsigned)std::min<long>((long)((o.n2 + JB - 1) / JB) * o.n3, 8L * nsm);
   const int tpb = o.n1 >= 256 ? 256 : (o.n1 >= 128 ? 128 : 64);
   cudaStream_t st = b.st;
-  k_split_df<<<nblk, tpb, 0, st>>>(p, b.R, b.Rlo, o.n1, o.n2, o.n3, b.part);
-  CANS_LAUNCH_CHECK();
   double nrhs = 0., nr = 0.;
-  if ((rc = read_norm(b.part, nblk, st, &nrhs))) return rc;
+  double *part0 = b.part + 2 * (size_t)nblk_r + 16;  // ||rhs||^2 partials of the first residual pass
   // Corrections are kept as FP32 fields (at most two pending) and summed into x in FP64 in
-  // the order x = e0 + e1 + ... : by k_flush, or by the last FP32 solve's x-backward pass.
+  // the order x = e0 + e1 + ... : by the residual pass that sees two pending corrections,
+  // by the last FP32 solve's x-backward pass, or (verified stop) by k_flush.
   int it = 0;
   double rel = 1.;
   if (max_iter == 0) {
-    // one FP32 solve written straight into p; no residual is evaluated
-    if ((rc = cans_plan_solve_f32_to64(P, b.R, p, 0, nullptr, nullptr))) return rc;
+    // one FP32 solve of the FP64 rhs written straight into p; no residual is evaluated
+    if ((rc = cans_plan_solve_f64io(P, p, p))) return rc;
   } else {
     float *pend[2] = {b.E, b.E2};
     int npend = 0, has_x = 0;  // has_x: p holds flushed corrections (else still the rhs)
@@ -326,22 +320,32 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
       npend = 0;
       return CANS_OK;
     };
-    if ((rc = cans_plan_solve_f32io(P, b.R, pend[0]))) return rc;  // e_0
+    if ((rc = cans_plan_solve_f64in_f32out(P, p, pend[0]))) return rc;  // e_0 from the FP64 rhs
     npend = 1;
+    bool first = true;
     for (;;) {
-      k_dfres<<<nblk_r, tpb, 0, st>>>(pend[npend - 1], b.R, b.Rlo, b.a2, b.c2, b.s2, o, b.part);
+      // two pending corrections are folded into x by this residual pass
+      const int xmode = npend == 2 ? (has_x ? 2 : 1) : 0;
+      k_dfres<<<nblk_r, tpb, 0, st>>>(pend[npend - 1], b.R, b.Rlo, npend == 2 ? pend[0] : nullptr, p, xmode, b.a2,
+                                      b.c2, b.s2, o, b.part, first ? p : nullptr, part0);
       CANS_LAUNCH_CHECK();
+      if (first && (rc = read_norm(part0, nblk_r, st, &nrhs))) return rc;
+      first = false;
+      if (xmode) {
+        has_x = 1;
+        npend = 0;
+      }
       if ((rc = read_norm(b.part, nblk_r, st, &nr))) return rc;
       if (!(nr == nr)) return CANS_ENONFINITE;
       rel = nrhs > 0. ? sqrt(nr / nrhs) : sqrt(nr);
       if (rel <= rtol) {
-        if ((rc = flush())) return rc;
+        if (npend && (rc = flush())) return rc;
         break;
       }
       if (it + 1 >= max_iter) {
         // the last correction allowed: its x-backward pass writes x = pending + e in FP64,
         // and its residual is not evaluated (rel stays the one measured before it)
-        if (has_x && (rc = flush())) return rc;
+        if (has_x && npend && (rc = flush())) return rc;
         if (has_x) {
           rc = cans_plan_solve_f32_to64(P, b.R, p, 1, nullptr, nullptr);
         } else {
@@ -351,7 +355,6 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
         it++;
         break;
       }
-      if (npend == 2 && (rc = flush())) return rc;
       if ((rc = cans_plan_solve_f32io(P, b.R, pend[npend]))) return rc;  // e_{k+1} = solve32(r)
       npend++;
       it++;

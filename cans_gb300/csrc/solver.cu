@@ -307,48 +307,87 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
   const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   if (fabs(lamcol[col]) >= lam32) {
-    // the loads do not depend on the recurrence: fetch 16 rows ahead so they overlap it
-    // (16 measured 10% faster than 8 at 512^3, 4 slower)
+    // software-pipelined sweeps: the loads of the next U rows are issued before the
+    // recurrence runs over the current U rows (the loads do not depend on it)
     constexpr int U = 16;
     const float normf = (float)norm;
     float y = 0.f;
-    int k = 0;
-    for (; k + U <= nn; k += U) {
+    const int nfull = nn / U;
+    {
       float sv[U], zv[U];
+      if (nfull > 0) {
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        const size_t idx = (size_t)(k + u) * ncol + col;
-        sv[u] = S[idx];
-        zv[u] = zinv32[idx];
+        for (int u = 0; u < U; u++) {
+          const size_t idx = (size_t)u * ncol + col;
+          sv[u] = S[idx];
+          zv[u] = zinv32[idx];
+        }
       }
+      for (int ch = 0; ch < nfull; ch++) {
+        const int k = ch * U;
+        float sn[U], zn[U];
+        const bool more = ch + 1 < nfull;
+        if (more) {
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        y = (sv[u] * normf - (float)a[k + u] * y) * zv[u];
-        S[(size_t)(k + u) * ncol + col] = y;
+          for (int u = 0; u < U; u++) {
+            const size_t idx = (size_t)(k + U + u) * ncol + col;
+            sn[u] = S[idx];
+            zn[u] = zinv32[idx];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          y = (sv[u] * normf - (float)a[k + u] * y) * zv[u];
+          S[(size_t)(k + u) * ncol + col] = y;
+        }
+        if (more) {
+#pragma unroll
+          for (int u = 0; u < U; u++) { sv[u] = sn[u]; zv[u] = zn[u]; }
+        }
       }
     }
-    for (; k < nn; k++) {
+    for (int k = nfull * U; k < nn; k++) {
       const size_t idx = (size_t)k * ncol + col;
       y = (S[idx] * normf - (float)a[k] * y) * zinv32[idx];
       S[idx] = y;
     }
     const float sn = y;
-    k = nn - 2;
-    for (; k - U + 1 >= 0; k -= U) {
+    // backward over rows nn-2 .. 0 in chunks of U, descending
+    const int nb = nn - 1, bfull = nb / U;
+    {
       float sv[U], dv[U];
+      if (bfull > 0) {
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        const size_t idx = (size_t)(k - u) * ncol + col;
-        sv[u] = S[idx];
-        dv[u] = dd32[idx];
+        for (int u = 0; u < U; u++) {
+          const size_t idx = (size_t)(nn - 2 - u) * ncol + col;
+          sv[u] = S[idx];
+          dv[u] = dd32[idx];
+        }
       }
+      for (int ch = 0; ch < bfull; ch++) {
+        const int k = nn - 2 - ch * U;
+        float sn2[U], dn[U];
+        const bool more = ch + 1 < bfull;
+        if (more) {
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        y = sv[u] - dv[u] * y;
-        S[(size_t)(k - u) * ncol + col] = y;
+          for (int u = 0; u < U; u++) {
+            const size_t idx = (size_t)(k - U - u) * ncol + col;
+            sn2[u] = S[idx];
+            dn[u] = dd32[idx];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          y = sv[u] - dv[u] * y;
+          S[(size_t)(k - u) * ncol + col] = y;
+        }
+        if (more) {
+#pragma unroll
+          for (int u = 0; u < U; u++) { sv[u] = sn2[u]; dv[u] = dn[u]; }
+        }
       }
     }
-    for (; k >= 0; k--) {
+    for (int k = nn - 2 - bfull * U; k >= 0; k--) {
       const size_t idx = (size_t)k * ncol + col;
       y = S[idx] - dd32[idx] * y;
       S[idx] = y;
@@ -1152,6 +1191,32 @@ int cans_plan_solve_f32_to64(cans_plan *P, const float *in, double *out, int acc
   if ((rc = launch_xbwd<float, double>(P, out, acc, add0, add1))) return rc;
   mark(P, 5);
   return CANS_OK;
+}
+
+// FP32 solve of an FP64 haloed field (converted as the x-forward pass loads it) into an FP32
+// haloed field, or into an FP64 haloed field (in == out allowed: the passes go through S)
+int cans_plan_solve_f64in_f32out(cans_plan *P, const double *in, float *out) {
+  if (P->precision != CANS_FP32) return CANS_EINVAL;
+  Factor *F = nullptr;
+  int rc;
+  if ((rc = get_factor(P, 0., false, &F))) return rc;
+  mark(P, 0);
+  if ((rc = launch_xfwd<float, double>(P, in))) return rc;
+  mark(P, 1);
+  if ((rc = launch_y<float>(P, 1))) return rc;
+  mark(P, 2);
+  if ((rc = launch_z(P, F, P->normfft, true))) return rc;
+  mark(P, 3);
+  if ((rc = launch_y<float>(P, 0))) return rc;
+  mark(P, 4);
+  if ((rc = launch_xbwd<float, float>(P, out, 0))) return rc;
+  mark(P, 5);
+  return CANS_OK;
+}
+int cans_plan_solve_f64io(cans_plan *P, const double *in, double *out) {
+  if (P->precision != CANS_FP32) return CANS_EINVAL;
+  if (in != out) return CANS_EINVAL;
+  return solve_impl<float, double>(P, out, 0., false, P->normfft);
 }
 
 int cans_plan_solve_f32io(cans_plan *P, const float *in, float *out) {
