@@ -40,6 +40,8 @@ struct cans_plan {
   double *lamcol = nullptr;   // device lambda in spectral column order (i*n2 + j)
   double *zw = nullptr;       // device diagonal D of the z operator T = D M, M symmetric (0:n3+1)
   double *a_d = nullptr, *b_d = nullptr, *c_d = nullptr, *bb_d = nullptr;
+  float *a32 = nullptr;       // a_k rounded to FP32 (FP32 z columns: no FP64 conversions in the sweep)
+  int *zorder = nullptr;      // FP32 plans: z column groups, those with FP64 columns first
   void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)
   double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
   float *R32 = nullptr;        // refinement: FP32 haloed residual (high part)
@@ -177,6 +179,60 @@ template <typename T, int M> struct PassGeo {
   static constexpr int SLD = sstage<M>(M);          // real staging line stride (16-byte rows)
 };
 
+// ---- FP64 <-> FP32 conversions without the FP64 pipe.  GB300 issues double<->float
+// conversions on its FP64 unit (1/58 of the FP32 rate), which made them the bottleneck of
+// the FP32 refinement kernels; these integer versions give bit-identical results (round to
+// nearest even, exact widening) on the normal range and fall back to the conversion
+// instructions elsewhere (zero, subnormal, huge, inf/nan).
+__device__ __forceinline__ float d2f_rn(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e < 1023 - 125 || e > 1023 + 126) return __double2float_rn(v);
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  unsigned q = (unsigned)(m >> 29);
+  const unsigned rb = (unsigned)(m & 0x1FFFFFFFull);
+  if (rb > 0x10000000u || (rb == 0x10000000u && (q & 1u))) q++;
+  int ef = e - 1023 + 127;
+  if (q >> 24) { q >>= 1; ef++; }
+  return __int_as_float((int)(((unsigned)(b >> 63) << 31) | ((unsigned)ef << 23) | (q & 0x7FFFFFu)));
+}
+// hi = RN(v), lo = RN(v - hi)
+__device__ __forceinline__ void d2f_split(double v, float &hi, float &lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e < 1075 - 126 || e > 1023 + 126) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
+    return;
+  }
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  unsigned q = (unsigned)(m >> 29);
+  const unsigned rb = (unsigned)(m & 0x1FFFFFFFull);
+  if (rb > 0x10000000u || (rb == 0x10000000u && (q & 1u))) q++;
+  const int r = (int)((long long)m - ((long long)q << 29));  // exact remainder, |r| <= 2^28
+  int ef = e - 1023 + 127;
+  unsigned qq = q;
+  if (qq >> 24) { qq >>= 1; ef++; }
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  hi = __int_as_float((int)(sign | ((unsigned)ef << 23) | (qq & 0x7FFFFFu)));
+  // lo = RN(r) * 2^(e - 1075): normal (e >= 949) and the scaling is exact
+  const float rf = (float)r * __int_as_float((e - 1075 + 127) << 23);
+  lo = sign ? -rf : rf;
+}
+// exact float -> double
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned b = (unsigned)__float_as_int(f);
+  const unsigned ef = (b >> 23) & 0xFF;
+  if (ef == 0 || ef == 0xFF) return (double)f;
+  const unsigned long long d = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)(ef + 896) << 52) |
+                               ((unsigned long long)(b & 0x7FFFFF) << 29);
+  return __longlong_as_double((long long)d);
+}
+// element conversion of a transform load / store.  The transform kernels keep the
+// conversion instructions: there the FP64 pipe is otherwise idle and the integer versions'
+// ALU work measured slower (x-forward from FP64 0.56 -> 0.87 ms at 512^3).
+template <typename T, typename TF> __device__ __forceinline__ T cvt_to(TF v) { return (T)v; }
+
 // 16-byte vector of T (global loads of contiguous rows in the compile-time path)
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; };
@@ -203,16 +259,16 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
   for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
     const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, i = e - r * nt, j = j0 + r;
     if constexpr (FACES)
-      stg[r * sld + i] = (j < n2) ? (T)face_add(p[hidx(i + 1, j + 1, k + 1, n1, n2)], i + 1, j + 1, k + 1, *fa) : T(0);
+      stg[r * sld + i] = (j < n2) ? cvt_to<T>(face_add(p[hidx(i + 1, j + 1, k + 1, n1, n2)], i + 1, j + 1, k + 1, *fa)) : T(0);
     else
-      stg[r * sld + i] = (j < n2) ? (T)p[hidx(i + 1, j + 1, k + 1, n1, n2)] : T(0);
+      stg[r * sld + i] = (j < n2) ? cvt_to<T, TF>(p[hidx(i + 1, j + 1, k + 1, n1, n2)]) : T(0);
   }
   if (!M && nt < n1)
     for (int r = threadIdx.x; r < lpb; r += blockDim.x) {
       if constexpr (FACES)
-        pass[r] = (j0 + r < n2) ? (T)face_add(p[hidx(n1, j0 + r + 1, k + 1, n1, n2)], n1, j0 + r + 1, k + 1, *fa) : T(0);
+        pass[r] = (j0 + r < n2) ? cvt_to<T>(face_add(p[hidx(n1, j0 + r + 1, k + 1, n1, n2)], n1, j0 + r + 1, k + 1, *fa)) : T(0);
       else
-        pass[r] = (j0 + r < n2) ? (T)p[hidx(n1, j0 + r + 1, k + 1, n1, n2)] : T(0);
+        pass[r] = (j0 + r < n2) ? cvt_to<T, TF>(p[hidx(n1, j0 + r + 1, k + 1, n1, n2)]) : T(0);
     }
   copy_tables<T>(P, m, nt, tw, post, pre);
   __syncthreads();
@@ -313,11 +369,11 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
 template <typename T, typename TF>
 __device__ __forceinline__ TF xbwd_value(const TF *__restrict__ p, size_t idx, int acc, T v, const T *add0,
                                          const T *add1) {
-  if (acc == 0) return (TF)v;
-  if (acc == 1) return (TF)(p[idx] + (TF)v);
-  TF x = (TF)add0[idx];
-  if (add1) x = x + (TF)add1[idx];
-  return x + (TF)v;
+  if (acc == 0) return cvt_to<TF, T>(v);
+  if (acc == 1) return (TF)(p[idx] + cvt_to<TF, T>(v));
+  TF x = cvt_to<TF, T>(add0[idx]);
+  if (add1) x = x + cvt_to<TF, T>(add1[idx]);
+  return x + cvt_to<TF, T>(v);
 }
 
 // 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k) (see xbwd_value)

@@ -137,11 +137,9 @@ struct Dot2 {
 
 // (R, Rlo) -= L e ;  ||R||^2 partials ;  folding of pending corrections into x (FP64), in the
 // order x = e0 + e1 + ... : xmode 0 none, 1 x = eprev + e, 2 x = (x + eprev) + e.
-// Work unit: JB consecutive j rows of one k plane; the CTA strides over these units and
-// its threads run along i.  Every load of a unit is issued before the arithmetic (the
-// j-1..j+JB column of e is a window in registers).  JB = 1 measured fastest at 512^3 (fewer
-// registers, more resident warps) against JB = 2 and 4.
-constexpr int JB = 1;
+// Work unit: one (j, k) row; the CTA strides over rows and its threads run along i.  Row
+// pointers (with the y/z ghost rules resolved per row) keep the per-cell work to loads and
+// the double-float arithmetic.
 __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, float *__restrict__ R,
                                                float *__restrict__ Rlo, const float *__restrict__ Eprev,
                                                double *__restrict__ x, int xmode,
@@ -152,79 +150,62 @@ __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, floa
   // rhs != nullptr (first residual): the current residual is the FP64 right-hand side itself,
   // split into (hi, lo) here, and part0 receives the partial sums of ||rhs||^2
   const int n1 = o.n1, n2 = o.n2, n3 = o.n3;
-  const size_t sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
-  const int nub = (n2 + JB - 1) / JB;
-  const long nunits = (long)nub * n3;
+  const long sy = n1 + 2, sz = (long)(n1 + 2) * (n2 + 2);
+  const long nrows = (long)n2 * n3;
+  const float2 mcx = make_float2(-o.cx.x, -o.cx.y), mcy = make_float2(-o.cy.x, -o.cy.y);
   float sq = 0.f, sq0 = 0.f;
-  for (long u = blockIdx.x; u < nunits; u += gridDim.x) {
-    const int j0 = (int)(u % nub) * JB + 1, k = (int)(u / nub) + 1;
-    const int kk = k - 1;
-    const float2 av = a2[kk], cv = c2[kk], sv = s2[kk];
+  for (long u = blockIdx.x; u < nrows; u += gridDim.x) {
+    const int j = (int)(u % n2) + 1, k = (int)(u / n2) + 1;
+    const float2 av = a2[k - 1], cv = c2[k - 1], sv = s2[k - 1];
+    const float2 mav = make_float2(-av.x, -av.y), mcv = make_float2(-cv.x, -cv.y), msv = make_float2(-sv.x, -sv.y);
+    const long c0 = (long)hidx(0, j, k, n1, n2);
+    const float *Ec = E + c0;
+    // neighbour rows: inside the box, the periodic wrap, or none (Neumann/Dirichlet rule)
+    const float *Es = j > 1 ? Ec - sy : (o.gy0 == 0 ? Ec + (long)(n2 - 1) * sy : nullptr);
+    const float *En = j < n2 ? Ec + sy : (o.gy1 == 0 ? Ec - (long)(n2 - 1) * sy : nullptr);
     const bool hasb = k > 1 || o.zper, hast = k < n3 || o.zper;
+    const float *Eb = k > 1 ? Ec - sz : Ec + (long)(n3 - 1) * sz;
+    const float *Et = k < n3 ? Ec + sz : Ec - (long)(n3 - 1) * sz;
+    float *Rr = R + c0;
+    float *Lr = Rlo + (long)n1 * u;  // low parts of the row: Lr[i - 1], i = 1..n1
     for (int i = threadIdx.x + 1; i <= n1; i += blockDim.x) {
-      // column e(i, j0-1 .. j0+JB, k) with the y ghost rule at the ends
-      float col[JB + 2], ew[JB], ee[JB], eb[JB], et[JB], rh[JB], rl[JB];
-      const size_t c0 = hidx(i, j0, k, n1, n2);
-#pragma unroll
-      for (int q = 0; q < JB; q++) {
-        const int j = j0 + q;
-        if (j > n2) { col[q + 1] = 0.f; continue; }
-        const size_t cc = c0 + (size_t)q * sy;
-        col[q + 1] = E[cc];
-        ew[q] = i > 1 ? E[cc - 1] : (o.gx0 == 0 ? E[cc + (n1 - 1)] : 0.f);
-        ee[q] = i < n1 ? E[cc + 1] : (o.gx1 == 0 ? E[cc - (n1 - 1)] : 0.f);
-        eb[q] = hasb ? (k > 1 ? E[cc - sz] : E[cc + (size_t)(n3 - 1) * sz]) : 0.f;
-        et[q] = hast ? (k < n3 ? E[cc + sz] : E[cc - (size_t)(n3 - 1) * sz]) : 0.f;
-        if (rhs) {
-          const double v = rhs[cc];
-          rh[q] = __double2float_rn(v);
-          rl[q] = __double2float_rn(v - (double)rh[q]);
-          sq0 = __fmaf_rn(rh[q], rh[q], sq0);
-        } else {
-          rh[q] = R[cc];
-          rl[q] = Rlo[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * kk)];
-        }
+      const float ec = Ec[i];
+      const float ew = i > 1 ? Ec[i - 1] : (o.gx0 == 0 ? Ec[n1] : 0.f);
+      const float ee = i < n1 ? Ec[i + 1] : (o.gx1 == 0 ? Ec[1] : 0.f);
+      const float es = Es ? Es[i] : 0.f, en = En ? En[i] : 0.f;
+      const float eb = hasb ? Eb[i] : 0.f, et = hast ? Et[i] : 0.f;
+      float rh, rl;
+      if (rhs) {
+        d2f_split(rhs[c0 + i], rh, rl);
+        sq0 = __fmaf_rn(rh, rh, sq0);
+      } else {
+        rh = Rr[i];
+        rl = Lr[i - 1];
       }
-      col[0] = j0 > 1 ? E[c0 - sy] : (o.gy0 == 0 ? E[c0 + (size_t)(n2 - 1) * sy] : 0.f);
-      {
-        const int jl = j0 + JB;  // row after the unit
-        col[JB + 1] = jl <= n2 ? E[c0 + (size_t)JB * sy] : 0.f;
+      const df dw = diff_nb(i > 1, o.gx0, ew, ec);
+      const df de = diff_nb(i < n1, o.gx1, ee, ec);
+      const df ds = diff_nb(j > 1, o.gy0, es, ec);
+      const df dn = diff_nb(j < n2, o.gy1, en, ec);
+      Dot2 acc{rh, rl};
+      acc.add_prod(mcx, de.h, de.l);
+      acc.add_prod(mcx, dw.h, dw.l);
+      acc.add_prod(mcy, dn.h, dn.l);
+      acc.add_prod(mcy, ds.h, ds.l);
+      if (hasb) {
+        const df db = two_sum(eb, -ec);
+        acc.add_prod(mav, db.h, db.l);
       }
-#pragma unroll
-      for (int q = 0; q < JB; q++) {
-        const int j = j0 + q;
-        if (j > n2) continue;
-        const float ec = col[q + 1];
-        // y neighbours from the window; the upper end of the domain uses the ghost rule
-        const float es = col[q];
-        const float en = j < n2 ? col[q + 2] : (o.gy1 == 0 ? E[c0 + (size_t)q * sy - (size_t)(n2 - 1) * sy] : 0.f);
-        const df dw = diff_nb(i > 1, o.gx0, ew[q], ec);
-        const df de = diff_nb(i < n1, o.gx1, ee[q], ec);
-        const df ds = diff_nb(j > 1, o.gy0, es, ec);
-        const df dn = diff_nb(j < n2, o.gy1, en, ec);
-        Dot2 acc{rh[q], rl[q]};
-        const float2 mcx = make_float2(-o.cx.x, -o.cx.y), mcy = make_float2(-o.cy.x, -o.cy.y);
-        acc.add_prod(mcx, de.h, de.l);
-        acc.add_prod(mcx, dw.h, dw.l);
-        acc.add_prod(mcy, dn.h, dn.l);
-        acc.add_prod(mcy, ds.h, ds.l);
-        if (hasb) {
-          const df db = two_sum(eb[q], -ec);
-          acc.add_prod(make_float2(-av.x, -av.y), db.h, db.l);
-        }
-        if (hast) {
-          const df dt = two_sum(et[q], -ec);
-          acc.add_prod(make_float2(-cv.x, -cv.y), dt.h, dt.l);
-        }
-        acc.add_prod(make_float2(-sv.x, -sv.y), ec, 0.f);
-        const df r = two_sum(acc.s, acc.err);  // |err| may exceed |s| after cancellation
-        const size_t cc = c0 + (size_t)q * sy;
-        R[cc] = r.h;
-        Rlo[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * kk)] = r.l;
-        if (xmode == 1) x[cc] = (double)Eprev[cc] + (double)ec;
-        else if (xmode == 2) x[cc] = (x[cc] + (double)Eprev[cc]) + (double)ec;
-        sq = __fmaf_rn(r.h, r.h, sq);
+      if (hast) {
+        const df dt = two_sum(et, -ec);
+        acc.add_prod(mcv, dt.h, dt.l);
       }
+      acc.add_prod(msv, ec, 0.f);
+      const df r = two_sum(acc.s, acc.err);  // |err| may exceed |s| after cancellation
+      Rr[i] = r.h;
+      Lr[i - 1] = r.l;
+      if (xmode == 1) x[c0 + i] = f2d(Eprev[c0 + i]) + f2d(ec);
+      else if (xmode == 2) x[c0 + i] = (x[c0 + i] + f2d(Eprev[c0 + i])) + f2d(ec);
+      sq = __fmaf_rn(r.h, r.h, sq);
     }
   }
   block_reduce_to(sq, &part[blockIdx.x]);
@@ -295,7 +276,7 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const unsigned nblk_r = (unsigned)std::min<long>((long)((o.n2 + JB - 1) / JB) * o.n3, 8L * nsm);
+  const unsigned nblk_r = (unsigned)std::min<long>((long)o.n2 * o.n3, 8L * nsm);
   const int tpb = o.n1 >= 256 ? 256 : (o.n1 >= 128 ? 128 : 64);
   cudaStream_t st = b.st;
   double nrhs = 0., nr = 0.;

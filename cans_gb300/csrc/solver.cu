@@ -31,6 +31,7 @@
 #include "fft_smem.cuh"
 #include "plan.cuh"
 
+static constexpr int kZGroup = 128;  // spectral columns per CTA of the z elimination
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 void cans_set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
 static std::atomic<long long> g_launches{0};
@@ -302,9 +303,11 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
                                                     const double *__restrict__ p2, const double *__restrict__ dcl,
                                                     const float *__restrict__ zinv32, const float *__restrict__ dd32,
                                                     const float *__restrict__ p232, const double *__restrict__ a,
-                                                    const double *__restrict__ c, long ncol, int nn, int zper,
+                                                    const double *__restrict__ c, const float *__restrict__ a32,
+                                                    const int *__restrict__ zorder, long ncol, int nn, int zper,
                                                     double norm) {
-  const long col = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  // groups holding FP64 columns run first, so their long FP64 sweeps do not form the tail
+  const long col = (long)zorder[blockIdx.x] * blockDim.x + threadIdx.x;
   if (col >= ncol) return;
   if (fabs(lamcol[col]) >= lam32) {
     // software-pipelined sweeps: the loads of the next U rows are issued before the
@@ -337,7 +340,7 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
         }
 #pragma unroll
         for (int u = 0; u < U; u++) {
-          y = (sv[u] * normf - (float)a[k + u] * y) * zv[u];
+          y = (sv[u] * normf - a32[k + u] * y) * zv[u];
           S[(size_t)(k + u) * ncol + col] = y;
         }
         if (more) {
@@ -348,7 +351,7 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
     }
     for (int k = nfull * U; k < nn; k++) {
       const size_t idx = (size_t)k * ncol + col;
-      y = (S[idx] * normf - (float)a[k] * y) * zinv32[idx];
+      y = (S[idx] * normf - a32[k] * y) * zinv32[idx];
       S[idx] = y;
     }
     const float sn = y;
@@ -520,7 +523,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   if (!P) return CANS_OK;
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
-  cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
+  cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->a32); cudaFree(P->zorder); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
   cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->E32b); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
   delete P;
@@ -666,15 +669,15 @@ template <typename T> static int launch_y(cans_plan *P, int fwd) {
 static int launch_z(cans_plan *P, const Factor *F, double norm, bool f32) {
   const long ncol = (long)P->n[0] * P->n[1];
   const int nn = P->zper ? P->nn - 1 : P->nn;
-  const int tpb = 128;
+  const int tpb = kZGroup;
   const unsigned grid = (unsigned)((ncol + tpb - 1) / tpb);
   if (!f32)
     k_zsolve64<<<grid, tpb, 0, P->stream>>>((double *)P->S, F->zinv, F->dd, F->p2, F->dcl, P->a_d, P->c_d, ncol,
                                             nn, P->zper, norm);
   else
     k_zsolve_hyb<<<grid, tpb, 0, P->stream>>>((float *)P->S, P->R64, P->lamcol, P->lam32, F->zinv, F->dd, F->p2,
-                                              F->dcl, F->zinv32, F->dd32, F->p232, P->a_d, P->c_d, ncol, nn, P->zper,
-                                              norm);
+                                              F->dcl, F->zinv32, F->dd32, F->p232, P->a_d, P->c_d, P->a32, P->zorder,
+                                              ncol, nn, P->zper, norm);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
@@ -814,6 +817,7 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
   if ((e = cudaMalloc(&P->lamcol, lamcol.size() * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->zw, (n3 + 2) * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->a_d, n3 * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&P->a32, n3 * sizeof(float))) != cudaSuccess ||
       (e = cudaMalloc(&P->b_d, n3 * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->c_d, n3 * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->bb_d, n3 * sizeof(double))) != cudaSuccess ||
@@ -832,7 +836,25 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
   }
   // tridmatrix rows are D_k * (symmetric second difference): D = dzfi (centred) or dzci (faces)
   const double *zw_h = c_or_f[2] == 'c' ? dzfi_g : dzci_g;
-  if (cudaMemcpy(P->zw, zw_h, (n3 + 2) * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+  std::vector<float> a32h(P->a_h.begin(), P->a_h.end());
+  if (precision == CANS_FP32) {
+    const long ngrp = ((long)n1 * n2 + kZGroup - 1) / kZGroup;
+    std::vector<int> first, rest;
+    for (long g = 0; g < ngrp; g++) {
+      bool f64 = false;
+      for (long c = g * kZGroup; c < std::min<long>((g + 1) * kZGroup, (long)n1 * n2); c++)
+        if (fabs(lamcol[c]) < P->lam32) { f64 = true; break; }
+      (f64 ? first : rest).push_back((int)g);
+    }
+    first.insert(first.end(), rest.begin(), rest.end());
+    if ((e = cudaMalloc(&P->zorder, ngrp * sizeof(int))) != cudaSuccess ||
+        (e = cudaMemcpy(P->zorder, first.data(), ngrp * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess) {
+      cans_set_last_cuda_error(e);
+      return fail(CANS_ECUDA);
+    }
+  }
+  if (cudaMemcpy(P->a32, a32h.data(), n3 * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(P->zw, zw_h, (n3 + 2) * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(P->lamcol, lamcol.data(), lamcol.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(P->a_d, P->a_h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(P->b_d, P->b_h.data(), n3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
