@@ -19,7 +19,7 @@ import numpy as np
 
 from . import build as _build
 
-OK, EINVAL, ENOMEM, ECUDA, ENOTSUP, ETIMEOUT, ENONFINITE = range(7)
+OK, EINVAL, ENOMEM, ECUDA, ENOTSUP, ETIMEOUT, ENONFINITE, EIO = range(8)
 FP64, FP32 = 0, 1
 HALO_LOWER, HALO_NONE, HALO_UPPER, HALO_BOTH = -1, 0, 1, 2
 
@@ -93,6 +93,8 @@ def _setup(L):
     L.cans_batch_solve.argtypes = [_V, C.POINTER(_V), _D, _I]
     L.cans_boxes_create.argtypes = [C.c_int, C.POINTER(CBox), C.c_int, C.c_int, _V, C.POINTER(_V)]
     L.cans_plan_autotune.argtypes = [_V, C.c_int, _D]
+    L.cans_save_field.argtypes = [C.c_char_p, _I, _V, C.c_double, C.c_int, _V]
+    L.cans_load_field.argtypes = [C.c_char_p, _I, _V, _D, _I, _V]
     L.cans_solver_adjoint.argtypes = [_V, _V]
     L.cans_solve_helmholtz_adjoint.argtypes = [_V, C.c_double, _V]
     L.cans_fillps_adjoint.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
@@ -399,3 +401,29 @@ def rk_adjoint(rkpar, n, dli, dzci, dzfi, dt, visc, u, v, w, gu, gv, gw, gdu, gd
                                  _ptr(gdw), _ptr(gp), gbf if want_gbf else None, _ptr(work), _stream(stream)),
            "cans_rk_adjoint")
     return np.array(list(gbf))
+
+
+# ------------------------------------------------------------------------------ checkpoints
+def save_field(path, n, p, time, istep, stream=None):
+    """load_one('w', ...) (src/load.f90:461): interior in Fortran order + [time, istep]."""
+    _check(lib().cans_save_field(str(path).encode(), _ints(n), _ptr(p), float(time), int(istep), _stream(stream)),
+           "cans_save_field")
+
+
+def load_field(path, n, p, stream=None):
+    """load_one('r', ...): fills the interior of p, returns (time, istep)."""
+    t, it = C.c_double(), C.c_int()
+    _check(lib().cans_load_field(str(path).encode(), _ints(n), _ptr(p), C.byref(t), C.byref(it), _stream(stream)),
+           "cans_load_field")
+    return t.value, it.value
+
+
+def read_field_file(path, n):
+    """Host reader of a checkpoint file (the layout of the reference's
+    utils/read_binary_data/python/read_single_field_binary.py): returns the Fortran-indexed
+    interior array [i, j, k], time and istep."""
+    a = np.fromfile(path, dtype=np.float64)
+    npts = n[0] * n[1] * n[2]
+    if a.size != npts + 2:
+        raise ValueError(f"{path}: {a.size} values, expected {npts + 2}")
+    return a[:npts].reshape((n[0], n[1], n[2]), order="F"), float(a[npts]), int(round(a[npts + 1]))

@@ -71,11 +71,14 @@ __global__ void __launch_bounds__(kTile) k_batch_x(const BSys *__restrict__ sys,
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ DirParams sq;
   __shared__ FaceAdd sfa;
+  int last = -1;  // system whose twiddle tables are in shared memory (consecutive items mostly share it)
   for (long w = blockIdx.x; w < total; w += gridDim.x) {
     const int s = find_sys(start, nsys, w);
     const BSys *b = sys + s;
-    copy_to_smem(&sq, &b->qx[FWD ? 0 : 1]);
-    if (FWD) copy_to_smem(&sfa, &b->fa);
+    const bool ready = s == last;
+    if (!ready) copy_to_smem(&sq, &b->qx[FWD ? 0 : 1]);
+    if (FWD && !ready) copy_to_smem(&sfa, &b->fa);
+    last = s;
     __syncthreads();
     const int n1 = b->n1, n2 = b->n2;
     const long r = w - __ldg(&start[s]);
@@ -83,16 +86,16 @@ __global__ void __launch_bounds__(kTile) k_batch_x(const BSys *__restrict__ sys,
     const int k = (int)(r / ntj), tile = (int)(r - (long)k * ntj);
     if (FWD) {
       if (b->has_faces) {
-#define XF(MM) xfwd_tile<double, double, MM, true>(b->p, b->S, n1, n2, sq, tile, k, smem, &sfa)
+#define XF(MM) xfwd_tile<double, double, MM, true>(b->p, b->S, n1, n2, sq, tile, k, smem, &sfa, ready)
         CANS_BATCH_SWITCH(sq.spec, XF)
 #undef XF
       } else {
-#define XF(MM) xfwd_tile<double, double, MM>(b->p, b->S, n1, n2, sq, tile, k, smem)
+#define XF(MM) xfwd_tile<double, double, MM>(b->p, b->S, n1, n2, sq, tile, k, smem, nullptr, ready)
         CANS_BATCH_SWITCH(sq.spec, XF)
 #undef XF
       }
     } else {
-#define XB(MM) xbwd_tile<double, double, MM>(b->S, b->p, n1, n2, sq, 0, tile, k, smem)
+#define XB(MM) xbwd_tile<double, double, MM>(b->S, b->p, n1, n2, sq, 0, tile, k, smem, nullptr, nullptr, ready)
       CANS_BATCH_SWITCH(sq.spec, XB)
 #undef XB
     }
@@ -106,13 +109,16 @@ __global__ void __launch_bounds__(kTile) k_batch_y(const BSys *__restrict__ sys,
                                                     int nsys, long total) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ DirParams sq;
+  int last = -1;
   for (long w = blockIdx.x; w < total; w += gridDim.x) {
     const int s = find_sys(start, nsys, w);
     const BSys *b = sys + s;
-    copy_to_smem(&sq, &b->qy[FWD ? 0 : 1]);
+    const bool ready = s == last;
+    if (!ready) copy_to_smem(&sq, &b->qy[FWD ? 0 : 1]);
+    last = s;
     __syncthreads();
     const long nlines = (long)b->n1 * b->n3;
-#define YL(MM) ylines_tile<double, MM>(b->S, nlines, b->n2, sq, w - __ldg(&start[s]), smem)
+#define YL(MM) ylines_tile<double, MM>(b->S, nlines, b->n2, sq, w - __ldg(&start[s]), smem, ready)
     CANS_BATCH_SWITCH(sq.spec, YL)
 #undef YL
     __syncthreads();

@@ -132,8 +132,13 @@ __host__ __device__ inline size_t tile_tables_offset(int ncx, int ld, int lpb, i
   const size_t b = a > (size_t)lpb * sld * sizeof(T) ? a : (size_t)lpb * sld * sizeof(T);
   return (a + b + (size_t)lpb * sizeof(T) + 15) & ~(size_t)15;
 }
+// FP32 tiles copy the twiddle tables into shared memory (their stalls were dominated by the
+// table loads); FP64 tiles are FP64-pipe bound and read them through L1, keeping the
+// shared memory (and the resident CTAs) of the batched kernels' largest systems
+template <typename T> constexpr bool kTablesInSmem = sizeof(T) == 4;
 template <typename T> inline size_t smem_bytes(const DirParams &q) {
-  return tile_tables_offset<T>(q.ncx, q.ld, q.lpb, q.sld) + (size_t)(q.m + 2 * q.nt) * sizeof(cplx_t<T>) + 16;
+  const size_t tables = kTablesInSmem<T> ? (size_t)(q.m + 2 * q.nt) * sizeof(cplx_t<T>) : 0;
+  return tile_tables_offset<T>(q.ncx, q.ld, q.lpb, q.sld) + tables + 16;
 }
 
 // copy the twiddle tables a pass uses into shared memory (before the tile's first barrier)
@@ -242,7 +247,7 @@ template <> struct Vec16<double> { using type = double2; };
 template <typename T, typename TF, int M, bool FACES = false>
 __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restrict__ S, int n1, int n2,
                                           const DirParams &P, int tile, int k, unsigned char *smem,
-                                          const FaceAdd *fa = nullptr) {
+                                          const FaceAdd *fa = nullptr, bool tables_ready = false) {
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
@@ -253,8 +258,10 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
   const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
                                                                                       : (size_t)lpb * sld * sizeof(T);
   T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
-  T2 *tw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
-  T2 *post = tw + m, *pre = post + nt;
+  T2 *stw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
+  const T2 *tw = kTablesInSmem<T> ? stw : reinterpret_cast<const T2 *>(P.tw);
+  const T2 *post = kTablesInSmem<T> ? stw + m : reinterpret_cast<const T2 *>(P.post);
+  const T2 *pre = kTablesInSmem<T> ? stw + m + nt : reinterpret_cast<const T2 *>(P.pre);
   const int j0 = tile * lpb;
   for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
     const int r = M ? (int)((unsigned)e / (unsigned)M) : e / nt, i = e - r * nt, j = j0 + r;
@@ -270,7 +277,7 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
       else
         pass[r] = (j0 + r < n2) ? cvt_to<T, TF>(p[hidx(n1, j0 + r + 1, k + 1, n1, n2)]) : T(0);
     }
-  copy_tables<T>(P, m, nt, tw, post, pre);
+  if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
   r2r_pre<T, M>(P, stg, A, post, pre);
   __syncthreads();
@@ -300,7 +307,7 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
 // 2./4. y pass, in place on contiguous lines S[l*n2 .. l*n2+n2-1], l = k*n1 + i
 template <typename T, int M>
 __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int n2, const DirParams &P, long tile,
-                                            unsigned char *smem) {
+                                            unsigned char *smem, bool tables_ready = false) {
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
@@ -308,8 +315,10 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
   T2 *A = reinterpret_cast<T2 *>(smem);
   T2 *B = A + (size_t)ncx * ld;
   T *stg = reinterpret_cast<T *>(B);
-  T2 *tw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
-  T2 *post = tw + m, *pre = post + nt;
+  T2 *stw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
+  const T2 *tw = kTablesInSmem<T> ? stw : reinterpret_cast<const T2 *>(P.tw);
+  const T2 *post = kTablesInSmem<T> ? stw + m : reinterpret_cast<const T2 *>(P.post);
+  const T2 *pre = kTablesInSmem<T> ? stw + m + nt : reinterpret_cast<const T2 *>(P.pre);
   const long l0 = tile * lpb;
   if constexpr (M > 0) {
     // the tile's lines are one contiguous, 16-byte aligned run of LPB*M values (n2 == M)
@@ -329,7 +338,7 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
       stg[r * sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
     }
   }
-  copy_tables<T>(P, m, nt, tw, post, pre);
+  if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
   r2r_pre<T, M>(P, stg, A, post, pre);
   __syncthreads();
@@ -380,7 +389,8 @@ __device__ __forceinline__ TF xbwd_value(const TF *__restrict__ p, size_t idx, i
 template <typename T, typename TF, int M>
 __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2,
                                           const DirParams &P, int acc, int tile, int k, unsigned char *smem,
-                                          const T *add0 = nullptr, const T *add1 = nullptr) {
+                                          const T *add0 = nullptr, const T *add1 = nullptr,
+                                          bool tables_ready = false) {
   using T2 = cplx_t<T>;
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, ld = M ? G::LD : P.ld;
@@ -391,8 +401,10 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
   const size_t bbytes = (size_t)ncx * ld * sizeof(T2) > (size_t)lpb * sld * sizeof(T) ? (size_t)ncx * ld * sizeof(T2)
                                                                                       : (size_t)lpb * sld * sizeof(T);
   T *pass = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(B) + bbytes);
-  T2 *tw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
-  T2 *post = tw + m, *pre = post + nt;
+  T2 *stw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(ncx, ld, lpb, sld));
+  const T2 *tw = kTablesInSmem<T> ? stw : reinterpret_cast<const T2 *>(P.tw);
+  const T2 *post = kTablesInSmem<T> ? stw + m : reinterpret_cast<const T2 *>(P.post);
+  const T2 *pre = kTablesInSmem<T> ? stw + m + nt : reinterpret_cast<const T2 *>(P.pre);
   const int j0 = tile * lpb;
   const T *Sk = S + (size_t)k * n1 * n2;
   constexpr int VW = 16 / (int)sizeof(T);
@@ -417,7 +429,7 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
   if (!M && nt < n1)
     for (int r = threadIdx.x; r < lpb; r += blockDim.x)
       pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
-  copy_tables<T>(P, m, nt, tw, post, pre);
+  if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
   r2r_pre<T, M>(P, stg, A, post, pre);
   __syncthreads();

@@ -47,6 +47,7 @@ extern "C" const char *cans_strerror(int s) {
     case CANS_ENOTSUP: return "not supported (transform length or boundary-condition combination)";
     case CANS_ETIMEOUT: return "bounded device wait expired";
     case CANS_ENONFINITE: return "non-finite value";
+    case CANS_EIO: return "checkpoint file could not be opened, read or written";
     default: return "unknown status";
   }
 }

@@ -85,14 +85,28 @@ class Simulation:
             if a is not None:
                 getattr(self, name).copy_(cans.to_device(a, self.device))
 
-    def start(self):
-        """src/main.f90:388-418: BCs on the initial fields and the first dt."""
+    def start(self, restart_dir=None):
+        """src/main.f90:372-418: the initial fields (or, with restart_dir, the checkpoint
+        fld_u/v/w/p.bin there), their BCs and the first dt."""
         n = self.n
+        restart = restart_dir is not None
+        self.istep, self.time = 0, 0.
+        if restart:
+            import os
+            for name in ("u", "v", "w", "p"):
+                self.time, self.istep = cans.load_field(os.path.join(restart_dir, f"fld_{name}.bin"), n,
+                                                        getattr(self, name))
         cans.bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
-                      self.w, False)
+                      self.w, restart)
         cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
         self._new_dt()
-        self.istep, self.time = 0, 0.
+
+    def save(self, datadir):
+        """Checkpoint (src/main.f90:578-616 with is_overwrite_save): fld_u/v/w/p.bin."""
+        import os
+        for name in ("u", "v", "w", "p"):
+            cans.save_field(os.path.join(datadir, f"fld_{name}.bin"), self.n, getattr(self, name), self.time,
+                            self.istep)
 
     def _new_dt(self):
         dt_cfl = cans.chkdt(self.n, self.dl, self.dzci, self.dzfi, self.visc, 1. / DBL_MAX, self.is_impdiff, 0,

@@ -36,6 +36,7 @@ extern "C" {
 #define CANS_ENOTSUP 4     /* transform length or BC combination not supported */
 #define CANS_ETIMEOUT 5    /* a bounded device wait expired */
 #define CANS_ENONFINITE 6  /* non-finite value detected in a checked result */
+#define CANS_EIO 7         /* a checkpoint file could not be opened, read or written */
 
 /* arithmetic of a plan */
 #define CANS_FP64 0        /* all transforms/eliminations in FP64 */
@@ -162,6 +163,19 @@ int cans_chkdt(const int n[3], const double dl[3], const double *dzci, const dou
 /* bulk_mean (src/utils.f90:15): device FP64 reduction, synchronises `stream` */
 int cans_bulk_mean(const int n[3], const double *grid_vol_ratio, const double *p, double *mean,
                    void *stream);
+
+/* ---------------------------------------------------------------- checkpoints
+ * load_one (src/load.f90:461-589) with the MPI-IO file layout on one rank: the file holds
+ * the n1*n2*n3 interior values of the haloed device field p in Fortran order (FP64,
+ * native byte order) followed by [time, istep] as two FP64 values (main.f90 names them
+ * fld_u.bin, fld_v.bin, fld_w.bin, fld_p.bin).  Both synchronise `stream`.
+ * cans_load_field returns CANS_EINVAL for a file whose size is not (n1*n2*n3 + 2) * 8
+ * bytes (the reference aborts the run), CANS_EIO when the file cannot be opened or read;
+ * ghost cells of p are left untouched (the caller applies bounduvw/boundp, main.f90:389). */
+int cans_save_field(const char *path, const int n[3], const double *p, double time, int istep,
+                    void *stream);
+int cans_load_field(const char *path, const int n[3], double *p, double *time, int *istep,
+                    void *stream);
 
 /* ---------------------------------------------------------------- adjoints
  * No counterpart in the reference.  Transposed (vector-Jacobian) products of the FP64

@@ -57,3 +57,16 @@ def test_null_arguments_are_rejected_without_a_gpu(so):
     """Argument checks run before any CUDA call, so they work on a machine without a GPU."""
     assert so.cans_fillps(None, None, None, C.c_double(1.0), None, None, None, None, None) == 1
     assert so.cans_solver(None, None) == 1
+
+
+def test_checkpoint_file_reader_checks_size(tmp_path):
+    """The host reader of the checkpoint layout (interior in Fortran order + [time, istep])."""
+    from cans_gb300 import cans
+    n = (4, 3, 2)
+    vals = np.arange(24, dtype=np.float64)
+    np.concatenate([vals, [0.5, 7.0]]).tofile(tmp_path / "f.bin")
+    inner, t, it = cans.read_field_file(tmp_path / "f.bin", n)
+    assert inner.shape == n and inner[1, 0, 0] == 1.0 and inner[0, 1, 0] == 4.0 and (t, it) == (0.5, 7)
+    vals.tofile(tmp_path / "g.bin")
+    with pytest.raises(ValueError):
+        cans.read_field_file(tmp_path / "g.bin", n)

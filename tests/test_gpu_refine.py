@@ -102,3 +102,33 @@ def test_accuracy_against_extended_precision(require_gpu):
     print(f"vs extended precision: fp64 path {e64:.2e}, fp32+refinement {e32:.2e}")
     assert e32 <= max(1.5 * e64, 1e-13), (e32, e64)
     assert e32 <= 1e-12
+
+
+@pytest.mark.parametrize("n,l,cbc,gr", CASES[:3])
+def test_fixed_corrections_schedule(require_gpu, n, l, cbc, gr):
+    """max_iter = K with rtol = 0: K + 1 FP32 solves, the last correction added by its
+    x-backward pass.  The error against the oracle falls with K, two corrections reach the
+    FP64 accuracy, and the result equals (bit for bit) the verified run that stops after the
+    same corrections (same order of FP64 additions: fold in the residual pass, then add)."""
+    import torch
+    from cans_gb300 import cans
+    dl, dli, dzc, dzf, dzci, dzfi, p, want = _setup(n, l, cbc, gr, seed=5)
+    plan = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc", precision=cans.FP32)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
+    w = want[1:-1, 1:-1, 1:-1]
+    errs = []
+    outs = {}
+    for k in (0, 1, 2, 3):
+        d = cans.to_device(p)
+        it, rr = plan.solve_refined(d, dli, T(dzci), T(dzfi), rtol=0.0, max_iter=k)
+        assert it == k
+        got = cans.fview(d)[1:-1, 1:-1, 1:-1]
+        errs.append(gauge_rel_l2(got, w, dzf) if singular(cbc) else rel_l2(got, w))
+        outs[k] = d
+    assert errs[0] < 1e-4 and errs[1] < errs[0] and errs[2] <= 1e-12, errs
+    # a verified run (every residual evaluated) that stops after `it` corrections sums the
+    # same corrections in the same order as the fixed schedule with max_iter = it
+    d = cans.to_device(p)
+    it, rr = plan.solve_refined(d, dli, T(dzci), T(dzfi), rtol=1e-9, max_iter=8)
+    assert it in outs and rr <= 1e-9
+    assert torch.equal(d, outs[it])
