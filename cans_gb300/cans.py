@@ -93,7 +93,17 @@ def _setup(L):
     L.cans_batch_solve.argtypes = [_V, C.POINTER(_V), _D, _I]
     L.cans_boxes_create.argtypes = [C.c_int, C.POINTER(CBox), C.c_int, C.c_int, _V, C.POINTER(_V)]
     L.cans_plan_autotune.argtypes = [_V, C.c_int, _D]
+    L.cans_rk_buoy.argtypes = [_D, _I, _D, _V, _V, _V, _V, C.c_double, C.c_double, _V, _I, _D, _D, C.c_int, _D,
+                               C.c_double, _V, _V, _V, _V, _V, _V, _V, _D, _V, _V]
+    L.cans_rk_scal.argtypes = [_D, _I, _D, _V, _V, _V, C.c_double, C.c_double, _V, _V, _V, C.c_int, C.c_double,
+                               C.c_double, C.c_int, _V, _V, _D, _V, _V]
+    L.cans_rk_scal_work_doubles.argtypes = [_I, C.c_int]
+    L.cans_rk_scal_work_doubles.restype = C.c_size_t
+    L.cans_bulk_forcing_s.argtypes = [_I, C.c_int, C.c_double, _V, _V]
     L.cans_save_field.argtypes = [C.c_char_p, _I, _V, C.c_double, C.c_int, _V]
+    L.cans_out1d.argtypes = [_I, _D, _D, C.c_int, _V, _V, _V, _V]
+    L.cans_out1d_chan.argtypes = [_I, _D, _D, C.c_int, _V, _V, _V, _V, _V]
+    L.cans_out2d_duct.argtypes = [_I, _D, _D, C.c_int, _V, _V, _V, _V, _V]
     L.cans_load_field.argtypes = [C.c_char_p, _I, _V, _D, _I, _V]
     L.cans_solver_adjoint.argtypes = [_V, _V]
     L.cans_solve_helmholtz_adjoint.argtypes = [_V, C.c_double, _V]
@@ -403,6 +413,39 @@ def rk_adjoint(rkpar, n, dli, dzci, dzfi, dt, visc, u, v, w, gu, gv, gw, gdu, gd
     return np.array(list(gbf))
 
 
+# ------------------------------------------------------------------------------ profile statistics
+def _stats_out(count, like):
+    import torch
+    return torch.empty(int(count), dtype=torch.float64, device=like.device)
+
+
+def out1d(n, l, dl, idir, dz, p, stream=None):
+    """out1d (src/output.f90:56-157): the profile of p along idir averaged over the other
+    two directions (device tensor of n[idir-1] values).  dz: device dzf/dzc (0..n3+1)."""
+    out = _stats_out(n[idir - 1], p)
+    _check(lib().cans_out1d(_ints(n), _dbls(l), _dbls(dl), int(idir), _ptr(dz), _ptr(p), _ptr(out),
+                            _stream(stream)), "cans_out1d")
+    return out
+
+
+def out1d_chan(n, l, dl, u, v, w, idir=3, stream=None):
+    """out1d_chan (src/output.f90:327-393): (7, n3) device tensor um, vm, wm, u2, v2, w2, uw."""
+    out = _stats_out(7 * n[2], u)
+    _check(lib().cans_out1d_chan(_ints(n), _dbls(l), _dbls(dl), int(idir), _ptr(u), _ptr(v), _ptr(w), _ptr(out),
+                                 _stream(stream)), "cans_out1d_chan")
+    return out.view(7, n[2])
+
+
+def out2d_duct(n, l, dl, idir, u, v, w, stream=None):
+    """out2d_duct (src/output.f90:395-529): (8, n3, q) device tensor, q = n2 (idir 1) or n1
+    (idir 2); rows um, vm, wm, u2, v2, w2 and uv, uw (idir 1) or vw, uv (idir 2)."""
+    q = n[1] if idir == 1 else n[0]
+    out = _stats_out(8 * q * n[2], u)
+    _check(lib().cans_out2d_duct(_ints(n), _dbls(l), _dbls(dl), int(idir), _ptr(u), _ptr(v), _ptr(w), _ptr(out),
+                                 _stream(stream)), "cans_out2d_duct")
+    return out.view(8, n[2], q)
+
+
 # ------------------------------------------------------------------------------ checkpoints
 def save_field(path, n, p, time, istep, stream=None):
     """load_one('w', ...) (src/load.f90:461): interior in Fortran order + [time, istep]."""
@@ -427,3 +470,37 @@ def read_field_file(path, n):
     if a.size != npts + 2:
         raise ValueError(f"{path}: {a.size} values, expected {npts + 2}")
     return a[:npts].reshape((n[0], n[1], n[2]), order="F"), float(a[npts]), int(round(a[npts + 1]))
+
+
+# ------------------------------------------------------------------------------ scalars
+def rk_buoy(rkpar, n, dli, dzci, dzfi, gvr_c, gvr_f, dt, visc, p, is_forced, velf, bforce, is_impdiff, gacc, beta,
+            s, dudtrko, dvdtrko, dwdtrko, u, v, w, work=None, stream=None):
+    f = (C.c_double * 3)()
+    _check(lib().cans_rk_buoy(_dbls(rkpar), _ints(n), _dbls(dli), _ptr(dzci), _ptr(dzfi), _ptr(gvr_c), _ptr(gvr_f),
+                              float(dt), float(visc), _ptr(p), _ints(is_forced), _dbls(velf), _dbls(bforce),
+                              int(is_impdiff), _dbls(gacc), float(beta), _ptr(s), _ptr(dudtrko), _ptr(dvdtrko),
+                              _ptr(dwdtrko), _ptr(u), _ptr(v), _ptr(w), f, _ptr(work), _stream(stream)),
+           "cans_rk_buoy")
+    return np.array(list(f))
+
+
+def rk_scal_work(n, is_impdiff, device="cuda"):
+    import torch
+    return torch.empty(int(lib().cans_rk_scal_work_doubles(_ints(n), int(is_impdiff))), dtype=torch.float64,
+                       device=device)
+
+
+def rk_scal(rkpar, n, dli, dzci, dzfi, gvr_f, alpha, dt, u, v, w, is_forced, scalf, ssource, is_impdiff, dsdtrko, s,
+            work, stream=None):
+    """rk_scal (src/rk.f90:335): returns f (scalf - mean when forced)"""
+    f = C.c_double()
+    _check(lib().cans_rk_scal(_dbls(rkpar), _ints(n), _dbls(dli), _ptr(dzci), _ptr(dzfi), _ptr(gvr_f), float(alpha),
+                              float(dt), _ptr(u), _ptr(v), _ptr(w), int(is_forced), float(scalf), float(ssource),
+                              int(is_impdiff), _ptr(dsdtrko), _ptr(s), C.byref(f), _ptr(work), _stream(stream)),
+           "cans_rk_scal")
+    return f.value
+
+
+def bulk_forcing_s(n, is_forced, f, s, stream=None):
+    _check(lib().cans_bulk_forcing_s(_ints(n), int(is_forced), float(f), _ptr(s), _stream(stream)),
+           "cans_bulk_forcing_s")

@@ -93,9 +93,10 @@ __global__ void __launch_bounds__(kTB) k_mom_rk(Dims d, double dxi, double dyi, 
                                                 const double *__restrict__ w, const double *__restrict__ p,
                                                 double *__restrict__ dudtrko, double *__restrict__ dvdtrko,
                                                 double *__restrict__ dwdtrko, double *__restrict__ unew,
-                                                double *__restrict__ dtd) {
+                                                double *__restrict__ dtd, const double *__restrict__ sb, double gbx,
+                                                double gby, double gbz, double beta) {
   mom_rk_cell(d, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, impdiff, dzci, dzfi, u, v, w, p, dudtrko, dvdtrko, dwdtrko,
-              unew, dtd, (long)blockIdx.x * blockDim.x + threadIdx.x);
+              unew, dtd, (long)blockIdx.x * blockDim.x + threadIdx.x, sb, gbx, gby, gbz, beta);
 }
 
 // copy-back of the new velocity with the per-block partial sums of the bulk means
@@ -217,13 +218,14 @@ extern "C" size_t cans_rk_work_doubles(const int n[3], int is_impdiff) {
   return (size_t)3 * np + (is_impdiff ? 3 * (size_t)np : 0) + 3 * (size_t)blocks_for(np) + 8;
 }
 
-extern "C" int cans_rk(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
-                       const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
-                       const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
-                       int is_impdiff, double *dudtrko, double *dvdtrko, double *dwdtrko, double *u, double *v,
-                       double *w, double f[3], double *work, void *stream) {
+static int rk_impl(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                   const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
+                   const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
+                   int is_impdiff, double *dudtrko, double *dvdtrko, double *dwdtrko, double *u, double *v,
+                   double *w, double f[3], double *work, void *stream, const double *sb, const double *gacc,
+                   double beta) {
   if (!rkpar || !n || !dli || !dzci || !dzfi || !gvr_c || !gvr_f || !p || !is_forced || !velf || !bforce ||
-      !dudtrko || !dvdtrko || !dwdtrko || !u || !v || !w)
+      !dudtrko || !dvdtrko || !dwdtrko || !u || !v || !w || (sb && !gacc))
     return CANS_EINVAL;
   if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   cudaStream_t st = as_stream(stream);
@@ -241,7 +243,8 @@ extern "C" int cans_rk(const double rkpar[2], const int n[3], const double dli[3
          *fdev = means + 3;
   const double f1 = rkpar[0] * dt, f2 = rkpar[1] * dt, f12 = f1 + f2;
   k_mom_rk<<<nblk, kTB, 0, st>>>(d, dli[0], dli[1], visc, f1, f2, f12, bforce[0], bforce[1], bforce[2],
-                                  is_impdiff ? 1 : 0, dzci, dzfi, u, v, w, p, dudtrko, dvdtrko, dwdtrko, unew, dtd);
+                                  is_impdiff ? 1 : 0, dzci, dzfi, u, v, w, p, dudtrko, dvdtrko, dwdtrko, unew, dtd,
+                                  sb, sb ? gacc[0] : 0., sb ? gacc[1] : 0., sb ? gacc[2] : 0., beta);
   CANS_LAUNCH_CHECK();
   k_rk_writeback<<<nblk, kTB, 0, st>>>(d, unew, gvr_c, gvr_f, u, v, w, partials);
   CANS_LAUNCH_CHECK();
@@ -260,6 +263,125 @@ extern "C" int cans_rk(const double rkpar[2], const int n[3], const double dli[3
       CANS_CUDA_TRY(cudaStreamSynchronize(st));
     }
   }
+  return CANS_OK;
+}
+
+extern "C" int cans_rk(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                       const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
+                       const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
+                       int is_impdiff, double *dudtrko, double *dvdtrko, double *dwdtrko, double *u, double *v,
+                       double *w, double f[3], double *work, void *stream) {
+  return rk_impl(rkpar, n, dli, dzci, dzfi, gvr_c, gvr_f, dt, visc, p, is_forced, velf, bforce, is_impdiff, dudtrko,
+                 dvdtrko, dwdtrko, u, v, w, f, work, stream, nullptr, nullptr, 0.);
+}
+
+// rk with the Boussinesq buoyancy of the first scalar s (src/rk.f90:24-25 with gacc, beta)
+extern "C" int cans_rk_buoy(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                            const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
+                            const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
+                            int is_impdiff, const double gacc[3], double beta, const double *s, double *dudtrko,
+                            double *dvdtrko, double *dwdtrko, double *u, double *v, double *w, double f[3],
+                            double *work, void *stream) {
+  if (!s || !gacc) return CANS_EINVAL;
+  return rk_impl(rkpar, n, dli, dzci, dzfi, gvr_c, gvr_f, dt, visc, p, is_forced, velf, bforce, is_impdiff, dudtrko,
+                 dvdtrko, dwdtrko, u, v, w, f, work, stream, s, gacc, beta);
+}
+
+// ------------------------------------------------------------------------------ scalars
+__global__ void __launch_bounds__(kTB) k_rk_scal(Dims d, double dxi, double dyi, double alpha, double f1, double f2,
+                                                 double f12, double ssource, int impdiff,
+                                                 const double *__restrict__ dzci, const double *__restrict__ dzfi,
+                                                 const double *__restrict__ u, const double *__restrict__ v,
+                                                 const double *__restrict__ w, const double *__restrict__ s,
+                                                 double *__restrict__ dsdtrko, double *__restrict__ snew,
+                                                 double *__restrict__ dtd) {
+  rk_scal_cell(d, dxi, dyi, alpha, f1, f2, f12, ssource, impdiff, dzci, dzfi, u, v, w, s, dsdtrko, snew, dtd,
+               (long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// write-back of the new scalar with per-block partial sums of its volume-weighted mean
+__global__ void __launch_bounds__(kTB) k_scal_writeback(Dims d, const double *__restrict__ snew,
+                                                        const double *__restrict__ gvr_f, double *__restrict__ s,
+                                                        double *__restrict__ partials) {
+  __shared__ double red[kTB / 32];
+  int i, j, k;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  double a = 0.;
+  if (cell3(t, d, i, j, k)) {
+    const double v = snew[t];
+    s[hidx(i, j, k, d.n1, d.n2)] = v;
+    a = v * gvr_f[k];
+  }
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.;
+    for (int q = 0; q < kTB / 32; q++) b += red[q];
+    partials[blockIdx.x] = b;
+  }
+}
+
+// s += c * dtd (interior; the implicit-diffusion right-hand side: c = -f12/2), or s += f
+__global__ void __launch_bounds__(kTB) k_scal_axpy(Dims d, double c, const double *__restrict__ dtd, double f,
+                                                   double *__restrict__ s) {
+  int i, j, k;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!cell3(t, d, i, j, k)) return;
+  const size_t x = hidx(i, j, k, d.n1, d.n2);
+  s[x] = dtd ? s[x] - c * dtd[t] : s[x] + f;
+}
+
+extern "C" size_t cans_rk_scal_work_doubles(const int n[3], int is_impdiff) {
+  if (!n) return 0;
+  const long np = (long)n[0] * n[1] * n[2];
+  return (size_t)np * (is_impdiff ? 2 : 1) + (size_t)blocks_for(np) + 8;
+}
+
+// rk_scal (src/rk.f90:335-491, no wall-flux output): returns in *f the forcing scalf - mean
+// (0 when not forced, which then needs no synchronisation); the forcing itself is applied
+// by cans_bulk_forcing_s, as in src/main.f90:442-444
+extern "C" int cans_rk_scal(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                            const double *dzfi, const double *gvr_f, double alpha, double dt, const double *u,
+                            const double *v, const double *w, int is_forced, double scalf, double ssource,
+                            int is_impdiff, double *dsdtrko, double *s, double *f, double *work, void *stream) {
+  if (!rkpar || !n || !dli || !dzci || !dzfi || !gvr_f || !u || !v || !w || !dsdtrko || !s || !work) return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const long np = (long)n[0] * n[1] * n[2];
+  const unsigned nblk = blocks_for(np);
+  double *snew = work, *dtd = work + np, *partials = work + np * (is_impdiff ? 2 : 1), *mean = partials + nblk;
+  const double f1 = rkpar[0] * dt, f2 = rkpar[1] * dt, f12 = f1 + f2;
+  k_rk_scal<<<nblk, kTB, 0, st>>>(d, dli[0], dli[1], alpha, f1, f2, f12, ssource, is_impdiff ? 1 : 0, dzci, dzfi, u,
+                                   v, w, s, dsdtrko, snew, dtd);
+  CANS_LAUNCH_CHECK();
+  k_scal_writeback<<<nblk, kTB, 0, st>>>(d, snew, gvr_f, s, partials);
+  CANS_LAUNCH_CHECK();
+  double ff = 0.;
+  if (is_forced) {
+    k_sum_partials<<<1, kTB, 0, st>>>(partials, nblk, 1, 1, mean);
+    CANS_LAUNCH_CHECK();
+    double m = 0.;
+    CANS_CUDA_TRY(cudaMemcpyAsync(&m, mean, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CANS_CUDA_TRY(cudaStreamSynchronize(st));
+    ff = scalf - m;
+  }
+  if (is_impdiff) {
+    k_scal_axpy<<<nblk, kTB, 0, st>>>(d, .5 * f12, dtd, 0., s);
+    CANS_LAUNCH_CHECK();
+  }
+  if (f) *f = ff;
+  return CANS_OK;
+}
+
+// bulk_forcing_s (src/scal.f90:301-319)
+extern "C" int cans_bulk_forcing_s(const int n[3], int is_forced, double f, double *s, void *stream) {
+  if (!n || !s || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  if (!is_forced) return CANS_OK;
+  Dims d{n[0], n[1], n[2]};
+  k_scal_axpy<<<blocks_for((long)n[0] * n[1] * n[2]), kTB, 0, as_stream(stream)>>>(d, 0., nullptr, f, s);
+  CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
 

@@ -78,7 +78,9 @@ __device__ __forceinline__ void mom_rk_cell(const Dims &d, double dxi, double dy
                                                 const double *__restrict__ w, const double *__restrict__ p,
                                                 double *__restrict__ dudtrko, double *__restrict__ dvdtrko,
                                                 double *__restrict__ dwdtrko, double *__restrict__ unew,
-                                                double *__restrict__ dtd, long t) {
+                                                double *__restrict__ dtd, long t,
+                                                const double *__restrict__ sb = nullptr, double gbx = 0.,
+                                                double gby = 0., double gbz = 0., double beta = 0.) {
   int i, j, k;
   if (!cell3(t, d, i, j, k)) return;
   const int n1 = d.n1, n2 = d.n2;
@@ -137,6 +139,13 @@ __device__ __forceinline__ void mom_rk_cell(const Dims &d, double dxi, double dy
   double un = u_ccc + f1 * dudt + f2 * dudtrko[h] + f12 * (bfx - dxi * (p[c + sx] - pc));
   double vn = v_ccc + f1 * dvdt + f2 * dvdtrko[h] + f12 * (bfy - dyi * (p[c + sy] - pc));
   double wn = w_ccc + f1 * dwdt + f2 * dwdtrko[h] + f12 * (bfz - dzci_k * (p[c + sz] - pc));
+  if (sb) {
+    // Boussinesq buoyancy of the first scalar (src/rk.f90:163-177), gacc * beta
+    const double sc = sb[c];
+    un = un - f12 * gbx * beta * 0.5 * (sb[c + sx] + sc);
+    vn = vn - f12 * gby * beta * 0.5 * (sb[c + sy] + sc);
+    wn = wn - f12 * gbz * beta * 0.5 * (sb[c + sz] + sc);
+  }
   if (impdiff) {
     un = un + f12 * dud; vn = vn + f12 * dvd; wn = wn + f12 * dwd;
     dtd[h] = dud; dtd[h + np] = dvd; dtd[h + 2 * np] = dwd;
@@ -180,4 +189,41 @@ __device__ __forceinline__ void set_bc_cell(double *p, int n1, int n2, int n3, c
     if (ib == 0) at(0) = 1. * factor + at(1);
     else { at(nn + 1) = at(nn); at(nn) = 1. * factor + at(nn - 1); }
   }
+}
+
+// scal (src/scal.f90:41-193, is_impdiff_1d = .false.) fused with the update of
+// src/rk.f90:405-421 at interior cell t: new scalar to snew (halo-free), dsdtrko <- dsdt
+// (the old value is read first), dsdtd to dtd (impdiff)
+__device__ __forceinline__ void rk_scal_cell(const Dims &d, double dxi, double dyi, double alpha, double f1, double f2,
+                                             double f12, double ssource, int impdiff,
+                                             const double *__restrict__ dzci, const double *__restrict__ dzfi,
+                                             const double *__restrict__ u, const double *__restrict__ v,
+                                             const double *__restrict__ w, const double *__restrict__ s,
+                                             double *__restrict__ dsdtrko, double *__restrict__ snew,
+                                             double *__restrict__ dtd, long t) {
+  int i, j, k;
+  if (!cell3(t, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
+  const size_t c = hidx(i, j, k, n1, n2);
+  const double sc = s[c], s_m = s[c - 1], s_p = s[c + 1], s_s = s[c - sy], s_n = s[c + sy], s_b = s[c - sz],
+               s_t = s[c + sz];
+  const double usim = 0.5 * (s_m + sc) * u[c - 1], usip = 0.5 * (s_p + sc) * u[c];
+  const double vsjm = 0.5 * (s_s + sc) * v[c - sy], vsjp = 0.5 * (s_n + sc) * v[c];
+  const double wskm = 0.5 * (s_b + sc) * w[c - sz], wskp = 0.5 * (s_t + sc) * w[c];
+  const double dsdxp = (s_p - sc) * dxi, dsdxm = (sc - s_m) * dxi;
+  const double dsdyp = (s_n - sc) * dyi, dsdym = (sc - s_s) * dyi;
+  const double dsdzp = (s_t - sc) * dzci[k], dsdzm = (sc - s_b) * dzci[k - 1];
+  double ds = dxi * (-usip + usim) + dyi * (-vsjp + vsjm) + dzfi[k] * (-wskp + wskm);
+  const double dxy = (dsdxp - dsdxm) * alpha * dxi + (dsdyp - dsdym) * alpha * dyi;
+  const double dz = (dsdzp - dsdzm) * alpha * dzfi[k];
+  const double dsd = dxy + dz;
+  if (!impdiff) ds = ds + dxy + dz;
+  double sn = sc + f1 * ds + f2 * dsdtrko[t] + f12 * ssource;
+  if (impdiff) {
+    sn = sn + f12 * dsd;
+    dtd[t] = dsd;
+  }
+  dsdtrko[t] = ds;
+  snew[t] = sn;
 }

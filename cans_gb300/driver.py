@@ -10,13 +10,17 @@ Fortran host would.
 
 `case` keys follow input.nml (&dns, &numerics): ng, l, gtype, gr, cfl, dtmax,
 dt_f, visci, icheck, cbcvel (18 chars, cbcvel(0:1,3,3) order), bcvel (18),
-cbcpre (6 chars), bcpre (6), bforce, is_forced, velf, is_impdiff, inivel.
+cbcpre (6 chars), bcpre (6), bforce, is_forced, velf, is_impdiff, inivel; and the
+&scalar keys (src/param.f90:144-151): nscal, alphai, cbcscal (6 chars each), bcscal
+(6 each), ssource, is_sforced, scalf, gacc, beta, is_boussinesq_buoyancy.  Scalars are
+advanced before the velocity in every substep (src/main.f90:440-451).
 """
 import ctypes as C
 
 import numpy as np
 
 from . import cans
+from . import output
 
 RKCOEFF = ((32. / 60., 0. / 60.), (25. / 60., -17. / 60.), (45. / 60., -25. / 60.))  # src/param.f90:20-22
 DBL_MAX = np.finfo(np.float64).max
@@ -77,13 +81,50 @@ class Simulation:
         self.time, self.istep, self.dt, self.dti = 0., 0, 0., 0.
         self.divtot = self.divmax = 0.
         self.dpdl = np.zeros(3)
+        self._init_scalars(case, device)
+
+    def _init_scalars(self, case, device):
+        """src/scal.f90:321-360 (initialize_scalars) and src/param.f90:277-317."""
+        import torch
+        n = self.n
+        nscal = max(0, int(case.get("nscal", 0)))
+        self.gacc = [float(x) for x in case.get("gacc", [0.] * 3)]
+        self.beta = float(case.get("beta", 0.))
+        self.is_buoyancy = bool(case.get("is_boussinesq_buoyancy", False))
+        if self.is_buoyancy and nscal == 0:
+            raise ValueError("is_boussinesq_buoyancy requires nscal > 0")
+        self.scalars = []
+        for i in range(nscal):
+            cbc = case["cbcscal"][i]
+            bc = list(case.get("bcscal", [[0.] * 6] * nscal)[i])
+            sc = {"alpha": 1. / float(case["alphai"][i]), "cbc": cbc, "bc": bc,
+                  "source": float(case.get("ssource", [0.] * nscal)[i]),
+                  "is_forced": int(case.get("is_sforced", [0] * nscal)[i]),
+                  "scalf": float(case.get("scalf", [0.] * nscal)[i]),
+                  "val": cans.field(n, device),
+                  "dsdtrko": torch.zeros((n[2], n[1], n[0]), dtype=torch.float64, device=device),
+                  "work": cans.rk_scal_work(n, self.is_impdiff, device), "f": 0.}
+            if self.is_impdiff:
+                sc["plan"] = cans.Plan(n, self.dli, self.dzci_h, self.dzfi_h, cbc, bc, "ccc")
+            self.scalars.append(sc)
+        self.fs = np.zeros(nscal)
+        # alpha_max: the largest diffusivity, for the time-step restriction
+        self.alpha_max = max([sc["alpha"] for sc in self.scalars], default=1. / DBL_MAX)
 
     # ------------------------------------------------------------------ initial conditions
-    def set_fields(self, u=None, v=None, w=None, p=None):
+    def set_fields(self, u=None, v=None, w=None, p=None, scalars=()):
         """Fortran-indexed host arrays (n1+2, n2+2, n3+2) -> device fields."""
         for name, a in (("u", u), ("v", v), ("w", w), ("p", p)):
             if a is not None:
                 getattr(self, name).copy_(cans.to_device(a, self.device))
+        for sc, a in zip(self.scalars, scalars):
+            if a is not None:
+                sc["val"].copy_(cans.to_device(a, self.device))
+
+    def _io_vars(self):
+        """(file stem, field) of every checkpointed variable, src/main.f90:360-368."""
+        out = [(name, getattr(self, name)) for name in ("u", "v", "w", "p")]
+        return out + [(f"s_{i + 1:03d}", sc["val"]) for i, sc in enumerate(self.scalars)]
 
     def start(self, restart_dir=None):
         """src/main.f90:372-418: the initial fields (or, with restart_dir, the checkpoint
@@ -93,23 +134,62 @@ class Simulation:
         self.istep, self.time = 0, 0.
         if restart:
             import os
-            for name in ("u", "v", "w", "p"):
-                self.time, self.istep = cans.load_field(os.path.join(restart_dir, f"fld_{name}.bin"), n,
-                                                        getattr(self, name))
+            for name, fld in self._io_vars():
+                self.time, self.istep = cans.load_field(os.path.join(restart_dir, f"fld_{name}.bin"), n, fld)
         cans.bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
                       self.w, restart)
         cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
+        for sc in self.scalars:
+            cans.boundp(sc["cbc"], n, sc["bc"], self.is_bound, self.dl, self.dzc, sc["val"])
         self._new_dt()
 
     def save(self, datadir):
-        """Checkpoint (src/main.f90:578-616 with is_overwrite_save): fld_u/v/w/p.bin."""
+        """Checkpoint (src/main.f90:578-616 with is_overwrite_save): fld_u/v/w/p.bin and
+        fld_s_001.bin ... for the scalars."""
         import os
-        for name in ("u", "v", "w", "p"):
-            cans.save_field(os.path.join(datadir, f"fld_{name}.bin"), self.n, getattr(self, name), self.time,
-                            self.istep)
+        for name, fld in self._io_vars():
+            cans.save_field(os.path.join(datadir, f"fld_{name}.bin"), self.n, fld, self.time, self.istep)
+
+    # ------------------------------------------------------------------ text output
+    def out0d(self, datadir):
+        """The 0d logs of src/main.f90:515-552: time.out, forcing.out and forcing_s_NNN.out."""
+        import os
+        output.out0d(os.path.join(datadir, "time.out"), [1. * self.istep, self.dt, self.time])
+        if any(self.is_forced) or any(abs(b) > 0. for b in self.bforce):
+            mean = [0., 0., 0.]
+            for d, (fld, gvr) in enumerate(((self.u, self.gvr_f), (self.v, self.gvr_f), (self.w, self.gvr_c))):
+                if self.is_forced[d] or abs(self.bforce[d]) > 0.:
+                    mean[d] = cans.bulk_mean(self.n, gvr, fld)
+            dpdl = list(self.dpdl) if any(self.is_forced) else [-b for b in self.bforce]
+            output.out0d(os.path.join(datadir, "forcing.out"), [self.time] + dpdl + mean)
+        for i, sc in enumerate(self.scalars):
+            if sc["is_forced"] or abs(sc["source"]) > 0.:
+                ms = cans.bulk_mean(self.n, self.gvr_f, sc["val"])
+                fs = self.fs[i] if sc["is_forced"] else sc["source"]
+                output.out0d(os.path.join(datadir, f"forcing_s_{i + 1:03d}.out"), [self.time, fs, ms])
+
+    def out1d(self, datadir, velstats=False):
+        """The profiles of src/out1d.h90: umean_z, vmean_z, wmean_z (and scal_01_mean with a
+        scalar) for step istep; velstats=True adds out1d_chan's velstats file."""
+        import os
+        import torch
+        n, fld = self.n, f"{self.istep:07d}"
+        dzf, dzc = (torch.tensor(a, dtype=torch.float64, device=self.u.device) for a in (self.dzf, self.dzc))
+        path = lambda name: os.path.join(datadir, f"{name}_fld_{fld}.out")
+        items = [("umean_z", self.zc, dzf, self.u), ("vmean_z", self.zc, dzf, self.v),
+                 ("wmean_z", self.zf, dzc, self.w)]
+        if self.scalars:
+            items.append(("scal_01_mean", self.zc, dzc, self.scalars[0]["val"]))
+        for name, z_g, dz, f in items:
+            p1d = cans.out1d(n, self.l, self.dl, 3, dz, f).cpu().numpy()
+            output.write_out1d(path(name), 3, n, self.dl, z_g, p1d)
+        if velstats:
+            st = cans.out1d_chan(n, self.l, self.dl, self.u, self.v, self.w).cpu().numpy()
+            output.write_out1d_chan(path("velstats"), n, self.zc, st)
+        torch.cuda.synchronize()
 
     def _new_dt(self):
-        dt_cfl = cans.chkdt(self.n, self.dl, self.dzci, self.dzfi, self.visc, 1. / DBL_MAX, self.is_impdiff, 0,
+        dt_cfl = cans.chkdt(self.n, self.dl, self.dzci, self.dzfi, self.visc, self.alpha_max, self.is_impdiff, 0,
                             self.u, self.v, self.w)
         self.dt = self.dt_f if self.dt_f > 0. else min(self.cfl * dt_cfl, self.dtmax)
         self.dti = 1. / self.dt
@@ -119,9 +199,22 @@ class Simulation:
         n = self.n
         dtrk = (RKCOEFF[irk][0] + RKCOEFF[irk][1]) * self.dt
         dtrki = 1. / dtrk
-        f = cans.rk(RKCOEFF[irk], n, self.dli, self.dzci, self.dzfi, self.gvr_c, self.gvr_f, self.dt, self.visc,
-                    self.p, self.is_forced, self.velf, self.bforce, self.is_impdiff, self.dudtrko, self.dvdtrko,
-                    self.dwdtrko, self.u, self.v, self.w)
+        for i, sc in enumerate(self.scalars):
+            sc["f"] = cans.rk_scal(RKCOEFF[irk], n, self.dli, self.dzci, self.dzfi, self.gvr_f, sc["alpha"], self.dt,
+                                   self.u, self.v, self.w, sc["is_forced"], sc["scalf"], sc["source"],
+                                   self.is_impdiff, sc["dsdtrko"], sc["val"], sc["work"])
+            cans.bulk_forcing_s(n, sc["is_forced"], sc["f"], sc["val"])
+            self.fs[i] += sc["f"]
+            if self.is_impdiff:
+                sc["plan"].solve_helmholtz(-.5 * sc["alpha"] * dtrk, self.is_bound, sc["val"])
+            cans.boundp(sc["cbc"], n, sc["bc"], self.is_bound, self.dl, self.dzc, sc["val"])
+        rk_args = (RKCOEFF[irk], n, self.dli, self.dzci, self.dzfi, self.gvr_c, self.gvr_f, self.dt, self.visc,
+                   self.p, self.is_forced, self.velf, self.bforce, self.is_impdiff)
+        fields = (self.dudtrko, self.dvdtrko, self.dwdtrko, self.u, self.v, self.w)
+        if self.is_buoyancy:
+            f = cans.rk_buoy(*rk_args, self.gacc, self.beta, self.scalars[0]["val"], *fields)
+        else:
+            f = cans.rk(*rk_args, *fields)
         self.dpdl += f
         alpha = 0.
         if self.is_impdiff:
@@ -145,9 +238,11 @@ class Simulation:
             self.istep += 1
             self.time += self.dt
             self.dpdl[:] = 0.
+            self.fs[:] = 0.
             for irk in range(3):
                 self.substep(irk)
             self.dpdl = -self.dpdl * self.dti
+            self.fs = self.fs * self.dti
             if self.icheck > 0 and self.istep % self.icheck == 0:
                 self._new_dt()
                 self.divtot, self.divmax = cans.chkdiv(self.n, self.l, self.dli, self.dzfi, self.u, self.v, self.w)

@@ -122,6 +122,28 @@ int cans_rk(const double rkpar[2], const int n[3], const double dli[3], const do
             const double bforce[3], int is_impdiff, double *dudtrko, double *dvdtrko, double *dwdtrko,
             double *u, double *v, double *w, double f[3], double *work, void *stream);
 size_t cans_rk_work_doubles(const int n[3], int is_impdiff);
+/* rk with the Boussinesq buoyancy of the first scalar (src/rk.f90:24-25, gacc/beta):
+ * u -= f12 * gacc * beta * (s interpolated to the face), same arguments as cans_rk plus
+ * gacc[3], beta and the haloed device scalar s */
+int cans_rk_buoy(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                 const double *dzfi, const double *grid_vol_ratio_c, const double *grid_vol_ratio_f,
+                 double dt, double visc, const double *p, const int is_forced[3], const double velf[3],
+                 const double bforce[3], int is_impdiff, const double gacc[3], double beta, const double *s,
+                 double *dudtrko, double *dvdtrko, double *dwdtrko, double *u, double *v, double *w,
+                 double f[3], double *work, void *stream);
+/* rk_scal (src/rk.f90:335-491) with scal (src/scal.f90:41-193): one RK3 substep of a
+ * cell-centred scalar s (haloed) with diffusivity alpha, source ssource, RHS history
+ * dsdtrko (halo-free); with is_impdiff the implicit part is left for the Helmholtz solve
+ * (s -= f12/2 * dsdtd).  *f (host) = scalf - bulk mean when is_forced (synchronises the
+ * stream), else 0.  work: cans_rk_scal_work_doubles(n, is_impdiff) device doubles. */
+int cans_rk_scal(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                 const double *dzfi, const double *grid_vol_ratio_f, double alpha, double dt,
+                 const double *u, const double *v, const double *w, int is_forced, double scalf,
+                 double ssource, int is_impdiff, double *dsdtrko, double *s, double *f, double *work,
+                 void *stream);
+size_t cans_rk_scal_work_doubles(const int n[3], int is_impdiff);
+/* bulk_forcing_s (src/scal.f90:301): s += f on the interior when is_forced */
+int cans_bulk_forcing_s(const int n[3], int is_forced, double f, double *s, void *stream);
 /* bounduvw (src/bound.f90:17), one GPU: halos_* are -1 lower, 0 none, 1 upper, 2 both
  * (argument absent in the reference).  dl: host; dzc, dzf: HOST arrays 0..n3+1
  * (only dzc(0), dzc(n3), dzf(0), dzf(n3) are read). */
@@ -163,6 +185,26 @@ int cans_chkdt(const int n[3], const double dl[3], const double *dzci, const dou
 /* bulk_mean (src/utils.f90:15): device FP64 reduction, synchronises `stream` */
 int cans_bulk_mean(const int n[3], const double *grid_vol_ratio, const double *p, double *mean,
                    void *stream);
+
+/* ---------------------------------------------------------------- profile statistics
+ * Plane/line averages of the output routines (device arrays in and out, asynchronous on
+ * `stream`); the host writes the files.
+ * cans_out1d: out1d (src/output.f90:56-157), the profile of p along idir (1..3) averaged over
+ *   the other two directions; out holds n[idir-1] values; dz (device, indices 0..n3+1, the
+ *   dzf or dzc array of the variable) weights the z sums of idir = 1, 2 and may be NULL for 3.
+ * cans_out1d_chan: out1d_chan (src/output.f90:327-393), idir = 3 only (1 and 2 compute
+ *   nothing, as in the reference): out = [um, vm, wm, u2, v2, w2, uw], n3 values each, the
+ *   second moments minus the products of the means.
+ * cans_out2d_duct: out2d_duct (src/output.f90:395-529), averages along the streamwise
+ *   direction idir = 1 (out = [um, vm, wm, u2, v2, w2, uv, uw], each (n2, n3), j fastest) or
+ *   idir = 2 (out = [um, vm, wm, u2, v2, w2, vw, uv], each (n1, n3), i fastest); idir = 3
+ *   computes nothing, as in the reference. */
+int cans_out1d(const int n[3], const double l[3], const double dl[3], int idir, const double *dz, const double *p,
+               double *out, void *stream);
+int cans_out1d_chan(const int n[3], const double l[3], const double dl[3], int idir, const double *u,
+                    const double *v, const double *w, double *out, void *stream);
+int cans_out2d_duct(const int n[3], const double l[3], const double dl[3], int idir, const double *u,
+                    const double *v, const double *w, double *out, void *stream);
 
 /* ---------------------------------------------------------------- checkpoints
  * load_one (src/load.f90:461-589) with the MPI-IO file layout on one rank: the file holds

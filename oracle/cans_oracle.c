@@ -645,11 +645,26 @@ double orc_bulk_mean(const int n[3], const double *gvr, const double *p) {
 }
 
 /* src/rk.f90:24-333 (+ cmpt_bulk_forcing 493-518, bulk_forcing mom.f90:725-769) */
+/* rk with the Boussinesq buoyancy of src/rk.f90:155-186 (default loop): s == NULL -> none */
+void orc_rk_buoy(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                 const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
+                 const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
+                 int is_impdiff, const double gacc[3], double beta, const double *sb, double *dudtrko,
+                 double *dvdtrko, double *dwdtrko, double *u, double *v, double *w, double f[3], double *work);
 void orc_rk(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
             const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
             const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
             int is_impdiff, double *dudtrko, double *dvdtrko, double *dwdtrko,
             double *u, double *v, double *w, double f[3], double *work) {
+  const double g0[3] = {0., 0., 0.};
+  orc_rk_buoy(rkpar, n, dli, dzci, dzfi, gvr_c, gvr_f, dt, visc, p, is_forced, velf, bforce, is_impdiff, g0, 0.,
+              NULL, dudtrko, dvdtrko, dwdtrko, u, v, w, f, work);
+}
+void orc_rk_buoy(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                 const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
+                 const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
+                 int is_impdiff, const double gacc[3], double beta, const double *sb, double *dudtrko,
+                 double *dvdtrko, double *dwdtrko, double *u, double *v, double *w, double f[3], double *work) {
   int n1 = n[0], n2 = n[1], n3 = n[2];
   size_t np = (size_t)n1 * n2 * n3;
   double *du = work, *dv = work + np, *dw = work + 2 * np;
@@ -664,6 +679,11 @@ void orc_rk(const double rkpar[2], const int n[3], const double dli[3], const do
         u[x] = u[x] + f1 * du[h] + f2 * dudtrko[h] + f12 * (bforce[0] - dli[0] * (p[IX(i + 1, j, k)] - p[x]));
         v[x] = v[x] + f1 * dv[h] + f2 * dvdtrko[h] + f12 * (bforce[1] - dli[1] * (p[IX(i, j + 1, k)] - p[x]));
         w[x] = w[x] + f1 * dw[h] + f2 * dwdtrko[h] + f12 * (bforce[2] - dzci[k] * (p[IX(i, j, k + 1)] - p[x]));
+        if (sb) {
+          u[x] = u[x] - f12 * gacc[0] * beta * 0.5 * (sb[IX(i + 1, j, k)] + sb[x]);
+          v[x] = v[x] - f12 * gacc[1] * beta * 0.5 * (sb[IX(i, j + 1, k)] + sb[x]);
+          w[x] = w[x] - f12 * gacc[2] * beta * 0.5 * (sb[IX(i, j, k + 1)] + sb[x]);
+        }
         if (is_impdiff) {
           u[x] = u[x] + f12 * dud[h];
           v[x] = v[x] + f12 * dvd[h];
@@ -698,6 +718,77 @@ void orc_rk(const double rkpar[2], const int n[3], const double dli[3], const do
           for (int i = 1; i <= n1; i++) q[IX(i, j, k)] = q[IX(i, j, k)] + ff;
     }
   }
+}
+
+/* ============================== scalars ============================== */
+/* scal (src/scal.f90:41-193, default loop, is_impdiff_1d = .false.): advective and
+   diffusive fluxes of a cell-centred scalar; dsdtd (implicit diffusion) may be NULL */
+void orc_scal(const int n[3], double dxi, double dyi, const double *dzci, const double *dzfi, double alpha,
+              const double *u, const double *v, const double *w, const double *s, double *dsdt, double *dsdtd,
+              int is_impdiff) {
+  int n1 = n[0], n2 = n[1], n3 = n[2];
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 1; k <= n3; k++)
+    for (int j = 1; j <= n2; j++)
+      for (int i = 1; i <= n1; i++) {
+        const size_t x = IX(i, j, k), h = IH(i, j, k);
+        const double sc = s[x];
+        const double usim = 0.5 * (s[IX(i - 1, j, k)] + sc) * u[IX(i - 1, j, k)];
+        const double usip = 0.5 * (s[IX(i + 1, j, k)] + sc) * u[x];
+        const double vsjm = 0.5 * (s[IX(i, j - 1, k)] + sc) * v[IX(i, j - 1, k)];
+        const double vsjp = 0.5 * (s[IX(i, j + 1, k)] + sc) * v[x];
+        const double wskm = 0.5 * (s[IX(i, j, k - 1)] + sc) * w[IX(i, j, k - 1)];
+        const double wskp = 0.5 * (s[IX(i, j, k + 1)] + sc) * w[x];
+        const double dsdxp = (s[IX(i + 1, j, k)] - sc) * dxi, dsdxm = (sc - s[IX(i - 1, j, k)]) * dxi;
+        const double dsdyp = (s[IX(i, j + 1, k)] - sc) * dyi, dsdym = (sc - s[IX(i, j - 1, k)]) * dyi;
+        const double dsdzp = (s[IX(i, j, k + 1)] - sc) * dzci[k], dsdzm = (sc - s[IX(i, j, k - 1)]) * dzci[k - 1];
+        double d = dxi * (-usip + usim) + dyi * (-vsjp + vsjm) + dzfi[k] * (-wskp + wskm);
+        const double dxy = (dsdxp - dsdxm) * alpha * dxi + (dsdyp - dsdym) * alpha * dyi;
+        const double dz = (dsdzp - dsdzm) * alpha * dzfi[k];
+        if (is_impdiff) dsdtd[h] = dxy + dz;
+        else d = d + dxy + dz;
+        dsdt[h] = d;
+      }
+}
+
+/* rk_scal (src/rk.f90:335-491, no wall flux): returns f = scalf - mean(s) when forced, else 0;
+   work: 2*n1*n2*n3 doubles */
+double orc_rk_scal(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                   const double *dzfi, const double *gvr_f, double alpha, double dt, const double *u,
+                   const double *v, const double *w, int is_forced, double scalf, double ssource, int is_impdiff,
+                   double *dsdtrko, double *s, double *work) {
+  int n1 = n[0], n2 = n[1], n3 = n[2];
+  size_t np = (size_t)n1 * n2 * n3;
+  double *ds = work, *dsd = work + np;
+  const double f1 = rkpar[0] * dt, f2 = rkpar[1] * dt, f12 = f1 + f2;
+  orc_scal(n, dli[0], dli[1], dzci, dzfi, alpha, u, v, w, s, ds, dsd, is_impdiff);
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 1; k <= n3; k++)
+    for (int j = 1; j <= n2; j++)
+      for (int i = 1; i <= n1; i++) {
+        const size_t x = IX(i, j, k), h = IH(i, j, k);
+        s[x] = s[x] + f1 * ds[h] + f2 * dsdtrko[h] + f12 * ssource;
+        if (is_impdiff) s[x] = s[x] + f12 * dsd[h];
+      }
+  double f = 0.;
+  if (is_forced) f = scalf - orc_bulk_mean(n, gvr_f, s);
+  if (is_impdiff) {
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 1; k <= n3; k++)
+      for (int j = 1; j <= n2; j++)
+        for (int i = 1; i <= n1; i++) s[IX(i, j, k)] = s[IX(i, j, k)] - .5 * f12 * dsd[IH(i, j, k)];
+  }
+  memcpy(dsdtrko, ds, sizeof(double) * np);
+  return f;
+}
+
+/* bulk_forcing_s (src/scal.f90:301-319) */
+void orc_bulk_forcing_s(const int n[3], int is_forced, double f, double *s) {
+  int n1 = n[0], n2 = n[1], n3 = n[2];
+  if (!is_forced) return;
+  for (int k = 1; k <= n3; k++)
+    for (int j = 1; j <= n2; j++)
+      for (int i = 1; i <= n1; i++) s[IX(i, j, k)] = s[IX(i, j, k)] + f;
 }
 
 /* ============================== boundary conditions ============================== */
@@ -917,6 +1008,9 @@ struct orc_state {
   int is_bound[6];
   double time, dt, dti, divtot, divmax, dpdl[3];
   int istep;
+  /* scalar (src/scal.f90:15-33): value, dsdtrko, rk_scal scratch, Helmholtz plan */
+  double *sval, *dsdtrko, *swork, salpha, alpha_max, fs;
+  double *lam_s, *as, *bs, *cs_, normfft_s, rhsb_s[6];
 };
 
 static const double RKC[3][2] = {{32. / 60., 0. / 60.}, {25. / 60., -17. / 60.}, {45. / 60., -25. / 60.}};
@@ -964,6 +1058,19 @@ orc_state *orc_state_new(const orc_case *cs) {
                      s->av[c], s->bv[c], s->cv[c], &s->normfft_v[c], s->rhsb_v[c]);
     }
   }
+  /* alpha_max = 1/min(alphai) (src/param.f90:308-310); 1/huge without scalars */
+  s->alpha_max = 1. / DBL_MAX;
+  if (cs->nscal > 0) {
+    s->salpha = 1. / cs->alphai;
+    s->alpha_max = s->salpha;
+    s->sval = calloc(nh, 8); s->dsdtrko = calloc(np, 8); s->swork = calloc(2 * np, 8);
+    if (cs->is_impdiff) {
+      s->lam_s = malloc(sizeof(double) * n1 * n2);
+      s->as = malloc(8 * n3); s->bs = malloc(8 * n3); s->cs_ = malloc(8 * n3);
+      orc_initsolver(cs->ng, s->dli, s->dzci, s->dzfi, cs->cbcscal, cs->bcscal, ccc, s->lam_s, s->as, s->bs, s->cs_,
+                     &s->normfft_s, s->rhsb_s);
+    }
+  }
   return s;
 }
 
@@ -974,12 +1081,14 @@ void orc_state_free(orc_state *s) {
   free(s->dzc); free(s->dzf); free(s->zc); free(s->zf); free(s->dzci); free(s->dzfi); free(s->gvr_c); free(s->gvr_f);
   free(s->lam_p); free(s->ap); free(s->bp); free(s->cp);
   for (int c = 0; c < 3; c++) { free(s->lam_v[c]); free(s->av[c]); free(s->bv[c]); free(s->cv[c]); }
+  free(s->sval); free(s->dsdtrko); free(s->swork); free(s->lam_s); free(s->as); free(s->bs); free(s->cs_);
   free(s);
 }
 
 double *orc_state_ptr(orc_state *s, int which) {
   switch (which) {
     case 0: return s->u; case 1: return s->v; case 2: return s->w; case 3: return s->p; case 4: return s->pp;
+    case 5: return s->sval;
     case 10: return s->dzc; case 11: return s->dzf; case 12: return s->zc; case 13: return s->zf;
     case 14: return s->dzci; case 15: return s->dzfi;
     case 20: return s->lam_p; case 21: return s->ap; case 22: return s->bp; case 23: return s->cp;
@@ -993,6 +1102,7 @@ double orc_state_scalar(orc_state *s, int which) {
     case 3: return s->divtot; case 4: return s->divmax;
     case 5: case 6: case 7: return s->dpdl[which - 5];
     case 8: return s->normfft_p;
+    case 9: return s->fs;
     default: return 0.;
   }
 }
@@ -1003,7 +1113,8 @@ void orc_state_start(orc_state *s) {
   orc_bounduvw(cs->cbcvel, s->n, cs->bcvel, s->is_bound, s->dl, s->dzc, s->dzf, s->u, s->v, s->w, 0, HALO_BOTH,
                HALO_BOTH);
   orc_boundp(cs->cbcpre, s->n, cs->bcpre, s->is_bound, s->dl, s->dzc, s->p, HALO_UPPER);
-  double dt_cfl = orc_chkdt(s->n, s->dl, s->dzci, s->dzfi, s->visc, 1. / DBL_MAX, cs->is_impdiff, 0, s->u, s->v, s->w);
+  if (cs->nscal > 0) orc_boundp(cs->cbcscal, s->n, cs->bcscal, s->is_bound, s->dl, s->dzc, s->sval, HALO_BOTH);
+  double dt_cfl = orc_chkdt(s->n, s->dl, s->dzci, s->dzfi, s->visc, s->alpha_max, cs->is_impdiff, 0, s->u, s->v, s->w);
   s->dt = cs->dt_f > 0. ? cs->dt_f : fmin(cs->cfl * dt_cfl, cs->dtmax);
   s->dti = 1. / s->dt;
   s->istep = 0; s->time = 0.;
@@ -1015,6 +1126,7 @@ void orc_state_step(orc_state *s) {
   s->istep += 1;
   s->time = s->time + s->dt;
   s->dpdl[0] = s->dpdl[1] = s->dpdl[2] = 0.;
+  s->fs = 0.;
   double alpha = 0.;
   const char ccc[3] = {'c', 'c', 'c'};
   double *fl[3] = {s->u, s->v, s->w};
@@ -1022,8 +1134,20 @@ void orc_state_step(orc_state *s) {
     double dtrk = (RKC[irk][0] + RKC[irk][1]) * s->dt;
     double dtrki = 1. / dtrk;
     double f[3];
-    orc_rk(RKC[irk], s->n, s->dli, s->dzci, s->dzfi, s->gvr_c, s->gvr_f, s->dt, s->visc, s->p, cs->is_forced,
-           cs->velf, cs->bforce, cs->is_impdiff, s->dudtrko, s->dvdtrko, s->dwdtrko, s->u, s->v, s->w, f, s->work);
+    if (cs->nscal > 0) { /* src/main.f90:440-451 */
+      double fsc = orc_rk_scal(RKC[irk], s->n, s->dli, s->dzci, s->dzfi, s->gvr_f, s->salpha, s->dt, s->u, s->v, s->w,
+                               cs->is_sforced, cs->scalf, cs->ssource, cs->is_impdiff, s->dsdtrko, s->sval, s->swork);
+      orc_bulk_forcing_s(s->n, cs->is_sforced, fsc, s->sval);
+      s->fs += fsc;
+      if (cs->is_impdiff)
+        orc_solve_helmholtz(s->n, s->normfft_s, -.5 * s->salpha * dtrk, s->lam_s, s->as, s->bs, s->cs_, s->rhsb_s,
+                            s->is_bound, cs->cbcscal, ccc, s->sval);
+      orc_boundp(cs->cbcscal, s->n, cs->bcscal, s->is_bound, s->dl, s->dzc, s->sval, HALO_BOTH);
+    }
+    orc_rk_buoy(RKC[irk], s->n, s->dli, s->dzci, s->dzfi, s->gvr_c, s->gvr_f, s->dt, s->visc, s->p, cs->is_forced,
+                cs->velf, cs->bforce, cs->is_impdiff, cs->gacc, cs->beta,
+                cs->nscal > 0 && cs->is_buoyancy ? s->sval : NULL, s->dudtrko, s->dvdtrko, s->dwdtrko, s->u, s->v,
+                s->w, f, s->work);
     for (int d = 0; d < 3; d++) s->dpdl[d] += f[d];
     if (cs->is_impdiff) {
       alpha = -.5 * s->visc * dtrk;
@@ -1044,8 +1168,9 @@ void orc_state_step(orc_state *s) {
     orc_boundp(cs->cbcpre, s->n, cs->bcpre, s->is_bound, s->dl, s->dzc, s->p, HALO_UPPER);
   }
   for (int d = 0; d < 3; d++) s->dpdl[d] = -s->dpdl[d] * s->dti;
+  s->fs = s->fs * s->dti;
   if (cs->icheck > 0 && s->istep % cs->icheck == 0) {
-    double dt_cfl = orc_chkdt(s->n, s->dl, s->dzci, s->dzfi, s->visc, 1. / DBL_MAX, cs->is_impdiff, 0, s->u, s->v, s->w);
+    double dt_cfl = orc_chkdt(s->n, s->dl, s->dzci, s->dzfi, s->visc, s->alpha_max, cs->is_impdiff, 0, s->u, s->v, s->w);
     s->dt = cs->dt_f > 0. ? cs->dt_f : fmin(cs->cfl * dt_cfl, cs->dtmax);
     s->dti = 1. / s->dt;
     orc_chkdiv(s->n, cs->l, s->dli, s->dzfi, s->u, s->v, s->w, &s->divtot, &s->divmax);

@@ -93,6 +93,19 @@ void orc_rk(const double rkpar[2], const int n[3], const double dli[3], const do
             const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
             int is_impdiff, double *dudtrko, double *dvdtrko, double *dwdtrko,
             double *u, double *v, double *w, double f[3], double *work);
+void orc_rk_buoy(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                 const double *dzfi, const double *gvr_c, const double *gvr_f, double dt, double visc,
+                 const double *p, const int is_forced[3], const double velf[3], const double bforce[3],
+                 int is_impdiff, const double gacc[3], double beta, const double *sb, double *dudtrko,
+                 double *dvdtrko, double *dwdtrko, double *u, double *v, double *w, double f[3], double *work);
+void orc_scal(const int n[3], double dxi, double dyi, const double *dzci, const double *dzfi, double alpha,
+              const double *u, const double *v, const double *w, const double *s, double *dsdt, double *dsdtd,
+              int is_impdiff);
+double orc_rk_scal(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
+                   const double *dzfi, const double *gvr_f, double alpha, double dt, const double *u,
+                   const double *v, const double *w, int is_forced, double scalf, double ssource, int is_impdiff,
+                   double *dsdtrko, double *s, double *work);
+void orc_bulk_forcing_s(const int n[3], int is_forced, double f, double *s);
 /* src/bound.f90:17-122 (CPU path, one rank, x-aligned pencils) */
 void orc_bounduvw(const char cbc[18], const int n[3], const double bc[18], const int is_bound[6],
                   const double dl[3], const double *dzc, const double *dzf,
@@ -126,20 +139,24 @@ typedef struct orc_case {
   char cbcpre[6];  double bcpre[6];
   double bforce[3]; int is_forced[3]; double velf[3];
   int is_impdiff;
+  /* one transported scalar when nscal = 1 (&scalar of src/param.f90:144-151) */
+  int nscal;
+  double alphai; char cbcscal[6]; double bcscal[6]; double ssource; int is_sforced; double scalf;
+  double gacc[3]; double beta; int is_buoyancy;
 } orc_case;
 
 typedef struct orc_state orc_state;
 /* setup: grid, solver(s), allocations; fields start at zero */
 orc_state *orc_state_new(const orc_case *cs);
 void orc_state_free(orc_state *s);
-/* raw pointers into the state: which = 0 u,1 v,2 w,3 p,4 pp (haloed),
+/* raw pointers into the state: which = 0 u,1 v,2 w,3 p,4 pp,5 scalar (haloed),
  * 10 dzc,11 dzf,12 zc,13 zf,14 dzci,15 dzfi (0..n3+1), 20 lambdaxy_p, 21 ap,22 bp,23 cp */
 double *orc_state_ptr(orc_state *s, int which);
 /* boundary conditions + initial dt (main.f90:388-418); call after fields are set */
 void orc_state_start(orc_state *s);
 /* one full time step (3 RK substeps + dt/divergence check when istep % icheck == 0) */
 void orc_state_step(orc_state *s);
-/* scalars: 0 time, 1 dt, 2 istep, 3 divtot, 4 divmax, 5..7 dpdl */
+/* scalars: 0 time, 1 dt, 2 istep, 3 divtot, 4 divmax, 5..7 dpdl, 8 normfft_p, 9 fs (scalar forcing) */
 double orc_state_scalar(orc_state *s, int which);
 
 #ifdef __cplusplus

@@ -54,6 +54,12 @@ def _setup(L):
     L.orc_bulk_mean.restype = C.c_double
     L.orc_rk.argtypes = [_D, _I, _D, _D, _D, _D, _D, C.c_double, C.c_double, _D, _I, _D, _D, C.c_int,
                          _D, _D, _D, _D, _D, _D, _D, _D]
+    L.orc_rk_buoy.argtypes = [_D, _I, _D, _D, _D, _D, _D, C.c_double, C.c_double, _D, _I, _D, _D, C.c_int,
+                              _D, C.c_double, _D, _D, _D, _D, _D, _D, _D, _D, _D]
+    L.orc_rk_scal.argtypes = [_D, _I, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, _D, C.c_int, C.c_double,
+                              C.c_double, C.c_int, _D, _D, _D]
+    L.orc_rk_scal.restype = C.c_double
+    L.orc_bulk_forcing_s.argtypes = [_I, C.c_int, C.c_double, _D]
     L.orc_bounduvw.argtypes = [C.c_char_p, _I, _D, _I, _D, _D, _D, _D, _D, _D, C.c_int, C.c_int, C.c_int]
     L.orc_boundp.argtypes = [C.c_char_p, _I, _D, _I, _D, _D, _D, C.c_int]
     L.orc_updt_rhs_b.argtypes = [C.c_char_p, C.c_char_p, _I, _I, _D, _D, C.c_double, C.c_int]
@@ -169,6 +175,29 @@ def solve_helmholtz(n, normfft, alpha, lambdaxy, a, b, c, rhsb, is_bound, cbc, c
                               _ip(is_bound), _cs(cbc), _cs(c_or_f), _p(p))
 
 
+def rk_buoy(rkpar, n, dli, dzci, dzfi, gvr_c, gvr_f, dt, visc, p, is_forced, velf, bforce, is_impdiff, gacc, beta,
+            s, dudtrko, dvdtrko, dwdtrko, u, v, w):
+    """orc_rk_buoy: rk with the Boussinesq buoyancy of scalar s"""
+    f = np.zeros(3)
+    work = np.zeros(6 * n[0] * n[1] * n[2])
+    lib().orc_rk_buoy(_dp(rkpar), _ip(n), _dp(dli), _p(dzci), _p(dzfi), _p(gvr_c), _p(gvr_f), float(dt), float(visc),
+                      _p(p), _ip(is_forced), _dp(velf), _dp(bforce), int(is_impdiff), _dp(gacc), float(beta), _p(s),
+                      _p(dudtrko), _p(dvdtrko), _p(dwdtrko), _p(u), _p(v), _p(w), _p(f), _p(work))
+    return f
+
+
+def rk_scal(rkpar, n, dli, dzci, dzfi, gvr_f, alpha, dt, u, v, w, is_forced, scalf, ssource, is_impdiff, dsdtrko, s):
+    """orc_rk_scal: returns f"""
+    work = np.zeros(2 * n[0] * n[1] * n[2])
+    return lib().orc_rk_scal(_dp(rkpar), _ip(n), _dp(dli), _p(dzci), _p(dzfi), _p(gvr_f), float(alpha), float(dt),
+                             _p(u), _p(v), _p(w), int(is_forced), float(scalf), float(ssource), int(is_impdiff),
+                             _p(dsdtrko), _p(s), _p(work))
+
+
+def bulk_forcing_s(n, is_forced, f, s):
+    lib().orc_bulk_forcing_s(_ip(n), int(is_forced), float(f), _p(s))
+
+
 def fillps(n, dli, dzfi, dti, u, v, w, p):
     lib().orc_fillps(_ip(n), _dp(dli), _p(dzfi), dti, _p(u), _p(v), _p(w), _p(p))
 
@@ -238,7 +267,10 @@ class _Case(C.Structure):
                 ("cfl", C.c_double), ("dtmax", C.c_double), ("dt_f", C.c_double), ("visci", C.c_double),
                 ("icheck", C.c_int), ("cbcvel", C.c_char * 18), ("bcvel", C.c_double * 18),
                 ("cbcpre", C.c_char * 6), ("bcpre", C.c_double * 6), ("bforce", C.c_double * 3),
-                ("is_forced", C.c_int * 3), ("velf", C.c_double * 3), ("is_impdiff", C.c_int)]
+                ("is_forced", C.c_int * 3), ("velf", C.c_double * 3), ("is_impdiff", C.c_int),
+                ("nscal", C.c_int), ("alphai", C.c_double), ("cbcscal", C.c_char * 6), ("bcscal", C.c_double * 6),
+                ("ssource", C.c_double), ("is_sforced", C.c_int), ("scalf", C.c_double), ("gacc", C.c_double * 3),
+                ("beta", C.c_double), ("is_buoyancy", C.c_int)]
 
 
 class Run:
@@ -246,7 +278,9 @@ class Run:
 
     `case` is a dict with the input.nml keys used here (ng, l, gtype, gr, cfl, dtmax, dt_f,
     visci, icheck, cbcvel (18 chars), bcvel (18), cbcpre (6 chars), bcpre (6), bforce,
-    is_forced, velf, is_impdiff)."""
+    is_forced, velf, is_impdiff) and, for one transported scalar, the &scalar keys nscal (0 or 1),
+    alphai, cbcscal, bcscal, ssource, is_sforced, scalf, gacc, beta, is_boussinesq_buoyancy, each
+    scalar entry given as a one-element list."""
 
     def __init__(self, case):
         cs = _Case()
@@ -263,6 +297,19 @@ class Run:
         cs.is_forced[:] = [int(x) for x in case.get("is_forced", [0] * 3)]
         cs.velf[:] = case.get("velf", [0.] * 3)
         cs.is_impdiff = int(case.get("is_impdiff", 0))
+        cs.nscal = min(1, max(0, int(case.get("nscal", 0))))
+        if int(case.get("nscal", 0)) > 1:
+            raise ValueError("the oracle run carries at most one scalar")
+        if cs.nscal:
+            cs.alphai = float(case["alphai"][0])
+            cs.cbcscal = _cs(case["cbcscal"][0])
+            cs.bcscal[:] = list(case.get("bcscal", [[0.] * 6])[0])
+            cs.ssource = float(case.get("ssource", [0.])[0])
+            cs.is_sforced = int(case.get("is_sforced", [0])[0])
+            cs.scalf = float(case.get("scalf", [0.])[0])
+        cs.gacc[:] = case.get("gacc", [0.] * 3)
+        cs.beta = float(case.get("beta", 0.))
+        cs.is_buoyancy = int(bool(case.get("is_boussinesq_buoyancy", False)))
         self._cs = cs
         self.n = list(case["ng"])
         self._h = lib().orc_state_new(C.byref(cs))
@@ -291,6 +338,7 @@ class Run:
     w = property(lambda s: s.array(2))
     p = property(lambda s: s.array(3))
     pp = property(lambda s: s.array(4))
+    s = property(lambda s: s.array(5))
 
     def grid(self):
         return {k: self.array(i) for k, i in
@@ -310,3 +358,4 @@ class Run:
     dt = property(lambda s: s.scalar(1))
     istep = property(lambda s: int(s.scalar(2)))
     divmax = property(lambda s: s.scalar(4))
+    fs = property(lambda s: s.scalar(9))

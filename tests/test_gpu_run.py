@@ -102,3 +102,41 @@ def test_channel_forced_field_by_field(require_gpu):
         assert rel_l2(got, want) < 1e-11, name
     got, want = cans.fview(sim.p)[1:-1, 1:-1, 1:-1], r.p[1:-1, 1:-1, 1:-1]
     assert gauge_rel_l2(got, want, r.grid()["dzf"]) < 1e-11
+
+
+@pytest.mark.parametrize("is_impdiff", [0, 1])
+def test_buoyant_channel_with_scalar(require_gpu, is_impdiff):
+    """Heated channel with a Boussinesq scalar (Dirichlet walls s = 1 / 0), forced flow,
+    seeded noise: velocity, pressure and scalar after 4 steps agree with the oracle run."""
+    from cans_gb300.driver import Simulation
+    from cans_gb300 import cans
+    n = [24, 16, 20]
+    case = dict(ng=n, l=[3.0, 1.5, 1.0], gtype=1, gr=1.2, cfl=0.5, dtmax=1e5, dt_f=-1., visci=900., icheck=2,
+                cbcvel="PPPPDD" * 3, cbcpre="PPPPNN", bcvel=[0.] * 18, bcpre=[0.] * 6,
+                is_forced=[1, 0, 0], velf=[1., 0., 0.], is_impdiff=is_impdiff,
+                nscal=1, alphai=[600.], cbcscal=["PPPPDD"], bcscal=[[0., 0., 0., 0., 1., 0.]], ssource=[0.3],
+                gacc=[0., 0., -9.8], beta=0.02, is_boussinesq_buoyancy=True)
+    r = O.Run(case)
+    zc = r.grid()["zc"]
+    u = O.field(n)
+    u[1:-1, 1:-1, 1:-1] = (6. * zc[1:-1] * (1. - zc[1:-1]))[None, None, :]
+    v, w, p, s = O.field(n), O.field(n), O.field(n), O.field(n)
+    s[1:-1, 1:-1, 1:-1] = (1. - zc[1:-1])[None, None, :]
+    for f, seed in ((u, 1), (v, 2), (w, 3), (s, 4)):
+        O.add_noise(n, seed, 0.05, f)
+    r.u[:] = u; r.v[:] = v; r.w[:] = w; r.s[:] = s
+    r.start()
+    sim = Simulation(case)
+    sim.set_fields(u, v, w, p, scalars=[s])
+    sim.start()
+    assert abs(sim.dt - r.dt) <= 1e-13 * r.dt
+    r.step(4)
+    sim.step(4)
+    for name in ("u", "v", "w"):
+        got = cans.fview(getattr(sim, name))[1:-1, 1:-1, 1:-1]
+        want = getattr(r, name)[1:-1, 1:-1, 1:-1]
+        assert rel_l2(got, want) < 1e-11, name
+    got = cans.fview(sim.scalars[0]["val"])
+    assert rel_l2(got, r.s) < 1e-11
+    got, want = cans.fview(sim.p)[1:-1, 1:-1, 1:-1], r.p[1:-1, 1:-1, 1:-1]
+    assert gauge_rel_l2(got, want, r.grid()["dzf"]) < 1e-11

@@ -163,3 +163,54 @@ def test_reference_pivot_rule_misses_stretched_zero_mode():
     pt = np.finfo(float).eps * max(abs(bl), abs(ad))
     assert abs(den) > pt  # not pinned by the reference's test
     assert abs(den) < 1e-9 * abs(bl)  # yet numerically singular
+
+
+def test_scalar_substep_conserves_mean_with_source():
+    """rk_scal restatement: with zero velocity and periodic ghosts the volume-weighted mean of
+    the scalar changes by exactly f12*ssource (diffusion conserves it), and a forced scalar
+    reports f = scalf - mean."""
+    n = (8, 6, 5)
+    rng = np.random.default_rng(4)
+    s = O.field(n)
+    s[1:-1, 1:-1, 1:-1] = rng.standard_normal(n)
+
+    def periodic(a):
+        a[0], a[-1] = a[-2], a[1]
+        a[:, 0], a[:, -1] = a[:, -2], a[:, 1]
+        a[:, :, 0], a[:, :, -1] = a[:, :, -2], a[:, :, 1]
+
+    periodic(s)
+    z = O.field(n)
+    dzci = np.ones(n[2] + 2) * n[2]
+    dzfi = np.ones(n[2] + 2) * n[2]
+    gvr = np.ones(n[2] + 2) / (n[0] * n[1] * n[2])
+    dli = [float(n[0]), float(n[1]), float(n[2])]
+    rkpar, dt, src = (32. / 60., 0.), 0.01, 0.7
+    mean0 = O.bulk_mean(n, gvr, s)
+    dso = np.zeros(n, order="F")
+    f = O.rk_scal(rkpar, n, dli, dzci, dzfi, gvr, 0.05, dt, z, z, z, 1, 2.0, src, 0, dso, s)
+    mean1 = O.bulk_mean(n, gvr, s)
+    assert abs((mean1 - mean0) - rkpar[0] * dt * src) < 1e-14
+    assert abs(f - (2.0 - mean1)) < 1e-15
+
+
+def test_run_with_passive_scalar():
+    """Whole-run oracle with one scalar: without buoyancy the velocity is bit-identical to a
+    run without the scalar; a uniform scalar with homogeneous Neumann walls stays uniform."""
+    n = [8, 6, 10]
+    base = dict(ng=n, l=[2.0, 1.0, 2.0], gtype=1, gr=1.2, cfl=0.5, visci=200., icheck=2,
+                cbcvel="PPPPDD" * 3, cbcpre="PPPPNN", is_forced=[1, 0, 0], velf=[1., 0., 0.], is_impdiff=1)
+    sc = dict(base, nscal=1, alphai=[140.], cbcscal=["PPPPNN"], bcscal=[[0.] * 6], gacc=[0., 0., -1.], beta=0.5)
+    runs = [O.Run(base), O.Run(sc)]
+    rng = np.random.default_rng(5)
+    uyz, vxz = rng.standard_normal((n[1], n[2])), rng.standard_normal((n[0], n[2]))
+    for r in runs:  # u(y, z) and v(x, z): discretely divergence-free from the first substep
+        r.u[1:-1, 1:-1, 1:-1] = 1.0 + 0.2 * uyz[None, :, :]
+        r.v[1:-1, 1:-1, 1:-1] = 0.2 * vxz[:, None, :]
+    runs[1].s[1:-1, 1:-1, 1:-1] = 0.7
+    for r in runs:
+        r.start()
+        r.step(3)
+    for name in ("u", "v", "w", "p"):
+        assert np.array_equal(getattr(runs[0], name), getattr(runs[1], name))
+    assert np.abs(runs[1].s[1:-1, 1:-1, 1:-1] - 0.7).max() < 1e-13
