@@ -227,74 +227,165 @@ __device__ __forceinline__ T2 *fft_any(T2 *A, T2 *B, const DirParams &P, const T
 }
 
 // ------------------------------------------------------------------------ r2r pre-processing
-// staging: real line r at stg[r*sld + i], i < nt.  Fills the complex sequences A[q*ld + k], k < m.
+// staging: real line r at stg[r*sld + i], i < nt.  Element k (< m) of complex sequence q.
 // tab, pre: the CTA's copies of the plan's post and pre tables
+template <typename T, int M = 0>
+__device__ __forceinline__ cplx_t<T> pre_value(const DirParams &P, const T *__restrict__ stg, int q, int k,
+                                               const cplx_t<T> *__restrict__ tab,
+                                               const cplx_t<T> *__restrict__ pre) {
+  using T2 = cplx_t<T>;
+  // with a compile-time M the kinds handled have nt == n == m (no extension)
+  const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? sstage<M>(M) : P.sld;
+  const T *x0 = stg + (2 * q) * sld, *x1 = x0 + sld;
+  T2 z;
+  switch (P.kind) {
+    case K_R2HC: z = cmk<T2>(x0[k], x1[k]); break;
+    case K_REDFT10:
+    case K_RODFT10: {
+      const int src = (k < (n + 1) / 2) ? 2 * k : 2 * (n - 1 - k) + 1;
+      const T sg = (P.kind == K_RODFT10 && (src & 1)) ? T(-1) : T(1);
+      z = cmk<T2>(sg * x0[src], sg * x1[src]);
+    } break;
+    case K_HC2R: {
+      T2 X, Y;
+      if (k == 0) { X = cmk<T2>(x0[0], T(0)); Y = cmk<T2>(x1[0], T(0)); }
+      else if (2 * k < n) { X = cmk<T2>(x0[k], x0[n - k]); Y = cmk<T2>(x1[k], x1[n - k]); }
+      else if (2 * k == n) { X = cmk<T2>(x0[k], T(0)); Y = cmk<T2>(x1[k], T(0)); }
+      else { X = cmk<T2>(x0[n - k], -x0[k]); Y = cmk<T2>(x1[n - k], -x1[k]); }
+      z = cmk<T2>(X.x - Y.y, X.y + Y.x);
+    } break;
+    case K_REDFT01:
+    case K_RODFT01: {
+      // V_k = exp(+i pi k/(2n)) (x_k - i x_{n-k}), x_n = 0; DST-III reads the reversed line
+      const T2 t = tab[k];  // (cos, -sin)
+      const T c = t.x, s = -t.y;
+      const bool rev = P.kind == K_RODFT01;
+      const int ka = rev ? n - 1 - k : k, kb = rev ? k - 1 : n - k;
+      const T a0 = x0[ka], a1 = x1[ka];
+      const T b0 = k == 0 ? T(0) : x0[kb], b1 = k == 0 ? T(0) : x1[kb];
+      const T2 V0 = cmk<T2>(c * a0 + s * b0, s * a0 - c * b0);
+      const T2 V1 = cmk<T2>(c * a1 + s * b1, s * a1 - c * b1);
+      z = cmk<T2>(V0.x - V1.y, V0.y + V1.x);
+    } break;
+    case K_RODFT00: {
+      if (k == 0 || k == nt + 1) z = cmk<T2>(T(0), T(0));
+      else if (k <= nt) z = cmk<T2>(x0[k - 1], x1[k - 1]);
+      else z = cmk<T2>(-x0[m - 1 - k], -x1[m - 1 - k]);
+    } break;
+    case K_REDFT00: {
+      const int s = k <= nt - 1 ? k : m - k;
+      z = cmk<T2>(x0[s], x1[s]);
+    } break;
+    default: {  // K_REDFT11 / K_RODFT11: one line per sequence, zero-padded to 2n
+      const T *x = stg + q * sld;
+      if (k < n) { const T2 w = pre[k]; z = cmk<T2>(x[k] * w.x, x[k] * w.y); }
+      else z = cmk<T2>(T(0), T(0));
+    } break;
+  }
+  return z;
+}
+
+// Fills the complex sequences A[q*ld + k], k < m, of the Stockham path.
 template <typename T, int M = 0>
 __device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict__ stg, cplx_t<T> *__restrict__ A,
                                         const cplx_t<T> *__restrict__ tab, const cplx_t<T> *__restrict__ pre) {
-  using T2 = cplx_t<T>;
-  // with a compile-time M the kinds handled have nt == n == m (no extension)
-  const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? sstage<M>(M) : P.sld, ld = M ? sline<M>(M) : P.ld;
+  const int m = M ? M : P.m, ld = M ? sline<M>(M) : P.ld;
   const int total = P.ncx * m;
   for (int e = threadIdx.x; e < total; e += blockDim.x) {
     const int q = M ? (int)((unsigned)e / (unsigned)m) : e / m, k = e - q * m;
-    const T *x0 = stg + (2 * q) * sld, *x1 = x0 + sld;
-    T2 z;
-    switch (P.kind) {
-      case K_R2HC: z = cmk<T2>(x0[k], x1[k]); break;
-      case K_REDFT10:
-      case K_RODFT10: {
-        const int src = (k < (n + 1) / 2) ? 2 * k : 2 * (n - 1 - k) + 1;
-        const T sg = (P.kind == K_RODFT10 && (src & 1)) ? T(-1) : T(1);
-        z = cmk<T2>(sg * x0[src], sg * x1[src]);
-      } break;
-      case K_HC2R: {
-        T2 X, Y;
-        if (k == 0) { X = cmk<T2>(x0[0], T(0)); Y = cmk<T2>(x1[0], T(0)); }
-        else if (2 * k < n) { X = cmk<T2>(x0[k], x0[n - k]); Y = cmk<T2>(x1[k], x1[n - k]); }
-        else if (2 * k == n) { X = cmk<T2>(x0[k], T(0)); Y = cmk<T2>(x1[k], T(0)); }
-        else { X = cmk<T2>(x0[n - k], -x0[k]); Y = cmk<T2>(x1[n - k], -x1[k]); }
-        z = cmk<T2>(X.x - Y.y, X.y + Y.x);
-      } break;
-      case K_REDFT01:
-      case K_RODFT01: {
-        // V_k = exp(+i pi k/(2n)) (x_k - i x_{n-k}), x_n = 0; DST-III reads the reversed line
-        const T2 t = tab[k];  // (cos, -sin)
-        const T c = t.x, s = -t.y;
-        const bool rev = P.kind == K_RODFT01;
-        const int ka = rev ? n - 1 - k : k, kb = rev ? k - 1 : n - k;
-        const T a0 = x0[ka], a1 = x1[ka];
-        const T b0 = k == 0 ? T(0) : x0[kb], b1 = k == 0 ? T(0) : x1[kb];
-        const T2 V0 = cmk<T2>(c * a0 + s * b0, s * a0 - c * b0);
-        const T2 V1 = cmk<T2>(c * a1 + s * b1, s * a1 - c * b1);
-        z = cmk<T2>(V0.x - V1.y, V0.y + V1.x);
-      } break;
-      case K_RODFT00: {
-        if (k == 0 || k == nt + 1) z = cmk<T2>(T(0), T(0));
-        else if (k <= nt) z = cmk<T2>(x0[k - 1], x1[k - 1]);
-        else z = cmk<T2>(-x0[m - 1 - k], -x1[m - 1 - k]);
-      } break;
-      case K_REDFT00: {
-        const int s = k <= nt - 1 ? k : m - k;
-        z = cmk<T2>(x0[s], x1[s]);
-      } break;
-      default: {  // K_REDFT11 / K_RODFT11: one line per sequence, zero-padded to 2n
-        const T *x = stg + q * sld;
-        if (k < n) { const T2 w = pre[k]; z = cmk<T2>(x[k] * w.x, x[k] * w.y); }
-        else z = cmk<T2>(T(0), T(0));
-      } break;
-    }
-    A[q * ld + spad<M>(k)] = z;
+    A[q * ld + spad<M>(k)] = pre_value<T, M>(P, stg, q, k, tab, pre);
+  }
+}
+
+// ------------------------------------------------------------- 512-point register FFT
+// For m = 512 = 8*8*8 each complex sequence is transformed by 64 threads that keep eight
+// values in registers through three radix-8 steps, with two shared-memory exchanges
+// (n = 64a + 8c + d, k = k1 + 8e + 64f):
+//   step 1 (thread b = 8c + d): DFT8 over a of z[64a + b], times W512^(b k1) -> T[k1][b]
+//   step 2 (thread (k1, d)):    DFT8 over c of T[k1][8c + d], times W64^(d e) -> V[k1][e][d]
+//   step 3 (thread (k1, e)):    DFT8 over d of V[k1][e][d] -> X[k1 + 8e + 64f]
+// Strides (complex elements): T row 72, V 72*k1 + 9*e + d, X position x + 2*(x/8); with
+// these the half-warps of every FP32 exchange touch 16 distinct bank pairs.  The first step
+// reads its inputs straight from the real staging rows (pre_value), so the pre-processing
+// needs no pass of its own.  Requires blockDim.x == 64 * (sequences per CTA).
+template <int M> struct RegFFT { static constexpr bool on = false; };
+template <> struct RegFFT<512> { static constexpr bool on = true; };
+__host__ __device__ constexpr int regx(int x) { return x + 2 * (x >> 3); }
+// complex line stride of the compile-time path's buffers
+__host__ __device__ constexpr int spec_ld(int m) { return m == 512 ? 640 : m + m / 16 + 1; }
+// position of element x of an FFT result line: layout of the register FFT (LAY 1) or of
+// the Stockham path (LAY 0)
+template <int M, int LAY> __device__ __forceinline__ int zpos(int x) { return LAY ? regx(x) : spad<M>(x); }
+template <int M> constexpr int kLay = RegFFT<M>::on ? 1 : 0;
+
+template <typename T, int M, int SIGN>
+__device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const T *__restrict__ stg,
+                                                       cplx_t<T> *__restrict__ A, cplx_t<T> *__restrict__ B,
+                                                       const cplx_t<T> *__restrict__ tab,
+                                                       const cplx_t<T> *__restrict__ pre,
+                                                       const cplx_t<T> *__restrict__ tw) {
+  using T2 = cplx_t<T>;
+  constexpr int LD = spec_ld(M);
+  const int q = threadIdx.x >> 6, p = threadIdx.x & 63;
+  T2 v[8];
+#pragma unroll
+  for (int a = 0; a < 8; a++) v[a] = pre_value<T, M>(P, stg, q, 64 * a + p, tab, pre);
+  dft<8, SIGN>(v);
+  T2 *Tq = A + q * LD;
+  Tq[p] = v[0];
+#pragma unroll
+  for (int k1 = 1; k1 < 8; k1++) {
+    T2 w = tw[(p * k1) & 511];
+    if (SIGN > 0) w.y = -w.y;
+    Tq[k1 * 72 + p] = cmul(v[k1], w);
+  }
+  __syncthreads();
+  const int k1 = p >> 3, d = p & 7;
+#pragma unroll
+  for (int c = 0; c < 8; c++) v[c] = Tq[k1 * 72 + 8 * c + d];
+  dft<8, SIGN>(v);
+  T2 *Vq = B + q * LD;
+  Vq[k1 * 72 + d] = v[0];
+#pragma unroll
+  for (int e = 1; e < 8; e++) {
+    T2 w = tw[(8 * d * e) & 511];
+    if (SIGN > 0) w.y = -w.y;
+    Vq[k1 * 72 + e * 9 + d] = cmul(v[e], w);
+  }
+  __syncthreads();
+  const int e3 = p & 7;
+#pragma unroll
+  for (int dd = 0; dd < 8; dd++) v[dd] = Vq[k1 * 72 + e3 * 9 + dd];
+  dft<8, SIGN>(v);
+#pragma unroll
+  for (int f = 0; f < 8; f++) Tq[regx(k1 + 8 * e3 + 64 * f)] = v[f];
+  __syncthreads();
+  return A;
+}
+
+// pre-processing + complex FFT of the CTA's sequences (staging rows in B on entry);
+// returns the buffer holding the result, laid out as zpos<M, kLay<M>>
+template <typename T, int M>
+__device__ __forceinline__ const cplx_t<T> *fft_in(const DirParams &P, const T *stg, cplx_t<T> *A, cplx_t<T> *B,
+                                                   const cplx_t<T> *tab, const cplx_t<T> *pre,
+                                                   const cplx_t<T> *tw) {
+  if constexpr (RegFFT<M>::on) {
+    return kind_sign(P.kind) > 0 ? fft512_reg<T, M, +1>(P, stg, A, B, tab, pre, tw)
+                                 : fft512_reg<T, M, -1>(P, stg, A, B, tab, pre, tw);
+  } else {
+    r2r_pre<T, M>(P, stg, A, tab, pre);
+    __syncthreads();
+    return kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P, tw) : fft_any<M, -1>(A, B, P, tw);
   }
 }
 
 // ----------------------------------------------------------------------- r2r post-processing
 // value of output index k (< nt) of real line r from the FFT result Z
-template <typename T, int M = 0>
+template <typename T, int M = 0, int LAY = 0>
 __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__restrict__ Z, int r, int k,
                                       const cplx_t<T> *__restrict__ tab) {
   using T2 = cplx_t<T>;
-  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? sline<M>(M) : P.ld;
+  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? spec_ld(M) : P.ld;
   if (!P.pairs) {  // kinds 11
     const T2 z = Z[r * ldz + k], w = tab[k];
     const T re = w.x * z.x - w.y * z.y, im = w.x * z.y + w.y * z.x;
@@ -304,34 +395,34 @@ __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__res
   const T2 *L = Z + q * ldz;
   switch (P.kind) {
     case K_R2HC: {
-      const T2 a = L[spad<M>(k)], b = L[spad<M>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
+      const T2 a = L[zpos<M, LAY>(k)], b = L[zpos<M, LAY>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
       if (2 * k <= n) return wsel == 0 ? T(0.5) * (a.x + b.x) : T(0.5) * (a.y + b.y);
       return wsel == 0 ? T(0.5) * (b.y - a.y) : T(0.5) * (a.x - b.x);
     }
     case K_REDFT10:
     case K_RODFT10: {
       const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
-      const T2 a = L[spad<M>(kk)], b = L[spad<M>(M ? ((m - kk) & (M - 1)) : ((m - kk) % m))], t = tab[kk];
+      const T2 a = L[zpos<M, LAY>(kk)], b = L[zpos<M, LAY>(M ? ((m - kk) & (M - 1)) : ((m - kk) % m))], t = tab[kk];
       const T c = t.x, s = -t.y;
       return wsel == 0 ? c * (a.x + b.x) + s * (a.y - b.y) : c * (a.y + b.y) - s * (a.x - b.x);
     }
     case K_HC2R: {
-      const T2 a = L[spad<M>(k)];
+      const T2 a = L[zpos<M, LAY>(k)];
       return wsel == 0 ? a.x : a.y;
     }
     case K_REDFT01:
     case K_RODFT01: {
       const int pos = (k & 1) == 0 ? (k >> 1) : n - 1 - ((k - 1) >> 1);
-      const T2 a = L[spad<M>(pos)];
+      const T2 a = L[zpos<M, LAY>(pos)];
       const T v = wsel == 0 ? a.x : a.y;
       return (P.kind == K_RODFT01 && (k & 1)) ? -v : v;
     }
     case K_RODFT00: {
-      const T2 a = L[spad<M>(k + 1)];
+      const T2 a = L[zpos<M, LAY>(k + 1)];
       return wsel == 0 ? -a.y : a.x;
     }
     default: {  // K_REDFT00
-      const T2 a = L[spad<M>(k)];
+      const T2 a = L[zpos<M, LAY>(k)];
       return wsel == 0 ? a.x : a.y;
     }
   }
@@ -339,22 +430,22 @@ __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__res
 
 // both real outputs (lines 2q and 2q+1) of output index k of a "pairs" kind, sharing the
 // loads of r2r_post (same arithmetic as r2r_post with r = 2q and r = 2q + 1)
-template <typename T, int M = 0>
+template <typename T, int M = 0, int LAY = 0>
 __device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *__restrict__ Z, int q, int k,
                                           const cplx_t<T> *__restrict__ tab, T &v0, T &v1) {
   using T2 = cplx_t<T>;
-  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? sline<M>(M) : P.ld;
+  const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? spec_ld(M) : P.ld;
   const T2 *L = Z + q * ldz;
   switch (P.kind) {
     case K_R2HC: {
-      const T2 a = L[spad<M>(k)], b = L[spad<M>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
+      const T2 a = L[zpos<M, LAY>(k)], b = L[zpos<M, LAY>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
       if (2 * k <= n) { v0 = T(0.5) * (a.x + b.x); v1 = T(0.5) * (a.y + b.y); }
       else { v0 = T(0.5) * (b.y - a.y); v1 = T(0.5) * (a.x - b.x); }
     } break;
     case K_REDFT10:
     case K_RODFT10: {
       const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
-      const T2 a = L[spad<M>(kk)], b = L[spad<M>(M ? ((m - kk) & (M - 1)) : ((m - kk) % m))], t = tab[kk];
+      const T2 a = L[zpos<M, LAY>(kk)], b = L[zpos<M, LAY>(M ? ((m - kk) & (M - 1)) : ((m - kk) % m))], t = tab[kk];
       const T c = t.x, s = -t.y;
       v0 = c * (a.x + b.x) + s * (a.y - b.y);
       v1 = c * (a.y + b.y) - s * (a.x - b.x);
@@ -362,18 +453,18 @@ __device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *_
     case K_REDFT01:
     case K_RODFT01: {
       const int pos = (k & 1) == 0 ? (k >> 1) : n - 1 - ((k - 1) >> 1);
-      const T2 a = L[spad<M>(pos)];
+      const T2 a = L[zpos<M, LAY>(pos)];
       const bool neg = P.kind == K_RODFT01 && (k & 1);
       v0 = neg ? -a.x : a.x;
       v1 = neg ? -a.y : a.y;
     } break;
     case K_RODFT00: {
-      const T2 a = L[spad<M>(k + 1)];
+      const T2 a = L[zpos<M, LAY>(k + 1)];
       v0 = -a.y;
       v1 = a.x;
     } break;
     default: {  // K_HC2R, K_REDFT00
-      const T2 a = L[spad<M>(k)];
+      const T2 a = L[zpos<M, LAY>(k)];
       v0 = a.x;
       v1 = a.y;
     } break;

@@ -98,7 +98,7 @@ template <typename T> inline DirParams make_params(const cans_plan *P, int d, in
   const bool pow2 = q.m >= 32 && q.m <= 1024 && (q.m & (q.m - 1)) == 0;
   q.spec = (pow2 && q.pairs && q.nt == q.m && q.n == q.nt && q.ncx == ncx0 && !P->nospec[d]) ? q.m : 0;
   if (q.spec) {
-    q.ld = q.m + q.m / 16 + 1;  // padded complex lines of the compile-time path (sline)
+    q.ld = spec_ld(q.m);        // padded complex lines of the compile-time path
     q.sld = q.nt + 4;           // 16-byte aligned staging rows (sstage)
   }
   return q;
@@ -180,8 +180,10 @@ int get_factor(cans_plan *P, double key, bool helm, Factor **out);
 template <typename T, int M> struct PassGeo {
   static constexpr int NCX = M ? ncx_for(M, (int)sizeof(cplx_t<T>)) : 0;
   static constexpr int LPB = 2 * NCX;
-  static constexpr int LD = M ? sline<M>(M) : 0;  // complex line stride (padded)
+  static constexpr int LD = M ? spec_ld(M) : 0;  // complex line stride (padded)
   static constexpr int SLD = sstage<M>(M);          // real staging line stride (16-byte rows)
+  // the register FFT runs 64 threads per complex sequence on the 256-thread pass CTAs
+  static_assert(!RegFFT<M>::on || NCX * 64 == 256, "register FFT geometry");
 };
 
 // ---- FP64 <-> FP32 conversions without the FP64 pipe.  GB300 issues double<->float
@@ -279,9 +281,7 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
     }
   if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
-  r2r_pre<T, M>(P, stg, A, post, pre);
-  __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P, tw) : fft_any<M, -1>(A, B, P, tw);
+  const T2 *Z = fft_in<T, M>(P, stg, A, B, post, pre, tw);
   T *Sk = S + (size_t)k * n1 * n2;
   if (P.pairs) {
     // both lines of a complex sequence per thread: runs of 2*ncx values along j per row i
@@ -289,7 +289,7 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
       const int i = M ? (int)((unsigned)e / (unsigned)G::NCX) : e / ncx, q = e - i * ncx, j = j0 + 2 * q;
       if (j >= n2) continue;
       T v0, v1;
-      if (i < nt) r2r_post2<T, M>(P, Z, q, i, post, v0, v1);
+      if (i < nt) r2r_post2<T, M, kLay<M>>(P, Z, q, i, post, v0, v1);
       else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
       T *dst = Sk + (size_t)i * n2 + j;
       if (((n2 & 1) == 0)) *reinterpret_cast<T2 *>(dst) = cmk<T2>(v0, v1);  // j even, n2 even: aligned pair
@@ -299,7 +299,7 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
     for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
       const int i = e / lpb, r = e - i * lpb, j = j0 + r;
       if (j >= n2) continue;
-      Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M>(P, Z, r, i, post) : pass[r];
+      Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M, kLay<M>>(P, Z, r, i, post) : pass[r];
     }
   }
 }
@@ -340,9 +340,7 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
   }
   if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
-  r2r_pre<T, M>(P, stg, A, post, pre);
-  __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P, tw) : fft_any<M, -1>(A, B, P, tw);
+  const T2 *Z = fft_in<T, M>(P, stg, A, B, post, pre, tw);
   if (M > 0) {
     // two neighbouring outputs of both lines per thread: 2-element vector stores
     for (int e = threadIdx.x; e < G::NCX * (M / 2); e += blockDim.x) {
@@ -350,8 +348,8 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
       const long l = l0 + 2 * q;
       if (l >= nlines) continue;
       T a0, a1, b0, b1;
-      r2r_post2<T, M>(P, Z, q, j, post, a0, a1);
-      r2r_post2<T, M>(P, Z, q, j + 1, post, b0, b1);
+      r2r_post2<T, M, kLay<M>>(P, Z, q, j, post, a0, a1);
+      r2r_post2<T, M, kLay<M>>(P, Z, q, j + 1, post, b0, b1);
       *reinterpret_cast<T2 *>(S + (size_t)l * M + j) = cmk<T2>(a0, b0);
       if (l + 1 < nlines) *reinterpret_cast<T2 *>(S + (size_t)(l + 1) * M + j) = cmk<T2>(a1, b1);
     }
@@ -361,14 +359,14 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
       const long l = l0 + 2 * q;
       if (l >= nlines) continue;
       T v0, v1;
-      r2r_post2<T, M>(P, Z, q, j, post, v0, v1);
+      r2r_post2<T, M, kLay<M>>(P, Z, q, j, post, v0, v1);
       S[(size_t)l * n2 + j] = v0;
       if (l + 1 < nlines) S[(size_t)(l + 1) * n2 + j] = v1;
     }
   } else {
     for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
       const int r = e / nt, j = e - r * nt;
-      if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M>(P, Z, r, j, post);
+      if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M, kLay<M>>(P, Z, r, j, post);
     }
   }
 }
@@ -431,15 +429,13 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
       pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
   if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
-  r2r_pre<T, M>(P, stg, A, post, pre);
-  __syncthreads();
-  const T2 *Z = kind_sign(P.kind) > 0 ? fft_any<M, +1>(A, B, P, tw) : fft_any<M, -1>(A, B, P, tw);
+  const T2 *Z = fft_in<T, M>(P, stg, A, B, post, pre, tw);
   if (P.pairs) {
     for (int e = threadIdx.x; e < ncx * n1; e += blockDim.x) {
       const int q = M ? (int)((unsigned)e / (unsigned)M) : e / n1, i = e - q * n1, j = j0 + 2 * q;
       if (j >= n2) continue;
       T v0, v1;
-      if (i < nt) r2r_post2<T, M>(P, Z, q, i, post, v0, v1);
+      if (i < nt) r2r_post2<T, M, kLay<M>>(P, Z, q, i, post, v0, v1);
       else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
       const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
       p[idx] = xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
@@ -453,7 +449,7 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
       const int r = e / n1, i = e - r * n1, j = j0 + r;
       if (j >= n2) continue;
       const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-      const T val = (i < nt) ? r2r_post<T, M>(P, Z, r, i, post) : pass[r];
+      const T val = (i < nt) ? r2r_post<T, M, kLay<M>>(P, Z, r, i, post) : pass[r];
       p[idx] = xbwd_value<T, TF>(p, idx, acc, val, add0, add1);
     }
   }

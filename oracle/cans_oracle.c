@@ -1176,3 +1176,125 @@ void orc_state_step(orc_state *s) {
     orc_chkdiv(s->n, cs->l, s->dli, s->dzfi, s->u, s->v, s->w, &s->divtot, &s->divmax);
   }
 }
+
+/* ============================== profile statistics ============================== */
+/* out1d (src/output.f90:56-157): out holds ng(idir) values; sums in the reference's loop order */
+void orc_out1d(const int n[3], const double l[3], const double dl[3], int idir, const double *dz, const double *p,
+               double *out) {
+  int n1 = n[0], n2 = n[1], n3 = n[2];
+  if (idir == 3) {
+    double gar = dl[0] * dl[1] / (l[0] * l[1]);
+    for (int k = 1; k <= n3; k++) {
+      double s = 0.;
+      for (int j = 1; j <= n2; j++)
+        for (int i = 1; i <= n1; i++) s = s + p[IX(i, j, k)] * gar;
+      out[k - 1] = s;
+    }
+  } else if (idir == 2) {
+    double gar = dl[0] / (l[0] * l[2]);
+    for (int j = 1; j <= n2; j++) {
+      double s = 0.;
+      for (int k = 1; k <= n3; k++)
+        for (int i = 1; i <= n1; i++) s = s + p[IX(i, j, k)] * dz[k] * gar;
+      out[j - 1] = s;
+    }
+  } else {
+    double gar = dl[1] / (l[1] * l[2]);
+    for (int i = 1; i <= n1; i++) {
+      double s = 0.;
+      for (int k = 1; k <= n3; k++)
+        for (int j = 1; j <= n2; j++) s = s + p[IX(i, j, k)] * dz[k] * gar;
+      out[i - 1] = s;
+    }
+  }
+}
+
+/* out1d_chan (src/output.f90:327-393), idir = 3: out = [um,vm,wm,u2,v2,w2,uw] x n3 */
+void orc_out1d_chan(const int n[3], const double l[3], const double dl[3], const double *u, const double *v,
+                    const double *w, double *out) {
+  int n1 = n[0], n2 = n[1], n3 = n[2];
+  double gar = dl[0] * dl[1] / (l[0] * l[1]);
+  for (int k = 1; k <= n3; k++) {
+    double a[7] = {0., 0., 0., 0., 0., 0., 0.};
+    for (int j = 1; j <= n2; j++)
+      for (int i = 1; i <= n1; i++) {
+        a[0] += u[IX(i, j, k)];
+        a[1] += v[IX(i, j, k)];
+        a[2] += 0.50 * (w[IX(i, j, k - 1)] + w[IX(i, j, k)]);
+        a[3] += u[IX(i, j, k)] * u[IX(i, j, k)];
+        a[4] += v[IX(i, j, k)] * v[IX(i, j, k)];
+        a[5] += 0.50 * (w[IX(i, j, k)] * w[IX(i, j, k)] + w[IX(i, j, k - 1)] * w[IX(i, j, k - 1)]);
+        a[6] += 0.25 * (u[IX(i - 1, j, k)] + u[IX(i, j, k)]) * (w[IX(i, j, k - 1)] + w[IX(i, j, k)]);
+      }
+    double mu = a[0] * gar, mv = a[1] * gar, mw = a[2] * gar;
+    out[k - 1] = mu;
+    out[k - 1 + n3] = mv;
+    out[k - 1 + 2 * n3] = mw;
+    out[k - 1 + 3 * n3] = a[3] * gar - mu * mu;
+    out[k - 1 + 4 * n3] = a[4] * gar - mv * mv;
+    out[k - 1 + 5 * n3] = a[5] * gar - mw * mw;
+    out[k - 1 + 6 * n3] = a[6] * gar - mu * mw;
+  }
+}
+
+/* out2d_duct (src/output.f90:395-529): idir = 1 out = [um,vm,wm,u2,v2,w2,uv,uw] x (n2,n3);
+ * idir = 2 out = [um,vm,wm,u2,v2,w2,vw,uv] x (n1,n3); first index fastest */
+void orc_out2d_duct(const int n[3], const double l[3], const double dl[3], int idir, const double *u,
+                    const double *v, const double *w, double *out) {
+  int n1 = n[0], n2 = n[1], n3 = n[2];
+  if (idir == 1) {
+    double gar = dl[0] / l[0];
+    size_t pq = (size_t)n2 * n3;
+    for (int k = 1; k <= n3; k++)
+      for (int j = 1; j <= n2; j++) {
+        double a[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+        for (int i = 1; i <= n1; i++) {
+          double uc = u[IX(i, j, k)], um = u[IX(i - 1, j, k)], vc = v[IX(i, j, k)], vm = v[IX(i, j - 1, k)];
+          double wc = w[IX(i, j, k)], wm = w[IX(i, j, k - 1)];
+          a[0] += uc;
+          a[1] += 0.5 * (vm + vc);
+          a[2] += 0.5 * (wm + wc);
+          a[3] += uc * uc;
+          a[4] += 0.5 * (vm * vm + vc * vc);
+          a[5] += 0.5 * (wm * wm + wc * wc);
+          a[6] += 0.25 * (um + uc) * (vm + vc);
+          a[7] += 0.25 * (um + uc) * (wm + wc);
+        }
+        size_t o = (size_t)(j - 1) + (size_t)n2 * (k - 1);
+        double mu = a[0] * gar, mv = a[1] * gar, mw = a[2] * gar;
+        out[o] = mu; out[o + pq] = mv; out[o + 2 * pq] = mw;
+        out[o + 3 * pq] = a[3] * gar - mu * mu;
+        out[o + 4 * pq] = a[4] * gar - mv * mv;
+        out[o + 5 * pq] = a[5] * gar - mw * mw;
+        out[o + 6 * pq] = a[6] * gar - mu * mv;
+        out[o + 7 * pq] = a[7] * gar - mu * mw;
+      }
+  } else if (idir == 2) {
+    double gar = dl[1] / l[1];
+    size_t pq = (size_t)n1 * n3;
+    for (int k = 1; k <= n3; k++)
+      for (int i = 1; i <= n1; i++) {
+        double a[8] = {0., 0., 0., 0., 0., 0., 0., 0.};
+        for (int j = 1; j <= n2; j++) {
+          double uc = u[IX(i, j, k)], um = u[IX(i - 1, j, k)], vc = v[IX(i, j, k)], vm = v[IX(i, j - 1, k)];
+          double wc = w[IX(i, j, k)], wm = w[IX(i, j, k - 1)];
+          a[0] += 0.5 * (um + uc);
+          a[1] += vc;
+          a[2] += 0.5 * (wm + wc);
+          a[3] += 0.5 * (um * um + uc * uc);
+          a[4] += vc * vc;
+          a[5] += 0.5 * (wm * wm + wc * wc);
+          a[6] += 0.25 * (vm + vc) * (wm + wc);
+          a[7] += 0.25 * (um + uc) * (vm + vc);
+        }
+        size_t o = (size_t)(i - 1) + (size_t)n1 * (k - 1);
+        double mu = a[0] * gar, mv = a[1] * gar, mw = a[2] * gar;
+        out[o] = mu; out[o + pq] = mv; out[o + 2 * pq] = mw;
+        out[o + 3 * pq] = a[3] * gar - mu * mu;
+        out[o + 4 * pq] = a[4] * gar - mv * mv;
+        out[o + 5 * pq] = a[5] * gar - mw * mw;
+        out[o + 6 * pq] = a[6] * gar - mv * mw;
+        out[o + 7 * pq] = a[7] * gar - mu * mv;
+      }
+  }
+}

@@ -129,6 +129,14 @@ void orc_chkdiv(const int n[3], const double l[3], const double dli[3], const do
 void orc_add_noise(const int n[3], unsigned long long seed, double norm, double *p);
 
 /* ---------- whole-run driver (src/main.f90:144-520, single rank, no I/O) ---------- */
+/* profile statistics of src/output.f90 (out1d 56-157, out1d_chan 327-393, out2d_duct 395-529) */
+void orc_out1d(const int n[3], const double l[3], const double dl[3], int idir, const double *dz, const double *p,
+               double *out);
+void orc_out1d_chan(const int n[3], const double l[3], const double dl[3], const double *u, const double *v,
+                    const double *w, double *out);
+void orc_out2d_duct(const int n[3], const double l[3], const double dl[3], int idir, const double *u,
+                    const double *v, const double *w, double *out);
+
 typedef struct orc_case {
   int ng[3];
   double l[3];

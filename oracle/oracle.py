@@ -198,6 +198,25 @@ def bulk_forcing_s(n, is_forced, f, s):
     lib().orc_bulk_forcing_s(_ip(n), int(is_forced), float(f), _p(s))
 
 
+def out1d(n, l, dl, idir, dz, p):
+    out = np.zeros(n[idir - 1])
+    lib().orc_out1d(_ip(n), _dp(l), _dp(dl), int(idir), _p(dz), _p(p), _p(out))
+    return out
+
+
+def out1d_chan(n, l, dl, u, v, w):
+    out = np.zeros(7 * n[2])
+    lib().orc_out1d_chan(_ip(n), _dp(l), _dp(dl), _p(u), _p(v), _p(w), _p(out))
+    return out.reshape(7, n[2])
+
+
+def out2d_duct(n, l, dl, idir, u, v, w):
+    q = n[1] if idir == 1 else n[0]
+    out = np.zeros(8 * q * n[2])
+    lib().orc_out2d_duct(_ip(n), _dp(l), _dp(dl), int(idir), _p(u), _p(v), _p(w), _p(out))
+    return out.reshape(8, n[2], q)
+
+
 def fillps(n, dli, dzfi, dti, u, v, w, p):
     lib().orc_fillps(_ip(n), _dp(dli), _p(dzfi), dti, _p(u), _p(v), _p(w), _p(p))
 

@@ -214,3 +214,31 @@ def test_run_with_passive_scalar():
     for name in ("u", "v", "w", "p"):
         assert np.array_equal(getattr(runs[0], name), getattr(runs[1], name))
     assert np.abs(runs[1].s[1:-1, 1:-1, 1:-1] - 0.7).max() < 1e-13
+
+
+def test_fortran_es_format():
+    """es24.16e3 records of the reference's text output (src/output.f90:16-17)."""
+    from cans_gb300 import output
+    assert output.es(1.0) == " 1.0000000000000000E+000"
+    assert output.es(-0.5) == "-5.0000000000000000E-001"
+    assert output.es(2.0 ** -20) == " 9.5367431640625000E-007"
+    assert output.es(-3 * 2.0 ** 1000).endswith("E+301")
+    assert output.es(0.0) == " 0.0000000000000000E+000"
+    assert output.es(123456.789) == " 1.2345678900000000E+005"
+    assert output.record([1.0, 2.0]) == " 1.0000000000000000E+000  2.0000000000000000E+000 "
+    assert float(output.es(np.pi)) == float(f"{np.pi:.16e}")
+
+
+def test_statistics_oracle_identities():
+    """out1d of a field constant on planes returns that constant; out1d_chan variances of
+    such a field are zero and its uw vanishes with w = 0."""
+    n = (6, 5, 4)
+    l, dl = (1.0, 2.0, 3.0), (1. / 6, 2. / 5, 3. / 4)
+    u, v, w = O.field(n), O.field(n), O.field(n)
+    prof = np.arange(n[2] + 2, dtype=float)
+    u[:] = prof[None, None, :]
+    got = O.out1d(n, l, dl, 3, np.ones(n[2] + 2), u)
+    assert np.allclose(got, prof[1:-1], rtol=1e-14)
+    st = O.out1d_chan(n, l, dl, u, v, w)
+    assert np.allclose(st[0], prof[1:-1], rtol=1e-14)
+    assert np.abs(st[3]).max() < 1e-12 and np.abs(st[6]).max() == 0.
