@@ -33,7 +33,7 @@ struct DirParams {
 
 // FFT sign a kind is defined with: the "backward" kinds (HC2R, REDFT01, RODFT01) use
 // exp(+i...), every other kind exp(-i...) -- whichever pass (forward/backward) uses it
-__host__ __device__ __forceinline__ int kind_sign(int kind) {
+__host__ __device__ constexpr int kind_sign(int kind) {
   return (kind == K_HC2R || kind == K_REDFT01 || kind == K_RODFT01) ? +1 : -1;
 }
 
@@ -229,21 +229,23 @@ __device__ __forceinline__ T2 *fft_any(T2 *A, T2 *B, const DirParams &P, const T
 // ------------------------------------------------------------------------ r2r pre-processing
 // staging: real line r at stg[r*sld + i], i < nt.  Element k (< m) of complex sequence q.
 // tab, pre: the CTA's copies of the plan's post and pre tables
-template <typename T, int M = 0>
+// KIND >= 0: the kind as a compile-time constant (the switch folds away); -1: P.kind
+template <typename T, int M = 0, int KIND = -1>
 __device__ __forceinline__ cplx_t<T> pre_value(const DirParams &P, const T *__restrict__ stg, int q, int k,
                                                const cplx_t<T> *__restrict__ tab,
                                                const cplx_t<T> *__restrict__ pre) {
   using T2 = cplx_t<T>;
   // with a compile-time M the kinds handled have nt == n == m (no extension)
   const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? sstage<M>(M) : P.sld;
+  const int kind = KIND >= 0 ? KIND : P.kind;
   const T *x0 = stg + (2 * q) * sld, *x1 = x0 + sld;
   T2 z;
-  switch (P.kind) {
+  switch (kind) {
     case K_R2HC: z = cmk<T2>(x0[k], x1[k]); break;
     case K_REDFT10:
     case K_RODFT10: {
       const int src = (k < (n + 1) / 2) ? 2 * k : 2 * (n - 1 - k) + 1;
-      const T sg = (P.kind == K_RODFT10 && (src & 1)) ? T(-1) : T(1);
+      const T sg = (kind == K_RODFT10 && (src & 1)) ? T(-1) : T(1);
       z = cmk<T2>(sg * x0[src], sg * x1[src]);
     } break;
     case K_HC2R: {
@@ -259,7 +261,7 @@ __device__ __forceinline__ cplx_t<T> pre_value(const DirParams &P, const T *__re
       // V_k = exp(+i pi k/(2n)) (x_k - i x_{n-k}), x_n = 0; DST-III reads the reversed line
       const T2 t = tab[k];  // (cos, -sin)
       const T c = t.x, s = -t.y;
-      const bool rev = P.kind == K_RODFT01;
+      const bool rev = kind == K_RODFT01;
       const int ka = rev ? n - 1 - k : k, kb = rev ? k - 1 : n - k;
       const T a0 = x0[ka], a1 = x1[ka];
       const T b0 = k == 0 ? T(0) : x0[kb], b1 = k == 0 ? T(0) : x1[kb];
@@ -318,7 +320,7 @@ __host__ __device__ constexpr int spec_ld(int m) { return m == 512 ? 640 : m + m
 template <int M, int LAY> __device__ __forceinline__ int zpos(int x) { return LAY ? regx(x) : spad<M>(x); }
 template <int M> constexpr int kLay = RegFFT<M>::on ? 1 : 0;
 
-template <typename T, int M, int SIGN>
+template <typename T, int M, int SIGN, int KIND = -1>
 __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const T *__restrict__ stg,
                                                        cplx_t<T> *__restrict__ A, cplx_t<T> *__restrict__ B,
                                                        const cplx_t<T> *__restrict__ tab,
@@ -329,7 +331,7 @@ __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const
   const int q = threadIdx.x >> 6, p = threadIdx.x & 63;
   T2 v[8];
 #pragma unroll
-  for (int a = 0; a < 8; a++) v[a] = pre_value<T, M>(P, stg, q, 64 * a + p, tab, pre);
+  for (int a = 0; a < 8; a++) v[a] = pre_value<T, M, KIND>(P, stg, q, 64 * a + p, tab, pre);
   dft<8, SIGN>(v);
   T2 *Tq = A + q * LD;
   Tq[p] = v[0];
@@ -365,11 +367,13 @@ __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const
 
 // pre-processing + complex FFT of the CTA's sequences (staging rows in B on entry);
 // returns the buffer holding the result, laid out as zpos<M, kLay<M>>
-template <typename T, int M>
+template <typename T, int M, int KIND = -1>
 __device__ __forceinline__ const cplx_t<T> *fft_in(const DirParams &P, const T *stg, cplx_t<T> *A, cplx_t<T> *B,
                                                    const cplx_t<T> *tab, const cplx_t<T> *pre,
                                                    const cplx_t<T> *tw) {
-  if constexpr (RegFFT<M>::on) {
+  if constexpr (RegFFT<M>::on && KIND >= 0) {
+    return fft512_reg<T, M, kind_sign(KIND), KIND>(P, stg, A, B, tab, pre, tw);
+  } else if constexpr (RegFFT<M>::on) {
     return kind_sign(P.kind) > 0 ? fft512_reg<T, M, +1>(P, stg, A, B, tab, pre, tw)
                                  : fft512_reg<T, M, -1>(P, stg, A, B, tab, pre, tw);
   } else {
@@ -379,21 +383,41 @@ __device__ __forceinline__ const cplx_t<T> *fft_in(const DirParams &P, const T *
   }
 }
 
+// f(KindC<kind>{}) with the pass's kind as a compile-time constant for the register-FFT
+// length (SET 1: the forward kinds, 0: the backward kinds, 2: both), f(KindC<-1>{}) otherwise
+template <int K> struct KindC { static constexpr int value = K; };
+template <int M, int SET, typename F> __device__ __forceinline__ void with_kind(int kind, F &&f) {
+  if constexpr (RegFFT<M>::on) {
+    if constexpr (SET != 0) {
+      if (kind == K_R2HC) { f(KindC<K_R2HC>{}); return; }
+      if (kind == K_REDFT10) { f(KindC<K_REDFT10>{}); return; }
+      if (kind == K_RODFT10) { f(KindC<K_RODFT10>{}); return; }
+    }
+    if constexpr (SET != 1) {
+      if (kind == K_HC2R) { f(KindC<K_HC2R>{}); return; }
+      if (kind == K_REDFT01) { f(KindC<K_REDFT01>{}); return; }
+      if (kind == K_RODFT01) { f(KindC<K_RODFT01>{}); return; }
+    }
+  }
+  f(KindC<-1>{});
+}
+
 // ----------------------------------------------------------------------- r2r post-processing
 // value of output index k (< nt) of real line r from the FFT result Z
-template <typename T, int M = 0, int LAY = 0>
+template <typename T, int M = 0, int LAY = 0, int KIND = -1>
 __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__restrict__ Z, int r, int k,
                                       const cplx_t<T> *__restrict__ tab) {
   using T2 = cplx_t<T>;
   const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? spec_ld(M) : P.ld;
+  const int kind = KIND >= 0 ? KIND : P.kind;
   if (!P.pairs) {  // kinds 11
     const T2 z = Z[r * ldz + k], w = tab[k];
     const T re = w.x * z.x - w.y * z.y, im = w.x * z.y + w.y * z.x;
-    return P.kind == K_REDFT11 ? T(2) * re : T(-2) * im;
+    return kind == K_REDFT11 ? T(2) * re : T(-2) * im;
   }
   const int q = r >> 1, wsel = r & 1;
   const T2 *L = Z + q * ldz;
-  switch (P.kind) {
+  switch (kind) {
     case K_R2HC: {
       const T2 a = L[zpos<M, LAY>(k)], b = L[zpos<M, LAY>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
       if (2 * k <= n) return wsel == 0 ? T(0.5) * (a.x + b.x) : T(0.5) * (a.y + b.y);
@@ -401,7 +425,7 @@ __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__res
     }
     case K_REDFT10:
     case K_RODFT10: {
-      const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
+      const int kk = kind == K_REDFT10 ? k : n - 1 - k;
       const T2 a = L[zpos<M, LAY>(kk)], b = L[zpos<M, LAY>(M ? ((m - kk) & (M - 1)) : ((m - kk) % m))], t = tab[kk];
       const T c = t.x, s = -t.y;
       return wsel == 0 ? c * (a.x + b.x) + s * (a.y - b.y) : c * (a.y + b.y) - s * (a.x - b.x);
@@ -415,7 +439,7 @@ __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__res
       const int pos = (k & 1) == 0 ? (k >> 1) : n - 1 - ((k - 1) >> 1);
       const T2 a = L[zpos<M, LAY>(pos)];
       const T v = wsel == 0 ? a.x : a.y;
-      return (P.kind == K_RODFT01 && (k & 1)) ? -v : v;
+      return (kind == K_RODFT01 && (k & 1)) ? -v : v;
     }
     case K_RODFT00: {
       const T2 a = L[zpos<M, LAY>(k + 1)];
@@ -430,13 +454,14 @@ __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__res
 
 // both real outputs (lines 2q and 2q+1) of output index k of a "pairs" kind, sharing the
 // loads of r2r_post (same arithmetic as r2r_post with r = 2q and r = 2q + 1)
-template <typename T, int M = 0, int LAY = 0>
+template <typename T, int M = 0, int LAY = 0, int KIND = -1>
 __device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *__restrict__ Z, int q, int k,
                                           const cplx_t<T> *__restrict__ tab, T &v0, T &v1) {
   using T2 = cplx_t<T>;
   const int m = M ? M : P.m, n = M ? M : P.nt, ldz = M ? spec_ld(M) : P.ld;
+  const int kind = KIND >= 0 ? KIND : P.kind;
   const T2 *L = Z + q * ldz;
-  switch (P.kind) {
+  switch (kind) {
     case K_R2HC: {
       const T2 a = L[zpos<M, LAY>(k)], b = L[zpos<M, LAY>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
       if (2 * k <= n) { v0 = T(0.5) * (a.x + b.x); v1 = T(0.5) * (a.y + b.y); }
@@ -444,7 +469,7 @@ __device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *_
     } break;
     case K_REDFT10:
     case K_RODFT10: {
-      const int kk = P.kind == K_REDFT10 ? k : n - 1 - k;
+      const int kk = kind == K_REDFT10 ? k : n - 1 - k;
       const T2 a = L[zpos<M, LAY>(kk)], b = L[zpos<M, LAY>(M ? ((m - kk) & (M - 1)) : ((m - kk) % m))], t = tab[kk];
       const T c = t.x, s = -t.y;
       v0 = c * (a.x + b.x) + s * (a.y - b.y);
@@ -454,7 +479,7 @@ __device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *_
     case K_RODFT01: {
       const int pos = (k & 1) == 0 ? (k >> 1) : n - 1 - ((k - 1) >> 1);
       const T2 a = L[zpos<M, LAY>(pos)];
-      const bool neg = P.kind == K_RODFT01 && (k & 1);
+      const bool neg = kind == K_RODFT01 && (k & 1);
       v0 = neg ? -a.x : a.x;
       v1 = neg ? -a.y : a.y;
     } break;

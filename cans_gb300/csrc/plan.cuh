@@ -281,25 +281,67 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
     }
   if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
-  const T2 *Z = fft_in<T, M>(P, stg, A, B, post, pre, tw);
-  T *Sk = S + (size_t)k * n1 * n2;
-  if (P.pairs) {
-    // both lines of a complex sequence per thread: runs of 2*ncx values along j per row i
-    for (int e = threadIdx.x; e < n1 * ncx; e += blockDim.x) {
-      const int i = M ? (int)((unsigned)e / (unsigned)G::NCX) : e / ncx, q = e - i * ncx, j = j0 + 2 * q;
-      if (j >= n2) continue;
+  with_kind<M, 1>(P.kind, [&](auto K) {
+    constexpr int KD = decltype(K)::value;
+    const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
+    T *Sk = S + (size_t)k * n1 * n2;
+    if (P.pairs) {
+      // both lines of a complex sequence per thread: runs of 2*ncx values along j per row i
+      for (int e = threadIdx.x; e < n1 * ncx; e += blockDim.x) {
+        const int i = M ? (int)((unsigned)e / (unsigned)G::NCX) : e / ncx, q = e - i * ncx, j = j0 + 2 * q;
+        if (j >= n2) continue;
+        T v0, v1;
+        if (i < nt) r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
+        else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
+        T *dst = Sk + (size_t)i * n2 + j;
+        if (((n2 & 1) == 0)) *reinterpret_cast<T2 *>(dst) = cmk<T2>(v0, v1);  // j even, n2 even: aligned pair
+        else { dst[0] = v0; if (j + 1 < n2) dst[1] = v1; }
+      }
+    } else {
+      for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
+        const int i = e / lpb, r = e - i * lpb, j = j0 + r;
+        if (j >= n2) continue;
+        Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M, kLay<M>, KD>(P, Z, r, i, post) : pass[r];
+      }
+    }
+  });
+}
+
+// FFT of the staged lines of a y tile and the store of the results (lines l0, l0+1, ...)
+template <typename T, int M, int KD>
+__device__ __forceinline__ void ylines_fft_store(T *__restrict__ S, long nlines, int n2, const DirParams &P, long l0,
+                                                 cplx_t<T> *A, cplx_t<T> *B, const T *stg, const cplx_t<T> *tw,
+                                                 const cplx_t<T> *post, const cplx_t<T> *pre) {
+  using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
+  const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, nt = M ? M : P.nt;
+  const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
+  if (M > 0) {
+    // two neighbouring outputs of both lines per thread: 2-element vector stores
+    for (int e = threadIdx.x; e < G::NCX * (M / 2); e += blockDim.x) {
+      const int q = e / (M / 2), j = 2 * (e - q * (M / 2));
+      const long l = l0 + 2 * q;
+      if (l >= nlines) continue;
+      T a0, a1, b0, b1;
+      r2r_post2<T, M, kLay<M>, KD>(P, Z, q, j, post, a0, a1);
+      r2r_post2<T, M, kLay<M>, KD>(P, Z, q, j + 1, post, b0, b1);
+      *reinterpret_cast<T2 *>(S + (size_t)l * M + j) = cmk<T2>(a0, b0);
+      if (l + 1 < nlines) *reinterpret_cast<T2 *>(S + (size_t)(l + 1) * M + j) = cmk<T2>(a1, b1);
+    }
+  } else if (P.pairs) {
+    for (int e = threadIdx.x; e < ncx * nt; e += blockDim.x) {
+      const int q = e / nt, j = e - q * nt;
+      const long l = l0 + 2 * q;
+      if (l >= nlines) continue;
       T v0, v1;
-      if (i < nt) r2r_post2<T, M, kLay<M>>(P, Z, q, i, post, v0, v1);
-      else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
-      T *dst = Sk + (size_t)i * n2 + j;
-      if (((n2 & 1) == 0)) *reinterpret_cast<T2 *>(dst) = cmk<T2>(v0, v1);  // j even, n2 even: aligned pair
-      else { dst[0] = v0; if (j + 1 < n2) dst[1] = v1; }
+      r2r_post2<T, M, kLay<M>, KD>(P, Z, q, j, post, v0, v1);
+      S[(size_t)l * n2 + j] = v0;
+      if (l + 1 < nlines) S[(size_t)(l + 1) * n2 + j] = v1;
     }
   } else {
-    for (int e = threadIdx.x; e < n1 * lpb; e += blockDim.x) {
-      const int i = e / lpb, r = e - i * lpb, j = j0 + r;
-      if (j >= n2) continue;
-      Sk[(size_t)i * n2 + j] = (i < nt) ? r2r_post<T, M, kLay<M>>(P, Z, r, i, post) : pass[r];
+    for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
+      const int r = e / nt, j = e - r * nt;
+      if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M, kLay<M>, KD>(P, Z, r, j, post);
     }
   }
 }
@@ -340,35 +382,57 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
   }
   if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
-  const T2 *Z = fft_in<T, M>(P, stg, A, B, post, pre, tw);
-  if (M > 0) {
-    // two neighbouring outputs of both lines per thread: 2-element vector stores
-    for (int e = threadIdx.x; e < G::NCX * (M / 2); e += blockDim.x) {
-      const int q = e / (M / 2), j = 2 * (e - q * (M / 2));
-      const long l = l0 + 2 * q;
-      if (l >= nlines) continue;
-      T a0, a1, b0, b1;
-      r2r_post2<T, M, kLay<M>>(P, Z, q, j, post, a0, a1);
-      r2r_post2<T, M, kLay<M>>(P, Z, q, j + 1, post, b0, b1);
-      *reinterpret_cast<T2 *>(S + (size_t)l * M + j) = cmk<T2>(a0, b0);
-      if (l + 1 < nlines) *reinterpret_cast<T2 *>(S + (size_t)(l + 1) * M + j) = cmk<T2>(a1, b1);
+  with_kind<M, 2>(P.kind, [&](auto K) {
+    ylines_fft_store<T, M, decltype(K)::value>(S, nlines, n2, P, l0, A, B, stg, tw, post, pre);
+  });
+}
+
+// persistent y pass of the compile-time path: each CTA loops over tiles tile0, tile0 +
+// gridDim.x, ...; the next tile's lines are loaded into registers while the current tile is
+// transformed (the loads stay in flight through the FFT), and the twiddle tables are copied
+// once per CTA
+template <typename T, int M>
+__device__ __forceinline__ void ylines_persist(T *__restrict__ S, long nlines, const DirParams &P, long ntiles,
+                                               unsigned char *smem) {
+  static_assert(M > 0, "compile-time lengths only");
+  using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
+  using V = typename Vec16<T>::type;
+  constexpr int VW = 16 / (int)sizeof(T), VPL = M / VW, PER = G::LPB * VPL / 256;
+  static_assert(G::LPB * VPL % 256 == 0, "whole vectors per thread");
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)G::NCX * G::LD;
+  T *stg = reinterpret_cast<T *>(B);
+  T2 *stw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(G::NCX, G::LD, G::LPB, G::SLD));
+  const T2 *tw = kTablesInSmem<T> ? stw : reinterpret_cast<const T2 *>(P.tw);
+  const T2 *post = kTablesInSmem<T> ? stw + M : reinterpret_cast<const T2 *>(P.post);
+  const T2 *pre = kTablesInSmem<T> ? stw + 2 * M : reinterpret_cast<const T2 *>(P.pre);
+  V nxt[PER];
+  auto load = [&](long tile) {
+    const V *src = reinterpret_cast<const V *>(S + (size_t)tile * G::LPB * M);
+    const long rows = nlines - tile * G::LPB;
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + 256 * u;
+      nxt[u] = (e / VPL < rows) ? src[e] : V{};
     }
-  } else if (P.pairs) {
-    for (int e = threadIdx.x; e < ncx * nt; e += blockDim.x) {
-      const int q = e / nt, j = e - q * nt;
-      const long l = l0 + 2 * q;
-      if (l >= nlines) continue;
-      T v0, v1;
-      r2r_post2<T, M, kLay<M>>(P, Z, q, j, post, v0, v1);
-      S[(size_t)l * n2 + j] = v0;
-      if (l + 1 < nlines) S[(size_t)(l + 1) * n2 + j] = v1;
+  };
+  long tile = blockIdx.x;
+  if (tile < ntiles) load(tile);
+  if (kTablesInSmem<T>) copy_tables<T>(P, M, M, stw, stw + M, stw + 2 * M);
+  with_kind<M, 2>(P.kind, [&](auto K) {
+    for (; tile < ntiles; tile += gridDim.x) {
+#pragma unroll
+      for (int u = 0; u < PER; u++) {
+        const int e = threadIdx.x + 256 * u, r = e / VPL, c = e - r * VPL;
+        *reinterpret_cast<V *>(stg + r * G::SLD + c * VW) = nxt[u];
+      }
+      __syncthreads();
+      if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
+      ylines_fft_store<T, M, decltype(K)::value>(S, nlines, M, P, tile * G::LPB, A, B, stg, tw, post, pre);
+      __syncthreads();  // the next tile's staging overwrites B, its first step A
     }
-  } else {
-    for (int e = threadIdx.x; e < lpb * nt; e += blockDim.x) {
-      const int r = e / nt, j = e - r * nt;
-      if (l0 + r < nlines) S[(size_t)(l0 + r) * n2 + j] = r2r_post<T, M, kLay<M>>(P, Z, r, j, post);
-    }
-  }
+  });
 }
 
 // value stored by the x-backward pass: acc 0 writes v, 1 adds v to p, 2 writes the sum of
@@ -429,30 +493,152 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
       pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
   if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
-  const T2 *Z = fft_in<T, M>(P, stg, A, B, post, pre, tw);
-  if (P.pairs) {
-    for (int e = threadIdx.x; e < ncx * n1; e += blockDim.x) {
-      const int q = M ? (int)((unsigned)e / (unsigned)M) : e / n1, i = e - q * n1, j = j0 + 2 * q;
-      if (j >= n2) continue;
-      T v0, v1;
-      if (i < nt) r2r_post2<T, M, kLay<M>>(P, Z, q, i, post, v0, v1);
-      else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
-      const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-      p[idx] = xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
-      if (j + 1 < n2) {
-        const size_t idx1 = idx + (size_t)(n1 + 2);
-        p[idx1] = xbwd_value<T, TF>(p, idx1, acc, v1, add0, add1);
+  with_kind<M, 0>(P.kind, [&](auto K) {
+    constexpr int KD = decltype(K)::value;
+    const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
+    if (P.pairs) {
+      for (int e = threadIdx.x; e < ncx * n1; e += blockDim.x) {
+        const int q = M ? (int)((unsigned)e / (unsigned)M) : e / n1, i = e - q * n1, j = j0 + 2 * q;
+        if (j >= n2) continue;
+        T v0, v1;
+        if (i < nt) r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
+        else { v0 = pass[2 * q]; v1 = pass[2 * q + 1]; }
+        const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+        p[idx] = xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
+        if (j + 1 < n2) {
+          const size_t idx1 = idx + (size_t)(n1 + 2);
+          p[idx1] = xbwd_value<T, TF>(p, idx1, acc, v1, add0, add1);
+        }
+      }
+    } else {
+      for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
+        const int r = e / n1, i = e - r * n1, j = j0 + r;
+        if (j >= n2) continue;
+        const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+        const T val = (i < nt) ? r2r_post<T, M, kLay<M>, KD>(P, Z, r, i, post) : pass[r];
+        p[idx] = xbwd_value<T, TF>(p, idx, acc, val, add0, add1);
       }
     }
-  } else {
-    for (int e = threadIdx.x; e < lpb * n1; e += blockDim.x) {
-      const int r = e / n1, i = e - r * n1, j = j0 + r;
-      if (j >= n2) continue;
-      const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-      const T val = (i < nt) ? r2r_post<T, M, kLay<M>>(P, Z, r, i, post) : pass[r];
-      p[idx] = xbwd_value<T, TF>(p, idx, acc, val, add0, add1);
+  });
+}
+
+// persistent x passes of the compile-time path (n1 == M): tiles t = k*ntj + jt strided by
+// the grid; the next tile's rows are loaded into registers while the current tile is
+// transformed, and the twiddle tables are copied once per CTA
+template <typename T, typename TF, int M>
+__device__ __forceinline__ void xfwd_persist(const TF *__restrict__ p, T *__restrict__ S, int n2, const DirParams &P,
+                                             int ntj, long ntiles, unsigned char *smem) {
+  static_assert(M > 0, "compile-time lengths only");
+  using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
+  constexpr int n1 = M, PER = G::LPB * M / 256;
+  static_assert(G::LPB * M % 256 == 0, "whole rows per CTA");
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)G::NCX * G::LD;
+  T *stg = reinterpret_cast<T *>(B);
+  T2 *stw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(G::NCX, G::LD, G::LPB, G::SLD));
+  const T2 *tw = kTablesInSmem<T> ? stw : reinterpret_cast<const T2 *>(P.tw);
+  const T2 *post = kTablesInSmem<T> ? stw + M : reinterpret_cast<const T2 *>(P.post);
+  const T2 *pre = kTablesInSmem<T> ? stw + 2 * M : reinterpret_cast<const T2 *>(P.pre);
+  TF nxt[PER];
+  auto load = [&](long t) {
+    const int k = (int)(t / ntj), j0 = (int)(t - (long)k * ntj) * G::LPB;
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + 256 * u, r = e / M, i = e % M, j = j0 + r;
+      nxt[u] = (j < n2) ? p[hidx(i + 1, j + 1, k + 1, n1, n2)] : TF(0);
     }
-  }
+  };
+  long tile = blockIdx.x;
+  if (tile < ntiles) load(tile);
+  if (kTablesInSmem<T>) copy_tables<T>(P, M, M, stw, stw + M, stw + 2 * M);
+  with_kind<M, 1>(P.kind, [&](auto K) {
+    constexpr int KD = decltype(K)::value;
+    for (; tile < ntiles; tile += gridDim.x) {
+      const int k = (int)(tile / ntj), j0 = (int)(tile - (long)k * ntj) * G::LPB;
+#pragma unroll
+      for (int u = 0; u < PER; u++) {
+        const int e = threadIdx.x + 256 * u, r = e / M, i = e % M;
+        stg[r * G::SLD + i] = cvt_to<T, TF>(nxt[u]);
+      }
+      __syncthreads();
+      if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
+      const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
+      T *Sk = S + (size_t)k * n1 * n2;
+      for (int e = threadIdx.x; e < n1 * G::NCX; e += blockDim.x) {
+        const int i = e / G::NCX, q = e - i * G::NCX, j = j0 + 2 * q;
+        if (j >= n2) continue;
+        T v0, v1;
+        r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
+        T *dst = Sk + (size_t)i * n2 + j;
+        if ((n2 & 1) == 0) *reinterpret_cast<T2 *>(dst) = cmk<T2>(v0, v1);  // j even, n2 even: aligned pair
+        else { dst[0] = v0; if (j + 1 < n2) dst[1] = v1; }
+      }
+      __syncthreads();  // the next tile's staging overwrites B, its first step A
+    }
+  });
+}
+
+// requires n2 % (16 / sizeof(T)) == 0 (whole 16-byte vectors of each row's run of LPB values)
+template <typename T, typename TF, int M>
+__device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__restrict__ p, int n2, const DirParams &P,
+                                             int acc, const T *add0, const T *add1, int ntj, long ntiles,
+                                             unsigned char *smem) {
+  static_assert(M > 0, "compile-time lengths only");
+  using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
+  using V = typename Vec16<T>::type;
+  constexpr int n1 = M, VW = 16 / (int)sizeof(T), VPR = G::LPB / VW, PER = M * VPR / 256;
+  static_assert(G::LPB % VW == 0 && M * VPR % 256 == 0, "whole vectors per thread");
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)G::NCX * G::LD;
+  T *stg = reinterpret_cast<T *>(B);
+  T2 *stw = reinterpret_cast<T2 *>(smem + tile_tables_offset<T>(G::NCX, G::LD, G::LPB, G::SLD));
+  const T2 *tw = kTablesInSmem<T> ? stw : reinterpret_cast<const T2 *>(P.tw);
+  const T2 *post = kTablesInSmem<T> ? stw + M : reinterpret_cast<const T2 *>(P.post);
+  const T2 *pre = kTablesInSmem<T> ? stw + 2 * M : reinterpret_cast<const T2 *>(P.pre);
+  V nxt[PER];
+  auto load = [&](long t) {
+    const int k = (int)(t / ntj), j0 = (int)(t - (long)k * ntj) * G::LPB;
+    const T *Sk = S + (size_t)k * n1 * n2;
+#pragma unroll
+    for (int u = 0; u < PER; u++) {
+      const int e = threadIdx.x + 256 * u, i = e / VPR, c = e - i * VPR, j = j0 + c * VW;
+      nxt[u] = (j < n2) ? *reinterpret_cast<const V *>(Sk + (size_t)i * n2 + j) : V{};
+    }
+  };
+  long tile = blockIdx.x;
+  if (tile < ntiles) load(tile);
+  if (kTablesInSmem<T>) copy_tables<T>(P, M, M, stw, stw + M, stw + 2 * M);
+  with_kind<M, 0>(P.kind, [&](auto K) {
+    constexpr int KD = decltype(K)::value;
+    for (; tile < ntiles; tile += gridDim.x) {
+      const int k = (int)(tile / ntj), j0 = (int)(tile - (long)k * ntj) * G::LPB;
+#pragma unroll
+      for (int u = 0; u < PER; u++) {
+        const int e = threadIdx.x + 256 * u, i = e / VPR, c = e - i * VPR;
+        const T *w = reinterpret_cast<const T *>(&nxt[u]);
+#pragma unroll
+        for (int q = 0; q < VW; q++) stg[(c * VW + q) * G::SLD + i] = w[q];
+      }
+      __syncthreads();
+      if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
+      const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
+      for (int e = threadIdx.x; e < G::NCX * n1; e += blockDim.x) {
+        const int q = e / M, i = e - q * M, j = j0 + 2 * q;
+        if (j >= n2) continue;
+        T v0, v1;
+        r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
+        const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+        p[idx] = xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
+        if (j + 1 < n2) {
+          const size_t idx1 = idx + (size_t)(n1 + 2);
+          p[idx1] = xbwd_value<T, TF>(p, idx1, acc, v1, add0, add1);
+        }
+      }
+      __syncthreads();
+    }
+  });
 }
 
 // z solve, FP64 spectral data, in place (one spectral column)

@@ -216,6 +216,27 @@ __global__ void __launch_bounds__(256) k_ylines(T *__restrict__ S, long nlines, 
   ylines_tile<T, M>(S, nlines, n2, P, blockIdx.x, smem);
 }
 
+// persistent x passes (compile-time lengths, n1 == M): tiles strided by the grid, next tile prefetched
+template <typename T, typename TF, int M>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xfwd_p(const TF *__restrict__ p, T *__restrict__ S, int n2, int ntj,
+                                                   long ntiles, DirParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  xfwd_persist<T, TF, M>(p, S, n2, P, ntj, ntiles, smem);
+}
+template <typename T, typename TF, int M>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xbwd_p(const T *__restrict__ S, TF *__restrict__ p, int n2, int ntj,
+                                                   long ntiles, DirParams P, int acc, const T *add0, const T *add1) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  xbwd_persist<T, TF, M>(S, p, n2, P, acc, add0, add1, ntj, ntiles, smem);
+}
+
+// persistent y pass (compile-time lengths): tiles strided by the grid, next tile prefetched
+template <typename T, int M>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_ylines_p(T *__restrict__ S, long nlines, long ntiles, DirParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  ylines_persist<T, M>(S, nlines, P, ntiles, smem);
+}
+
 template <typename T, typename TF, int M>
 __global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2, DirParams P,
                                               int acc, const T *add0, const T *add1) {
@@ -616,12 +637,51 @@ template <typename T> static int set_smem(const void *fn, size_t bytes) {
     default: CALL(0); break;        \
   }
 
+// CTAs of a persistent pass kernel: resident CTAs per SM x SMs, at most one per tile
+static int resident_grid(const void *fn, size_t smem, long tiles, unsigned *grid) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    CANS_CUDA_TRY(cudaGetDevice(&dev));
+    CANS_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  int per = 0;
+  CANS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, smem));
+  if (per < 1) return CANS_ENOTSUP;
+  *grid = (unsigned)std::max(1L, std::min<long>(tiles, (long)per * nsm));
+  return CANS_OK;
+}
+
+// persistent pass kernels exist for these compile-time lengths (the others use one CTA per tile)
+#define CANS_DISPATCH_MP(mlen, CALL) \
+  switch (mlen) {                    \
+    case 128: CALL(128); break;      \
+    case 256: CALL(256); break;      \
+    case 512: CALL(512); break;      \
+    default: CALL(1024); break;      \
+  }
+static inline bool persistent_len(int M) { return M >= 128 && M <= 1024; }
+
 template <typename T, typename TF> static int launch_xfwd(cans_plan *P, const TF *p) {
   DirParams q = make_params<T>(P, 0, 1);
   const size_t sm = smem_bytes<T>(q);
   const int M = spec_len(q);
   dim3 grid((P->n[1] + q.lpb - 1) / q.lpb, P->n[2]);
   int rc = CANS_OK;
+  if (persistent_len(M)) {
+    const long ntiles = (long)grid.x * grid.y;
+    unsigned pg = 0;
+#define CALL_XFP(MM)                                                                             \
+  do {                                                                                           \
+    if ((rc = set_smem<T>((const void *)k_xfwd_p<T, TF, MM>, sm))) return rc;                    \
+    if ((rc = resident_grid((const void *)k_xfwd_p<T, TF, MM>, sm, ntiles, &pg))) return rc;     \
+    k_xfwd_p<T, TF, MM><<<pg, 256, sm, P->stream>>>(p, (T *)P->S, P->n[1], (int)grid.x, ntiles, q); \
+  } while (0)
+    CANS_DISPATCH_MP(M, CALL_XFP)
+#undef CALL_XFP
+    CANS_LAUNCH_CHECK();
+    return CANS_OK;
+  }
 #define CALL_XF(MM)                                                                        \
   do {                                                                                     \
     if ((rc = set_smem<T>((const void *)k_xfwd<T, TF, MM>, sm))) return rc;                \
@@ -639,6 +699,21 @@ static int launch_xbwd(cans_plan *P, TF *p, int acc = 0, const T *add0 = nullptr
   const int M = spec_len(q);
   dim3 grid((P->n[1] + q.lpb - 1) / q.lpb, P->n[2]);
   int rc = CANS_OK;
+  if (persistent_len(M) && P->n[1] % (16 / (int)sizeof(T)) == 0) {
+    const long ntiles = (long)grid.x * grid.y;
+    unsigned pg = 0;
+#define CALL_XBP(MM)                                                                             \
+  do {                                                                                           \
+    if ((rc = set_smem<T>((const void *)k_xbwd_p<T, TF, MM>, sm))) return rc;                    \
+    if ((rc = resident_grid((const void *)k_xbwd_p<T, TF, MM>, sm, ntiles, &pg))) return rc;     \
+    k_xbwd_p<T, TF, MM><<<pg, 256, sm, P->stream>>>((const T *)P->S, p, P->n[1], (int)grid.x, ntiles, q, acc, \
+                                                     add0, add1);                                \
+  } while (0)
+    CANS_DISPATCH_MP(M, CALL_XBP)
+#undef CALL_XBP
+    CANS_LAUNCH_CHECK();
+    return CANS_OK;
+  }
 #define CALL_XB(MM)                                                                               \
   do {                                                                                            \
     if ((rc = set_smem<T>((const void *)k_xbwd<T, TF, MM>, sm))) return rc;                       \
@@ -656,6 +731,20 @@ template <typename T> static int launch_y(cans_plan *P, int fwd) {
   const long nlines = (long)P->n[0] * P->n[2];
   const unsigned grid = (unsigned)((nlines + q.lpb - 1) / q.lpb);
   int rc = CANS_OK;
+  if (persistent_len(M)) {
+    const long ntiles = grid;
+    unsigned pg = 0;
+#define CALL_YP(MM)                                                                              \
+  do {                                                                                           \
+    if ((rc = set_smem<T>((const void *)k_ylines_p<T, MM>, sm))) return rc;                      \
+    if ((rc = resident_grid((const void *)k_ylines_p<T, MM>, sm, ntiles, &pg))) return rc;       \
+    k_ylines_p<T, MM><<<pg, 256, sm, P->stream>>>((T *)P->S, nlines, ntiles, q);                  \
+  } while (0)
+    CANS_DISPATCH_MP(M, CALL_YP)
+#undef CALL_YP
+    CANS_LAUNCH_CHECK();
+    return CANS_OK;
+  }
 #define CALL_Y(MM)                                                                       \
   do {                                                                                   \
     if ((rc = set_smem<T>((const void *)k_ylines<T, MM>, sm))) return rc;                \
