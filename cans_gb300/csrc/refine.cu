@@ -276,7 +276,7 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const unsigned nblk_r = (unsigned)std::min<long>((long)o.n2 * o.n3, 12L * nsm);
+  const unsigned nblk_r = (unsigned)std::min<long>((long)o.n2 * o.n3, (long)kResidualCtasPerSM * nsm);
   const int tpb = o.n1 >= 256 ? 256 : (o.n1 >= 128 ? 128 : 64);
   cudaStream_t st = b.st;
   double nrhs = 0., nr = 0.;

@@ -1245,7 +1245,10 @@ int cans_plan_refine_buffers(cans_plan *P, RefineBufs *b) {
     CANS_CUDA_TRY(cudaMemsetAsync(P->R32, 0, nh * sizeof(float), P->stream));
     CANS_CUDA_TRY(cudaMemsetAsync(P->E32, 0, nh * sizeof(float), P->stream));
     CANS_CUDA_TRY(cudaMalloc(&P->Rlo, np * sizeof(float)));
-    const size_t nrblk = 8 * 1024;  // the refinement kernels use at most 8 CTAs per SM
+    int dev = 0, nsm = 0;
+    CANS_CUDA_TRY(cudaGetDevice(&dev));
+    CANS_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const size_t nrblk = 3 * (size_t)kResidualCtasPerSM * nsm + 16;  // residual partials (refine.cu)
     CANS_CUDA_TRY(cudaMalloc(&P->rpart, (std::max(nblk, nrblk) + 8) * sizeof(double)));
     // double-float z coefficients; the residue of each row of the operator the solver inverts
     // (interior rows a+b+c, wall rows without the absent neighbour) exact in extended precision
