@@ -185,14 +185,20 @@ def bench_ours(args, rank, world):
     del p64, plan64
     torch.cuda.empty_cache()
     hbm, kind = peaks()
-    # dominant kernel of the refined solve: the FP32 y pass (two launches per FP32 solve,
-    # the largest share of the launch list); 8 algorithmic bytes per cell (read + write FP32)
+    # dominant kernel of the refined solve (largest share of the launch list): the
+    # double-float residual k_dfres, timed per launch by CUDA events on the plan's stream
+    # inside the timed region; algorithmic bytes per launch = mean bytes/cell x cells
+    res_bytes = ref["residual_bytes_per_cell"] * ncell
+    achieved = res_bytes / (ref["residual_ms"] * 1e-3) / 1e9
     y_ms = 0.5 * (ref["fp32_pass_ms"]["solve_yfwd"] + ref["fp32_pass_ms"]["solve_ybwd"])
-    achieved = 8 * ncell / (y_ms * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_ylines<float> (FP32 y transform, in place)", "achieved": round(achieved, 1),
-            "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_source": kind,
-            "traffic": traffic_for("solve_y_fp32", workload + "_fp32"), "algorithmic_bytes_per_launch": 8 * ncell,
-            "kernel_ms": round(y_ms, 4),
+    roof = {"bound": "hbm", "kernel": "k_dfres (double-float residual of the refinement)",
+            "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+            "peak_source": kind, "traffic": traffic_for("residual", workload + "_fp32"),
+            "algorithmic_bytes_per_launch": int(res_bytes), "kernel_ms": ref["residual_ms"],
+            "next_kernel": {"kernel": "k_ylines_p<float,512> (FP32 y transform, in place)",
+                            "achieved": round(8 * ncell / (y_ms * 1e-3) / 1e9, 1), "kernel_ms": round(y_ms, 4),
+                            "algorithmic_bytes_per_launch": 8 * ncell,
+                            "traffic": traffic_for("solve_y_fp32", workload + "_fp32")},
             "solve_passes_ms": ref["fp32_pass_ms"]}
     rk3 = None
     if not args.skip_rk3:
@@ -220,6 +226,23 @@ def bench_ours(args, rank, world):
         out["batched_boxes"] = bench_boxes(args.boxes, dev, max(1, min(args.steps, 5)),
                                            unbatched_boxes=min(args.boxes, 32))
     return out
+
+
+def residual_bytes(k):
+    """Mean algorithmic bytes per cell of the k residual launches of a fixed k-correction
+    refinement: every launch reads the correction e (4 B), the residual hi/lo (8 B; the
+    first reads the FP64 rhs instead, 8 B) and writes hi/lo (8 B); a launch that folds two
+    pending corrections into x adds 4 B (the older correction), 8 B written (x) and, when
+    x already holds corrections, 8 B read."""
+    npend, has_x, tot = 1, False, 0
+    for j in range(k):
+        b = 20
+        if npend == 2:
+            b += 12 + (8 if has_x else 0)
+            has_x, npend = True, 0
+        tot += b
+        npend += 1
+    return tot / k
 
 
 def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
@@ -268,6 +291,8 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
     st = torch.cuda.current_stream()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     l0 = cans.launch_count()
+    # per-pass and per-residual-launch CUDA events on the plan's stream, over the timed solves
+    plan.set_timing(True)
     for e0, e1 in ev:
         p.copy_(src)  # each step solves the same compatible RHS; the restore is outside the events
         e0.record(st)
@@ -276,6 +301,9 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
     torch.cuda.synchronize()
     ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / args.steps
     launches = cans.launch_count() - l0
+    pass_ms, nrec = plan.get_timing()
+    res_ms, nres = plan.get_residual_timing()
+    plan.set_timing(False)
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -283,31 +311,34 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
     e2e_out = None
     if e2e:
         # end to end through the C ABI with host buffers: every step copies its RHS from
-        # pinned host memory, solves, and copies the solution back.  Two device buffers and
+        # pinned host memory, solves, and copies the solution back.  Three device buffers and
         # two copy streams pipeline the steps: the H2D of step k+1 and the D2H of step k-1
-        # run on the copy engines while step k solves.  Host clock around all K steps.
-        k2 = max(2, min(args.steps, 6))
-        host_in = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True) for _ in range(2)]
-        host_out = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True) for _ in range(2)]
+        # run on the copy engines while step k solves (the H2D target buffer's last D2H, of
+        # step k-2, has finished by then).  Host clock around all K steps, fill and drain
+        # of the pipeline included.
+        nbuf = 3
+        k2 = max(nbuf, min(2 * args.steps, 12))
+        host_in = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True) for _ in range(nbuf)]
+        host_out = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True) for _ in range(nbuf)]
         for h in host_in:
             h.copy_(src.cpu())
-        bufs = [p, torch.empty_like(p)]
+        bufs = [p] + [torch.empty_like(p) for _ in range(nbuf - 1)]
         s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
-        ev_in = [torch.cuda.Event() for _ in range(2)]
-        ev_solved = [torch.cuda.Event() for _ in range(2)]
-        ev_out = [torch.cuda.Event() for _ in range(2)]
+        ev_in = [torch.cuda.Event() for _ in range(nbuf)]
+        ev_solved = [torch.cuda.Event() for _ in range(nbuf)]
+        ev_out = [torch.cuda.Event() for _ in range(nbuf)]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with torch.cuda.stream(s_in):
             bufs[0].copy_(host_in[0], non_blocking=True)
             ev_in[0].record(s_in)
         for kk in range(k2):
-            b = kk % 2
+            b = kk % nbuf
             st.wait_event(ev_in[b])
             if kk + 1 < k2:
-                nb = (kk + 1) % 2
+                nb = (kk + 1) % nbuf
                 with torch.cuda.stream(s_in):
-                    if kk >= 1:
+                    if kk + 1 >= nbuf:
                         s_in.wait_event(ev_out[nb])  # the buffer's previous solution is on the host
                     bufs[nb].copy_(host_in[nb], non_blocking=True)
                     ev_in[nb].record(s_in)
@@ -322,19 +353,16 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
         nbytes = p.numel() * 8
         e2e_out = {"value": round(world / (ms_e2e * 1e-3), 3), "unit": "solves/s", "h2d_bytes_per_step": nbytes,
                    "d2h_bytes_per_step": nbytes, "steps": k2,
-                   "note": "pipelined: H2D(k+1) and D2H(k-1) overlap solve k (two buffers, two copy streams)"}
+                   "note": "pipelined: H2D(k+1) and D2H(k-1) overlap solve k (three buffers, two copy streams)"}
         del host_in, host_out, bufs
-    plan.set_timing(True)
-    plan.solve_refined(p, dli, dzci, dzfi, rtol=0.0, max_iter=k_cal)
-    pass_ms, nrec = plan.get_timing()
-    plan.set_timing(False)
     names = ["solve_xfwd", "solve_yfwd", "solve_zthomas", "solve_ybwd", "solve_xbwd"]
     del p, plan
     torch.cuda.empty_cache()
     return {"value": round(world / (ms * 1e-3), 3), "unit": "solves/s", "ms_per_step": round(ms, 4),
             "rtol": rtol, "corrections_per_solve": k_cal, "fp32_solves_per_solve": k_cal + 1,
             "residual_passes_per_solve": k_cal, "accuracy": acc, "gpu_launches": launches,
-            "fp32_pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)}, "e2e": e2e_out}
+            "fp32_pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)}, "residual_ms": round(res_ms, 4),
+            "residual_launches_timed": nres, "residual_bytes_per_cell": residual_bytes(k_cal), "e2e": e2e_out}
 
 
 def bench_rk3(size, dev, steps):

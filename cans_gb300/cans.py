@@ -72,6 +72,7 @@ def _setup(L):
     L.cans_plan_device_bytes.restype = C.c_longlong
     L.cans_plan_set_timing.argtypes = [_V, C.c_int]
     L.cans_plan_get_timing.argtypes = [_V, _D, _I]
+    L.cans_plan_get_residual_timing.argtypes = [_V, _D, _I]
     L.cans_launch_count.restype = C.c_longlong
     L.cans_solver.argtypes = [_V, _V]
     L.cans_solver_f32.argtypes = [_V, _V]
@@ -219,6 +220,13 @@ class Plan:
         cnt = C.c_int()
         _check(lib().cans_plan_get_timing(self._h, ms, C.byref(cnt)), "cans_plan_get_timing")
         return list(ms), cnt.value
+
+    def get_residual_timing(self):
+        """mean ms of the refinement's residual launches since timing was enabled, and their count"""
+        ms, cnt = C.c_double(), C.c_int()
+        _check(lib().cans_plan_get_residual_timing(self._h, C.byref(ms), C.byref(cnt)),
+               "cans_plan_get_residual_timing")
+        return ms.value, cnt.value
 
     def solve(self, p):
         """solver (src/solver_gpu.f90:34) in place on a haloed float64 (or float32) field."""

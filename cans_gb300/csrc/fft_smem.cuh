@@ -306,21 +306,26 @@ __device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict_
 //   step 1 (thread b = 8c + d): DFT8 over a of z[64a + b], times W512^(b k1) -> T[k1][b]
 //   step 2 (thread (k1, d)):    DFT8 over c of T[k1][8c + d], times W64^(d e) -> V[k1][e][d]
 //   step 3 (thread (k1, e)):    DFT8 over d of V[k1][e][d] -> X[k1 + 8e + 64f]
-// Strides (complex elements): T row 72, V 72*k1 + 9*e + d, X position x + 2*(x/8); with
-// these the half-warps of every FP32 exchange touch 16 distinct bank pairs.  The first step
+// Strides (complex elements): T row 72, V 72*k1 + 9*e + d, X position x + 2*(x/16); with
+// these the half-warps of every FP32 exchange, and the post-processing reads of 16
+// consecutive outputs, touch 16 distinct bank pairs (the mirrored reads X[m-k] one pair
+// twice).  Line stride 580 = 4 mod 16 keeps the four sequences of a CTA on different banks
+// when a half-warp reads four neighbouring outputs of each (x-forward stores).  The first step
 // reads its inputs straight from the real staging rows (pre_value), so the pre-processing
 // needs no pass of its own.  Requires blockDim.x == 64 * (sequences per CTA).
 template <int M> struct RegFFT { static constexpr bool on = false; };
 template <> struct RegFFT<512> { static constexpr bool on = true; };
-__host__ __device__ constexpr int regx(int x) { return x + 2 * (x >> 3); }
+__host__ __device__ constexpr int regx(int x) { return x + 2 * (x >> 4); }
 // complex line stride of the compile-time path's buffers
-__host__ __device__ constexpr int spec_ld(int m) { return m == 512 ? 640 : m + m / 16 + 1; }
+__host__ __device__ constexpr int spec_ld(int m) { return m == 512 ? 580 : m + m / 16 + 1; }
 // position of element x of an FFT result line: layout of the register FFT (LAY 1) or of
 // the Stockham path (LAY 0)
 template <int M, int LAY> __device__ __forceinline__ int zpos(int x) { return LAY ? regx(x) : spad<M>(x); }
 template <int M> constexpr int kLay = RegFFT<M>::on ? 1 : 0;
 
-template <typename T, int M, int SIGN, int KIND = -1>
+// tw: the plan's table exp(-2 pi i e/512), or (FP32, shared memory) the reordered copy of
+// copy_tables (SMEMTW)
+template <typename T, int M, int SIGN, int KIND = -1, bool SMEMTW = sizeof(T) == 4>
 __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const T *__restrict__ stg,
                                                        cplx_t<T> *__restrict__ A, cplx_t<T> *__restrict__ B,
                                                        const cplx_t<T> *__restrict__ tab,
@@ -337,7 +342,7 @@ __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const
   Tq[p] = v[0];
 #pragma unroll
   for (int k1 = 1; k1 < 8; k1++) {
-    T2 w = tw[(p * k1) & 511];
+    T2 w = SMEMTW ? tw[(k1 - 1) * 64 + p] : tw[(p * k1) & 511];
     if (SIGN > 0) w.y = -w.y;
     Tq[k1 * 72 + p] = cmul(v[k1], w);
   }
@@ -350,7 +355,7 @@ __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const
   Vq[k1 * 72 + d] = v[0];
 #pragma unroll
   for (int e = 1; e < 8; e++) {
-    T2 w = tw[(8 * d * e) & 511];
+    T2 w = SMEMTW ? tw[448 + (e - 1) * 8 + d] : tw[(8 * d * e) & 511];
     if (SIGN > 0) w.y = -w.y;
     Vq[k1 * 72 + e * 9 + d] = cmul(v[e], w);
   }

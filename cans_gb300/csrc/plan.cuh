@@ -58,8 +58,10 @@ struct cans_plan {
   bool timing = false;
   std::vector<cudaEvent_t> ev;  // kTimedSolves x (kPasses + 1)
   int nrec = 0;
+  std::vector<cudaEvent_t> rev; // kTimedResiduals x 2: the refinement's residual launches
+  int nres = 0;
 };
-static const int kPasses = 5, kTimedSolves = 256;
+static const int kPasses = 5, kTimedSolves = 256, kTimedResiduals = 512;
 
 // complex sequences per CTA: the largest power of two (<= 16) keeping the two FFT buffers
 // within a budget, so several CTAs share an SM and the transposed x stores are runs of
@@ -141,13 +143,24 @@ template <typename T> inline size_t smem_bytes(const DirParams &q) {
   return tile_tables_offset<T>(q.ncx, q.ld, q.lpb, q.sld) + tables + 16;
 }
 
-// copy the twiddle tables a pass uses into shared memory (before the tile's first barrier)
-template <typename T>
+// copy the twiddle tables a pass uses into shared memory (before the tile's first barrier).
+// For the register FFT the twiddles are stored in the order its threads read them
+// (regfft_tw): step 1 W512^(p k1) at [(k1-1)*64 + p], step 2 W64^(d e) at [448 + (e-1)*8 + d],
+// so each warp reads consecutive entries (the plain table read at p*k1 or 8*d*e has 2- to
+// 8-way bank conflicts)
+template <typename T, int M = 0>
 __device__ __forceinline__ void copy_tables(const DirParams &P, int m, int nt, cplx_t<T> *tw, cplx_t<T> *post,
                                             cplx_t<T> *pre) {
   using T2 = cplx_t<T>;
   const T2 *gtw = reinterpret_cast<const T2 *>(P.tw);
-  for (int e = threadIdx.x; e < m; e += blockDim.x) tw[e] = gtw[e];
+  if constexpr (RegFFT<M>::on) {
+    for (int e = threadIdx.x; e < 7 * 64 + 7 * 8; e += blockDim.x) {
+      if (e < 7 * 64) tw[e] = gtw[((e & 63) * ((e >> 6) + 1)) & 511];
+      else tw[e] = gtw[(8 * ((e - 448) & 7) * (((e - 448) >> 3) + 1)) & 511];
+    }
+  } else {
+    for (int e = threadIdx.x; e < m; e += blockDim.x) tw[e] = gtw[e];
+  }
   const int kd = P.kind;
   if (kd == K_REDFT10 || kd == K_RODFT10 || kd == K_REDFT01 || kd == K_RODFT01 || kd == K_REDFT11 ||
       kd == K_RODFT11) {
@@ -283,7 +296,7 @@ __device__ __forceinline__ void xfwd_tile(const TF *__restrict__ p, T *__restric
       else
         pass[r] = (j0 + r < n2) ? cvt_to<T, TF>(p[hidx(n1, j0 + r + 1, k + 1, n1, n2)]) : T(0);
     }
-  if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
+  if (kTablesInSmem<T> && !tables_ready) copy_tables<T, M>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
   with_kind<M, 1>(P.kind, [&](auto K) {
     constexpr int KD = decltype(K)::value;
@@ -320,7 +333,18 @@ __device__ __forceinline__ void ylines_fft_store(T *__restrict__ S, long nlines,
   using G = PassGeo<T, M>;
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, nt = M ? M : P.nt;
   const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
-  if (M > 0) {
+  if constexpr (kLay<M> == 1) {
+    // register-FFT layout: consecutive outputs on consecutive threads (conflict-free reads)
+    for (int e = threadIdx.x; e < G::NCX * M; e += blockDim.x) {
+      const int q = e / M, j = e - q * M;
+      const long l = l0 + 2 * q;
+      if (l >= nlines) continue;
+      T v0, v1;
+      r2r_post2<T, M, kLay<M>, KD>(P, Z, q, j, post, v0, v1);
+      S[(size_t)l * M + j] = v0;
+      if (l + 1 < nlines) S[(size_t)(l + 1) * M + j] = v1;
+    }
+  } else if (M > 0) {
     // two neighbouring outputs of both lines per thread: 2-element vector stores
     for (int e = threadIdx.x; e < G::NCX * (M / 2); e += blockDim.x) {
       const int q = e / (M / 2), j = 2 * (e - q * (M / 2));
@@ -384,7 +408,7 @@ __device__ __forceinline__ void ylines_tile(T *__restrict__ S, long nlines, int 
       stg[r * sld + j] = (l0 + r < nlines) ? S[(size_t)(l0 + r) * n2 + j] : T(0);
     }
   }
-  if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
+  if (kTablesInSmem<T> && !tables_ready) copy_tables<T, M>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
   with_kind<M, 2>(P.kind, [&](auto K) {
     ylines_fft_store<T, M, decltype(K)::value>(S, nlines, n2, P, l0, A, B, stg, tw, post, pre);
@@ -423,7 +447,7 @@ __device__ __forceinline__ void ylines_persist(T *__restrict__ S, long nlines, c
   };
   long tile = blockIdx.x;
   if (tile < ntiles) load(tile);
-  if (kTablesInSmem<T>) copy_tables<T>(P, M, M, stw, stw + M, stw + 2 * M);
+  if (kTablesInSmem<T>) copy_tables<T, M>(P, M, M, stw, stw + M, stw + 2 * M);
   with_kind<M, 2>(P.kind, [&](auto K) {
     for (; tile < ntiles; tile += gridDim.x) {
 #pragma unroll
@@ -495,7 +519,7 @@ __device__ __forceinline__ void xbwd_tile(const T *__restrict__ S, TF *__restric
   if (!M && nt < n1)
     for (int r = threadIdx.x; r < lpb; r += blockDim.x)
       pass[r] = (j0 + r < n2) ? Sk[(size_t)(n1 - 1) * n2 + j0 + r] : T(0);
-  if (kTablesInSmem<T> && !tables_ready) copy_tables<T>(P, m, nt, stw, stw + m, stw + m + nt);
+  if (kTablesInSmem<T> && !tables_ready) copy_tables<T, M>(P, m, nt, stw, stw + m, stw + m + nt);
   __syncthreads();
   with_kind<M, 0>(P.kind, [&](auto K) {
     constexpr int KD = decltype(K)::value;
@@ -555,7 +579,7 @@ __device__ __forceinline__ void xfwd_persist(const TF *__restrict__ p, T *__rest
   };
   long tile = blockIdx.x;
   if (tile < ntiles) load(tile);
-  if (kTablesInSmem<T>) copy_tables<T>(P, M, M, stw, stw + M, stw + 2 * M);
+  if (kTablesInSmem<T>) copy_tables<T, M>(P, M, M, stw, stw + M, stw + 2 * M);
   with_kind<M, 1>(P.kind, [&](auto K) {
     constexpr int KD = decltype(K)::value;
     for (; tile < ntiles; tile += gridDim.x) {
@@ -613,7 +637,7 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
   };
   long tile = blockIdx.x;
   if (tile < ntiles) load(tile);
-  if (kTablesInSmem<T>) copy_tables<T>(P, M, M, stw, stw + M, stw + 2 * M);
+  if (kTablesInSmem<T>) copy_tables<T, M>(P, M, M, stw, stw + M, stw + 2 * M);
   with_kind<M, 0>(P.kind, [&](auto K) {
     constexpr int KD = decltype(K)::value;
     for (; tile < ntiles; tile += gridDim.x) {

@@ -272,7 +272,7 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   auto rule = [](char ch) { return ch == 'P' ? 0 : (ch == 'N' ? 1 : -1); };
   o.gx0 = rule(b.cbc[0]); o.gx1 = rule(b.cbc[1]); o.gy0 = rule(b.cbc[2]); o.gy1 = rule(b.cbc[3]);
   o.zper = b.cbc[4] == 'P' && b.cbc[5] == 'P';
-  // fixed grid (8 CTAs per SM) striding over the rows: gridDim.x partial sums
+  // fixed grid (kResidualCtasPerSM CTAs per SM) striding over the rows: gridDim.x partial sums
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -303,27 +303,37 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
     };
     if ((rc = cans_plan_solve_f64in_f32out(P, p, pend[0]))) return rc;  // e_0 from the FP64 rhs
     npend = 1;
-    bool first = true;
+    bool first = true, have_nrhs = false;
     for (;;) {
       // two pending corrections are folded into x by this residual pass
       const int xmode = npend == 2 ? (has_x ? 2 : 1) : 0;
+      const bool timed = P->timing && P->nres < kTimedResiduals;
+      if (timed) cudaEventRecord(P->rev[2 * (size_t)P->nres], st);
       k_dfres<<<nblk_r, tpb, 0, st>>>(pend[npend - 1], b.R, b.Rlo, npend == 2 ? pend[0] : nullptr, p, xmode, b.a2,
                                       b.c2, b.s2, o, b.part, first ? p : nullptr, part0);
       CANS_LAUNCH_CHECK();
-      if (first && (rc = read_norm(part0, nblk_r, st, &nrhs))) return rc;
+      if (timed) cudaEventRecord(P->rev[2 * (size_t)P->nres++ + 1], st);
       first = false;
       if (xmode) {
         has_x = 1;
         npend = 0;
       }
-      if ((rc = read_norm(b.part, nblk_r, st, &nr))) return rc;
-      if (!(nr == nr)) return CANS_ENONFINITE;
-      rel = nrhs > 0. ? sqrt(nr / nrhs) : sqrt(nr);
-      if (rel <= rtol) {
-        if (npend && (rc = flush())) return rc;
-        break;
+      // the norms (one host synchronisation each) are read when the stop test needs them:
+      // every residual with rtol > 0, only the last one of a fixed schedule (rtol <= 0).
+      // ||rhs||^2 partials stay in part0 until then.
+      const bool last = it + 1 >= max_iter;
+      if (rtol > 0. || last) {
+        if (!have_nrhs && (rc = read_norm(part0, nblk_r, st, &nrhs))) return rc;
+        have_nrhs = true;
+        if ((rc = read_norm(b.part, nblk_r, st, &nr))) return rc;
+        if (!(nr == nr)) return CANS_ENONFINITE;
+        rel = nrhs > 0. ? sqrt(nr / nrhs) : sqrt(nr);
+        if (rel <= rtol) {
+          if (npend && (rc = flush())) return rc;
+          break;
+        }
       }
-      if (it + 1 >= max_iter) {
+      if (last) {
         // the last correction allowed: its x-backward pass writes x = pending + e in FP64,
         // and its residual is not evaluated (rel stays the one measured before it)
         if (has_x && npend && (rc = flush())) return rc;

@@ -548,6 +548,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->a32); cudaFree(P->zorder); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
   cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->E32b); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
+  for (auto &e : P->rev) cudaEventDestroy(e);
   delete P;
   return CANS_OK;
 }
@@ -802,9 +803,28 @@ extern "C" int cans_plan_set_timing(cans_plan *P, int enable) {
   if (enable && P->ev.empty()) {
     P->ev.resize((size_t)kTimedSolves * (kPasses + 1));
     for (auto &e : P->ev) CANS_CUDA_TRY(cudaEventCreate(&e));
+    P->rev.resize((size_t)kTimedResiduals * 2);
+    for (auto &e : P->rev) CANS_CUDA_TRY(cudaEventCreate(&e));
   }
   P->timing = enable != 0;
   P->nrec = 0;
+  P->nres = 0;
+  return CANS_OK;
+}
+
+extern "C" int cans_plan_get_residual_timing(cans_plan *P, double *ms, int *count) {
+  if (!P || !ms) return CANS_EINVAL;
+  *ms = 0.;
+  if (count) *count = P->nres;
+  if (P->nres == 0) return CANS_OK;
+  CANS_CUDA_TRY(cudaStreamSynchronize(P->stream));
+  for (int r = 0; r < P->nres; r++) {
+    float t = 0.f;
+    CANS_CUDA_TRY(cudaEventElapsedTime(&t, P->rev[2 * (size_t)r], P->rev[2 * (size_t)r + 1]));
+    *ms += t;
+  }
+  *ms /= P->nres;
+  P->nres = 0;
   return CANS_OK;
 }
 

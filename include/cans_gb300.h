@@ -74,6 +74,9 @@ long long cans_plan_device_bytes(const cans_plan *plan);
  * (at most 256 since the last call) and clears them. */
 int cans_plan_set_timing(cans_plan *plan, int enable);
 int cans_plan_get_timing(cans_plan *plan, double ms[5], int *nsolves);
+/* mean ms of the residual launches of cans_solver_refined recorded while timing is enabled
+ * (count of them in *count); synchronises the plan's stream */
+int cans_plan_get_residual_timing(cans_plan *plan, double *ms, int *count);
 /* running total of CUDA kernel launches issued by this library in this process */
 long long cans_launch_count(void);
 
