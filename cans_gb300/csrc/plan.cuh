@@ -334,11 +334,16 @@ __device__ __forceinline__ void ylines_fft_store(T *__restrict__ S, long nlines,
   const int ncx = M ? G::NCX : P.ncx, lpb = M ? G::LPB : P.lpb, nt = M ? M : P.nt;
   const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
   if constexpr (kLay<M> == 1) {
-    // register-FFT layout: consecutive outputs on consecutive threads (conflict-free reads)
-    for (int e = threadIdx.x; e < G::NCX * M; e += blockDim.x) {
-      const int q = e / M, j = e - q * M;
+    // register-FFT layout: consecutive outputs on consecutive threads (conflict-free reads);
+    // compile-time trip count and strides (the pass CTAs have 256 threads)
+    constexpr int U = G::NCX * M / 256;
+    static_assert(G::NCX * M % 256 == 0, "whole iterations");
+    const bool full = l0 + G::LPB <= nlines;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int e = (int)threadIdx.x + 256 * u, q = e / M, j = e % M;
       const long l = l0 + 2 * q;
-      if (l >= nlines) continue;
+      if (!full && l >= nlines) continue;
       T v0, v1;
       r2r_post2<T, M, kLay<M>, KD>(P, Z, q, j, post, v0, v1);
       S[(size_t)l * M + j] = v0;
@@ -593,8 +598,9 @@ __device__ __forceinline__ void xfwd_persist(const TF *__restrict__ p, T *__rest
       if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
       const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
       T *Sk = S + (size_t)k * n1 * n2;
-      for (int e = threadIdx.x; e < n1 * G::NCX; e += blockDim.x) {
-        const int i = e / G::NCX, q = e - i * G::NCX, j = j0 + 2 * q;
+#pragma unroll
+      for (int u = 0; u < n1 * G::NCX / 256; u++) {
+        const int e = (int)threadIdx.x + 256 * u, i = e / G::NCX, q = e % G::NCX, j = j0 + 2 * q;
         if (j >= n2) continue;
         T v0, v1;
         r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
@@ -652,8 +658,9 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
       __syncthreads();
       if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
       const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
-      for (int e = threadIdx.x; e < G::NCX * n1; e += blockDim.x) {
-        const int q = e / M, i = e - q * M, j = j0 + 2 * q;
+#pragma unroll
+      for (int u = 0; u < G::NCX * n1 / 256; u++) {
+        const int e = (int)threadIdx.x + 256 * u, q = e / M, i = e % M, j = j0 + 2 * q;
         if (j >= n2) continue;
         T v0, v1;
         r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
