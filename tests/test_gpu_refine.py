@@ -13,6 +13,8 @@ CASES = [
     ((30, 20, 16), (1.0, 1.0, 1.0), "DDNNDD", 1.1),
     ((16, 16, 16), (6.2831853, 6.2831853, 6.2831853), "PPPPPP", 0.0),
     ((24, 16, 20), (1.0, 1.0, 2.0), "NNDDNN", 1.3),
+    ((512, 12, 10), (4.0, 1.0, 2.0), "PPDDNN", 1.3),           # FP32 register-FFT x pass
+    ((10, 512, 12), (1.0, 4.0, 2.0), "NNPPNN", 1.3),           # FP32 register-FFT y pass
 ]
 
 

@@ -25,6 +25,13 @@ CASES = [
     ((12, 10, 9), (1.0, 1.0, 1.0), "DDDDDD", "ccf", 1.2),      # face-centred Dirichlet top in z
     ((9, 10, 8), (1.0, 1.0, 1.0), "NNNNDD", "fcc", 0.0),       # face-centred NN (REDFT00)
     ((64, 48, 32), (4.0, 2.0, 2.0), "PPPPNN", "ccc", 1.4),
+    # 512-point lines: the register-FFT tiles and the persistent pass kernels, every kind
+    ((512, 8, 6), (2.0, 1.0, 1.0), "PPNNNN", "ccc", 1.2),      # x R2HC / HC2R
+    ((512, 6, 6), (2.0, 1.0, 1.0), "NNDDNN", "ccc", 1.2),      # x REDFT10 / REDFT01
+    ((512, 6, 6), (2.0, 1.0, 1.0), "DDPPNN", "ccc", 1.2),      # x RODFT10 / RODFT01
+    ((8, 512, 6), (1.0, 2.0, 1.0), "NNPPNN", "ccc", 1.2),      # y R2HC / HC2R
+    ((6, 512, 6), (1.0, 2.0, 1.0), "DDNNDD", "ccc", 1.2),      # y REDFT10 / REDFT01
+    ((6, 512, 5), (1.0, 2.0, 1.0), "NNDDNN", "ccc", 1.2),      # y RODFT10 / RODFT01, odd tile count
 ]
 
 
