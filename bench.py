@@ -317,7 +317,7 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
         # step k-2, has finished by then).  Host clock around all K steps, fill and drain
         # of the pipeline included.
         nbuf = 3
-        k2 = max(nbuf, min(2 * args.steps, 12))
+        k2 = max(nbuf, min(4 * args.steps, 24))
         host_in = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True) for _ in range(nbuf)]
         host_out = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True) for _ in range(nbuf)]
         for h in host_in:

@@ -657,18 +657,31 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
       }
       __syncthreads();
       if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
+      // accumulating store (acc 1): the old values of this thread's outputs are loaded now
+      // and stay in flight through the FFT
+      constexpr int U = G::NCX * n1 / 256;
+      TF old0[U], old1[U];
+      if (acc == 1) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int e = (int)threadIdx.x + 256 * u, q = e / M, i = e % M, j = j0 + 2 * q;
+          const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+          old0[u] = j < n2 ? p[idx] : TF(0);
+          old1[u] = j + 1 < n2 ? p[idx + (size_t)(n1 + 2)] : TF(0);
+        }
+      }
       const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
 #pragma unroll
-      for (int u = 0; u < G::NCX * n1 / 256; u++) {
+      for (int u = 0; u < U; u++) {
         const int e = (int)threadIdx.x + 256 * u, q = e / M, i = e % M, j = j0 + 2 * q;
         if (j >= n2) continue;
         T v0, v1;
         r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
         const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-        p[idx] = xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
+        p[idx] = acc == 1 ? (TF)(old0[u] + cvt_to<TF, T>(v0)) : xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
         if (j + 1 < n2) {
           const size_t idx1 = idx + (size_t)(n1 + 2);
-          p[idx1] = xbwd_value<T, TF>(p, idx1, acc, v1, add0, add1);
+          p[idx1] = acc == 1 ? (TF)(old1[u] + cvt_to<TF, T>(v1)) : xbwd_value<T, TF>(p, idx1, acc, v1, add0, add1);
         }
       }
       __syncthreads();

@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xfwd_p(const TF
   xfwd_persist<T, TF, M>(p, S, n2, P, ntj, ntiles, smem);
 }
 template <typename T, typename TF, int M>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_xbwd_p(const T *__restrict__ S, TF *__restrict__ p, int n2, int ntj,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 && sizeof(TF) == 4 ? 3 : 2) k_xbwd_p(const T *__restrict__ S, TF *__restrict__ p, int n2, int ntj,
                                                    long ntiles, DirParams P, int acc, const T *add0, const T *add1) {
   extern __shared__ __align__(16) unsigned char smem[];
   xbwd_persist<T, TF, M>(S, p, n2, P, acc, add0, add1, ntj, ntiles, smem);
