@@ -13,7 +13,9 @@ dt_f, visci, icheck, cbcvel (18 chars, cbcvel(0:1,3,3) order), bcvel (18),
 cbcpre (6 chars), bcpre (6), bforce, is_forced, velf, is_impdiff, inivel; and the
 &scalar keys (src/param.f90:144-151): nscal, alphai, cbcscal (6 chars each), bcscal
 (6 each), ssource, is_sforced, scalf, gacc, beta, is_boussinesq_buoyancy.  Scalars are
-advanced before the velocity in every substep (src/main.f90:440-451).
+advanced before the velocity in every substep (src/main.f90:440-451).  With
+pressure_refine = {"rtol": r, "max_iter": K} the pressure solve runs on an FP32 plan with
+FP64 iterative refinement (cans_solver_refined) instead of the FP64 path.
 """
 import ctypes as C
 
@@ -67,7 +69,12 @@ class Simulation:
         self.dzci, self.dzfi, self.gvr_c, self.gvr_f = t(self.dzci_h), t(self.dzfi_h), t(gvr_c), t(gvr_f)
         # is_bound on one GPU with x-aligned pencils (src/initmpi.f90:193-267)
         self.is_bound = [1, 1] + [0 if self.cbcpre[2 * d:2 * d + 2] == "PP" else 1 for d in (1, 2) for _ in (0, 1)]
-        self.plan_p = cans.Plan(n, self.dli, self.dzci_h, self.dzfi_h, self.cbcpre, self.bcpre, "ccc")
+        # pressure_refine = {"rtol": r, "max_iter": K}: the pressure solve runs on an FP32 plan
+        # with FP64 iterative refinement (cans_solver_refined) instead of the FP64 path
+        self.p_refine = dict(case["pressure_refine"]) if case.get("pressure_refine") else None
+        self.p_refine_iters = 0
+        self.plan_p = cans.Plan(n, self.dli, self.dzci_h, self.dzfi_h, self.cbcpre, self.bcpre, "ccc",
+                                precision=cans.FP32 if self.p_refine else cans.FP64)
         self.plans_v = []
         if self.is_impdiff:
             for c in range(3):
@@ -225,7 +232,12 @@ class Simulation:
                       self.w, False, cans.HALO_LOWER)
         cans.fillps(n, self.dli, self.dzfi, dtrki, self.u, self.v, self.w, self.pp)
         cans.updt_rhs_b("ccc", self.cbcpre, n, self.is_bound, self.plan_p.rhsb, self.pp)
-        self.plan_p.solve(self.pp)
+        if self.p_refine:
+            it, _ = self.plan_p.solve_refined(self.pp, self.dli, self.dzci, self.dzfi,
+                                              rtol=self.p_refine.get("rtol", 0.), max_iter=self.p_refine["max_iter"])
+            self.p_refine_iters = max(self.p_refine_iters, it)
+        else:
+            self.plan_p.solve(self.pp)
         cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.pp)
         cans.correc(n, self.dli, self.dzci, dtrk, self.pp, self.u, self.v, self.w)
         cans.bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,

@@ -74,14 +74,18 @@ def test_taylor_green_field_by_field(require_gpu):
     assert abs(sim.dt - r.dt) <= 1e-13 * r.dt
 
 
-def test_channel_forced_field_by_field(require_gpu):
-    """Stretched-grid channel with constant flow rate, seeded noise, 5 steps vs the oracle."""
+@pytest.mark.parametrize("refine", [None, {"rtol": 1e-13, "max_iter": 6}])
+def test_channel_forced_field_by_field(require_gpu, refine):
+    """Stretched-grid channel with constant flow rate, seeded noise, 5 steps vs the oracle;
+    also with the pressure solved on an FP32 plan with FP64 refinement."""
     from cans_gb300.driver import Simulation
     from cans_gb300 import cans
     n = [32, 16, 24]
     case = dict(ng=n, l=[4.0, 2.0, 2.0], gtype=1, gr=1.4, cfl=0.5, dtmax=1e5, dt_f=-1., visci=5600., icheck=2,
                 cbcvel="PPPPDD" * 3, cbcpre="PPPPNN", bcvel=[0.] * 18, bcpre=[0.] * 6,
                 is_forced=[1, 0, 0], velf=[1., 0., 0.])
+    if refine:
+        case["pressure_refine"] = refine
     r = O.Run(case)
     zc = r.grid()["zc"]
     u = O.field(n)
