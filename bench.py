@@ -311,12 +311,12 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
     e2e_out = None
     if e2e:
         # end to end through the C ABI with host buffers: every step copies its RHS from
-        # pinned host memory, solves, and copies the solution back.  Three device buffers and
+        # pinned host memory, solves, and copies the solution back.  Four device buffers and
         # two copy streams pipeline the steps: the H2D of step k+1 and the D2H of step k-1
         # run on the copy engines while step k solves (the H2D target buffer's last D2H, of
-        # step k-2, has finished by then).  Host clock around all K steps, fill and drain
-        # of the pipeline included.
-        nbuf = 3
+        # step k+1-nbuf, has finished by then).  Host clock around all K steps, fill and
+        # drain of the pipeline included.
+        nbuf = 4
         k2 = max(nbuf, min(4 * args.steps, 24))
         host_in = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True) for _ in range(nbuf)]
         host_out = [torch.empty(p.shape, dtype=torch.float64, pin_memory=True) for _ in range(nbuf)]
@@ -353,7 +353,7 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
         nbytes = p.numel() * 8
         e2e_out = {"value": round(world / (ms_e2e * 1e-3), 3), "unit": "solves/s", "h2d_bytes_per_step": nbytes,
                    "d2h_bytes_per_step": nbytes, "steps": k2,
-                   "note": "pipelined: H2D(k+1) and D2H(k-1) overlap solve k (three buffers, two copy streams)"}
+                   "note": "pipelined: H2D(k+1) and D2H(k-1) overlap solve k (four buffers, two copy streams)"}
         del host_in, host_out, bufs
     names = ["solve_xfwd", "solve_yfwd", "solve_zthomas", "solve_ybwd", "solve_xbwd"]
     del p, plan

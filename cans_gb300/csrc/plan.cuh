@@ -175,7 +175,7 @@ __device__ __forceinline__ void copy_tables(const DirParams &P, int m, int nt, c
 
 // CTAs per SM of the refinement's residual kernel (it strides over (j,k) rows; many small
 // CTAs balance the rows best); its partial-sum buffer holds 3 * this * SMs + 16 doubles
-constexpr int kResidualCtasPerSM = 48;
+constexpr int kResidualCtasPerSM = 96;
 
 // device buffers of the FP32 + FP64 refinement of an FP32 plan (solver.cu allocates, refine.cu uses)
 struct RefineBufs {

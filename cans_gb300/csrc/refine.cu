@@ -98,13 +98,6 @@ __device__ __forceinline__ df diff_nb(bool inside, int rule, float enb, float ec
   return {-2.f * ec, 0.f};  // exact
 }
 
-// the same difference rounded to FP32
-__device__ __forceinline__ float diff_nb32(bool inside, int rule, float enb, float ec) {
-  if (inside || rule == 0) return __fsub_rn(enb, ec);
-  if (rule > 0) return 0.f;
-  return -2.f * ec;
-}
-
 // block sum of a per-thread FP32 value: warp shuffles in FP32 (the FP64 pipe is 58x slower),
 // per-warp partials accumulated in FP64 by one thread
 __device__ __forceinline__ void block_reduce_to(float v, double *out) {
@@ -153,7 +146,7 @@ __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, floa
                                                const float2 *__restrict__ a2, const float2 *__restrict__ c2,
                                                const float2 *__restrict__ s2, OpParams o,
                                                double *__restrict__ part, const double *__restrict__ rhs,
-                                               double *__restrict__ part0, int lowp) {
+                                               double *__restrict__ part0) {
   // rhs != nullptr (first residual): the current residual is the FP64 right-hand side itself,
   // split into (hi, lo) here, and part0 receives the partial sums of ||rhs||^2
   const int n1 = o.n1, n2 = o.n2, n3 = o.n3;
@@ -181,24 +174,6 @@ __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, floa
       const float ee = i < n1 ? Ec[i + 1] : (o.gx1 == 0 ? Ec[1] : 0.f);
       const float es = Es ? Es[i] : 0.f, en = En ? En[i] : 0.f;
       const float eb = hasb ? Eb[i] : 0.f, et = hast ? Et[i] : 0.f;
-      if (lowp) {
-        // the last residual of a fixed schedule, whose input is already a residual: its
-        // correction only needs the residual to FP32 relative accuracy (the hi part; the
-        // low part is neither read nor written)
-        float a = Rr[i];
-        a = __fmaf_rn(mcx.x, diff_nb32(i < n1, o.gx1, ee, ec), a);
-        a = __fmaf_rn(mcx.x, diff_nb32(i > 1, o.gx0, ew, ec), a);
-        a = __fmaf_rn(mcy.x, diff_nb32(j < n2, o.gy1, en, ec), a);
-        a = __fmaf_rn(mcy.x, diff_nb32(j > 1, o.gy0, es, ec), a);
-        if (hasb) a = __fmaf_rn(mav.x, __fsub_rn(eb, ec), a);
-        if (hast) a = __fmaf_rn(mcv.x, __fsub_rn(et, ec), a);
-        a = __fmaf_rn(msv.x, ec, a);
-        Rr[i] = a;
-        if (xmode == 1) x[c0 + i] = f2d(Eprev[c0 + i]) + f2d(ec);
-        else if (xmode == 2) x[c0 + i] = (x[c0 + i] + f2d(Eprev[c0 + i])) + f2d(ec);
-        sq = __fmaf_rn(a, a, sq);
-        continue;
-      }
       float rh, rl;
       if (rhs) {
         d2f_split(rhs[c0 + i], rh, rl);
@@ -302,7 +277,7 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const unsigned nblk_r = (unsigned)std::min<long>((long)o.n2 * o.n3, (long)kResidualCtasPerSM * nsm);
-  const int tpb = o.n1 >= 256 ? 256 : (o.n1 >= 128 ? 128 : 64);
+  const int tpb = 64;  // several cells per thread and row amortise the per-row set-up
   cudaStream_t st = b.st;
   double nrhs = 0., nr = 0.;
   double *part0 = b.part + 2 * (size_t)nblk_r + 16;  // ||rhs||^2 partials of the first residual pass
@@ -334,11 +309,8 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
       const int xmode = npend == 2 ? (has_x ? 2 : 1) : 0;
       const bool timed = P->timing && P->nres < kTimedResiduals;
       if (timed) cudaEventRecord(P->rev[2 * (size_t)P->nres], st);
-      // the last residual of a fixed schedule (rtol <= 0) that is not the first is evaluated
-      // in FP32: it only feeds the final correction, whose own FP32 solve error dominates
-      const int lowp = (rtol <= 0. && !first && it + 1 >= max_iter) ? 1 : 0;
       k_dfres<<<nblk_r, tpb, 0, st>>>(pend[npend - 1], b.R, b.Rlo, npend == 2 ? pend[0] : nullptr, p, xmode, b.a2,
-                                      b.c2, b.s2, o, b.part, first ? p : nullptr, part0, lowp);
+                                      b.c2, b.s2, o, b.part, first ? p : nullptr, part0);
       CANS_LAUNCH_CHECK();
       if (timed) cudaEventRecord(P->rev[2 * (size_t)P->nres++ + 1], st);
       first = false;

@@ -92,9 +92,7 @@ int cans_solver_f32(cans_plan *plan, float *p);
  * number of corrections in *iters and the last evaluated relative residual in *relres
  * (both may be NULL).  When the iteration ends at max_iter, the last correction is
  * added to p by its own x-backward pass and its residual is not evaluated (saves one
- * residual pass), so *relres is the residual before that correction; with rtol <= 0 the
- * last evaluated residual, when it is not the first, is computed in FP32 (it only feeds
- * the final correction, itself an FP32 solve); max_iter = 0 is one
+ * residual pass), so *relres is the residual before that correction; max_iter = 0 is one
  * FP32 solve written to p (*relres = 1).  dzci/dzfi: device grid arrays (0..n3+1). */
 int cans_solver_refined(cans_plan *plan, double *p, const double dli[3], const double *dzci,
                         const double *dzfi, double rtol, int max_iter, int *iters, double *relres);

@@ -32,6 +32,11 @@ CASES = [
     ((8, 512, 6), (1.0, 2.0, 1.0), "NNPPNN", "ccc", 1.2),      # y R2HC / HC2R
     ((6, 512, 6), (1.0, 2.0, 1.0), "DDNNDD", "ccc", 1.2),      # y REDFT10 / REDFT01
     ((6, 512, 5), (1.0, 2.0, 1.0), "NNDDNN", "ccc", 1.2),      # y RODFT10 / RODFT01, odd tile count
+    # the other persistent lengths (128, 256, 1024), x and y
+    ((128, 10, 6), (1.0, 1.0, 1.0), "PPDDNN", "ccc", 1.2),
+    ((10, 256, 6), (1.0, 1.0, 1.0), "DDNNNN", "ccc", 1.2),
+    ((1024, 4, 5), (2.0, 1.0, 1.0), "NNPPNN", "ccc", 1.2),
+    ((4, 1024, 5), (1.0, 2.0, 1.0), "PPDDNN", "ccc", 1.2),
 ]
 
 
