@@ -620,8 +620,10 @@ def main():
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2),
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                "data": "synthetic (seeded N(0,1) RHS)",
-               "config": {"workload": f"poisson_{args.size}x{args.size}x{args.size}_PPPPNN_fp64",
-                          "grid": [args.size] * 3, "bc_pressure": "PP,PP,NN", "z_grid": "tanh gr=1.4"},
+               "config": {"workload": f"poisson_{args.size}x{args.size}x{args.size}_PPPPNN_fp32_refined_to_fp64_accuracy",
+                          "grid": [args.size] * 3, "bc_pressure": "PP,PP,NN", "z_grid": "tanh gr=1.4",
+                          "domain": [round(x, 6) for x in L_CH],
+                          "precision": "the reference's FP64 solve (the accuracy the GPU arm matches)"},
                "cpu_baseline": {"value": round(val, 5), "unit": "solves/s", "cores": cores, "kind": "port",
                                 "sample": f"{args.steps} full {args.size}^3 solves of the C/OpenMP restatement "
                                           "of src/solver.f90 (reference Fortran/MPI/FFTW build unavailable)"},
