@@ -1,4 +1,4 @@
-"""FP32 transforms + FP64 refinement against the FP64 oracle (the benchmark spec precision form)."""
+"""FP32 transforms + FP64 refinement against the FP64 oracle (the refined precision form of the solve)."""
 import numpy as np
 import pytest
 
