@@ -144,3 +144,30 @@ def test_buoyant_channel_with_scalar(require_gpu, is_impdiff):
     assert rel_l2(got, r.s) < 1e-11
     got, want = cans.fview(sim.p)[1:-1, 1:-1, 1:-1], r.p[1:-1, 1:-1, 1:-1]
     assert gauge_rel_l2(got, want, r.grid()["dzf"]) < 1e-11
+
+
+def test_taylor_green_64_100_steps(require_gpu):
+    """The TGV 64^3 protocol: 100 steps field by field against the oracle run (relative L2
+    <= 1e-12 per velocity component after step 1; the drift is checked at step 100)."""
+    from cans_gb300.driver import Simulation
+    from cans_gb300 import cans
+    n = 64
+    case = _tgv_case(n)
+    u, v, w, p = _tgv_fields(n, 2 * np.pi, 2 * np.pi / n)
+    r = O.Run(case)
+    r.u[:] = u; r.v[:] = v; r.w[:] = w; r.p[:] = p
+    r.start()
+    sim = Simulation(case)
+    sim.set_fields(u, v, w, p)
+    sim.start()
+    errs = []
+    for step in range(100):
+        r.step(1)
+        sim.step(1)
+        if step in (0, 9, 49, 99):
+            e = max(rel_l2(cans.fview(getattr(sim, c))[1:-1, 1:-1, 1:-1], getattr(r, c)[1:-1, 1:-1, 1:-1])
+                    for c in ("u", "v", "w"))
+            errs.append(e)
+    print("TGV 64^3 drift (steps 1, 10, 50, 100):", errs)
+    assert errs[0] <= 1e-12, errs
+    assert errs[-1] <= 1e-12, errs
