@@ -173,6 +173,8 @@ def bench_ours(args, rank, world):
         return {"rk3_step": bench_rk3(args.size, dev, 20)}
     if args.only == "mx":
         return {"poisson_mx": bench_mx(args, dev, world)}
+    if args.only == "ch":
+        return {"channel_ch": bench_ch(dev)}
     if args.only == "adjoint":
         return {"adjoint_duct": bench_adjoint(dev, nsteps=args.adjoint_steps, ndir=args.adjoint_dirs)}
     if args.only == "boxes":
@@ -206,6 +208,10 @@ def bench_ours(args, rank, world):
     if not args.skip_mx and world == 1:
         torch.cuda.empty_cache()
         mx = bench_mx(args, dev, world)
+    ch = None
+    if not args.skip_ch and world == 1:
+        torch.cuda.empty_cache()
+        ch = bench_ch(dev)
     rk3 = None
     if not args.skip_rk3:
         torch.cuda.empty_cache()
@@ -226,6 +232,8 @@ def bench_ours(args, rank, world):
         out["rk3_step"] = rk3
     if mx:
         out["poisson_mx"] = mx
+    if ch:
+        out["channel_ch"] = ch
     if not args.skip_adjoint:
         torch.cuda.empty_cache()
         out["adjoint_duct"] = bench_adjoint(dev, nsteps=args.adjoint_steps, ndir=args.adjoint_dirs)
@@ -234,6 +242,53 @@ def bench_ours(args, rank, world):
         out["batched_boxes"] = bench_boxes(args.boxes, dev, max(1, min(args.steps, 5)),
                                            unbatched_boxes=min(args.boxes, 32))
     return out
+
+
+def bench_ch(dev, steps=200):
+    """The channel run (CH): 512 x 256 x 256, tanh z (gr 1.4), domain 6 x 3 x 1, Re_b 5600,
+    constant flow rate, Poiseuille + uniform(-0.1, 0.1) noise, CFL 0.95; `steps` timed RK3
+    steps after 3 warm-up steps, with the FP64 pressure solve and with the refined FP32 one
+    (two corrections).  Reported with the bulk velocity held by the forcing and the
+    divergence at the end."""
+    import torch
+    from cans_gb300 import cans
+    from cans_gb300.driver import Simulation
+    n = [512, 256, 256]
+
+    def run(refine):
+        case = dict(ng=n, l=[6.0, 3.0, 1.0], gtype=1, gr=1.4, cfl=0.95, dtmax=1e5, dt_f=-1., visci=5600.,
+                    icheck=10, cbcvel="PPPPDD" * 3, cbcpre="PPPPNN", bcvel=[0.] * 18, bcpre=[0.] * 6,
+                    is_forced=[1, 0, 0], velf=[1., 0., 0.])
+        if refine:
+            case["pressure_refine"] = {"rtol": 0.0, "max_iter": 2}
+        sim = Simulation(case, device=dev)
+        zc = torch.tensor(sim.zc[1:-1], device=dev, dtype=torch.float64)
+        g = torch.Generator(device=dev)
+        g.manual_seed(20260101)
+        noise = lambda: 0.2 * (torch.rand((n[2], n[1], n[0]), generator=g, device=dev, dtype=torch.float64) - 0.5)
+        sim.u[1:-1, 1:-1, 1:-1] = (6. * zc * (1. - zc))[:, None, None] + noise()
+        sim.v[1:-1, 1:-1, 1:-1] = noise()
+        sim.w[1:-1, 1:-1, 1:-1] = noise()
+        sim.start()
+        sim.step(3)
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sim.step(steps)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        ub = cans.bulk_mean(n, sim.gvr_f, sim.u)
+        divtot, divmax = cans.chkdiv(n, sim.l, sim.dli, sim.dzfi, sim.u, sim.v, sim.w)
+        out = {"ms_per_step": round(ms, 3), "Mcell_steps_per_s": round(n[0] * n[1] * n[2] / (ms * 1e-3) / 1e6, 2),
+               "bulk_velocity": ub, "divmax": divmax, "time": sim.time}
+        del sim
+        torch.cuda.empty_cache()
+        return out
+
+    return {"workload": "channel_512x256x256_Reb5600_rk3", "steps": steps, "warmup_steps": 3,
+            "fp64_pressure": run(False), "fp32_refined_pressure": run(True)}
 
 
 def bench_mx(args, dev, world):
@@ -629,6 +684,7 @@ def main():
     ap.add_argument("--size", type=int, default=N_DEFAULT)
     ap.add_argument("--skip-rk3", action="store_true")
     ap.add_argument("--skip-mx", action="store_true", help="skip the 1024x512x384 Poisson leg")
+    ap.add_argument("--skip-ch", action="store_true", help="skip the 512x256x256 channel run")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-refine", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
@@ -637,7 +693,7 @@ def main():
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=50)
     ap.add_argument("--adjoint-dirs", type=int, default=8)
-    ap.add_argument("--only", choices=["refined", "rk3", "adjoint", "boxes", "mx"], default=None,
+    ap.add_argument("--only", choices=["refined", "rk3", "adjoint", "boxes", "mx", "ch"], default=None,
                     help="profiling aid: run one secondary leg and print its JSON")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
