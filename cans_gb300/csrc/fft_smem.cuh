@@ -315,12 +315,15 @@ __device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict_
 // needs no pass of its own.  Requires blockDim.x == 64 * (sequences per CTA).
 template <int M> struct RegFFT { static constexpr bool on = false; };
 template <> struct RegFFT<512> { static constexpr bool on = true; };
-__host__ __device__ constexpr int regx(int x) { return x + 2 * (x >> 4); }
-// complex line stride of the compile-time path's buffers
-__host__ __device__ constexpr int spec_ld(int m) { return m == 512 ? 580 : m + m / 16 + 1; }
+template <> struct RegFFT<1024> { static constexpr bool on = true; };
+// output position of element x of a register-FFT line
+template <int M> __host__ __device__ constexpr int regx(int x) { return M == 1024 ? x + (x >> 4) : x + 2 * (x >> 4); }
+// complex line stride of the compile-time path's buffers (register FFTs: the largest
+// exchange array, = 4 (512) or 8 (1024) mod 16 so the CTA's sequences sit on different banks)
+__host__ __device__ constexpr int spec_ld(int m) { return m == 512 ? 580 : (m == 1024 ? 1672 : m + m / 16 + 1); }
 // position of element x of an FFT result line: layout of the register FFT (LAY 1) or of
 // the Stockham path (LAY 0)
-template <int M, int LAY> __device__ __forceinline__ int zpos(int x) { return LAY ? regx(x) : spad<M>(x); }
+template <int M, int LAY> __device__ __forceinline__ int zpos(int x) { return LAY ? regx<M>(x) : spad<M>(x); }
 template <int M> constexpr int kLay = RegFFT<M>::on ? 1 : 0;
 
 // tw: the plan's table exp(-2 pi i e/512), or (FP32, shared memory) the reordered copy of
@@ -365,9 +368,81 @@ __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const
   for (int dd = 0; dd < 8; dd++) v[dd] = Vq[k1 * 72 + e3 * 9 + dd];
   dft<8, SIGN>(v);
 #pragma unroll
-  for (int f = 0; f < 8; f++) Tq[regx(k1 + 8 * e3 + 64 * f)] = v[f];
+  for (int f = 0; f < 8; f++) Tq[regx<M>(k1 + 8 * e3 + 64 * f)] = v[f];
   __syncthreads();
   return A;
+}
+
+// For m = 1024 = 8*8*8*2: 128 threads per sequence, eight values each, four steps and three
+// exchanges (n = 128a + 16c + 2g + h, k = k1 + 8e + 64f + 512m):
+//   step 1 (thread b = 16c + 2g + h): DFT8 over a, times W1024^(b k1)  -> T1[k1][b]
+//   step 2 (thread (k1, d = 2g + h)):  DFT8 over c, times W128^(d e)    -> T2[k1][e][d]
+//   step 3 (thread (k1, e, h)):        DFT8 over g, times W16^(h f)     -> T3[k1][e][f][h]
+//   step 4 (thread (k1, r)):           DFT2 over h for (e, f) = (r%8, r/8 + 2t), t < 4
+// Strides: T1 row 128, T2 144*k1 + 18*e + d, T3 208*k1 + 26*e + 3*f + h, output x + x/16,
+// line 1672: every FP32 half-warp touches 16 distinct bank pairs.
+template <typename T, int M, int SIGN, int KIND = -1, bool SMEMTW = sizeof(T) == 4>
+__device__ __forceinline__ const cplx_t<T> *fft1024_reg(const DirParams &P, const T *__restrict__ stg,
+                                                        cplx_t<T> *__restrict__ A, cplx_t<T> *__restrict__ B,
+                                                        const cplx_t<T> *__restrict__ tab,
+                                                        const cplx_t<T> *__restrict__ pre,
+                                                        const cplx_t<T> *__restrict__ tw) {
+  using T2 = cplx_t<T>;
+  constexpr int LD = spec_ld(M);
+  const int q = threadIdx.x >> 7, p = threadIdx.x & 127;
+  T2 v[8];
+#pragma unroll
+  for (int a = 0; a < 8; a++) v[a] = pre_value<T, M, KIND>(P, stg, q, 128 * a + p, tab, pre);
+  dft<8, SIGN>(v);
+  T2 *T1 = A + q * LD;
+  T1[p] = v[0];
+#pragma unroll
+  for (int k1 = 1; k1 < 8; k1++) {
+    T2 w = SMEMTW ? tw[(k1 - 1) * 128 + p] : tw[(p * k1) & 1023];
+    if (SIGN > 0) w.y = -w.y;
+    T1[k1 * 128 + p] = cmul(v[k1], w);
+  }
+  __syncthreads();
+  const int k1 = p >> 4, d = p & 15;
+#pragma unroll
+  for (int c = 0; c < 8; c++) v[c] = T1[k1 * 128 + 16 * c + d];
+  dft<8, SIGN>(v);
+  T2 *T2b = B + q * LD;
+  T2b[k1 * 144 + d] = v[0];
+#pragma unroll
+  for (int e = 1; e < 8; e++) {
+    T2 w = SMEMTW ? tw[896 + (e - 1) * 16 + d] : tw[(8 * d * e) & 1023];
+    if (SIGN > 0) w.y = -w.y;
+    T2b[k1 * 144 + e * 18 + d] = cmul(v[e], w);
+  }
+  __syncthreads();
+  const int e3 = (p >> 1) & 7, h = p & 1;
+#pragma unroll
+  for (int g = 0; g < 8; g++) v[g] = T2b[k1 * 144 + e3 * 18 + 2 * g + h];
+  dft<8, SIGN>(v);
+  T2 *T3 = A + q * LD;  // T1 was consumed by step 2
+#pragma unroll
+  for (int f = 0; f < 8; f++) {
+    T2 x = v[f];
+    if (h && f) {
+      T2 w = SMEMTW ? tw[1008 + f - 1] : tw[(64 * f) & 1023];
+      if (SIGN > 0) w.y = -w.y;
+      x = cmul(x, w);
+    }
+    T3[k1 * 208 + e3 * 26 + f * 3 + h] = x;
+  }
+  __syncthreads();
+  const int r = p & 15, e4 = r & 7;
+  T2 *X = B + q * LD;  // T2 was consumed by step 3
+#pragma unroll
+  for (int t = 0; t < 4; t++) {
+    const int f = (r >> 3) + 2 * t, base = k1 * 208 + e4 * 26 + f * 3;
+    const T2 a0 = T3[base], a1 = T3[base + 1];
+    X[regx<M>(k1 + 8 * e4 + 64 * f)] = cadd(a0, a1);
+    X[regx<M>(k1 + 8 * e4 + 64 * f + 512)] = csub(a0, a1);
+  }
+  __syncthreads();
+  return B;
 }
 
 // pre-processing + complex FFT of the CTA's sequences (staging rows in B on entry);
@@ -376,7 +451,12 @@ template <typename T, int M, int KIND = -1>
 __device__ __forceinline__ const cplx_t<T> *fft_in(const DirParams &P, const T *stg, cplx_t<T> *A, cplx_t<T> *B,
                                                    const cplx_t<T> *tab, const cplx_t<T> *pre,
                                                    const cplx_t<T> *tw) {
-  if constexpr (RegFFT<M>::on && KIND >= 0) {
+  if constexpr (M == 1024 && KIND >= 0) {
+    return fft1024_reg<T, M, kind_sign(KIND), KIND>(P, stg, A, B, tab, pre, tw);
+  } else if constexpr (M == 1024) {
+    return kind_sign(P.kind) > 0 ? fft1024_reg<T, M, +1>(P, stg, A, B, tab, pre, tw)
+                                 : fft1024_reg<T, M, -1>(P, stg, A, B, tab, pre, tw);
+  } else if constexpr (RegFFT<M>::on && KIND >= 0) {
     return fft512_reg<T, M, kind_sign(KIND), KIND>(P, stg, A, B, tab, pre, tw);
   } else if constexpr (RegFFT<M>::on) {
     return kind_sign(P.kind) > 0 ? fft512_reg<T, M, +1>(P, stg, A, B, tab, pre, tw)

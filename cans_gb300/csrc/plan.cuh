@@ -153,7 +153,15 @@ __device__ __forceinline__ void copy_tables(const DirParams &P, int m, int nt, c
                                             cplx_t<T> *pre) {
   using T2 = cplx_t<T>;
   const T2 *gtw = reinterpret_cast<const T2 *>(P.tw);
-  if constexpr (RegFFT<M>::on) {
+  if constexpr (M == 1024) {
+    // fft1024_reg: W1024^(p k1) at [(k1-1)*128 + p], W128^(d e) at [896 + (e-1)*16 + d],
+    // W16^f at [1008 + f - 1]
+    for (int e = threadIdx.x; e < 7 * 128 + 7 * 16 + 7; e += blockDim.x) {
+      if (e < 896) tw[e] = gtw[((e & 127) * ((e >> 7) + 1)) & 1023];
+      else if (e < 1008) tw[e] = gtw[(8 * ((e - 896) & 15) * (((e - 896) >> 4) + 1)) & 1023];
+      else tw[e] = gtw[(64 * (e - 1007)) & 1023];
+    }
+  } else if constexpr (RegFFT<M>::on) {
     for (int e = threadIdx.x; e < 7 * 64 + 7 * 8; e += blockDim.x) {
       if (e < 7 * 64) tw[e] = gtw[((e & 63) * ((e >> 6) + 1)) & 511];
       else tw[e] = gtw[(8 * ((e - 448) & 7) * (((e - 448) >> 3) + 1)) & 511];
@@ -199,8 +207,8 @@ template <typename T, int M> struct PassGeo {
   static constexpr int LPB = 2 * NCX;
   static constexpr int LD = M ? spec_ld(M) : 0;  // complex line stride (padded)
   static constexpr int SLD = sstage<M>(M);          // real staging line stride (16-byte rows)
-  // the register FFT runs 64 threads per complex sequence on the 256-thread pass CTAs
-  static_assert(!RegFFT<M>::on || NCX * 64 == 256, "register FFT geometry");
+  // the register FFTs run M/8 threads per complex sequence on the 256-thread pass CTAs
+  static_assert(!RegFFT<M>::on || NCX * (M / 8) == 256, "register FFT geometry");
 };
 
 // ---- FP64 <-> FP32 conversions without the FP64 pipe.  GB300 issues double<->float
@@ -349,7 +357,7 @@ __device__ __forceinline__ void ylines_fft_store(T *__restrict__ S, long nlines,
       S[(size_t)l * M + j] = v0;
       if (l + 1 < nlines) S[(size_t)(l + 1) * M + j] = v1;
     }
-  } else if (M > 0) {
+  } else if constexpr (M > 0) {
     // two neighbouring outputs of both lines per thread: 2-element vector stores
     for (int e = threadIdx.x; e < G::NCX * (M / 2); e += blockDim.x) {
       const int q = e / (M / 2), j = 2 * (e - q * (M / 2));
