@@ -56,6 +56,28 @@ def traffic_for(kernel, workload):
         return None
 
 
+def rank_barrier(world):
+    """Barrier of the replica ranks around a timed region (no-op on one rank)."""
+    if world > 1:
+        import torch
+        torch.distributed.barrier()
+
+
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time: whole-job throughput is units of all ranks / this time."""
+    if world == 1:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(ms, world):
+    """Solves per second of the whole job: world replicas, each one solve per ms."""
+    return world / (ms * 1e-3)
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -126,8 +148,7 @@ def bench_fp64(args, n, dli, dzc, dzf, dev, world):
     for _ in range(args.warmup):
         plan.solve(p)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    rank_barrier(world)
     plan.set_timing(True)
     st = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -140,10 +161,7 @@ def bench_fp64(args, n, dli, dzc, dzf, dev, world):
     ms = e0.elapsed_time(e1) / args.steps
     pass_ms, nrec = plan.get_timing()
     plan.set_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     names = ["solve_xfwd", "solve_yfwd", "solve_zthomas", "solve_ybwd", "solve_xbwd"]
     top = int(np.argmax(pass_ms))
     hbm, kind = peaks()
@@ -153,7 +171,7 @@ def bench_fp64(args, n, dli, dzc, dzf, dev, world):
             "frac": round(achieved / hbm, 4), "peak_source": kind, "traffic": traffic_for(names[top], workload),
             "algorithmic_bytes_per_launch": BYTES_PER_CELL_PASS * ncell,
             "note": "FP64-pipe bound on GB300 (1.2 TFLOP/s FP64): 72% FP64 pipe busy in the transform passes"}
-    return plan, p, {"value": round(world / (ms * 1e-3), 4), "unit": "solves/s", "ms_per_step": round(ms, 4),
+    return plan, p, {"value": round(job_throughput(ms, world), 4), "unit": "solves/s", "ms_per_step": round(ms, 4),
                      "pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)}, "roofline": roof}
 
 
@@ -373,6 +391,7 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
         p.copy_(src)
         plan.solve_refined(p, dli, dzci, dzfi, rtol=0.0, max_iter=k_cal)
     torch.cuda.synchronize()
+    rank_barrier(world)
     st = torch.cuda.current_stream()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     l0 = cans.launch_count()
@@ -389,10 +408,8 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
     pass_ms, nrec = plan.get_timing()
     res_ms, nres = plan.get_residual_timing()
     plan.set_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    rank_barrier(world)
+    ms = max_over_ranks(ms, world, dev)
     e2e_out = None
     if e2e:
         # end to end through the C ABI with host buffers: every step copies its RHS from
@@ -413,6 +430,7 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
         ev_solved = [torch.cuda.Event() for _ in range(nbuf)]
         ev_out = [torch.cuda.Event() for _ in range(nbuf)]
         torch.cuda.synchronize()
+        rank_barrier(world)
         t0 = time.perf_counter()
         with torch.cuda.stream(s_in):
             bufs[0].copy_(host_in[0], non_blocking=True)
@@ -434,16 +452,16 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
                 host_out[b].copy_(bufs[b], non_blocking=True)
                 ev_out[b].record(s_out)
         torch.cuda.synchronize()
-        ms_e2e = (time.perf_counter() - t0) * 1e3 / k2
+        ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3 / k2, world, dev)
         nbytes = p.numel() * 8
-        e2e_out = {"value": round(world / (ms_e2e * 1e-3), 3), "unit": "solves/s", "h2d_bytes_per_step": nbytes,
+        e2e_out = {"value": round(job_throughput(ms_e2e, world), 3), "unit": "solves/s", "h2d_bytes_per_step": nbytes,
                    "d2h_bytes_per_step": nbytes, "steps": k2,
                    "note": "pipelined: H2D(k+1) and D2H(k-1) overlap solve k (four buffers, two copy streams)"}
         del host_in, host_out, bufs
     names = ["solve_xfwd", "solve_yfwd", "solve_zthomas", "solve_ybwd", "solve_xbwd"]
     del p, plan
     torch.cuda.empty_cache()
-    return {"value": round(world / (ms * 1e-3), 3), "unit": "solves/s", "ms_per_step": round(ms, 4),
+    return {"value": round(job_throughput(ms, world), 3), "unit": "solves/s", "ms_per_step": round(ms, 4),
             "rtol": rtol, "corrections_per_solve": k_cal, "fp32_solves_per_solve": k_cal + 1,
             "residual_passes_per_solve": k_cal, "accuracy": acc, "gpu_launches": launches,
             "fp32_pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)}, "residual_ms": round(res_ms, 4),
