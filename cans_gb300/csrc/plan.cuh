@@ -584,10 +584,12 @@ __device__ __forceinline__ void xfwd_persist(const TF *__restrict__ p, T *__rest
   TF nxt[PER];
   auto load = [&](long t) {
     const int k = (int)(t / ntj), j0 = (int)(t - (long)k * ntj) * G::LPB;
+    const TF *row0 = p + hidx(1, j0 + 1, k + 1, n1, n2);  // (i = 1, j = j0 + 1, k + 1)
+    const int nrows = n2 - j0;
 #pragma unroll
     for (int u = 0; u < PER; u++) {
-      const int e = threadIdx.x + 256 * u, r = e / M, i = e % M, j = j0 + r;
-      nxt[u] = (j < n2) ? p[hidx(i + 1, j + 1, k + 1, n1, n2)] : TF(0);
+      const int e = threadIdx.x + 256 * u, r = e / M, i = e % M;
+      nxt[u] = r < nrows ? row0[(size_t)r * (n1 + 2) + i] : TF(0);
     }
   };
   long tile = blockIdx.x;
@@ -669,13 +671,14 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
       // and stay in flight through the FFT
       constexpr int U = G::NCX * n1 / 256;
       TF old0[U], old1[U];
+      TF *row0 = p + hidx(1, j0 + 1, k + 1, n1, n2);  // (i = 1, j = j0 + 1, k + 1)
       if (acc == 1) {
 #pragma unroll
         for (int u = 0; u < U; u++) {
           const int e = (int)threadIdx.x + 256 * u, q = e / M, i = e % M, j = j0 + 2 * q;
-          const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
-          old0[u] = j < n2 ? p[idx] : TF(0);
-          old1[u] = j + 1 < n2 ? p[idx + (size_t)(n1 + 2)] : TF(0);
+          const size_t idx = (size_t)(2 * q) * (n1 + 2) + i;
+          old0[u] = j < n2 ? row0[idx] : TF(0);
+          old1[u] = j + 1 < n2 ? row0[idx + (size_t)(n1 + 2)] : TF(0);
         }
       }
       const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
@@ -685,7 +688,7 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
         if (j >= n2) continue;
         T v0, v1;
         r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
-        const size_t idx = hidx(i + 1, j + 1, k + 1, n1, n2);
+        const size_t idx = (size_t)(row0 - p) + (size_t)(2 * q) * (n1 + 2) + i;
         p[idx] = acc == 1 ? (TF)(old0[u] + cvt_to<TF, T>(v0)) : xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
         if (j + 1 < n2) {
           const size_t idx1 = idx + (size_t)(n1 + 2);
