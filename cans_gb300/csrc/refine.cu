@@ -48,40 +48,13 @@ constexpr int kTB = 256;
 struct df {
   float h, l;
 };
-// error-free transformations (Knuth two-sum, Dekker fast-two-sum, FMA two-product)
+// error-free transformation of a sum (Knuth two-sum); products use the FMA two-product inline
 __device__ __forceinline__ df two_sum(float a, float b) {
   const float s = __fadd_rn(a, b);
   const float bb = __fsub_rn(s, a);
   const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
   return {s, e};
 }
-__device__ __forceinline__ df fast_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ df df_add(df x, df y) {
-  df s = two_sum(x.h, y.h);
-  const df t = two_sum(x.l, y.l);
-  s.l = __fadd_rn(s.l, t.h);
-  s = fast_two_sum(s.h, s.l);
-  s.l = __fadd_rn(s.l, t.l);
-  return fast_two_sum(s.h, s.l);
-}
-__device__ __forceinline__ df df_neg(df x) { return {-x.h, -x.l}; }
-__device__ __forceinline__ df df_mul(df x, df y) {
-  const float p = __fmul_rn(x.h, y.h);
-  float e = __fmaf_rn(x.h, y.h, -p);
-  e = __fmaf_rn(x.h, y.l, e);
-  e = __fmaf_rn(x.l, y.h, e);
-  return fast_two_sum(p, e);
-}
-__device__ __forceinline__ df df_mul_f(df x, float y) {
-  const float p = __fmul_rn(x.h, y);
-  float e = __fmaf_rn(x.h, y, -p);
-  e = __fmaf_rn(x.l, y, e);
-  return fast_two_sum(p, e);
-}
-__device__ __forceinline__ df dfv(float2 v) { return {v.x, v.y}; }
 
 struct OpParams {
   int n1, n2, n3;

@@ -90,9 +90,8 @@ __device__ __forceinline__ void mom_rk_cell(const Dims &d, double dxi, double dy
   const double dzci_k = dzci[k], dzci_km = dzci[k - 1], dzfi_k = dzfi[k], dzfi_kp = dzfi[k + 1];
   const double rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
   const double u_ccm = u[c - sz], u_cmc = u[c - sy], u_mcc = u[c - sx], u_ccc = u[c], u_pcc = u[c + sx],
-               u_mpc = u[c - sx + sy], u_cpc = u[c + sy], u_cmp = u[c - sy + sz], u_mcp = u[c - sx + sz],
-               u_ccp = u[c + sz];
-  const double v_ccm = v[c - sz], v_pcm = v[c + sx - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx],
+               u_mpc = u[c - sx + sy], u_cpc = u[c + sy], u_mcp = u[c - sx + sz], u_ccp = u[c + sz];
+  const double v_ccm = v[c - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx],
                v_ccc = v[c], v_pcc = v[c + sx], v_cpc = v[c + sy], v_ccp = v[c + sz], v_cmp = v[c - sy + sz];
   const double w_ccm = w[c - sz], w_pcm = w[c + sx - sz], w_cpm = w[c + sy - sz], w_cmc = w[c - sy], w_mcc = w[c - sx],
                w_ccc = w[c], w_pcc = w[c + sx], w_cpc = w[c + sy], w_ccp = w[c + sz];
