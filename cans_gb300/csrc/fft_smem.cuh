@@ -229,16 +229,29 @@ __device__ __forceinline__ T2 *fft_any(T2 *A, T2 *B, const DirParams &P, const T
 // ------------------------------------------------------------------------ r2r pre-processing
 // staging: real line r at stg[r*sld + i], i < nt.  Element k (< m) of complex sequence q.
 // tab, pre: the CTA's copies of the plan's post and pre tables
-// KIND >= 0: the kind as a compile-time constant (the switch folds away); -1: P.kind
-template <typename T, int M = 0, int KIND = -1>
-__device__ __forceinline__ cplx_t<T> pre_value(const DirParams &P, const T *__restrict__ stg, int q, int k,
-                                               const cplx_t<T> *__restrict__ tab,
-                                               const cplx_t<T> *__restrict__ pre) {
+// Pair-interleaved staging (the x-backward pass of the register FFTs): complex sequence q
+// keeps its two real lines as (x0[i], x1[i]) pairs at stg_pair[q * pair_sld + i], so a
+// transposed 16-byte row load is stored with 8- or 16-byte stores and the first FFT step
+// reads both lines with one load.  Row stride = 4 (FP32) or 2 (FP64) mod 8 pairs: the
+// stores of a half-warp (FP32) / quarter-warp (FP64) fall on distinct bank groups.
+template <typename T, int M> __host__ __device__ constexpr int pair_sld() { return sizeof(T) == 4 ? M + 4 : M + 2; }
+template <typename T, int C> struct PairLine {
+  const cplx_t<T> *p;
+  __device__ __forceinline__ T operator[](int i) const {
+    if constexpr (C == 0) return p[i].x;
+    else return p[i].y;
+  }
+};
+
+// element k of complex sequence q from its two real lines x0, x1 (any indexable type)
+template <typename T, int M, int KIND, typename X0, typename X1>
+__device__ __forceinline__ cplx_t<T> pre_body(const DirParams &P, const X0 &x0, const X1 &x1, const T *__restrict__ stg,
+                                              int q, int k, const cplx_t<T> *__restrict__ tab,
+                                              const cplx_t<T> *__restrict__ pre) {
   using T2 = cplx_t<T>;
   // with a compile-time M the kinds handled have nt == n == m (no extension)
   const int m = M ? M : P.m, nt = M ? M : P.nt, n = nt, sld = M ? sstage<M>(M) : P.sld;
   const int kind = KIND >= 0 ? KIND : P.kind;
-  const T *x0 = stg + (2 * q) * sld, *x1 = x0 + sld;
   T2 z;
   switch (kind) {
     case K_R2HC: z = cmk<T2>(x0[k], x1[k]); break;
@@ -287,6 +300,23 @@ __device__ __forceinline__ cplx_t<T> pre_value(const DirParams &P, const T *__re
   return z;
 }
 
+// KIND >= 0: the kind as a compile-time constant (the switch folds away); -1: P.kind.
+// PSTG: pair-interleaved staging (compile-time lengths only)
+template <typename T, int M = 0, int KIND = -1, bool PSTG = false>
+__device__ __forceinline__ cplx_t<T> pre_value(const DirParams &P, const T *__restrict__ stg, int q, int k,
+                                               const cplx_t<T> *__restrict__ tab,
+                                               const cplx_t<T> *__restrict__ pre) {
+  if constexpr (PSTG) {
+    static_assert(M > 0, "pair staging needs a compile-time length");
+    const cplx_t<T> *xp = reinterpret_cast<const cplx_t<T> *>(stg) + q * pair_sld<T, M>();
+    return pre_body<T, M, KIND>(P, PairLine<T, 0>{xp}, PairLine<T, 1>{xp}, stg, q, k, tab, pre);
+  } else {
+    const int sld = M ? sstage<M>(M) : P.sld;
+    const T *x0 = stg + (2 * q) * sld, *x1 = x0 + sld;
+    return pre_body<T, M, KIND>(P, x0, x1, stg, q, k, tab, pre);
+  }
+}
+
 // Fills the complex sequences A[q*ld + k], k < m, of the Stockham path.
 template <typename T, int M = 0>
 __device__ __forceinline__ void r2r_pre(const DirParams &P, const T *__restrict__ stg, cplx_t<T> *__restrict__ A,
@@ -328,7 +358,7 @@ template <int M> constexpr int kLay = RegFFT<M>::on ? 1 : 0;
 
 // tw: the plan's table exp(-2 pi i e/512), or (FP32, shared memory) the reordered copy of
 // copy_tables (SMEMTW)
-template <typename T, int M, int SIGN, int KIND = -1, bool SMEMTW = sizeof(T) == 4>
+template <typename T, int M, int SIGN, int KIND = -1, bool PSTG = false, bool SMEMTW = sizeof(T) == 4>
 __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const T *__restrict__ stg,
                                                        cplx_t<T> *__restrict__ A, cplx_t<T> *__restrict__ B,
                                                        const cplx_t<T> *__restrict__ tab,
@@ -339,7 +369,7 @@ __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const
   const int q = threadIdx.x >> 6, p = threadIdx.x & 63;
   T2 v[8];
 #pragma unroll
-  for (int a = 0; a < 8; a++) v[a] = pre_value<T, M, KIND>(P, stg, q, 64 * a + p, tab, pre);
+  for (int a = 0; a < 8; a++) v[a] = pre_value<T, M, KIND, PSTG>(P, stg, q, 64 * a + p, tab, pre);
   dft<8, SIGN>(v);
   T2 *Tq = A + q * LD;
   Tq[p] = v[0];
@@ -381,7 +411,7 @@ __device__ __forceinline__ const cplx_t<T> *fft512_reg(const DirParams &P, const
 //   step 4 (thread (k1, r)):           DFT2 over h for (e, f) = (r%8, r/8 + 2t), t < 4
 // Strides: T1 row 128, T2 144*k1 + 18*e + d, T3 208*k1 + 26*e + 3*f + h, output x + x/16,
 // line 1672: every FP32 half-warp touches 16 distinct bank pairs.
-template <typename T, int M, int SIGN, int KIND = -1, bool SMEMTW = sizeof(T) == 4>
+template <typename T, int M, int SIGN, int KIND = -1, bool PSTG = false, bool SMEMTW = sizeof(T) == 4>
 __device__ __forceinline__ const cplx_t<T> *fft1024_reg(const DirParams &P, const T *__restrict__ stg,
                                                         cplx_t<T> *__restrict__ A, cplx_t<T> *__restrict__ B,
                                                         const cplx_t<T> *__restrict__ tab,
@@ -392,7 +422,7 @@ __device__ __forceinline__ const cplx_t<T> *fft1024_reg(const DirParams &P, cons
   const int q = threadIdx.x >> 7, p = threadIdx.x & 127;
   T2 v[8];
 #pragma unroll
-  for (int a = 0; a < 8; a++) v[a] = pre_value<T, M, KIND>(P, stg, q, 128 * a + p, tab, pre);
+  for (int a = 0; a < 8; a++) v[a] = pre_value<T, M, KIND, PSTG>(P, stg, q, 128 * a + p, tab, pre);
   dft<8, SIGN>(v);
   T2 *T1 = A + q * LD;
   T1[p] = v[0];
@@ -447,20 +477,21 @@ __device__ __forceinline__ const cplx_t<T> *fft1024_reg(const DirParams &P, cons
 
 // pre-processing + complex FFT of the CTA's sequences (staging rows in B on entry);
 // returns the buffer holding the result, laid out as zpos<M, kLay<M>>
-template <typename T, int M, int KIND = -1>
+template <typename T, int M, int KIND = -1, bool PSTG = false>
 __device__ __forceinline__ const cplx_t<T> *fft_in(const DirParams &P, const T *stg, cplx_t<T> *A, cplx_t<T> *B,
                                                    const cplx_t<T> *tab, const cplx_t<T> *pre,
                                                    const cplx_t<T> *tw) {
+  static_assert(!PSTG || RegFFT<M>::on, "pair staging feeds the register FFTs only");
   if constexpr (M == 1024 && KIND >= 0) {
-    return fft1024_reg<T, M, kind_sign(KIND), KIND>(P, stg, A, B, tab, pre, tw);
+    return fft1024_reg<T, M, kind_sign(KIND), KIND, PSTG>(P, stg, A, B, tab, pre, tw);
   } else if constexpr (M == 1024) {
-    return kind_sign(P.kind) > 0 ? fft1024_reg<T, M, +1>(P, stg, A, B, tab, pre, tw)
-                                 : fft1024_reg<T, M, -1>(P, stg, A, B, tab, pre, tw);
+    return kind_sign(P.kind) > 0 ? fft1024_reg<T, M, +1, -1, PSTG>(P, stg, A, B, tab, pre, tw)
+                                 : fft1024_reg<T, M, -1, -1, PSTG>(P, stg, A, B, tab, pre, tw);
   } else if constexpr (RegFFT<M>::on && KIND >= 0) {
-    return fft512_reg<T, M, kind_sign(KIND), KIND>(P, stg, A, B, tab, pre, tw);
+    return fft512_reg<T, M, kind_sign(KIND), KIND, PSTG>(P, stg, A, B, tab, pre, tw);
   } else if constexpr (RegFFT<M>::on) {
-    return kind_sign(P.kind) > 0 ? fft512_reg<T, M, +1>(P, stg, A, B, tab, pre, tw)
-                                 : fft512_reg<T, M, -1>(P, stg, A, B, tab, pre, tw);
+    return kind_sign(P.kind) > 0 ? fft512_reg<T, M, +1, -1, PSTG>(P, stg, A, B, tab, pre, tw)
+                                 : fft512_reg<T, M, -1, -1, PSTG>(P, stg, A, B, tab, pre, tw);
   } else {
     r2r_pre<T, M>(P, stg, A, tab, pre);
     __syncthreads();

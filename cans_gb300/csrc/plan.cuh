@@ -209,6 +209,8 @@ template <typename T, int M> struct PassGeo {
   static constexpr int SLD = sstage<M>(M);          // real staging line stride (16-byte rows)
   // the register FFTs run M/8 threads per complex sequence on the 256-thread pass CTAs
   static_assert(!RegFFT<M>::on || NCX * (M / 8) == 256, "register FFT geometry");
+  // the pair-interleaved staging of the x-backward pass fits in the second FFT buffer
+  static_assert(!RegFFT<M>::on || pair_sld<T, M>() <= LD, "pair staging size");
 };
 
 // ---- FP64 <-> FP32 conversions without the FP64 pipe.  GB300 issues double<->float
@@ -662,8 +664,16 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
       for (int u = 0; u < PER; u++) {
         const int e = threadIdx.x + 256 * u, i = e / VPR, c = e - i * VPR;
         const T *w = reinterpret_cast<const T *>(&nxt[u]);
+        if constexpr (RegFFT<M>::on) {
+          // pair-interleaved staging: lines (2s, 2s+1) at column i as one pair
+          T2 *sp = reinterpret_cast<T2 *>(stg);
 #pragma unroll
-        for (int q = 0; q < VW; q++) stg[(c * VW + q) * G::SLD + i] = w[q];
+          for (int s2 = 0; s2 < VW / 2; s2++)
+            sp[(c * VW / 2 + s2) * pair_sld<T, M>() + i] = cmk<T2>(w[2 * s2], w[2 * s2 + 1]);
+        } else {
+#pragma unroll
+          for (int q = 0; q < VW; q++) stg[(c * VW + q) * G::SLD + i] = w[q];
+        }
       }
       __syncthreads();
       if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
@@ -681,7 +691,7 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
           old1[u] = j + 1 < n2 ? row0[idx + (size_t)(n1 + 2)] : TF(0);
         }
       }
-      const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
+      const T2 *Z = fft_in<T, M, KD, RegFFT<M>::on>(P, stg, A, B, post, pre, tw);
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const int e = (int)threadIdx.x + 256 * u, q = e / M, i = e % M, j = j0 + 2 * q;
