@@ -583,6 +583,9 @@ __device__ __forceinline__ void xfwd_persist(const TF *__restrict__ p, T *__rest
   const T2 *tw = kTablesInSmem<T> ? stw : reinterpret_cast<const T2 *>(P.tw);
   const T2 *post = kTablesInSmem<T> ? stw + M : reinterpret_cast<const T2 *>(P.post);
   const T2 *pre = kTablesInSmem<T> ? stw + 2 * M : reinterpret_cast<const T2 *>(P.pre);
+  // register FFTs: pair-interleaved staging, each thread loads the two rows (2s, 2s+1) of a
+  // complex sequence at the same i; otherwise rows in order
+  constexpr bool PSTG = RegFFT<M>::on;
   TF nxt[PER];
   auto load = [&](long t) {
     const int k = (int)(t / ntj), j0 = (int)(t - (long)k * ntj) * G::LPB;
@@ -590,7 +593,8 @@ __device__ __forceinline__ void xfwd_persist(const TF *__restrict__ p, T *__rest
     const int nrows = n2 - j0;
 #pragma unroll
     for (int u = 0; u < PER; u++) {
-      const int e = threadIdx.x + 256 * u, r = e / M, i = e % M;
+      const int e = threadIdx.x + 256 * (PSTG ? (u >> 1) : u);
+      const int r = PSTG ? 2 * (e / M) + (u & 1) : e / M, i = e % M;
       nxt[u] = r < nrows ? row0[(size_t)r * (n1 + 2) + i] : TF(0);
     }
   };
@@ -601,14 +605,23 @@ __device__ __forceinline__ void xfwd_persist(const TF *__restrict__ p, T *__rest
     constexpr int KD = decltype(K)::value;
     for (; tile < ntiles; tile += gridDim.x) {
       const int k = (int)(tile / ntj), j0 = (int)(tile - (long)k * ntj) * G::LPB;
+      if constexpr (PSTG) {
+        T2 *sp = reinterpret_cast<T2 *>(stg);
 #pragma unroll
-      for (int u = 0; u < PER; u++) {
-        const int e = threadIdx.x + 256 * u, r = e / M, i = e % M;
-        stg[r * G::SLD + i] = cvt_to<T, TF>(nxt[u]);
+        for (int u = 0; u < PER; u += 2) {
+          const int e = threadIdx.x + 256 * (u >> 1), s2 = e / M, i = e % M;
+          sp[s2 * pair_sld<T, M>() + i] = cmk<T2>(cvt_to<T, TF>(nxt[u]), cvt_to<T, TF>(nxt[u + 1]));
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < PER; u++) {
+          const int e = threadIdx.x + 256 * u, r = e / M, i = e % M;
+          stg[r * G::SLD + i] = cvt_to<T, TF>(nxt[u]);
+        }
       }
       __syncthreads();
       if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
-      const T2 *Z = fft_in<T, M, KD>(P, stg, A, B, post, pre, tw);
+      const T2 *Z = fft_in<T, M, KD, PSTG>(P, stg, A, B, post, pre, tw);
       T *Sk = S + (size_t)k * n1 * n2;
 #pragma unroll
       for (int u = 0; u < n1 * G::NCX / 256; u++) {
