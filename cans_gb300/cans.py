@@ -354,10 +354,14 @@ def updt_rhs_b(c_or_f, cbc, n, is_bound, rhsb, p, alpha=None, stream=None):
            "cans_updt_rhs_b")
 
 
-def chkdiv(n, l, dli, dzfi, u, v, w, stream=None):
+def chkdiv(n, l, dli, dzfi, u, v, w, stream=None, allow_nonfinite=False):
+    """chkdiv (src/chkdiv.f90:15): (divtot, divmax).  A non-finite result raises CansError
+    (CANS_ENONFINITE) unless allow_nonfinite, which returns the values as they are."""
     a, b = C.c_double(), C.c_double()
-    _check(lib().cans_chkdiv(_ints(n), _dbls(l), _dbls(dli), _ptr(dzfi), _ptr(u), _ptr(v), _ptr(w), C.byref(a),
-                             C.byref(b), _stream(stream)), "cans_chkdiv")
+    rc = lib().cans_chkdiv(_ints(n), _dbls(l), _dbls(dli), _ptr(dzfi), _ptr(u), _ptr(v), _ptr(w), C.byref(a),
+                           C.byref(b), _stream(stream))
+    if not (allow_nonfinite and rc == ENONFINITE):
+        _check(rc, "cans_chkdiv")
     return a.value, b.value
 
 

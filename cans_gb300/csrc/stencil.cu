@@ -190,25 +190,37 @@ __global__ void __launch_bounds__(kTB) k_rk_forcing(Dims d, const double *__rest
 }
 
 namespace {
-struct RkScratch {
+// Library-owned scratch, one buffer per device.  The mutex guards the lookup and the
+// growth; a grown buffer replaces the old one with cudaFree, which waits for the device's
+// outstanding work, so kernels of earlier calls never see their buffer freed under them.
+constexpr int kMaxDevices = 64;
+struct DevScratch {
   double *buf = nullptr;
   size_t bytes = 0;
-  int dev = -1;
-} g_rk;
+};
+
+int dev_scratch(DevScratch *tab, size_t bytes, double **out) {
+  int dev = 0;
+  CANS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return CANS_EINVAL;
+  DevScratch &b = tab[dev];
+  if (b.bytes < bytes) {
+    if (b.buf) CANS_CUDA_TRY(cudaFree(b.buf));
+    b.buf = nullptr;
+    b.bytes = 0;
+    CANS_CUDA_TRY(cudaMalloc(&b.buf, bytes));
+    b.bytes = bytes;
+  }
+  *out = b.buf;
+  return CANS_OK;
+}
+
+std::mutex g_rk_mu;
+DevScratch g_rk[kMaxDevices];
 
 int rk_scratch(size_t bytes, double **out) {
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (g_rk.bytes < bytes || g_rk.dev != dev) {
-    if (g_rk.buf) cudaFree(g_rk.buf);
-    g_rk.buf = nullptr;
-    g_rk.bytes = 0;
-    CANS_CUDA_TRY(cudaMalloc(&g_rk.buf, bytes));
-    g_rk.bytes = bytes;
-    g_rk.dev = dev;
-  }
-  *out = g_rk.buf;
-  return CANS_OK;
+  std::lock_guard<std::mutex> lk(g_rk_mu);
+  return dev_scratch(g_rk, bytes, out);
 }
 }  // namespace
 
@@ -481,25 +493,13 @@ __global__ void __launch_bounds__(kTB) k_chkdiv(Dims d, double dxi, double dyi, 
 }
 
 namespace {
-struct RedScratch {
-  double *buf = nullptr;
-  size_t n = 0;
-  int dev = -1;
-} g_red;
-int red_scratch(size_t count, double **out) {
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (g_red.n < count || g_red.dev != dev) {
-    if (g_red.buf) cudaFree(g_red.buf);
-    g_red.buf = nullptr;
-    g_red.n = 0;
-    CANS_CUDA_TRY(cudaMalloc(&g_red.buf, count * sizeof(double)));
-    g_red.n = count;
-    g_red.dev = dev;
-  }
-  *out = g_red.buf;
-  return CANS_OK;
-}
+// Scratch of the synchronising reductions (chkdiv, chkdt, bulk_mean): one buffer per device.
+// A reduction holds g_red_mu from the lookup until its result is on the host (the calls
+// synchronise their stream), so calls from several host threads or devices serialise
+// instead of sharing or freeing a buffer in use.
+std::mutex g_red_mu;
+DevScratch g_red[kMaxDevices];
+int red_scratch(size_t count, double **out) { return dev_scratch(g_red, count * sizeof(double), out); }
 }  // namespace
 
 extern "C" int cans_chkdiv(const int n[3], const double l[3], const double dli[3], const double *dzfi, const double *u,
@@ -510,6 +510,7 @@ extern "C" int cans_chkdiv(const int n[3], const double l[3], const double dli[3
   const long np = (long)n[0] * n[1] * n[2];
   const unsigned nblk = blocks_for(np);
   double *s;
+  std::lock_guard<std::mutex> lk(g_red_mu);
   int rc = red_scratch(2 * (size_t)nblk + 4, &s);
   if (rc) return rc;
   k_chkdiv<<<nblk, kTB, 0, st>>>(d, dli[0], dli[1], dzfi, u, v, w, s, s + nblk);
@@ -523,7 +524,7 @@ extern "C" int cans_chkdiv(const int n[3], const double l[3], const double dli[3
   CANS_CUDA_TRY(cudaStreamSynchronize(st));
   *divtot = h[0] / (l[0] * l[1] * l[2]);
   *divmax = h[1];
-  return CANS_OK;
+  return (isfinite(*divtot) && isfinite(*divmax)) ? CANS_OK : CANS_ENONFINITE;
 }
 
 // ------------------------------------------------------------------------------ chkdiv, no allocation
@@ -545,6 +546,10 @@ extern "C" int cans_chkdiv_noalloc(const int n[3], const double l[3], const doub
                                    double *divmax, void *stream) {
   if (!n || !l || !dli || !dzfi || !u || !v || !w || !divtot || !divmax) return CANS_EINVAL;
   if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  // each extent alone must fit before the product is formed (no overflow on absurd sizes)
+  constexpr long kMaxCells = kNoAllocMaxBlocks * kTB;
+  if (n[0] > kMaxCells || n[1] > kMaxCells || n[2] > kMaxCells) return CANS_EINVAL;
+  if ((long)n[0] * n[1] > kMaxCells) return CANS_EINVAL;
   const long np = (long)n[0] * n[1] * n[2];
   const long nblk = (np + kTB - 1) / kTB;
   if (nblk > kNoAllocMaxBlocks) return CANS_EINVAL;  // beyond the fixed scratch: rejected, nothing launched
@@ -575,7 +580,7 @@ extern "C" int cans_chkdiv_noalloc(const int n[3], const double l[3], const doub
   CANS_CUDA_TRY(cudaStreamSynchronize(st));
   *divtot = h[0] / (l[0] * l[1] * l[2]);
   *divmax = h[1];
-  return CANS_OK;
+  return (isfinite(*divtot) && isfinite(*divmax)) ? CANS_OK : CANS_ENONFINITE;
 }
 
 __global__ void __launch_bounds__(kTB) k_chkdt(Dims d, double dxi, double dyi, const double *__restrict__ dzci,
@@ -623,6 +628,7 @@ extern "C" int cans_chkdt(const int n[3], const double dl[3], const double *dzci
   const long np = (long)n[0] * n[1] * n[2];
   const unsigned nblk = blocks_for(np);
   double *s;
+  std::lock_guard<std::mutex> lk(g_red_mu);
   int rc = red_scratch((size_t)nblk + 4, &s);
   if (rc) return rc;
   k_chkdt<<<nblk, kTB, 0, st>>>(d, 1. / dl[0], 1. / dl[1], dzci, dzfi, u, v, w, s);
@@ -667,6 +673,7 @@ extern "C" int cans_bulk_mean(const int n[3], const double *gvr, const double *p
   Dims d{n[0], n[1], n[2]};
   const unsigned nblk = blocks_for((long)n[0] * n[1] * n[2]);
   double *s;
+  std::lock_guard<std::mutex> lk(g_red_mu);
   int rc = red_scratch((size_t)nblk + 2, &s);
   if (rc) return rc;
   k_bulk_mean<<<nblk, kTB, 0, st>>>(d, gvr, p, s);

@@ -26,6 +26,15 @@ from . import output
 
 RKCOEFF = ((32. / 60., 0. / 60.), (25. / 60., -17. / 60.), (45. / 60., -25. / 60.))  # src/param.f90:20-22
 DBL_MAX = np.finfo(np.float64).max
+# src/param.f90:18, small = epsilon(1._rp)*10**(precision(1._rp)/2) with rp = dp: precision is
+# 15 decimal digits and 15/2 is integer division, so small = 2.22e-16 * 1e7
+SMALL = np.finfo(np.float64).eps * 10 ** (15 // 2)
+
+
+class SimulationAborted(RuntimeError):
+    """The run stopped on a failed stability check (src/main.f90:489-510): the time step is
+    too small, or the divergence is too large or NaN.  `Simulation.kill` is then True and,
+    as in the reference, no further step runs and nothing is saved."""
 
 
 def initgrid(gtype, n, gr, lz, is_periodic):
@@ -57,6 +66,8 @@ class Simulation:
         self.velf = list(case.get("velf", [0.] * 3))
         self.is_impdiff = int(case.get("is_impdiff", 0))
         self.icheck = int(case.get("icheck", 10))
+        self.is_mask_divergence_check = bool(case.get("is_mask_divergence_check", False))
+        self.kill = False
         self.cfl, self.dtmax, self.dt_f = case.get("cfl", 0.95), case.get("dtmax", 1e5), case.get("dt_f", -1.)
         zper = self.cbcpre[4:6] == "PP"
         dzc, dzf, zc, zf = initgrid(case.get("gtype", 1), n[2], case.get("gr", 0.), self.l[2], zper)
@@ -245,7 +256,26 @@ class Simulation:
         cans.updatep(n, self.dli, self.dzci, self.dzfi, alpha, self.is_impdiff, self.pp, self.p)
         cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
 
+    def _abort(self, why):
+        self.kill = True
+        raise SimulationAborted(f"step {self.istep}: {why}; aborting (src/main.f90:489-510)")
+
+    def check(self):
+        """The stability checks of src/main.f90:489-510: new dt from chkdt (abort when dt_cfl <
+        small), then chkdiv (abort when divmax > small or divtot is NaN, unless
+        is_mask_divergence_check)."""
+        dt_cfl = self._new_dt()
+        if dt_cfl < SMALL:
+            self._abort(f"time step is too small (dt_cfl = {dt_cfl:.3e})")
+        self.divtot, self.divmax = cans.chkdiv(self.n, self.l, self.dli, self.dzfi, self.u, self.v, self.w,
+                                               allow_nonfinite=True)
+        if not self.is_mask_divergence_check and (self.divmax > SMALL or np.isnan(self.divtot)):
+            self._abort(f"maximum divergence is too large (divtot = {self.divtot:.3e}, "
+                        f"divmax = {self.divmax:.3e})")
+
     def step(self, nsteps=1):
+        if self.kill:
+            raise SimulationAborted("the run was stopped by a failed stability check")
         for _ in range(nsteps):
             self.istep += 1
             self.time += self.dt
@@ -256,8 +286,7 @@ class Simulation:
             self.dpdl = -self.dpdl * self.dti
             self.fs = self.fs * self.dti
             if self.icheck > 0 and self.istep % self.icheck == 0:
-                self._new_dt()
-                self.divtot, self.divmax = cans.chkdiv(self.n, self.l, self.dli, self.dzfi, self.u, self.v, self.w)
+                self.check()
 
 
 class Boxes:

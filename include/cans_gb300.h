@@ -115,7 +115,9 @@ int cans_updatep(const int n[3], const double dli[3], const double *dzci, const 
  * the momentum equations (explicit pressure gradient, constant-flow-rate forcing).
  * dudtrko..: halo-free (n1,n2,n3) device arrays (previous substep RHS, updated).
  * work: device scratch of at least cans_rk_work_doubles(n, is_impdiff) doubles, or NULL
- * to use a scratch buffer the library allocates on first use and keeps.
+ * to use a scratch buffer the library allocates on first use and keeps (one per device,
+ * shared by every call that passes NULL: calls that may overlap on the GPU, from other
+ * streams or host threads, pass their own work).
  * f[3] (host out): the bulk-velocity forcing applied (velf - mean).  The forcing
  * reduction is done on the device; the call synchronises `stream` once when any
  * is_forced is set. */
@@ -160,23 +162,27 @@ int cans_boundp(const char cbc[6], const int n[3], const double bc[6], const int
  * has_alpha = 0 when the reference's optional alpha is absent */
 int cans_updt_rhs_b(const char c_or_f[3], const char cbc[6], const int n[3], const int is_bound[6],
                     const double rhsb[6], double *p, double alpha, int has_alpha, void *stream);
-/* chkdiv (src/chkdiv.f90:15): device FP64 reduction, synchronises `stream` */
+/* chkdiv (src/chkdiv.f90:15): device FP64 reduction, synchronises `stream`.  Returns
+ * CANS_ENONFINITE (with both outputs written) when divtot or divmax is not finite -- the
+ * reference's NaN test of src/main.f90:504.  cans_chkdiv, cans_chkdt and cans_bulk_mean use
+ * one library-owned scratch buffer per device behind a lock, so calls from several host
+ * threads are safe; they serialise. */
 int cans_chkdiv(const int n[3], const double l[3], const double dli[3], const double *dzfi,
                 const double *u, const double *v, const double *w, double *divtot, double *divmax,
                 void *stream);
 /* Divergence check that allocates nothing.  No counterpart in the reference: it is
  * cans_chkdiv with its scratch moved into a fixed device array inside the library, for
- * callers that cannot call cudaMalloc -- e.g. a host whose device memory is owned by the
- * OpenACC runtime's pool, a host that is capturing the stream into a CUDA graph (cudaMalloc
- * is not allowed during capture), or a long run that fixes its memory budget up front.
+ * callers that cannot call cudaMalloc -- e.g. a Fortran host whose device memory is owned
+ * by the OpenACC runtime's pool, or a long run that fixes its memory budget up front.
  * Limit: n1*n2*n3 <= 16,777,216 interior cells (65,536 blocks of 256 threads); larger sizes
  * return CANS_EINVAL and launch nothing.  The array (1 MiB) is held on every device that
  * loads the library until the process exits.  The first call on each device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  All calls share the one array and it keeps the last
  * call's contents (each call writes every slot it reads), so calls that overlap on the GPU
- * (different streams or host threads at the same time) race: serialise them.  Results,
- * arguments and the stream synchronisation are those of cans_chkdiv. */
+ * (different streams or host threads at the same time) race: serialise them.  Like
+ * cans_chkdiv, the call copies the two results to the host and synchronises `stream`
+ * before it returns; results and arguments are those of cans_chkdiv. */
 int cans_chkdiv_noalloc(const int n[3], const double l[3], const double dli[3], const double *dzfi,
                         const double *u, const double *v, const double *w, double *divtot,
                         double *divmax, void *stream);

@@ -983,6 +983,46 @@ static uint64_t splitmix64(uint64_t x) {
   x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
   return x ^ (x >> 31);
 }
+/* r = rhs - L x in extended precision (long double: 64-bit significand on x86-64, IEEE
+ * binary128 on aarch64), for the discrete operator the solver inverts with cell-centred x/y:
+ * second differences times dli^2 with homogeneous ghosts (P: periodic, N: x0 = x1, D: x0 =
+ * -x1; the eigenvalues of src/initsolver.f90:85-144), and in z the rows a, b, c of
+ * src/initsolver.f90:146-187 (boundary conditions already folded into b), wrapping when z is
+ * periodic.  x, rhs haloed (interior read only); r halo-free (n1,n2,n3).  Test
+ * infrastructure: one extended-precision refinement step x + S(r) of an FP64 solve gives
+ * an accuracy reference for ill-conditioned stretched-grid problems. */
+void orc_poisson_residual_ld(const int n[3], const double dli[3], const char cbc[6], const double *a,
+                             const double *b, const double *c, const double *x, const double *rhs, double *r) {
+  const int n1 = n[0], n2 = n[1], n3 = n[2];
+  const long double cx = (long double)dli[0] * (long double)dli[0];
+  const long double cy = (long double)dli[1] * (long double)dli[1];
+  const int zper = cbc[4] == 'P' && cbc[5] == 'P';
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 1; k <= n3; k++)
+    for (int j = 1; j <= n2; j++) {
+      for (int i = 1; i <= n1; i++) {
+        const long double xc = x[IX(i, j, k)];
+        long double xm, xp, ym, yp;
+        /* x neighbours */
+        if (i > 1) xm = x[IX(i - 1, j, k)];
+        else xm = cbc[0] == 'P' ? (long double)x[IX(n1, j, k)] : (cbc[0] == 'N' ? xc : -xc);
+        if (i < n1) xp = x[IX(i + 1, j, k)];
+        else xp = cbc[1] == 'P' ? (long double)x[IX(1, j, k)] : (cbc[1] == 'N' ? xc : -xc);
+        if (j > 1) ym = x[IX(i, j - 1, k)];
+        else ym = cbc[2] == 'P' ? (long double)x[IX(i, n2, k)] : (cbc[2] == 'N' ? xc : -xc);
+        if (j < n2) yp = x[IX(i, j + 1, k)];
+        else yp = cbc[3] == 'P' ? (long double)x[IX(i, 1, k)] : (cbc[3] == 'N' ? xc : -xc);
+        long double lz = (long double)b[k - 1] * xc;
+        if (k > 1) lz += (long double)a[k - 1] * (long double)x[IX(i, j, k - 1)];
+        else if (zper) lz += (long double)a[0] * (long double)x[IX(i, j, n3)];
+        if (k < n3) lz += (long double)c[k - 1] * (long double)x[IX(i, j, k + 1)];
+        else if (zper) lz += (long double)c[n3 - 1] * (long double)x[IX(i, j, 1)];
+        const long double lap = ((xp - xc) - (xc - xm)) * cx + ((yp - xc) - (xc - ym)) * cy + lz;
+        r[IH(i, j, k)] = (double)((long double)rhs[IX(i, j, k)] - lap);
+      }
+    }
+}
+
 void orc_add_noise(const int n[3], unsigned long long seed, double norm, double *p) {
   int n1 = n[0], n2 = n[1], n3 = n[2];
   for (int k = 1; k <= n3; k++)

@@ -124,6 +124,11 @@ double orc_chkdt(const int n[3], const double dl[3], const double *dzci, const d
 void orc_chkdiv(const int n[3], const double l[3], const double dli[3], const double *dzfi,
                 const double *u, const double *v, const double *w, double *divtot, double *divmax);
 
+/* r = rhs - L x in long double for the cell-centred Poisson operator the solver inverts
+ * (x/y second differences with P/N/D ghosts, z rows a, b, c); r halo-free */
+void orc_poisson_residual_ld(const int n[3], const double dli[3], const char cbc[6], const double *a,
+                             const double *b, const double *c, const double *x, const double *rhs, double *r);
+
 /* seeded uniform noise (this project's generator, NOT gfortran's random_number):
  * p(i,j,k) += 2*(r-0.5)*norm over the interior, r = splitmix64 of (seed, global index) */
 void orc_add_noise(const int n[3], unsigned long long seed, double norm, double *p);

@@ -67,6 +67,7 @@ def _setup(L):
     L.orc_chkdt.restype = C.c_double
     L.orc_chkdiv.argtypes = [_I, _D, _D, _D, _D, _D, _D, _D, _D]
     L.orc_add_noise.argtypes = [_I, C.c_ulonglong, C.c_double, _D]
+    L.orc_poisson_residual_ld.argtypes = [_I, _D, C.c_char_p, _D, _D, _D, _D, _D, _D]
     L.orc_state_new.argtypes = [C.c_void_p]
     L.orc_state_new.restype = C.c_void_p
     L.orc_state_free.argtypes = [C.c_void_p]
@@ -274,6 +275,15 @@ def chkdiv(n, l, dli, dzfi, u, v, w):
     a, b = C.c_double(), C.c_double()
     lib().orc_chkdiv(_ip(n), _dp(l), _dp(dli), _p(dzfi), _p(u), _p(v), _p(w), C.byref(a), C.byref(b))
     return a.value, b.value
+
+
+def poisson_residual_ld(n, dli, cbc, a, b, c, x, rhs):
+    """rhs - L x in extended precision for the cell-centred Poisson operator (halo-free
+    (n1, n2, n3) Fortran-ordered result); x, rhs haloed"""
+    r = np.zeros(tuple(n), order="F")
+    a, b, c = (np.ascontiguousarray(v, dtype=np.float64) for v in (a, b, c))
+    lib().orc_poisson_residual_ld(_ip(n), _dp(dli), _cs(cbc), _p(a), _p(b), _p(c), _p(x), _p(rhs), _p(r))
+    return r
 
 
 def add_noise(n, seed, norm, p):

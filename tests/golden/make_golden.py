@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures in tests/golden/ from the reference checkout.
 
-Run in the development container, where the reference sources are mounted:
-    python tests/golden/make_golden.py /root/reference
+Run where a checkout of the reference is available, giving its root directory:
+    python tests/golden/make_golden.py <path to the CaNS checkout>
 It copies the reference's own lid-driven-cavity golden v-profile
 (tests/lid_driven_cavity/data_ldc_re1000.txt, compared at rtol=1e-7 by the
 reference's tests/lid_driven_cavity/test.py:5-8) and records the run
@@ -32,4 +32,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path to the CaNS checkout>")
+    main(sys.argv[1])

@@ -1,0 +1,154 @@
+"""Parity at the benchmark's own sizes: the 512^3 and 1024x512x384 channel Poisson solves and
+the 512x256x256 channel run, against the oracle (the restatement of src/solver.f90).
+
+The stretched channel operator (tanh z, gr = 1.4) is ill-conditioned: its low-wavenumber
+columns have condition numbers of ~1e7, so any FP64 solve -- the reference's, the oracle's,
+this library's FP64 path -- carries a rounding error of that order times 1e-16 in the
+low modes that dominate the solution.  Each FP64 result is therefore also measured against an
+accuracy reference: the oracle's solve plus one refinement step whose residual is evaluated
+in extended precision (orc_poisson_residual_ld), x_t = x_o + S(rhs - L x_o).  The FP64 path
+must match the oracle at 1e-12 (it does by ~1e-14: both make the same rounding errors in the
+z recursion); the FP32 + refinement path must reach 1e-12 against x_t -- against the oracle it
+then differs by the oracle's own error (1.1e-11 at 512^3 on GB300).  On a well-conditioned
+(triperiodic) 512^3 problem both paths match the oracle at 1e-12 directly.  Host memory:
+~10 GB at the largest size.
+"""
+import numpy as np
+import pytest
+
+from gpu_common import demean, grid_for, rel_l2
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CH_L = (4 * np.pi, 2 * np.pi, 2.0)
+
+
+def _rhs(n, dzf, seed, zero_mean):
+    """seeded N(0,1) right-hand side with the volume-weighted mean removed when singular"""
+    rng = np.random.default_rng(seed)
+    p = O.field(n)
+    inner = rng.standard_normal(tuple(n)).astype(np.float64)
+    if zero_mean:
+        w = dzf[1:-1][None, None, :]
+        inner -= (inner * w).sum() / (w.sum() * n[0] * n[1])
+    p[1:-1, 1:-1, 1:-1] = inner
+    return p
+
+
+def _gauge_err(got, want, dzf):
+    return rel_l2(demean(got, dzf), demean(want, dzf))
+
+
+def _solve_case(n, l, cbc, gr, seed):
+    import torch
+    from cans_gb300 import cans
+    dl = [l[d] / n[d] for d in range(3)]
+    dli = [1. / x for x in dl]
+    dzc, dzf, dzci, dzfi = grid_for(n, l, cbc, gr)
+    s = O.initsolver(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc")
+    rhs = _rhs(n, dzf, seed, "D" not in cbc)
+    i3 = (slice(1, -1),) * 3
+    # oracle FP64 solve
+    xo = rhs.copy(order="F")
+    O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], cbc, "ccc", xo)
+    # accuracy reference: one refinement step with an extended-precision residual
+    e = O.field(n)
+    e[i3] = O.poisson_residual_ld(n, dli, cbc, s["a"], s["b"], s["c"], xo, rhs)
+    O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], cbc, "ccc", e)
+    xt = xo[i3] + e[i3]
+    del e
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
+    out = {}
+    plan64 = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc")
+    d = cans.to_device(rhs)
+    plan64.solve(d)
+    out["fp64"] = cans.fview(d)[i3].copy()
+    del d, plan64
+    torch.cuda.empty_cache()
+    plan32 = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc", precision=cans.FP32)
+    d = cans.to_device(rhs)
+    plan32.solve_refined(d, dli, T(dzci), T(dzfi), rtol=0.0, max_iter=2)  # the benchmark's schedule
+    out["refined"] = cans.fview(d)[i3].copy()
+    del d, plan32
+    torch.cuda.empty_cache()
+    return xo[i3], xt, out, dzf
+
+
+def _report(tag, xo, xt, out, dzf):
+    r = {"oracle_vs_ref": _gauge_err(xo, xt, dzf)}
+    for k, v in out.items():
+        r[f"{k}_vs_ref"] = _gauge_err(v, xt, dzf)
+        r[f"{k}_vs_oracle"] = _gauge_err(v, xo, dzf)
+    print(tag, {k: f"{v:.3e}" for k, v in r.items()})
+    return r
+
+
+@pytest.mark.parametrize("n", [(512, 512, 512), (1024, 512, 384)])
+def test_channel_poisson_at_benchmark_size(require_gpu, n):
+    xo, xt, out, dzf = _solve_case(list(n), CH_L, "PPPPNN", 1.4, 20260101)
+    r = _report(f"channel {n}", xo, xt, out, dzf)
+    # the FP64 path against the reference's FP64 solver (its restatement): both run the same
+    # Thomas recursion on the ill-conditioned columns, so they agree far below their error
+    # (measured on GB300: 2.9e-14 at 512^3, 9.5e-16 at 1024x512x384)
+    assert r["fp64_vs_oracle"] <= 1e-12, r
+    # the benchmark spec's bound against an accurate solution of the same discrete operator
+    assert r["refined_vs_ref"] <= 1e-12, r
+    # the FP64 path is as accurate as the oracle's (the reference's) own FP64 solve
+    assert r["fp64_vs_ref"] <= max(2.0 * r["oracle_vs_ref"], 1e-12), r
+    # and the two FP64 solves differ only by their own rounding errors
+    assert r["fp64_vs_oracle"] <= r["fp64_vs_ref"] + r["oracle_vs_ref"] + 1e-13, r
+    assert r["refined_vs_oracle"] <= r["oracle_vs_ref"] + 1e-12, r
+
+
+def test_triperiodic_poisson_512_matches_oracle(require_gpu):
+    """Well-conditioned operator (the 512^3 TGV grid): FP64 path vs oracle at 1e-12 flat."""
+    n = [512, 512, 512]
+    xo, xt, out, dzf = _solve_case(n, (2 * np.pi,) * 3, "PPPPPP", 0.0, 7)
+    r = _report("triperiodic 512^3", xo, xt, out, dzf)
+    assert r["fp64_vs_oracle"] <= 1e-12, r
+    assert r["refined_vs_oracle"] <= 1e-12, r
+    assert r["refined_vs_ref"] <= 1e-12, r
+
+
+@pytest.mark.parametrize("refine", [None, {"rtol": 0.0, "max_iter": 2}])
+def test_channel_run_512x256x256_field_by_field(require_gpu, refine):
+    """The CH configuration (512 x 256 x 256, Lx = 4 pi, Ly = 2 pi, Lz = 2, tanh gr = 1.4,
+    Re_b = 5600, constant flow rate, Poiseuille + seeded uniform(-0.1, 0.1) noise): 5 RK3 steps
+    of the library against the oracle's run, field by field; with the FP64 pressure solve and
+    with FP32 + two refinement corrections."""
+    from cans_gb300 import cans
+    from cans_gb300.driver import Simulation
+    n = [512, 256, 256]
+    case = dict(ng=n, l=list(CH_L), gtype=1, gr=1.4, cfl=0.95, dtmax=1e5, dt_f=-1., visci=5600., icheck=5,
+                cbcvel="PPPPDD" * 3, cbcpre="PPPPNN", bcvel=[0.] * 18, bcpre=[0.] * 6,
+                is_forced=[1, 0, 0], velf=[1., 0., 0.])
+    r = O.Run(case)
+    zc = r.grid()["zc"]
+    u = O.field(n)
+    u[1:-1, 1:-1, 1:-1] = (6. * (zc[1:-1] / CH_L[2]) * (1. - zc[1:-1] / CH_L[2]))[None, None, :]
+    v, w, p = O.field(n), O.field(n), O.field(n)
+    for f, s in ((u, 11), (v, 12), (w, 13)):
+        O.add_noise(n, s, 0.1, f)
+    r.u[:] = u; r.v[:] = v; r.w[:] = w
+    r.start()
+    if refine:
+        case = dict(case, pressure_refine=refine)
+    sim = Simulation(case)
+    sim.set_fields(u, v, w, p)
+    sim.start()
+    del u, v, w, p
+    assert abs(sim.dt - r.dt) <= 1e-13 * r.dt
+    r.step(5)
+    sim.step(5)
+    errs = {}
+    for name in ("u", "v", "w"):
+        got = cans.fview(getattr(sim, name))[1:-1, 1:-1, 1:-1]
+        errs[name] = rel_l2(got, getattr(r, name)[1:-1, 1:-1, 1:-1])
+    got, want = cans.fview(sim.p)[1:-1, 1:-1, 1:-1], r.p[1:-1, 1:-1, 1:-1]
+    errs["p"] = _gauge_err(got, want, r.grid()["dzf"])
+    print("channel 512x256x256, 5 steps,", "refined" if refine else "fp64", {k: f"{v:.2e}" for k, v in errs.items()},
+          f"divmax gpu {sim.divmax:.2e} oracle {r.scalar(4):.2e}")
+    for name in ("u", "v", "w"):
+        assert errs[name] <= 1e-11, errs
+    assert errs["p"] <= 1e-10, errs

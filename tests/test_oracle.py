@@ -242,3 +242,37 @@ def test_statistics_oracle_identities():
     st = O.out1d_chan(n, l, dl, u, v, w)
     assert np.allclose(st[0], prof[1:-1], rtol=1e-14)
     assert np.abs(st[3]).max() < 1e-12 and np.abs(st[6]).max() == 0.
+
+
+@pytest.mark.parametrize("cbc", ["PPPPNN", "PPNNNN", "NNDDNN", "PPPPPP", "DDPPDD"])
+def test_extended_residual_refinement(cbc):
+    """orc_poisson_residual_ld applies the operator the solver inverts: the residual of an FP64
+    oracle solve is at rounding level, and one extended-precision refinement step x + S(r)
+    agrees with the dense long-double solve (tests/gpu_common.solve_extended) better than the
+    FP64 solve itself (periodic x/y cases; solve_extended handles only those)."""
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    from gpu_common import gauge_rel_l2, grid_for, random_field, rel_l2, singular, solve_extended
+    n, l = (12, 10, 64), (4 * np.pi, 2 * np.pi, 2.0)
+    dl = [l[d] / n[d] for d in range(3)]
+    dli = [1 / x for x in dl]
+    dzc, dzf, dzci, dzfi = grid_for(n, l, cbc, 1.4)
+    s = O.initsolver(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc")
+    rhs = random_field(n, 3, zero_mean=singular(cbc), dzf=dzf)
+    x = rhs.copy(order="F")
+    O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], cbc, "ccc", x)
+    r = O.poisson_residual_ld(n, dli, cbc, s["a"], s["b"], s["c"], x, rhs)
+    i3 = (slice(1, -1),) * 3
+    assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(rhs[i3]), np.linalg.norm(r)
+    e = O.field(n)
+    e[i3] = r
+    O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], cbc, "ccc", e)
+    xt = x[i3] + e[i3]
+    if cbc[:4] == "PPPP" and cbc[4:] != "PP":
+        exact, _ = solve_extended(n, dli, s["a"], s["b"], s["c"], rhs[i3])
+        cmp = (lambda a, b: gauge_rel_l2(a, b, dzf)) if singular(cbc) else rel_l2
+        e64, et = cmp(x[i3], exact), cmp(xt, exact)
+        assert et <= max(0.1 * e64, 1e-15), (et, e64)
+    # a second step changes nothing measurable
+    r2 = O.poisson_residual_ld(n, dli, cbc, s["a"], s["b"], s["c"], np.asfortranarray(np.pad(xt, 1)), rhs)
+    assert np.linalg.norm(r2) <= np.linalg.norm(r) + 1e-300

@@ -1,10 +1,10 @@
 """The allocation-free divergence check (cans_chkdiv_noalloc) against the allocating one.
 
 Some callers of this library cannot call cudaMalloc: a Fortran host whose device memory
-belongs to the OpenACC runtime, a host recording its time step into a CUDA graph (no
-allocation is allowed while a stream is captured), or a run that fixes its memory budget at
-start-up.  cans_chkdiv_noalloc serves them from a fixed 1 MiB device array inside the
-library (at most 16,777,216 interior cells).  This file is collected last on purpose.
+belongs to the OpenACC runtime's pool, or a run that fixes its memory budget at start-up.
+cans_chkdiv_noalloc serves them from a fixed 1 MiB device array inside the library (at most
+16,777,216 interior cells).  Like cans_chkdiv it synchronises its stream before returning.
+This file is collected last on purpose.
 """
 import ctypes as C
 
@@ -39,6 +39,11 @@ def test_size_limit_rejected_before_any_device_work():
     p = C.cast(dummy, C.c_void_p)
     tot, mx = C.c_double(), C.c_double()
     rc = L.cans_chkdiv_noalloc((C.c_int * 3)(4096, 4096, 2), (C.c_double * 3)(1, 1, 1),
+                               (C.c_double * 3)(1, 1, 1), p, p, p, p, C.byref(tot), C.byref(mx), None)
+    assert rc == 1
+    # extents whose product would overflow a 64-bit count are rejected, not wrapped
+    big = 2 ** 31 - 1
+    rc = L.cans_chkdiv_noalloc((C.c_int * 3)(big, big, big), (C.c_double * 3)(1, 1, 1),
                                (C.c_double * 3)(1, 1, 1), p, p, p, p, C.byref(tot), C.byref(mx), None)
     assert rc == 1
 
