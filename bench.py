@@ -124,17 +124,30 @@ class Clocks:
                 "samples": len(rows)}
 
 
+_RHS_CACHE = {}
+
+
+def host_rhs(n, dzf, seed=20260101):
+    """seeded N(0,1) RHS (numpy PCG64) with the volume-weighted mean removed (compatible with
+    Neumann z); interior as a C-ordered (n3, n2, n1) array -- the bytes of the device tensor
+    interior and of the Fortran array p(1:n1,1:n2,1:n3).  The oracle solves the same values."""
+    key = (tuple(n), seed)
+    if key not in _RHS_CACHE:
+        rng = np.random.default_rng(seed)
+        inner = rng.standard_normal((n[2], n[1], n[0]))
+        w = np.asarray(dzf)[1:-1][:, None, None]
+        inner -= (inner * w).sum() / (w.sum() * n[0] * n[1])
+        _RHS_CACHE.clear()
+        _RHS_CACHE[key] = inner
+    return _RHS_CACHE[key]
+
+
 def make_rhs(n, dzf, device, seed=20260101):
-    """seeded N(0,1) RHS with the volume-weighted mean removed (compatible with Neumann z)"""
+    """the host_rhs values in a haloed device field"""
     import torch
     from cans_gb300 import cans
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
     p = cans.field(n, device)
-    inner = torch.randn((n[2], n[1], n[0]), generator=g, device=device, dtype=torch.float64)
-    w = torch.tensor(dzf[1:-1], device=device, dtype=torch.float64)[:, None, None]
-    inner -= (inner * w).sum() / (w.sum() * n[0] * n[1])
-    p[1:-1, 1:-1, 1:-1] = inner
+    p[1:-1, 1:-1, 1:-1] = torch.from_numpy(host_rhs(n, dzf, seed)).to(device)
     return p
 
 
@@ -189,8 +202,14 @@ def bench_ours(args, rank, world):
         return {"fp32_refined": bench_refined(args, n, dli, dzc, dzf, None, None, dev, world)}
     if args.only == "rk3":
         return {"rk3_step": bench_rk3(args.size, dev, 20)}
+    if args.only == "rk3-fp32":  # profiling aid: the FP32 run of the TGV only
+        return {"rk3_step_fp32": bench_rk3(args.size, dev, max(1, args.steps), legs=("fp32",))}
+    if args.only == "fp32-solve":  # profiling aid: plain FP32 solves (the passes of the refinement)
+        return {"fp32_solve": bench_fp32_solve(args, n, dli, dzc, dzf, dev)}
     if args.only == "mx":
         return {"poisson_mx": bench_mx(args, dev, world)}
+    if args.only == "mx-run":
+        return {"channel_mx_run": bench_mx_run(dev)}
     if args.only == "ch":
         return {"channel_ch": bench_ch(dev)}
     if args.only == "adjoint":
@@ -206,6 +225,10 @@ def bench_ours(args, rank, world):
         ref = bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=True)
     del p64, plan64
     torch.cuda.empty_cache()
+    sols = None
+    if rank == 0 and not args.skip_cpu:
+        # the solutions of the headline RHS, compared with the oracle's in the CPU leg
+        sols = gpu_solutions(n, dli, dzc, dzf, dev, ref["corrections_per_solve"])
     hbm, kind = peaks()
     # dominant kernel of the refined solve (largest share of the launch list): the
     # double-float residual k_dfres, timed per launch by CUDA events on the plan's stream
@@ -234,11 +257,15 @@ def bench_ours(args, rank, world):
     if not args.skip_rk3:
         torch.cuda.empty_cache()
         rk3 = bench_rk3(args.size, dev, 20)  # the TGV protocol: 3 warm-up + 20 timed steps
+    mx_run = None
+    if not args.skip_mx and world == 1:
+        torch.cuda.empty_cache()
+        mx_run = bench_mx_run(dev)
     out = {"metric": METRIC, "value": ref["value"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ref["ms_per_step"], "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32+f64 (FP32 transforms, FP64 residual/z/reductions)",
            "data": "synthetic (seeded N(0,1) RHS, mean removed)",
-           "config": {"workload": workload + "_fp32_refined_to_fp64_accuracy", "grid": n, "bc_pressure": "PP,PP,NN",
+           "config": {"workload": workload, "grid": n, "bc_pressure": "PP,PP,NN",
                       "z_grid": "tanh gr=1.4", "domain": [round(x, 6) for x in L_CH],
                       "precision": "FP32 solve + FP64 iterative refinement, accuracy <= FP64 path",
                       "l2": "working set 2+ GB per solve >> 129 MB L2 (no flush needed)",
@@ -246,10 +273,14 @@ def bench_ours(args, rank, world):
            "e2e": ref.pop("e2e"), "roofline": roof, "clocks": clk.summary(), "gpu_launches": ref["gpu_launches"],
            "fp32_refined": ref, "fp64_path": fp64,
            "speedup_refined_over_fp64": round(ref["value"] / fp64["value"], 3)}
+    if sols is not None:
+        out["_gpu_solutions"] = sols
     if rk3:
         out["rk3_step"] = rk3
     if mx:
         out["poisson_mx"] = mx
+    if mx_run:
+        out["channel_mx_run"] = mx_run
     if ch:
         out["channel_ch"] = ch
     if not args.skip_adjoint:
@@ -262,51 +293,151 @@ def bench_ours(args, rank, world):
     return out
 
 
-def bench_ch(dev, steps=200):
-    """The channel run (CH): 512 x 256 x 256, tanh z (gr 1.4), domain 6 x 3 x 1, Re_b 5600,
-    constant flow rate, Poiseuille + uniform(-0.1, 0.1) noise, CFL 0.95; `steps` timed RK3
-    steps after 3 warm-up steps, with the FP64 pressure solve and with the refined FP32 one
-    (two corrections).  Reported with the bulk velocity held by the forcing and the
-    divergence at the end."""
+def channel_case(n, l, dt_f=-1., precision="fp64", refine=False):
+    """The channel of the CH / MX configurations: tanh z (gr = 1.4), no-slip walls at z = 0, Lz,
+    periodic x/y, Re_b = 5600 (visc = 1/5600), constant flow rate U_b = 1, explicit diffusion"""
+    case = dict(ng=list(n), l=list(l), gtype=1, gr=1.4, cfl=0.95, dtmax=1e5, dt_f=dt_f, visci=5600., icheck=10,
+                cbcvel="PPPPDD" * 3, cbcpre="PPPPNN", bcvel=[0.] * 18, bcpre=[0.] * 6, is_forced=[1, 0, 0],
+                velf=[1., 0., 0.], precision=precision)
+    if refine:
+        case["pressure_refine"] = {"rtol": 0.0, "max_iter": 2}
+    return case
+
+
+def channel_init(sim, seed=20260101):
+    """initflow 'poi' (src/initflow.f90:56-58): the laminar profile 6 z/Lz (1 - z/Lz) U_b plus
+    seeded uniform(-0.1, 0.1) U_b perturbations with their mean removed, rounded to FP32 so
+    that the FP64 and FP32 runs start from the same values"""
+    import torch
+    n = sim.n
+    dev = sim.u.device
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    zc = torch.tensor(sim.zc[1:-1], device=dev, dtype=torch.float64) / sim.l[2]
+
+    def noise():
+        x = 0.2 * (torch.rand((n[2], n[1], n[0]), generator=g, device=dev, dtype=torch.float64) - 0.5)
+        return x - x.mean()
+
+    vals = [(6. * zc * (1. - zc))[:, None, None] + noise(), noise(), noise()]
+    for fld, x in zip((sim.u, sim.v, sim.w), vals):
+        fld[1:-1, 1:-1, 1:-1] = x.float().double().to(fld.dtype)
+
+
+def run_and_time(sim, warm, steps):
+    """warm untimed steps, then `steps` steps timed with CUDA events on the current stream"""
+    import torch
+    from cans_gb300 import cans
+    sim.step(warm)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = cans.launch_count()
+    e0.record(st)
+    sim.step(steps)
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, (cans.launch_count() - l0) // max(steps, 1)
+
+
+def field_errors(sim, ref):
+    """relative L2 of u, v, w and of the mean-free p of `sim` against the saved fields `ref`"""
+    import torch
+    out = {}
+    for name in ("u", "v", "w", "p"):
+        a = getattr(sim, name)[1:-1, 1:-1, 1:-1].double()
+        b = ref[name]
+        if name == "p":
+            a, b = a - a.mean(), b - b.mean()
+        out[name] = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+    return out
+
+
+def channel_legs(n, l, dev, warm, steps):
+    """The FP64 run, the FP64 run with the refined FP32 pressure solve and the FP32 run of the
+    channel, each `warm` + `steps` RK3 steps at one fixed dt (0.8 x the CFL-0.95 step of the
+    initial field), with the per-field error of the other two against the FP64 run"""
     import torch
     from cans_gb300 import cans
     from cans_gb300.driver import Simulation
-    n = [512, 256, 256]
-
-    def run(refine):
-        case = dict(ng=n, l=[6.0, 3.0, 1.0], gtype=1, gr=1.4, cfl=0.95, dtmax=1e5, dt_f=-1., visci=5600.,
-                    icheck=10, cbcvel="PPPPDD" * 3, cbcpre="PPPPNN", bcvel=[0.] * 18, bcpre=[0.] * 6,
-                    is_forced=[1, 0, 0], velf=[1., 0., 0.])
-        if refine:
-            case["pressure_refine"] = {"rtol": 0.0, "max_iter": 2}
-        sim = Simulation(case, device=dev)
-        zc = torch.tensor(sim.zc[1:-1], device=dev, dtype=torch.float64)
-        g = torch.Generator(device=dev)
-        g.manual_seed(20260101)
-        noise = lambda: 0.2 * (torch.rand((n[2], n[1], n[0]), generator=g, device=dev, dtype=torch.float64) - 0.5)
-        sim.u[1:-1, 1:-1, 1:-1] = (6. * zc * (1. - zc))[:, None, None] + noise()
-        sim.v[1:-1, 1:-1, 1:-1] = noise()
-        sim.w[1:-1, 1:-1, 1:-1] = noise()
+    ncell = n[0] * n[1] * n[2]
+    sim = Simulation(channel_case(n, l), device=dev)
+    channel_init(sim)
+    sim.start()
+    dt = 0.8 * sim.dt
+    del sim
+    torch.cuda.empty_cache()
+    out, ref = {}, None
+    for leg, prec, refine in (("fp64", "fp64", False), ("fp64_refined_pressure", "fp64", True),
+                              ("fp32_run", "fp32", False)):
+        sim = Simulation(channel_case(n, l, dt, prec, refine), device=dev)
+        channel_init(sim)
         sim.start()
-        sim.step(3)
-        torch.cuda.synchronize()
-        st = torch.cuda.current_stream()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        sim.step(steps)
-        e1.record(st)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / steps
-        ub = cans.bulk_mean(n, sim.gvr_f, sim.u)
-        divtot, divmax = cans.chkdiv(n, sim.l, sim.dli, sim.dzfi, sim.u, sim.v, sim.w)
-        out = {"ms_per_step": round(ms, 3), "Mcell_steps_per_s": round(n[0] * n[1] * n[2] / (ms * 1e-3) / 1e6, 2),
-               "bulk_velocity": ub, "divmax": divmax, "time": sim.time}
+        ms, launches = run_and_time(sim, warm, steps)
+        r = {"ms_per_step": round(ms, 3), "Mcell_steps_per_s": round(ncell / (ms * 1e-3) / 1e6, 2),
+             "gpu_launches_per_step": launches}
+        if prec == "fp32":
+            r["precision"] = "FP32 fields and stencils, pressure correction FP32 solve + 2 FP64 refinement corrections"
+            ub = cans.bulk_mean_f32(n, sim.gvr_f32, sim.u)
+            divtot, divmax = cans.chkdiv_f32(n, sim.l, sim.dli, sim.dzfi32, sim.u, sim.v, sim.w)
+        else:
+            ub = cans.bulk_mean(n, sim.gvr_f, sim.u)
+            divtot, divmax = cans.chkdiv(n, sim.l, sim.dli, sim.dzfi, sim.u, sim.v, sim.w)
+        r.update({"bulk_velocity": ub, "divmax": divmax, "time": sim.time})
+        if ref is None:
+            ref = {name: getattr(sim, name)[1:-1, 1:-1, 1:-1].clone() for name in ("u", "v", "w", "p")}
+        else:
+            r["rel_l2_vs_fp64_run"] = field_errors(sim, ref)
+        out[leg] = r
         del sim
         torch.cuda.empty_cache()
-        return out
+    del ref
+    torch.cuda.empty_cache()
+    out["dt"] = dt
+    return out
 
-    return {"workload": "channel_512x256x256_Reb5600_rk3", "steps": steps, "warmup_steps": 3,
-            "fp64_pressure": run(False), "fp32_refined_pressure": run(True)}
+
+def bench_ch(dev, steps=200):
+    """The channel run (CH): 512 x 256 x 256, Lx = 4 pi, Ly = 2 pi, Lz = 2, tanh z (gr 1.4),
+    Re_b 5600, constant flow rate, Poiseuille + uniform(-0.1, 0.1) noise; `steps` timed RK3
+    steps after 3 warm-up steps: FP64, FP64 with the refined FP32 pressure solve, and the FP32
+    run (per-field error of the latter two against the FP64 run after all steps)."""
+    n = [512, 256, 256]
+    out = {"workload": "channel_512x256x256_Reb5600_rk3", "steps": steps, "warmup_steps": 3}
+    out.update(channel_legs(n, L_CH, dev, 3, steps))
+    return out
+
+
+def bench_mx_run(dev, steps=10):
+    """The mixed-precision channel (MX): 1024 x 512 x 384, the CH geometry and flow; `steps`
+    timed RK3 steps after 3 warm-up steps of the FP64 run and of the FP32 run (FP32 fields
+    and stencils, FP64-accurate refined pressure), with the FP32 run's per-field error."""
+    n = [1024, 512, 384]
+    out = {"workload": "channel_1024x512x384_Reb5600_rk3", "steps": steps, "warmup_steps": 3}
+    out.update(channel_legs(n, L_CH, dev, 3, steps))
+    return out
+
+
+def bench_fp32_solve(args, n, dli, dzc, dzf, dev):
+    """Plain FP32 solves (cans_solver_f32) of the headline RHS rounded to FP32: the five FP32
+    passes the refinement runs, for profiling them on their own"""
+    import torch
+    from cans_gb300 import cans
+    plan = cans.Plan(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc", precision=cans.FP32)
+    src = make_rhs(n, dzf, dev).float()
+    p = src.clone()
+    for _ in range(args.warmup):
+        p.copy_(src)
+        plan.solve(p)
+    torch.cuda.synchronize()
+    plan.set_timing(True)
+    for _ in range(args.steps):
+        p.copy_(src)
+        plan.solve(p)
+    pass_ms, nrec = plan.get_timing()
+    plan.set_timing(False)
+    names = ["solve_xfwd", "solve_yfwd", "solve_zthomas", "solve_ybwd", "solve_xbwd"]
+    return {"pass_ms": {k: round(v, 4) for k, v in zip(names, pass_ms)}, "solves": nrec}
 
 
 def bench_mx(args, dev, world):
@@ -468,62 +599,71 @@ def bench_refined(args, n, dli, dzc, dzf, plan64, p64, dev, world, e2e=False):
             "residual_launches_timed": nres, "residual_bytes_per_cell": residual_bytes(k_cal), "e2e": e2e_out}
 
 
-def bench_rk3(size, dev, steps):
-    """RK3 time steps of the 512^3 Taylor-Green vortex: the FP64 path, and the same steps
-    with the pressure solved on an FP32 plan with FP64 refinement (two corrections); the
-    refined run's velocity is compared with the FP64 path's after the same steps."""
+def tgv_init(sim):
+    """initflow 'tgv' (src/initflow.f90:102-117) with the analytic pressure of the TGV
+    configuration, rounded to FP32 so that every leg starts from the same values"""
     import torch
-    from cans_gb300 import cans
+    n = sim.n[0]
+    dev = sim.u.device
+    dl = 2 * np.pi / n
+    x = (torch.arange(1, n + 1, device=dev, dtype=torch.float64) - 0.5) * dl
+    xf = torch.arange(1, n + 1, device=dev, dtype=torch.float64) * dl
+    put = lambda fld, val: fld[1:-1, 1:-1, 1:-1].copy_(val.float().double().to(fld.dtype))
+    Z, Y, X = torch.meshgrid(x, x, xf, indexing="ij")
+    put(sim.u, torch.sin(X) * torch.cos(Y) * torch.cos(Z))
+    Z, Y, X = torch.meshgrid(x, xf, x, indexing="ij")
+    put(sim.v, -torch.cos(X) * torch.sin(Y) * torch.cos(Z))
+    Z, Y, X = torch.meshgrid(x, x, x, indexing="ij")
+    put(sim.p, (torch.cos(2 * X) + torch.cos(2 * Y)) * (torch.cos(2 * Z) + 2.) / 16.)
+    del X, Y, Z
+
+
+def bench_rk3(size, dev, steps, legs=("fp64", "fp64_refined_pressure", "fp32_run")):
+    """RK3 time steps of the 512^3 Taylor-Green vortex (Re 1600, explicit diffusion, fixed dt
+    from CFL 0.5 at t = 0; 3 warm-up + `steps` timed steps): the FP64 path, the FP64 path with
+    the pressure solved on an FP32 plan with two FP64 refinement corrections, and the FP32
+    run (FP32 fields and stencils + the refined pressure); the latter two's velocity and
+    pressure are compared with the FP64 path's after the same steps."""
+    import torch
     from cans_gb300.driver import Simulation
     n = size
+    ncell = n ** 3
 
-    def run(refine):
-        case = dict(ng=[n, n, n], l=[2 * np.pi] * 3, gtype=1, gr=0., cfl=0.5, dtmax=1e5, dt_f=-1., visci=1600.,
-                    icheck=0, cbcvel="PP" * 9, cbcpre="PP" * 3, bcvel=[0.] * 18, bcpre=[0.] * 6)
+    def case(dt_f, prec, refine):
+        c = dict(ng=[n, n, n], l=[2 * np.pi] * 3, gtype=1, gr=0., cfl=0.5, dtmax=1e5, dt_f=dt_f, visci=1600.,
+                 icheck=0, cbcvel="PP" * 9, cbcpre="PP" * 3, bcvel=[0.] * 18, bcpre=[0.] * 6, precision=prec)
         if refine:
-            # fixed schedule of two corrections (the count calibrated for the 512^3 Poisson
-            # headline); the velocity is checked against the FP64 path below
-            case["pressure_refine"] = {"rtol": 0.0, "max_iter": 2}
-        sim = Simulation(case, device=dev)
-        dl = 2 * np.pi / n
-        x = (torch.arange(1, n + 1, device=dev, dtype=torch.float64) - 0.5) * dl
-        xf = torch.arange(1, n + 1, device=dev, dtype=torch.float64) * dl
-        # initflow 'tgv' (src/initflow.f90:102-117) with the analytic pressure
-        Z, Y, X = torch.meshgrid(x, x, xf, indexing="ij")
-        sim.u[1:-1, 1:-1, 1:-1] = torch.sin(X) * torch.cos(Y) * torch.cos(Z)
-        Z, Y, X = torch.meshgrid(x, xf, x, indexing="ij")
-        sim.v[1:-1, 1:-1, 1:-1] = -torch.cos(X) * torch.sin(Y) * torch.cos(Z)
-        Z, Y, X = torch.meshgrid(x, x, x, indexing="ij")
-        sim.p[1:-1, 1:-1, 1:-1] = (torch.cos(2 * X) + torch.cos(2 * Y)) * (torch.cos(2 * Z) + 2.) / 16.
-        del X, Y, Z
+            c["pressure_refine"] = {"rtol": 0.0, "max_iter": 2}
+        return c
+
+    sim = Simulation(case(-1., "fp64", False), device=dev)
+    tgv_init(sim)
+    sim.start()
+    dt = sim.dt
+    del sim
+    torch.cuda.empty_cache()
+    spec = {"fp64": ("fp64", False), "fp64_refined_pressure": ("fp64", True), "fp32_run": ("fp32", False)}
+    out, ref = {"workload": f"tgv_{n}^3_rk3", "steps": steps, "warmup_steps": 3, "dt": dt}, None
+    for leg in legs:
+        prec, refine = spec[leg]
+        sim = Simulation(case(dt, prec, refine), device=dev)
+        tgv_init(sim)
         sim.start()
-        sim.step(3)  # warm-up
-        torch.cuda.synchronize()
-        st = torch.cuda.current_stream()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        l0 = cans.launch_count()
-        e0.record(st)
-        sim.step(steps)
-        e1.record(st)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / steps
-        out = {"value": round(n ** 3 / (ms * 1e-3) / 1e6, 2), "unit": "Mcell/s", "ms_per_step": round(ms, 3),
-               "steps": steps, "gpu_launches_per_step": (cans.launch_count() - l0) // steps}
-        if refine:
-            out["pressure_corrections"] = sim.p_refine["max_iter"]
-        u = sim.u[1:-1, 1:-1, 1:-1].clone()
+        ms, launches = run_and_time(sim, 3, steps)
+        r = {"value": round(ncell / (ms * 1e-3) / 1e6, 2), "unit": "Mcell/s", "ms_per_step": round(ms, 3),
+             "gpu_launches_per_step": launches}
+        if refine or prec == "fp32":
+            r["pressure_corrections"] = sim.p_refine["max_iter"]
+        if ref is None and leg == "fp64":
+            ref = {name: getattr(sim, name)[1:-1, 1:-1, 1:-1].clone() for name in ("u", "v", "w", "p")}
+        elif ref is not None:
+            r["rel_l2_vs_fp64_path"] = field_errors(sim, ref)
+        out[leg] = r
         del sim
         torch.cuda.empty_cache()
-        return out, u
-
-    r64, u64 = run(False)
-    r32, u32 = run(True)
-    r32["u_rel_l2_vs_fp64_path"] = float(torch.linalg.vector_norm(u32 - u64) / torch.linalg.vector_norm(u64))
-    del u32, u64
+    del ref
     torch.cuda.empty_cache()
-    r64.update({"workload": f"tgv_{n}^3_rk3_fp64"})
-    r64["fp32_refined_pressure"] = r32
-    return r64
+    return out
 
 
 def bx_cases(nbox, seed=7):
@@ -670,8 +810,36 @@ def bench_adjoint(dev, n=(256, 128, 128), nsteps=50, ckpt=10, ndir=8, seed=11):
             "bforce_check": bchk, "clock": "host, synchronised"}
 
 
-def bench_cpu(size, steps, warmup, threads=None):
-    """The oracle (CPU restatement of src/solver.f90 with FFTW r2r semantics), all host cores."""
+def gpu_solutions(n, dli, dzc, dzf, dev, k):
+    """The headline RHS solved by the FP64 path and by FP32 + k refinement corrections (the
+    timed schedule), copied to the host ((n3, n2, n1) interiors) for the comparison with the
+    oracle in the CPU leg"""
+    import torch
+    from cans_gb300 import cans
+    out = {}
+    plan = cans.Plan(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc")
+    p = make_rhs(n, dzf, dev)
+    plan.solve(p)
+    out["fp64_path"] = p[1:-1, 1:-1, 1:-1].cpu().numpy()
+    del plan, p
+    torch.cuda.empty_cache()
+    plan = cans.Plan(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc", precision=cans.FP32)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device=dev)
+    p = make_rhs(n, dzf, dev)
+    plan.solve_refined(p, dli, T(1. / dzc), T(1. / dzf), rtol=0.0, max_iter=k)
+    out["fp32_refined"] = p[1:-1, 1:-1, 1:-1].cpu().numpy()
+    del plan, p
+    torch.cuda.empty_cache()
+    return out
+
+
+def bench_cpu(size, steps, warmup, threads=None, gpu=None):
+    """The oracle (CPU restatement of src/solver.f90 with FFTW r2r semantics) on all host
+    cores, solving the GPU arm's right-hand side (host_rhs): mean seconds per solve over
+    `steps` solves after `warmup`.  With `gpu` (gpu_solutions) it also returns the accuracy
+    block: each GPU solution against the oracle's, and every solution against an accuracy
+    reference -- the oracle's solve plus one refinement step with an extended-precision
+    residual (orc_poisson_residual_ld) -- relative L2 of the mean-free parts."""
     from oracle import oracle as O
     if threads:
         O.set_num_threads(threads)
@@ -680,17 +848,40 @@ def bench_cpu(size, steps, warmup, threads=None):
     dli = [1. / x for x in dl]
     dzc, dzf, zc, zf = O.initgrid(1, n[2], 1.4, L_CH[2], False)
     s = O.initsolver(n, dli, 1. / dzc, 1. / dzf, "PPPPNN", [0.] * 6, "ccc")
-    p = O.field(n)
-    rng = np.random.default_rng(20260101)
-    p[1:-1, 1:-1, 1:-1] = rng.standard_normal(n)
+    rhs = O.field(n)
+    rhs[1:-1, 1:-1, 1:-1] = host_rhs(n, dzf).transpose(2, 1, 0)
+    solve = lambda q: O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], "PPPPNN", "ccc", q)
     times = []
+    p = None
     for it in range(warmup + steps):
+        p = rhs.copy(order="F")
         t0 = time.perf_counter()
-        O.solver(n, s["normfft"], s["lambdaxy"], s["a"], s["b"], s["c"], "PPPPNN", "ccc", p)
+        solve(p)
         if it >= warmup:
             times.append(time.perf_counter() - t0)
     sec = float(np.mean(times))
-    return sec, O.num_threads()
+    acc = None
+    if gpu is not None:
+        i3 = (slice(1, -1),) * 3
+        xo = p[i3].transpose(2, 1, 0)  # (n3, n2, n1) view
+        e = O.field(n)
+        e[i3] = O.poisson_residual_ld(n, dli, "PPPPNN", s["a"], s["b"], s["c"], p, rhs)
+        solve(e)
+        xt = xo + e[i3].transpose(2, 1, 0)
+        del e
+        w = dzf[1:-1][:, None, None]
+        wsum = w.sum() * n[0] * n[1]
+        dm = lambda f: f - (f * w).sum() / wsum
+        xt_m, xo_m = dm(xt), dm(xo)
+        nt, no = np.linalg.norm(xt_m), np.linalg.norm(xo_m)
+        acc = {"reference": "oracle FP64 solve + one refinement step with an extended-precision residual",
+               "metric": "relative L2 of the volume-weighted mean-free parts",
+               "oracle_fp64_vs_reference": float(np.linalg.norm(xo_m - xt_m) / nt)}
+        for name, x in gpu.items():
+            xm = dm(x)
+            acc[f"{name}_vs_oracle"] = float(np.linalg.norm(xm - xo_m) / no)
+            acc[f"{name}_vs_reference"] = float(np.linalg.norm(xm - xt_m) / nt)
+    return sec, O.num_threads(), acc
 
 
 def main():
@@ -711,7 +902,8 @@ def main():
     ap.add_argument("--skip-adjoint", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=50)
     ap.add_argument("--adjoint-dirs", type=int, default=8)
-    ap.add_argument("--only", choices=["refined", "rk3", "adjoint", "boxes", "mx", "ch"], default=None,
+    ap.add_argument("--only", choices=["refined", "rk3", "rk3-fp32", "fp32-solve", "adjoint", "boxes", "mx",
+                                       "mx-run", "ch"], default=None,
                     help="profiling aid: run one secondary leg and print its JSON")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -719,16 +911,16 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        sec, cores = bench_cpu(args.size, args.steps, min(args.warmup, 1))
+        sec, cores, _ = bench_cpu(args.size, args.steps, min(args.warmup, 1))
         val = 1.0 / sec
         out = {"metric": METRIC, "impl": "reference", "value": round(val, 5), "unit": "solves/s", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 2),
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-               "data": "synthetic (seeded N(0,1) RHS)",
-               "config": {"workload": f"poisson_{args.size}x{args.size}x{args.size}_PPPPNN_fp32_refined_to_fp64_accuracy",
+               "data": "synthetic (seeded N(0,1) RHS, volume-weighted mean removed; the GPU arm's values)",
+               "config": {"workload": f"poisson_{args.size}x{args.size}x{args.size}_PPPPNN",
                           "grid": [args.size] * 3, "bc_pressure": "PP,PP,NN", "z_grid": "tanh gr=1.4",
                           "domain": [round(x, 6) for x in L_CH],
-                          "precision": "the reference's FP64 solve (the accuracy the GPU arm matches)"},
+                          "precision": "FP64 solve (the reference's CPU solver, src/solver.f90)"},
                "cpu_baseline": {"value": round(val, 5), "unit": "solves/s", "cores": cores, "kind": "port",
                                 "sample": f"{args.steps} full {args.size}^3 solves of the C/OpenMP restatement "
                                           "of src/solver.f90 (reference Fortran/MPI/FFTW build unavailable)"},
@@ -741,10 +933,14 @@ def main():
     out = bench_ours(args, rank, world)
     if rank == 0:
         if not args.skip_cpu:
-            sec, cores = bench_cpu(args.size, 1, 0)
+            sols = out.pop("_gpu_solutions", None)
+            sec, cores, acc = bench_cpu(args.size, 3, 1, gpu=sols)
             out["cpu_baseline"] = {"value": round(1.0 / sec, 5), "unit": "solves/s", "cores": cores, "kind": "port",
-                                   "sample": f"1 full {args.size}^3 solve of the C/OpenMP restatement of "
-                                             "src/solver.f90 on the host cores"}
+                                   "sample": f"3 full {args.size}^3 FP64 solves (after 1 warm-up) of the C/OpenMP "
+                                             "restatement of src/solver.f90 on the host cores, same RHS"}
+            if acc is not None:
+                out["accuracy_vs_oracle"] = acc
+        out.pop("_gpu_solutions", None)
         print(json.dumps(out))
     if world > 1:
         import torch

@@ -124,6 +124,19 @@ def _setup(L):
     L.cans_boxes_step.argtypes = [_V, C.c_int]
     L.cans_boxes_graph_nodes.argtypes = [_V]
     L.cans_boxes_graph_nodes.restype = C.c_longlong
+    # the FP32 run
+    L.cans_fillps_f32.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
+    L.cans_correc_f32.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
+    L.cans_updatep_f32.argtypes = [_I, _D, _V, _V, C.c_double, C.c_int, _V, _V, _V]
+    L.cans_rk_f32.argtypes = [_D, _I, _D, _V, _V, _V, _V, C.c_double, C.c_double, _V, _I, _D, _D, C.c_int,
+                              _V, _V, _V, _V, _V, _V, _V, _V, _V, _D, _V, _V]
+    L.cans_rk_f32_work_bytes.argtypes = [_I, C.c_int]
+    L.cans_rk_f32_work_bytes.restype = C.c_size_t
+    L.cans_bounduvw_f32.argtypes = L.cans_bounduvw.argtypes
+    L.cans_boundp_f32.argtypes = L.cans_boundp.argtypes
+    L.cans_chkdiv_f32.argtypes = L.cans_chkdiv.argtypes
+    L.cans_chkdt_f32.argtypes = L.cans_chkdt.argtypes
+    L.cans_bulk_mean_f32.argtypes = L.cans_bulk_mean.argtypes
 
 
 def _check(rc, where):
@@ -516,3 +529,76 @@ def rk_scal(rkpar, n, dli, dzci, dzfi, gvr_f, alpha, dt, u, v, w, is_forced, sca
 def bulk_forcing_s(n, is_forced, f, s, stream=None):
     _check(lib().cans_bulk_forcing_s(_ints(n), int(is_forced), float(f), _ptr(s), _stream(stream)),
            "cans_bulk_forcing_s")
+
+
+# ------------------------------------------------------------------------------ the FP32 run
+# The same routines on float32 fields and float32 device grid arrays; pp stays float64 (the
+# refined solve's right-hand side and solution).
+def fillps_f32(n, dli, dzfi, dti, u, v, w, p, stream=None):
+    _check(lib().cans_fillps_f32(_ints(n), _dbls(dli), _ptr(dzfi), float(dti), _ptr(u), _ptr(v), _ptr(w), _ptr(p),
+                                 _stream(stream)), "cans_fillps_f32")
+
+
+def correc_f32(n, dli, dzci, dt, p, u, v, w, stream=None):
+    _check(lib().cans_correc_f32(_ints(n), _dbls(dli), _ptr(dzci), float(dt), _ptr(p), _ptr(u), _ptr(v), _ptr(w),
+                                 _stream(stream)), "cans_correc_f32")
+
+
+def updatep_f32(n, dli, dzci, dzfi, alpha, is_impdiff, pp, p, stream=None):
+    _check(lib().cans_updatep_f32(_ints(n), _dbls(dli), _ptr(dzci), _ptr(dzfi), float(alpha), int(is_impdiff),
+                                  _ptr(pp), _ptr(p), _stream(stream)), "cans_updatep_f32")
+
+
+def rk_f32_work(n, in_place=False, device="cuda"):
+    import torch
+    nb = int(lib().cans_rk_f32_work_bytes(_ints(n), int(bool(in_place))))
+    return torch.empty(nb, dtype=torch.uint8, device=device)
+
+
+def rk_f32(rkpar, n, dli, dzci, dzfi, gvr_c, gvr_f, dt, visc, p, is_forced, velf, bforce, dudtrko, dvdtrko,
+           dwdtrko, u, v, w, unew, vnew, wnew, work, stream=None):
+    """rk + mom_xyz_ad on FP32 fields; out of place into (unew, vnew, wnew) unless they are u, v, w"""
+    f = (C.c_double * 3)()
+    _check(lib().cans_rk_f32(_dbls(rkpar), _ints(n), _dbls(dli), _ptr(dzci), _ptr(dzfi), _ptr(gvr_c), _ptr(gvr_f),
+                             float(dt), float(visc), _ptr(p), _ints(is_forced), _dbls(velf), _dbls(bforce), 0,
+                             _ptr(dudtrko), _ptr(dvdtrko), _ptr(dwdtrko), _ptr(u), _ptr(v), _ptr(w), _ptr(unew),
+                             _ptr(vnew), _ptr(wnew), f, _ptr(work), _stream(stream)), "cans_rk_f32")
+    return np.array(list(f))
+
+
+def bounduvw_f32(cbc, n, bc, is_bound, dl, dzc_h, dzf_h, u, v, w, keep_norm=False, halos_norm=HALO_BOTH,
+                 halos_tang=HALO_BOTH, stream=None):
+    dzc_h, pc = _hp(dzc_h)
+    dzf_h, pf = _hp(dzf_h)
+    _check(lib().cans_bounduvw_f32(_chars(cbc), _ints(n), _dbls(bc), _ints(is_bound), _dbls(dl), pc, pf, _ptr(u),
+                                   _ptr(v), _ptr(w), int(keep_norm), int(halos_norm), int(halos_tang),
+                                   _stream(stream)), "cans_bounduvw_f32")
+
+
+def boundp_f32(cbc, n, bc, is_bound, dl, dzc_h, p, halo_side=HALO_BOTH, stream=None):
+    dzc_h, pc = _hp(dzc_h)
+    _check(lib().cans_boundp_f32(_chars(cbc), _ints(n), _dbls(bc), _ints(is_bound), _dbls(dl), pc, _ptr(p),
+                                 int(halo_side), _stream(stream)), "cans_boundp_f32")
+
+
+def chkdiv_f32(n, l, dli, dzfi, u, v, w, stream=None, allow_nonfinite=False):
+    a, b = C.c_double(), C.c_double()
+    rc = lib().cans_chkdiv_f32(_ints(n), _dbls(l), _dbls(dli), _ptr(dzfi), _ptr(u), _ptr(v), _ptr(w), C.byref(a),
+                               C.byref(b), _stream(stream))
+    if not (allow_nonfinite and rc == ENONFINITE):
+        _check(rc, "cans_chkdiv_f32")
+    return a.value, b.value
+
+
+def chkdt_f32(n, dl, dzci, dzfi, visc, alpha, is_impdiff, is_impdiff_1d, u, v, w, stream=None):
+    r = C.c_double()
+    _check(lib().cans_chkdt_f32(_ints(n), _dbls(dl), _ptr(dzci), _ptr(dzfi), float(visc), float(alpha),
+                                int(is_impdiff), int(is_impdiff_1d), _ptr(u), _ptr(v), _ptr(w), C.byref(r),
+                                _stream(stream)), "cans_chkdt_f32")
+    return r.value
+
+
+def bulk_mean_f32(n, gvr, p, stream=None):
+    r = C.c_double()
+    _check(lib().cans_bulk_mean_f32(_ints(n), _ptr(gvr), _ptr(p), C.byref(r), _stream(stream)), "cans_bulk_mean_f32")
+    return r.value

@@ -67,8 +67,10 @@ __global__ void __launch_bounds__(kTB) k_boxes_cells(const BoxK *__restrict__ bo
     const BoxK &b = box[s];
     const long t = (blk - __ldg(&start[s])) * kTB + threadIdx.x;
     if (OP == OP_MOM) {
-      mom_rk_cell(b.d, b.dxi, b.dyi, b.visc, b.f1[irk], b.f2[irk], b.f12[irk], b.bf[0], b.bf[1], b.bf[2], b.impdiff,
-                  b.dzci, b.dzfi, b.u, b.v, b.w, b.p, b.dudtrko, b.dvdtrko, b.dwdtrko, b.unew, b.dtd, t);
+      const size_t np = (size_t)b.d.n1 * b.d.n2 * b.d.n3;
+      mom_rk_cell<double>(b.d, b.dxi, b.dyi, b.visc, b.f1[irk], b.f2[irk], b.f12[irk], b.bf[0], b.bf[1], b.bf[2],
+                          b.impdiff, b.dzci, b.dzfi, b.u, b.v, b.w, b.p, b.dudtrko, b.dvdtrko, b.dwdtrko, b.unew,
+                          b.unew + np, b.unew + 2 * np, b.dtd, t);
     } else if (OP == OP_WRITEBACK) {
       // rk.f90 write-back, then (implicit diffusion) u = (u - f12/2 dudtd) + f with f = 0
       // (no forcing): the expressions of k_rk_writeback and k_rk_forcing, fused

@@ -95,8 +95,10 @@ __global__ void __launch_bounds__(kTB) k_mom_rk(Dims d, double dxi, double dyi, 
                                                 double *__restrict__ dwdtrko, double *__restrict__ unew,
                                                 double *__restrict__ dtd, const double *__restrict__ sb, double gbx,
                                                 double gby, double gbz, double beta) {
-  mom_rk_cell(d, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, impdiff, dzci, dzfi, u, v, w, p, dudtrko, dvdtrko, dwdtrko,
-              unew, dtd, (long)blockIdx.x * blockDim.x + threadIdx.x, sb, gbx, gby, gbz, beta);
+  const size_t np = (size_t)d.n1 * d.n2 * d.n3;
+  mom_rk_cell<double>(d, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, impdiff, dzci, dzfi, u, v, w, p, dudtrko,
+                      dvdtrko, dwdtrko, unew, unew + np, unew + 2 * np, dtd,
+                      (long)blockIdx.x * blockDim.x + threadIdx.x, sb, gbx, gby, gbz, beta);
 }
 
 // copy-back of the new velocity with the per-block partial sums of the bulk means
@@ -398,58 +400,118 @@ extern "C" int cans_bulk_forcing_s(const int n[3], int is_forced, double f, doub
 }
 
 // ------------------------------------------------------------------------------ boundaries
-// periodic self-exchange (one GPU) along dir 1 (y) or 2 (z): full extent of the other dims
-__global__ void k_halo_copy(double *p, int n1, int n2, int n3, int dir, int up, int lo) {
-  halo_copy_cell(p, n1, n2, n3, dir, up, lo, (long)blockIdx.x * blockDim.x + threadIdx.x);
-}
+// The face operations of bounduvw / boundp (bound_ops.h, in the reference's order) run as
+// phases: consecutive operations of the same kind and direction -- the y halo copies of all
+// components, the z halo copies, the set_bc of x (both sides, all components), of y, of z --
+// write disjoint cells and read only cells no other operation of the phase writes (for every
+// extent >= 3), so one launch covers a phase and the phases keep the reference's order
+// (edges and corners are filled by the later phases from the earlier ones' ghosts).
+// Extents below 3 fall back to one launch per operation.
+namespace {
+constexpr int kPhaseOps = 12;
+template <typename T> struct BcPhase {
+  int nops, n1, n2, n3;
+  T *f[kPhaseOps];
+  long start[kPhaseOps + 1];  // prefix sums of the operations' cells
+  int op[kPhaseOps], dir[kPhaseOps], ib[kPhaseOps], centered[kPhaseOps], up[kPhaseOps], lo[kPhaseOps];
+  char ctype[kPhaseOps];
+  T factor[kPhaseOps], sgn[kPhaseOps];
+};
 
-// set_bc (src/bound.f90:182-463), nh = 1
-__global__ void k_set_bc(double *p, int n1, int n2, int n3, char ctype, int ib, int dir, int centered, double factor,
-                         double sgn) {
-  set_bc_cell(p, n1, n2, n3, ctype, ib, dir, centered, factor, sgn, (long)blockIdx.x * blockDim.x + threadIdx.x);
-}
-
-static int launch_op(double *p, const int n[3], const BcOp &o, cudaStream_t st) {
-  const unsigned g = blocks_for(bc_op_cells(o, n));
-  if (o.op == 0)
-    k_set_bc<<<g, kTB, 0, st>>>(p, n[0], n[1], n[2], o.ctype, o.ib, o.dir, o.centered, o.factor, o.sgn);
+template <typename T> __global__ void __launch_bounds__(kTB) k_bc_phase(const BcPhase<T> ph) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ph.start[ph.nops]) return;
+  int o = 0;
+  while (t >= ph.start[o + 1]) o++;
+  const long tl = t - ph.start[o];
+  if (ph.op[o] == 0)
+    set_bc_cell<T>(ph.f[o], ph.n1, ph.n2, ph.n3, ph.ctype[o], ph.ib[o], ph.dir[o], ph.centered[o], ph.factor[o],
+                   ph.sgn[o], tl);
   else
-    k_halo_copy<<<g, kTB, 0, st>>>(p, n[0], n[1], n[2], o.dir, o.up, o.lo);
-  CANS_LAUNCH_CHECK();
+    halo_copy_cell<T>(ph.f[o], ph.n1, ph.n2, ph.n3, ph.dir[o], ph.up[o], ph.lo[o], tl);
+}
+
+template <typename T> int run_bc_ops(const std::vector<BcOp> &ops, T *const *fields, const int n[3], cudaStream_t st) {
+  const bool grouped = n[0] >= 3 && n[1] >= 3 && n[2] >= 3;
+  size_t a = 0;
+  while (a < ops.size()) {
+    size_t b = a + 1;
+    if (grouped)
+      while (b < ops.size() && b - a < (size_t)kPhaseOps && ops[b].op == ops[a].op && ops[b].dir == ops[a].dir) b++;
+    BcPhase<T> ph;
+    memset(&ph, 0, sizeof(ph));
+    ph.nops = (int)(b - a);
+    ph.n1 = n[0]; ph.n2 = n[1]; ph.n3 = n[2];
+    ph.start[0] = 0;
+    for (size_t q = a; q < b; q++) {
+      const int e = (int)(q - a);
+      const BcOp &o = ops[q];
+      ph.f[e] = fields[o.field];
+      ph.op[e] = o.op; ph.dir[e] = o.dir; ph.ib[e] = o.ib; ph.centered[e] = o.centered;
+      ph.up[e] = o.up; ph.lo[e] = o.lo; ph.ctype[e] = o.ctype;
+      ph.factor[e] = (T)o.factor; ph.sgn[e] = (T)o.sgn;
+      ph.start[e + 1] = ph.start[e] + bc_op_cells(o, n);
+    }
+    k_bc_phase<T><<<blocks_for(ph.start[ph.nops]), kTB, 0, st>>>(ph);
+    CANS_LAUNCH_CHECK();
+    a = b;
+  }
   return CANS_OK;
 }
 
-static bool bc_char_ok(char c) { return c == 'P' || c == 'D' || c == 'N'; }
+bool bc_char_ok(char c) { return c == 'P' || c == 'D' || c == 'N'; }
 
 // bounduvw, one GPU with x-aligned pencils (is_bound in x always true; periodic y/z
 // ghosts are local copies): CPU-path order of src/bound.f90:17-122
-extern "C" int cans_bounduvw(const char cbc[18], const int n[3], const double bc[18], const int is_bound[6],
-                             const double dl[3], const double *dzc, const double *dzf, double *u, double *v,
-                             double *w, int keep_norm, int halos_norm, int halos_tang, void *stream) {
+template <typename T>
+int bounduvw_impl(const char cbc[18], const int n[3], const double bc[18], const int is_bound[6], const double dl[3],
+                  const double *dzc, const double *dzf, T *u, T *v, T *w, int keep_norm, int halos_norm,
+                  int halos_tang, void *stream) {
   if (!cbc || !n || !bc || !is_bound || !dl || !dzc || !dzf || !u || !v || !w) return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   for (int e = 0; e < 18; e++) if (!bc_char_ok(cbc[e])) return CANS_EINVAL;
   std::vector<BcOp> ops;
   bounduvw_ops(cbc, n, bc, is_bound, dl, dzc, dzf, keep_norm, halos_norm, halos_tang, ops);
-  double *f[3] = {u, v, w};
-  for (const BcOp &o : ops) {
-    const int rc = launch_op(f[o.field], n, o, as_stream(stream));
-    if (rc) return rc;
-  }
-  return CANS_OK;
+  T *f[3] = {u, v, w};
+  return run_bc_ops<T>(ops, f, n, as_stream(stream));
 }
 
 // boundp (src/bound.f90:124-180)
-extern "C" int cans_boundp(const char cbc[6], const int n[3], const double bc[6], const int is_bound[6],
-                           const double dl[3], const double *dzc, double *p, int halo_side, void *stream) {
+template <typename T>
+int boundp_impl(const char cbc[6], const int n[3], const double bc[6], const int is_bound[6], const double dl[3],
+                const double *dzc, T *p, int halo_side, void *stream) {
   if (!cbc || !n || !bc || !is_bound || !dl || !dzc || !p) return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   for (int e = 0; e < 6; e++) if (!bc_char_ok(cbc[e])) return CANS_EINVAL;
   std::vector<BcOp> ops;
   boundp_ops(cbc, n, bc, is_bound, dl, dzc, halo_side, ops);
-  for (const BcOp &o : ops) {
-    const int rc = launch_op(p, n, o, as_stream(stream));
-    if (rc) return rc;
-  }
-  return CANS_OK;
+  T *f[1] = {p};
+  return run_bc_ops<T>(ops, f, n, as_stream(stream));
+}
+}  // namespace
+
+extern "C" int cans_bounduvw(const char cbc[18], const int n[3], const double bc[18], const int is_bound[6],
+                             const double dl[3], const double *dzc, const double *dzf, double *u, double *v,
+                             double *w, int keep_norm, int halos_norm, int halos_tang, void *stream) {
+  return bounduvw_impl<double>(cbc, n, bc, is_bound, dl, dzc, dzf, u, v, w, keep_norm, halos_norm, halos_tang,
+                               stream);
+}
+
+extern "C" int cans_bounduvw_f32(const char cbc[18], const int n[3], const double bc[18], const int is_bound[6],
+                                 const double dl[3], const double *dzc, const double *dzf, float *u, float *v,
+                                 float *w, int keep_norm, int halos_norm, int halos_tang, void *stream) {
+  return bounduvw_impl<float>(cbc, n, bc, is_bound, dl, dzc, dzf, u, v, w, keep_norm, halos_norm, halos_tang,
+                              stream);
+}
+
+extern "C" int cans_boundp(const char cbc[6], const int n[3], const double bc[6], const int is_bound[6],
+                           const double dl[3], const double *dzc, double *p, int halo_side, void *stream) {
+  return boundp_impl<double>(cbc, n, bc, is_bound, dl, dzc, p, halo_side, stream);
+}
+
+extern "C" int cans_boundp_f32(const char cbc[6], const int n[3], const double bc[6], const int is_bound[6],
+                               const double dl[3], const double *dzc, float *p, int halo_side, void *stream) {
+  return boundp_impl<float>(cbc, n, bc, is_bound, dl, dzc, p, halo_side, stream);
 }
 
 int cans_rhsb_add(const char c_or_f[3], const char cbc[6], const int n[3], const int is_bound[6],

@@ -1,0 +1,477 @@
+// The FP32 run: projection, momentum and reduction kernels with FP32 fields, the form of
+// the reference's single-precision build (src/types.f90:12-18, rp = sp) in which the
+// pressure correction pp stays FP64 -- it is the input and output of the FP64-accurate
+// refined solve (cans_solver_refined).  The per-cell arithmetic is the FP64 kernels'
+// (stencil_body.cuh, same operation order) in float; pp enters through the integer-pipe
+// splits of fpconv.cuh (GB300 runs double<->float conversions on its FP64 unit, 1/58 of the
+// FP32 rate), and the global sums accumulate per-warp FP32 partial sums in FP64.
+//
+//   fillps    src/fillps.f90:13-51       (FP32 divergence, written widened into FP64 pp)
+//   correc    src/correc.f90:13-60       (gradient of the FP64 pp as a hi/lo float pair)
+//   updatep   src/updatep.f90:14-88      (explicit form)
+//   rk        src/rk.f90:24-333 + mom_xyz_ad src/mom.f90:771-1019 (out of place or in place)
+//   checks    src/chkdiv.f90, src/chkdt.f90, src/utils.f90
+#include <math.h>
+#include <string.h>
+
+#include <cfloat>
+#include <mutex>
+#include <vector>
+
+#include "cans_internal.cuh"
+#include "fpconv.cuh"
+#include "stencil_body.cuh"
+
+namespace {
+constexpr int kTB = 256;
+unsigned blocks_for(long count, int tb = kTB) { return (unsigned)((count + tb - 1) / tb); }
+
+// FP64 sum over a block of per-thread FP32 values: FP32 warp sums, widened exactly, then
+// added in FP64 by warp 0 (the block total in lane 0 of warp 0)
+template <int NC> __device__ __forceinline__ void block_sum_f64(float (&v)[NC], double (&out)[NC]) {
+  __shared__ double red[NC][kTB / 32];
+  for (int c = 0; c < NC; c++)
+    for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int c = 0; c < NC; c++) red[c][wid] = f2d(v[c]);
+  __syncthreads();
+  for (int c = 0; c < NC; c++) {
+    double s = 0.;
+    if (threadIdx.x == 0)
+      for (int q = 0; q < kTB / 32; q++) s += red[c][q];
+    out[c] = s;
+  }
+}
+}  // namespace
+
+// ------------------------------------------------------------------------------ fillps
+__global__ void __launch_bounds__(kTB) k_fillps32(Dims d, float dti, float dtidxi, float dtidyi,
+                                                  const float *__restrict__ dzfi, const float *__restrict__ u,
+                                                  const float *__restrict__ v, const float *__restrict__ w,
+                                                  double *__restrict__ p) {
+  int i, j, k;
+  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t c = hidx(i, j, k, n1, n2);
+  const float r = ((w[c] - w[hidx(i, j, k - 1, n1, n2)]) * dti * dzfi[k] + (v[c] - v[hidx(i, j - 1, k, n1, n2)]) * dtidyi) +
+                  (u[c] - u[hidx(i - 1, j, k, n1, n2)]) * dtidxi;
+  p[c] = f2d(r);
+}
+
+extern "C" int cans_fillps_f32(const int n[3], const double dli[3], const float *dzfi, double dti, const float *u,
+                               const float *v, const float *w, double *p, void *stream) {
+  if (!n || !dli || !dzfi || !u || !v || !w || !p || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  Dims d{n[0], n[1], n[2]};
+  const long cnt = (long)n[0] * n[1] * n[2];
+  k_fillps32<<<blocks_for(cnt), kTB, 0, as_stream(stream)>>>(d, (float)dti, (float)(dti * dli[0]),
+                                                              (float)(dti * dli[1]), dzfi, u, v, w, p);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ correc
+// u -= dt*dxi*(pp(i+1) - pp(i)) with the FP64 difference taken on hi/lo float pairs: the hi
+// parts of neighbouring values differ by far less than a factor 2 on a resolved field, so
+// their difference is exact and the result matches the rounded FP64 difference to ~1 ulp
+__device__ __forceinline__ float ddiff(double a, float bh, float bl) {
+  float ah, al;
+  d2f_split(a, ah, al);
+  return (ah - bh) + (al - bl);
+}
+
+__global__ void __launch_bounds__(kTB) k_correc32(Dims d, float fi, float fj, float dt,
+                                                  const float *__restrict__ dzci, const double *__restrict__ p,
+                                                  float *__restrict__ u, float *__restrict__ v,
+                                                  float *__restrict__ w) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long nx = d.n1 + 2, ny = d.n2 + 2;
+  if (t >= nx * ny * (d.n3 + 2)) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / (nx * ny));
+  const int n1 = d.n1, n2 = d.n2;
+  const size_t c = (size_t)t;
+  float ph, pl;
+  d2f_split(p[c], ph, pl);
+  if (i <= d.n1) u[c] = u[c] - fi * ddiff(p[c + 1], ph, pl);
+  if (j <= d.n2) v[c] = v[c] - fj * ddiff(p[hidx(i, j + 1, k, n1, n2)], ph, pl);
+  if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * ddiff(p[hidx(i, j, k + 1, n1, n2)], ph, pl);
+}
+
+extern "C" int cans_correc_f32(const int n[3], const double dli[3], const float *dzci, double dt, const double *p,
+                               float *u, float *v, float *w, void *stream) {
+  if (!n || !dli || !dzci || !p || !u || !v || !w || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  Dims d{n[0], n[1], n[2]};
+  const long cnt = (long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+  k_correc32<<<blocks_for(cnt), kTB, 0, as_stream(stream)>>>(d, (float)(dt * dli[0]), (float)(dt * dli[1]),
+                                                              (float)dt, dzci, p, u, v, w);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ updatep
+__global__ void __launch_bounds__(kTB) k_updatep32(Dims d, const double *__restrict__ pp, float *__restrict__ p) {
+  int i, j, k;
+  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const size_t c = hidx(i, j, k, d.n1, d.n2);
+  p[c] = p[c] + d2f_rn(pp[c]);
+}
+
+extern "C" int cans_updatep_f32(const int n[3], const double dli[3], const float *dzci, const float *dzfi,
+                                double alpha, int is_impdiff, const double *pp, float *p, void *stream) {
+  (void)alpha;
+  if (!n || !dli || !dzci || !dzfi || !pp || !p || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  if (is_impdiff) return CANS_ENOTSUP;  // the FP32 run has explicit diffusion only
+  Dims d{n[0], n[1], n[2]};
+  k_updatep32<<<blocks_for((long)n[0] * n[1] * n[2]), kTB, 0, as_stream(stream)>>>(d, pp, p);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ momentum
+// mom_xyz_ad + RK update with the new velocity written to haloed arrays (the second velocity
+// buffer, or the library scratch of the in-place call); with `partials` each block also
+// writes the FP64 sums of gvr_f*u_new, gvr_f*v_new, gvr_c*w_new (the bulk means of
+// src/utils.f90:15-42) to partials[3*block + c]
+__global__ void __launch_bounds__(kTB) k_mom_rk32(Dims d, float dxi, float dyi, float visc, float f1, float f2,
+                                                  float f12, float bfx, float bfy, float bfz,
+                                                  const float *__restrict__ dzci, const float *__restrict__ dzfi,
+                                                  const float *__restrict__ u, const float *__restrict__ v,
+                                                  const float *__restrict__ w, const float *__restrict__ p,
+                                                  float *__restrict__ dudtrko, float *__restrict__ dvdtrko,
+                                                  float *__restrict__ dwdtrko, float *__restrict__ un,
+                                                  float *__restrict__ vn, float *__restrict__ wn,
+                                                  const float *__restrict__ gvr_c, const float *__restrict__ gvr_f,
+                                                  double *__restrict__ partials) {
+  float nv[3] = {0.f, 0.f, 0.f};
+  int k = 0;
+  const bool in = mom_rk_cell<float, true>(d, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, 0, dzci, dzfi, u, v, w, p,
+                                           dudtrko, dvdtrko, dwdtrko, un, vn, wn, nullptr,
+                                           (long)blockIdx.x * blockDim.x + threadIdx.x, nullptr, 0.f, 0.f, 0.f,
+                                           0.f, nv, &k);
+  if (!partials) return;  // uniform over the grid
+  float s[3] = {0.f, 0.f, 0.f};
+  if (in) {
+    s[0] = nv[0] * gvr_f[k];
+    s[1] = nv[1] * gvr_f[k];
+    s[2] = nv[2] * gvr_c[k];
+  }
+  double tot[3];
+  block_sum_f64<3>(s, tot);
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; c++) partials[(size_t)blockIdx.x * 3 + c] = tot[c];
+}
+
+// bulk means (FP64 sums of the block partials) and the forcing f_c = velf_c - mean_c of
+// rk.f90:310-326: fout[0..2] in FP64, fout[3..5] as floats (read by every forcing thread)
+__global__ void k_rk_means32(const double *__restrict__ partials, long nblk, double vfx, double vfy, double vfz,
+                             int fx, int fy, int fz, double *__restrict__ fout) {
+  __shared__ double red[kTB];
+  const double vf[3] = {vfx, vfy, vfz};
+  const int on[3] = {fx, fy, fz};
+  for (int c = 0; c < 3; c++) {
+    double s = 0.;
+    for (long b = threadIdx.x; b < nblk; b += blockDim.x) s += partials[(size_t)b * 3 + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const double f = on[c] ? vf[c] - red[0] : 0.;
+      fout[c] = f;
+      reinterpret_cast<float *>(fout + 3)[c] = (float)f;
+    }
+    __syncthreads();
+  }
+}
+
+// u += f (explicit diffusion) on the interior of the new velocity
+__global__ void __launch_bounds__(kTB) k_rk_forcing32(Dims d, const double *__restrict__ fout, int fx, int fy, int fz,
+                                                      float *__restrict__ u, float *__restrict__ v,
+                                                      float *__restrict__ w) {
+  int i, j, k;
+  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const float *ff = reinterpret_cast<const float *>(fout + 3);
+  const size_t c = hidx(i, j, k, d.n1, d.n2);
+  if (fx) u[c] = u[c] + ff[0];
+  if (fy) v[c] = v[c] + ff[1];
+  if (fz) w[c] = w[c] + ff[2];
+}
+
+// in-place form: copy the interior of the new velocity back
+__global__ void __launch_bounds__(kTB) k_copy_interior32(Dims d, const float *__restrict__ un,
+                                                         const float *__restrict__ vn, const float *__restrict__ wn,
+                                                         float *__restrict__ u, float *__restrict__ v,
+                                                         float *__restrict__ w) {
+  int i, j, k;
+  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const size_t c = hidx(i, j, k, d.n1, d.n2);
+  u[c] = un[c]; v[c] = vn[c]; w[c] = wn[c];
+}
+
+extern "C" size_t cans_rk_f32_work_bytes(const int n[3], int in_place) {
+  if (!n) return 0;
+  const size_t nh = (size_t)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+  const size_t nblk = blocks_for((long)n[0] * n[1] * n[2]);
+  size_t b = (3 * nblk + 8) * sizeof(double);
+  b = (b + 255) & ~(size_t)255;
+  return b + (in_place ? 3 * nh * sizeof(float) : 0);
+}
+
+extern "C" int cans_rk_f32(const double rkpar[2], const int n[3], const double dli[3], const float *dzci,
+                           const float *dzfi, const float *gvr_c, const float *gvr_f, double dt, double visc,
+                           const float *p, const int is_forced[3], const double velf[3], const double bforce[3],
+                           int is_impdiff, float *dudtrko, float *dvdtrko, float *dwdtrko, float *u, float *v,
+                           float *w, float *unew, float *vnew, float *wnew, double f[3], void *work, void *stream) {
+  if (!rkpar || !n || !dli || !dzci || !dzfi || !gvr_c || !gvr_f || !p || !is_forced || !velf || !bforce ||
+      !dudtrko || !dvdtrko || !dwdtrko || !u || !v || !w || !unew || !vnew || !wnew || !work)
+    return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  if (is_impdiff) return CANS_ENOTSUP;  // the FP32 run has explicit diffusion only
+  const bool in_place = unew == u;
+  if (in_place != (vnew == v) || in_place != (wnew == w)) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const long np = (long)n[0] * n[1] * n[2];
+  const unsigned nblk = blocks_for(np);
+  const bool forced = is_forced[0] || is_forced[1] || is_forced[2];
+  // work: partials (3 nblk) + f (3 doubles + 3 floats) doubles, then (in place) three haloed buffers
+  double *partials = static_cast<double *>(work), *fdev = partials + 3 * (size_t)nblk;
+  size_t off = ((3 * (size_t)nblk + 8) * sizeof(double) + 255) & ~(size_t)255;
+  const size_t nh = (size_t)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+  float *un = unew, *vn = vnew, *wn = wnew;
+  if (in_place) {
+    un = reinterpret_cast<float *>(static_cast<char *>(work) + off);
+    vn = un + nh;
+    wn = vn + nh;
+  }
+  const float f1 = (float)(rkpar[0] * dt), f2 = (float)(rkpar[1] * dt), f12 = (float)((rkpar[0] + rkpar[1]) * dt);
+  k_mom_rk32<<<nblk, kTB, 0, st>>>(d, (float)dli[0], (float)dli[1], (float)visc, f1, f2, f12, (float)bforce[0],
+                                    (float)bforce[1], (float)bforce[2], dzci, dzfi, u, v, w, p, dudtrko, dvdtrko,
+                                    dwdtrko, un, vn, wn, gvr_c, gvr_f, forced ? partials : nullptr);
+  CANS_LAUNCH_CHECK();
+  if (in_place) {
+    k_copy_interior32<<<nblk, kTB, 0, st>>>(d, un, vn, wn, u, v, w);
+    CANS_LAUNCH_CHECK();
+  }
+  if (forced) {
+    k_rk_means32<<<1, kTB, 0, st>>>(partials, nblk, velf[0], velf[1], velf[2], is_forced[0], is_forced[1],
+                                     is_forced[2], fdev);
+    CANS_LAUNCH_CHECK();
+    k_rk_forcing32<<<nblk, kTB, 0, st>>>(d, fdev, is_forced[0], is_forced[1], is_forced[2], unew, vnew, wnew);
+    CANS_LAUNCH_CHECK();
+  }
+  if (f) {
+    f[0] = f[1] = f[2] = 0.;
+    if (forced) {
+      CANS_CUDA_TRY(cudaMemcpyAsync(f, fdev, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CANS_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+  }
+  return CANS_OK;
+}
+
+// ------------------------------------------------------------------------------ reductions
+// Scratch of the FP32 reductions: one buffer per device behind a lock held until the result
+// is on the host (the calls synchronise their stream).
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_red32_mu;
+double *g_red32[kMaxDevices] = {};
+size_t g_red32_n[kMaxDevices] = {};
+int red32_scratch(size_t count, double **out) {
+  int dev = 0;
+  CANS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return CANS_EINVAL;
+  if (g_red32_n[dev] < count) {
+    if (g_red32[dev]) CANS_CUDA_TRY(cudaFree(g_red32[dev]));
+    g_red32[dev] = nullptr;
+    g_red32_n[dev] = 0;
+    CANS_CUDA_TRY(cudaMalloc(&g_red32[dev], count * sizeof(double)));
+    g_red32_n[dev] = count;
+  }
+  *out = g_red32[dev];
+  return CANS_OK;
+}
+
+__global__ void k_sum1(const double *__restrict__ part, long nblk, double *__restrict__ out) {
+  __shared__ double red[kTB];
+  double s = 0.;
+  for (long b = threadIdx.x; b < nblk; b += blockDim.x) s += part[b];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
+}
+
+__global__ void k_max1(const float *__restrict__ part, long nblk, double *__restrict__ out) {
+  __shared__ float red[kTB];
+  float s = 0.f;
+  for (long b = threadIdx.x; b < nblk; b += blockDim.x) s = fmaxf(s, part[b]);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = f2d(red[0]);
+}
+
+// block max of per-thread FP32 values into part[block]
+__device__ __forceinline__ void block_max_f32(float mx, float *__restrict__ part) {
+  __shared__ float rm[kTB / 32];
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) rm[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = 0.f;
+    for (int q = 0; q < kTB / 32; q++) b = fmaxf(b, rm[q]);
+    part[blockIdx.x] = b;
+  }
+}
+}  // namespace
+
+// chkdiv (src/chkdiv.f90:15-54): divergence in FP32, sum in FP64, max exact.  A NaN anywhere
+// makes the sum NaN (fmaxf ignores NaN, as the FP64 kernel's fmax does).
+__global__ void __launch_bounds__(kTB) k_chkdiv32(Dims d, float dxi, float dyi, const float *__restrict__ dzfi,
+                                                  const float *__restrict__ u, const float *__restrict__ v,
+                                                  const float *__restrict__ w, double *__restrict__ part_sum,
+                                                  float *__restrict__ part_max) {
+  int i, j, k;
+  float s[1] = {0.f}, mx = 0.f;
+  if (cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) {
+    const int n1 = d.n1, n2 = d.n2;
+    const size_t c = hidx(i, j, k, n1, n2);
+    const float div = ((w[c] - w[hidx(i, j, k - 1, n1, n2)]) * dzfi[k] + (v[c] - v[hidx(i, j - 1, k, n1, n2)]) * dyi) +
+                      (u[c] - u[c - 1]) * dxi;
+    mx = fabsf(div);
+    s[0] = fabsf(div) / (dxi * dyi * dzfi[k]);
+  }
+  block_max_f32(mx, part_max);
+  double tot[1];
+  block_sum_f64<1>(s, tot);
+  if (threadIdx.x == 0) part_sum[blockIdx.x] = tot[0];
+}
+
+extern "C" int cans_chkdiv_f32(const int n[3], const double l[3], const double dli[3], const float *dzfi,
+                               const float *u, const float *v, const float *w, double *divtot, double *divmax,
+                               void *stream) {
+  if (!n || !l || !dli || !dzfi || !u || !v || !w || !divtot || !divmax) return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const unsigned nblk = blocks_for((long)n[0] * n[1] * n[2]);
+  std::lock_guard<std::mutex> lk(g_red32_mu);
+  double *s;
+  int rc = red32_scratch(2 * (size_t)nblk + 4, &s);
+  if (rc) return rc;
+  float *pm = reinterpret_cast<float *>(s + nblk);
+  k_chkdiv32<<<nblk, kTB, 0, st>>>(d, (float)dli[0], (float)dli[1], dzfi, u, v, w, s, pm);
+  CANS_LAUNCH_CHECK();
+  k_sum1<<<1, kTB, 0, st>>>(s, nblk, s + 2 * nblk);
+  CANS_LAUNCH_CHECK();
+  k_max1<<<1, kTB, 0, st>>>(pm, nblk, s + 2 * nblk + 1);
+  CANS_LAUNCH_CHECK();
+  double h[2];
+  CANS_CUDA_TRY(cudaMemcpyAsync(h, s + 2 * nblk, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaStreamSynchronize(st));
+  *divtot = h[0] / (l[0] * l[1] * l[2]);
+  *divmax = h[1];
+  return (isfinite(*divtot) && isfinite(*divmax)) ? CANS_OK : CANS_ENONFINITE;
+}
+
+// chkdt (src/chkdt.f90:16-78) in FP32
+__global__ void __launch_bounds__(kTB) k_chkdt32(Dims d, float dxi, float dyi, const float *__restrict__ dzci,
+                                                 const float *__restrict__ dzfi, const float *__restrict__ u,
+                                                 const float *__restrict__ v, const float *__restrict__ w,
+                                                 float *__restrict__ part) {
+  int i, j, k;
+  float mx = 0.f;
+  if (cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) {
+    const int n1 = d.n1, n2 = d.n2;
+    auto U = [&](int a, int b, int cc) { return u[hidx(a, b, cc, n1, n2)]; };
+    auto V = [&](int a, int b, int cc) { return v[hidx(a, b, cc, n1, n2)]; };
+    auto W = [&](int a, int b, int cc) { return w[hidx(a, b, cc, n1, n2)]; };
+    const float q = 0.25f;
+    const float ux = fabsf(U(i, j, k));
+    const float vx = q * fabsf(V(i, j, k) + V(i, j - 1, k) + V(i + 1, j, k) + V(i + 1, j - 1, k));
+    const float wx = q * fabsf(W(i, j, k) + W(i, j, k - 1) + W(i + 1, j, k) + W(i + 1, j, k - 1));
+    const float dtix = ux * dxi + vx * dyi + wx * dzfi[k];
+    const float uy = q * fabsf(U(i, j, k) + U(i, j + 1, k) + U(i - 1, j + 1, k) + U(i - 1, j, k));
+    const float vy = fabsf(V(i, j, k));
+    const float wy = q * fabsf(W(i, j, k) + W(i, j + 1, k) + W(i, j + 1, k - 1) + W(i, j, k - 1));
+    const float dtiy = uy * dxi + vy * dyi + wy * dzfi[k];
+    const float uz = q * fabsf(U(i, j, k) + U(i - 1, j, k) + U(i - 1, j, k + 1) + U(i, j, k + 1));
+    const float vz = q * fabsf(V(i, j, k) + V(i, j - 1, k) + V(i, j - 1, k + 1) + V(i, j, k + 1));
+    const float wz = fabsf(W(i, j, k));
+    const float dtiz = uz * dxi + vz * dyi + wz * dzci[k];
+    mx = fmaxf(fmaxf(dtix, dtiy), dtiz);
+  }
+  block_max_f32(mx, part);
+}
+
+extern "C" int cans_chkdt_f32(const int n[3], const double dl[3], const float *dzci, const float *dzfi, double visc,
+                              double alpha, int is_impdiff, int is_impdiff_1d, const float *u, const float *v,
+                              const float *w, double *dtmax, void *stream) {
+  if (!n || !dl || !dzci || !dzfi || !u || !v || !w || !dtmax) return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const unsigned nblk = blocks_for((long)n[0] * n[1] * n[2]);
+  std::lock_guard<std::mutex> lk(g_red32_mu);
+  double *s;
+  int rc = red32_scratch((size_t)nblk + 4, &s);
+  if (rc) return rc;
+  float *pm = reinterpret_cast<float *>(s + 2);
+  k_chkdt32<<<nblk, kTB, 0, st>>>(d, (float)(1. / dl[0]), (float)(1. / dl[1]), dzci, dzfi, u, v, w, pm);
+  CANS_LAUNCH_CHECK();
+  k_max1<<<1, kTB, 0, st>>>(pm, nblk, s);
+  CANS_LAUNCH_CHECK();
+  double dti = 0.;
+  std::vector<float> hz((size_t)n[2] + 2);
+  CANS_CUDA_TRY(cudaMemcpyAsync(&dti, s, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaMemcpyAsync(hz.data(), dzfi, hz.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaStreamSynchronize(st));
+  float dlmin = fminf((float)dl[0], (float)dl[1]);
+  if (!is_impdiff_1d)
+    for (float z : hz) dlmin = fminf(dlmin, 1.f / z);
+  if (dti < FLT_EPSILON) dti = 1.;
+  const float sq3 = sqrtf(3.0f), c165 = 1.65f / 12.0f;  // the reference's literals (single precision)
+  if (is_impdiff && !is_impdiff_1d) *dtmax = (double)(sq3 / (float)dti);
+  else *dtmax = (double)fminf(c165 / fmaxf((float)visc, (float)alpha) * (dlmin * dlmin), sq3 / (float)dti);
+  return CANS_OK;
+}
+
+// bulk_mean (src/utils.f90:15-42): FP32 products, FP64 sum
+__global__ void __launch_bounds__(kTB) k_bulk_mean32(Dims d, const float *__restrict__ gvr,
+                                                     const float *__restrict__ p, double *__restrict__ part) {
+  int i, j, k;
+  float s[1] = {0.f};
+  if (cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) s[0] = p[hidx(i, j, k, d.n1, d.n2)] * gvr[k];
+  double tot[1];
+  block_sum_f64<1>(s, tot);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot[0];
+}
+
+extern "C" int cans_bulk_mean_f32(const int n[3], const float *gvr, const float *p, double *mean, void *stream) {
+  if (!n || !gvr || !p || !mean) return CANS_EINVAL;
+  if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  cudaStream_t st = as_stream(stream);
+  Dims d{n[0], n[1], n[2]};
+  const unsigned nblk = blocks_for((long)n[0] * n[1] * n[2]);
+  std::lock_guard<std::mutex> lk(g_red32_mu);
+  double *s;
+  int rc = red32_scratch((size_t)nblk + 2, &s);
+  if (rc) return rc;
+  k_bulk_mean32<<<nblk, kTB, 0, st>>>(d, gvr, p, s);
+  CANS_LAUNCH_CHECK();
+  k_sum1<<<1, kTB, 0, st>>>(s, nblk, s + nblk);
+  CANS_LAUNCH_CHECK();
+  CANS_CUDA_TRY(cudaMemcpyAsync(mean, s + nblk, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CANS_CUDA_TRY(cudaStreamSynchronize(st));
+  return CANS_OK;
+}

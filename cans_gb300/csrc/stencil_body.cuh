@@ -70,62 +70,68 @@ __device__ __forceinline__ void updatep_cell(const Dims &d, double dxi, double d
 }
 
 // mom_xyz_ad (src/mom.f90:771-1019) fused with the RK update of src/rk.f90:155-186 at
-// interior cell t: new velocity to unew (halo-free), dudtrko in place, dudtd to dtd (impdiff)
-__device__ __forceinline__ void mom_rk_cell(const Dims &d, double dxi, double dyi, double visc, double f1, double f2,
-                                                double f12, double bfx, double bfy, double bfz, int impdiff,
-                                                const double *__restrict__ dzci, const double *__restrict__ dzfi,
-                                                const double *__restrict__ u, const double *__restrict__ v,
-                                                const double *__restrict__ w, const double *__restrict__ p,
-                                                double *__restrict__ dudtrko, double *__restrict__ dvdtrko,
-                                                double *__restrict__ dwdtrko, double *__restrict__ unew,
-                                                double *__restrict__ dtd, long t,
-                                                const double *__restrict__ sb = nullptr, double gbx = 0.,
-                                                double gby = 0., double gbz = 0., double beta = 0.) {
+// interior cell t, in the field precision T (double; float for the FP32 run, the reference's
+// single-precision build of src/types.f90:12-18).  The new velocity goes to un/vn/wn: halo-free
+// index (HALO_OUT false: the FP64 kernels' scratch) or haloed index (HALO_OUT true: the
+// out-of-place FP32 kernel writing the second velocity buffer); dudtrko in place, dudtd to
+// dtd (impdiff, halo-free, 3 fields).  Returns false past the end.
+template <typename T, bool HALO_OUT = false>
+__device__ __forceinline__ bool mom_rk_cell(const Dims &d, T dxi, T dyi, T visc, T f1, T f2, T f12, T bfx, T bfy,
+                                            T bfz, int impdiff, const T *__restrict__ dzci,
+                                            const T *__restrict__ dzfi, const T *__restrict__ u,
+                                            const T *__restrict__ v, const T *__restrict__ w,
+                                            const T *__restrict__ p, T *__restrict__ dudtrko,
+                                            T *__restrict__ dvdtrko, T *__restrict__ dwdtrko, T *__restrict__ un_out,
+                                            T *__restrict__ vn_out, T *__restrict__ wn_out, T *__restrict__ dtd,
+                                            long t, const T *__restrict__ sb = nullptr, T gbx = T(0),
+                                            T gby = T(0), T gbz = T(0), T beta = T(0), T *newvel = nullptr,
+                                            int *kout = nullptr) {
   int i, j, k;
-  if (!cell3(t, d, i, j, k)) return;
+  if (!cell3(t, d, i, j, k)) return false;
   const int n1 = d.n1, n2 = d.n2;
   const size_t np = (size_t)d.n1 * d.n2 * d.n3;
   const size_t sx = 1, sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
   const size_t c = hidx(i, j, k, n1, n2);
-  const double dzci_k = dzci[k], dzci_km = dzci[k - 1], dzfi_k = dzfi[k], dzfi_kp = dzfi[k + 1];
-  const double rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
-  const double u_ccm = u[c - sz], u_cmc = u[c - sy], u_mcc = u[c - sx], u_ccc = u[c], u_pcc = u[c + sx],
-               u_mpc = u[c - sx + sy], u_cpc = u[c + sy], u_mcp = u[c - sx + sz], u_ccp = u[c + sz];
-  const double v_ccm = v[c - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx],
-               v_ccc = v[c], v_pcc = v[c + sx], v_cpc = v[c + sy], v_ccp = v[c + sz], v_cmp = v[c - sy + sz];
-  const double w_ccm = w[c - sz], w_pcm = w[c + sx - sz], w_cpm = w[c + sy - sz], w_cmc = w[c - sy], w_mcc = w[c - sx],
-               w_ccc = w[c], w_pcc = w[c + sx], w_cpc = w[c + sy], w_ccp = w[c + sz];
+  const T q = T(0.25);
+  const T dzci_k = dzci[k], dzci_km = dzci[k - 1], dzfi_k = dzfi[k], dzfi_kp = dzfi[k + 1];
+  const T rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
+  const T u_ccm = u[c - sz], u_cmc = u[c - sy], u_mcc = u[c - sx], u_ccc = u[c], u_pcc = u[c + sx],
+          u_mpc = u[c - sx + sy], u_cpc = u[c + sy], u_mcp = u[c - sx + sz], u_ccp = u[c + sz];
+  const T v_ccm = v[c - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx],
+          v_ccc = v[c], v_pcc = v[c + sx], v_cpc = v[c + sy], v_ccp = v[c + sz], v_cmp = v[c - sy + sz];
+  const T w_ccm = w[c - sz], w_pcm = w[c + sx - sz], w_cpm = w[c + sy - sz], w_cmc = w[c - sy], w_mcc = w[c - sx],
+          w_ccc = w[c], w_pcc = w[c + sx], w_cpc = w[c + sy], w_ccp = w[c + sz];
   // x
-  const double dudxp = (u_pcc - u_ccc) * dxi, dudxm = (u_ccc - u_mcc) * dxi;
-  const double dudyp = (u_cpc - u_ccc) * dyi, dudym = (u_ccc - u_cmc) * dyi;
-  const double dudzp = (u_ccp - u_ccc) * dzci_k, dudzm = (u_ccc - u_ccm) * dzci_km;
-  const double uuip = 0.25 * (u_ccc + u_pcc) * u_pcc, uuim = 0.25 * (u_ccc + u_mcc) * u_mcc;
-  const double vujp = 0.25 * (v_ccc + v_pcc) * u_cpc, vujm = 0.25 * (v_cmc + v_pmc) * u_cmc;
-  const double wukp = 0.25 * (w_ccc + w_pcc) * u_ccp, wukm = 0.25 * (w_ccm + w_pcm) * u_ccm;
-  const double dudtd_xy = visc * (dudxp - dudxm) * dxi + visc * (dudyp - dudym) * dyi;
-  const double dudtd_z = visc * (dudzp - dudzm) * dzfi_k;
-  double dudt = -(uuip - uuim) * dxi - (vujp - vujm) * dyi - (wukp - wukm) * dzfi_k;
+  const T dudxp = (u_pcc - u_ccc) * dxi, dudxm = (u_ccc - u_mcc) * dxi;
+  const T dudyp = (u_cpc - u_ccc) * dyi, dudym = (u_ccc - u_cmc) * dyi;
+  const T dudzp = (u_ccp - u_ccc) * dzci_k, dudzm = (u_ccc - u_ccm) * dzci_km;
+  const T uuip = q * (u_ccc + u_pcc) * u_pcc, uuim = q * (u_ccc + u_mcc) * u_mcc;
+  const T vujp = q * (v_ccc + v_pcc) * u_cpc, vujm = q * (v_cmc + v_pmc) * u_cmc;
+  const T wukp = q * (w_ccc + w_pcc) * u_ccp, wukm = q * (w_ccm + w_pcm) * u_ccm;
+  const T dudtd_xy = visc * (dudxp - dudxm) * dxi + visc * (dudyp - dudym) * dyi;
+  const T dudtd_z = visc * (dudzp - dudzm) * dzfi_k;
+  T dudt = -(uuip - uuim) * dxi - (vujp - vujm) * dyi - (wukp - wukm) * dzfi_k;
   // y
-  const double dvdxp = (v_pcc - v_ccc) * dxi, dvdxm = (v_ccc - v_mcc) * dxi;
-  const double dvdyp = (v_cpc - v_ccc) * dyi, dvdym = (v_ccc - v_cmc) * dyi;
-  const double dvdzp = (v_ccp - v_ccc) * dzci_k, dvdzm = (v_ccc - v_ccm) * dzci_km;
-  const double uvip = 0.25 * (u_ccc + u_cpc) * v_pcc, uvim = 0.25 * (u_mcc + u_mpc) * v_mcc;
-  const double vvjp = 0.25 * (v_ccc + v_cpc) * v_cpc, vvjm = 0.25 * (v_ccc + v_cmc) * v_cmc;
-  const double wvkp = 0.25 * (w_ccc + w_cpc) * v_ccp, wvkm = 0.25 * (w_ccm + w_cpm) * v_ccm;
-  const double dvdtd_xy = visc * (dvdxp - dvdxm) * dxi + visc * (dvdyp - dvdym) * dyi;
-  const double dvdtd_z = visc * (dvdzp - dvdzm) * dzfi_k;
-  double dvdt = -(uvip - uvim) * dxi - (vvjp - vvjm) * dyi - (wvkp - wvkm) * dzfi_k;
+  const T dvdxp = (v_pcc - v_ccc) * dxi, dvdxm = (v_ccc - v_mcc) * dxi;
+  const T dvdyp = (v_cpc - v_ccc) * dyi, dvdym = (v_ccc - v_cmc) * dyi;
+  const T dvdzp = (v_ccp - v_ccc) * dzci_k, dvdzm = (v_ccc - v_ccm) * dzci_km;
+  const T uvip = q * (u_ccc + u_cpc) * v_pcc, uvim = q * (u_mcc + u_mpc) * v_mcc;
+  const T vvjp = q * (v_ccc + v_cpc) * v_cpc, vvjm = q * (v_ccc + v_cmc) * v_cmc;
+  const T wvkp = q * (w_ccc + w_cpc) * v_ccp, wvkm = q * (w_ccm + w_cpm) * v_ccm;
+  const T dvdtd_xy = visc * (dvdxp - dvdxm) * dxi + visc * (dvdyp - dvdym) * dyi;
+  const T dvdtd_z = visc * (dvdzp - dvdzm) * dzfi_k;
+  T dvdt = -(uvip - uvim) * dxi - (vvjp - vvjm) * dyi - (wvkp - wvkm) * dzfi_k;
   // z
-  const double dwdxp = (w_pcc - w_ccc) * dxi, dwdxm = (w_ccc - w_mcc) * dxi;
-  const double dwdyp = (w_cpc - w_ccc) * dyi, dwdym = (w_ccc - w_cmc) * dyi;
-  const double dwdzp = (w_ccp - w_ccc) * dzfi_kp, dwdzm = (w_ccc - w_ccm) * dzfi_k;
-  const double uwip = 0.25 * (rdzm * u_ccc + rdzp * u_ccp) * w_pcc, uwim = 0.25 * (rdzm * u_mcc + rdzp * u_mcp) * w_mcc;
-  const double vwjp = 0.25 * (rdzm * v_ccc + rdzp * v_ccp) * w_cpc, vwjm = 0.25 * (rdzm * v_cmc + rdzp * v_cmp) * w_cmc;
-  const double wwkp = 0.25 * (w_ccc + w_ccp) * w_ccp, wwkm = 0.25 * (w_ccc + w_ccm) * w_ccm;
-  const double dwdtd_xy = visc * (dwdxp - dwdxm) * dxi + visc * (dwdyp - dwdym) * dyi;
-  const double dwdtd_z = visc * (dwdzp - dwdzm) * dzci_k;
-  double dwdt = -(uwip - uwim) * dxi - (vwjp - vwjm) * dyi - (wwkp - wwkm) * dzci_k;
-  double dud = 0., dvd = 0., dwd = 0.;
+  const T dwdxp = (w_pcc - w_ccc) * dxi, dwdxm = (w_ccc - w_mcc) * dxi;
+  const T dwdyp = (w_cpc - w_ccc) * dyi, dwdym = (w_ccc - w_cmc) * dyi;
+  const T dwdzp = (w_ccp - w_ccc) * dzfi_kp, dwdzm = (w_ccc - w_ccm) * dzfi_k;
+  const T uwip = q * (rdzm * u_ccc + rdzp * u_ccp) * w_pcc, uwim = q * (rdzm * u_mcc + rdzp * u_mcp) * w_mcc;
+  const T vwjp = q * (rdzm * v_ccc + rdzp * v_ccp) * w_cpc, vwjm = q * (rdzm * v_cmc + rdzp * v_cmp) * w_cmc;
+  const T wwkp = q * (w_ccc + w_ccp) * w_ccp, wwkm = q * (w_ccc + w_ccm) * w_ccm;
+  const T dwdtd_xy = visc * (dwdxp - dwdxm) * dxi + visc * (dwdyp - dwdym) * dyi;
+  const T dwdtd_z = visc * (dwdzp - dwdzm) * dzci_k;
+  T dwdt = -(uwip - uwim) * dxi - (vwjp - vwjm) * dyi - (wwkp - wwkm) * dzci_k;
+  T dud = T(0), dvd = T(0), dwd = T(0);
   if (impdiff) {
     dud = dudtd_xy + dudtd_z; dvd = dvdtd_xy + dvdtd_z; dwd = dwdtd_xy + dwdtd_z;
   } else {
@@ -134,27 +140,32 @@ __device__ __forceinline__ void mom_rk_cell(const Dims &d, double dxi, double dy
     dwdt = dwdt + dwdtd_xy + dwdtd_z;
   }
   const size_t h = (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
-  const double pc = p[c];
-  double un = u_ccc + f1 * dudt + f2 * dudtrko[h] + f12 * (bfx - dxi * (p[c + sx] - pc));
-  double vn = v_ccc + f1 * dvdt + f2 * dvdtrko[h] + f12 * (bfy - dyi * (p[c + sy] - pc));
-  double wn = w_ccc + f1 * dwdt + f2 * dwdtrko[h] + f12 * (bfz - dzci_k * (p[c + sz] - pc));
+  const T pc = p[c];
+  T un = u_ccc + f1 * dudt + f2 * dudtrko[h] + f12 * (bfx - dxi * (p[c + sx] - pc));
+  T vn = v_ccc + f1 * dvdt + f2 * dvdtrko[h] + f12 * (bfy - dyi * (p[c + sy] - pc));
+  T wn = w_ccc + f1 * dwdt + f2 * dwdtrko[h] + f12 * (bfz - dzci_k * (p[c + sz] - pc));
   if (sb) {
     // Boussinesq buoyancy of the first scalar (src/rk.f90:163-177), gacc * beta
-    const double sc = sb[c];
-    un = un - f12 * gbx * beta * 0.5 * (sb[c + sx] + sc);
-    vn = vn - f12 * gby * beta * 0.5 * (sb[c + sy] + sc);
-    wn = wn - f12 * gbz * beta * 0.5 * (sb[c + sz] + sc);
+    const T sc = sb[c];
+    un = un - f12 * gbx * beta * T(0.5) * (sb[c + sx] + sc);
+    vn = vn - f12 * gby * beta * T(0.5) * (sb[c + sy] + sc);
+    wn = wn - f12 * gbz * beta * T(0.5) * (sb[c + sz] + sc);
   }
   if (impdiff) {
     un = un + f12 * dud; vn = vn + f12 * dvd; wn = wn + f12 * dwd;
     dtd[h] = dud; dtd[h + np] = dvd; dtd[h + 2 * np] = dwd;
   }
   dudtrko[h] = dudt; dvdtrko[h] = dvdt; dwdtrko[h] = dwdt;
-  unew[h] = un; unew[h + np] = vn; unew[h + 2 * np] = wn;
+  const size_t o = HALO_OUT ? c : h;
+  un_out[o] = un; vn_out[o] = vn; wn_out[o] = wn;
+  if (newvel) { newvel[0] = un; newvel[1] = vn; newvel[2] = wn; }
+  if (kout) *kout = k;
+  return true;
 }
 
-// periodic self-exchange along dir 1 (y) or 2 (z) at face cell t
-__device__ __forceinline__ void halo_copy_cell(double *p, int n1, int n2, int n3, int dir, int up, int lo, long t) {
+// periodic self-exchange along dir 1 (y) or 2 (z) at face cell t (T: field precision)
+template <typename T>
+__device__ __forceinline__ void halo_copy_cell(T *p, int n1, int n2, int n3, int dir, int up, int lo, long t) {
   const int e1 = n1 + 2, e2 = dir == 1 ? n3 + 2 : n2 + 2;
   if (t >= (long)e1 * e2) return;
   const int a = (int)(t % e1), b = (int)(t / e1);
@@ -167,14 +178,16 @@ __device__ __forceinline__ void halo_copy_cell(double *p, int n1, int n2, int n3
   }
 }
 
-// set_bc (src/bound.f90:182-463), nh = 1, at face cell t
-__device__ __forceinline__ void set_bc_cell(double *p, int n1, int n2, int n3, char ctype, int ib, int dir,
-                                            int centered, double factor, double sgn, long t) {
+// set_bc (src/bound.f90:182-463), nh = 1, at face cell t; factor and sgn are the host-side
+// coefficients of bc_op, rounded to the field precision T
+template <typename T>
+__device__ __forceinline__ void set_bc_cell(T *p, int n1, int n2, int n3, char ctype, int ib, int dir, int centered,
+                                            T factor, T sgn, long t) {
   const int e1 = (dir == 0 ? n2 : n1) + 2, e2 = (dir == 2 ? n2 : n3) + 2;
   if (t >= (long)e1 * e2) return;
   const int b1 = (int)(t % e1), b2 = (int)(t / e1);
   const int nn = dir == 0 ? n1 : (dir == 1 ? n2 : n3);
-  auto at = [&](int m) -> double & {
+  auto at = [&](int m) -> T & {
     return dir == 0 ? p[hidx(m, b1, b2, n1, n2)] : (dir == 1 ? p[hidx(b1, m, b2, n1, n2)] : p[hidx(b1, b2, m, n1, n2)]);
   };
   if (ctype == 'P') {
@@ -185,8 +198,8 @@ __device__ __forceinline__ void set_bc_cell(double *p, int n1, int n2, int n3, c
     if (ib == 0) at(0) = factor;
     else { at(nn + 1) = at(nn - 1); at(nn) = factor; }
   } else {
-    if (ib == 0) at(0) = 1. * factor + at(1);
-    else { at(nn + 1) = at(nn); at(nn) = 1. * factor + at(nn - 1); }
+    if (ib == 0) at(0) = T(1) * factor + at(1);
+    else { at(nn + 1) = at(nn); at(nn) = T(1) * factor + at(nn - 1); }
   }
 }
 

@@ -29,6 +29,8 @@ DBL_MAX = np.finfo(np.float64).max
 # src/param.f90:18, small = epsilon(1._rp)*10**(precision(1._rp)/2) with rp = dp: precision is
 # 15 decimal digits and 15/2 is integer division, so small = 2.22e-16 * 1e7
 SMALL = np.finfo(np.float64).eps * 10 ** (15 // 2)
+# the same with rp = sp (precision 6 digits): the threshold of the FP32 run
+SMALL_SP = float(np.finfo(np.float32).eps) * 10 ** (6 // 2)
 
 
 class SimulationAborted(RuntimeError):
@@ -83,6 +85,16 @@ class Simulation:
         # pressure_refine = {"rtol": r, "max_iter": K}: the pressure solve runs on an FP32 plan
         # with FP64 iterative refinement (cans_solver_refined) instead of the FP64 path
         self.p_refine = dict(case["pressure_refine"]) if case.get("pressure_refine") else None
+        # precision = "fp32": the FP32 run -- FP32 fields and stencils (the reference's
+        # single-precision build, src/types.f90:12-18) with the pressure correction solved to
+        # FP64 accuracy by refinement (two corrections unless pressure_refine says otherwise)
+        self.fp32 = case.get("precision", "fp64") == "fp32"
+        if self.fp32:
+            if self.is_impdiff or int(case.get("nscal", 0)) > 0:
+                raise ValueError("precision 'fp32' runs explicit diffusion without scalars")
+            if self.p_refine is None:
+                self.p_refine = {"rtol": 0.0, "max_iter": 2}
+        self.small = SMALL_SP if self.fp32 else SMALL
         self.p_refine_iters = 0
         self.plan_p = cans.Plan(n, self.dli, self.dzci_h, self.dzfi_h, self.cbcpre, self.bcpre, "ccc",
                                 precision=cans.FP32 if self.p_refine else cans.FP64)
@@ -93,9 +105,18 @@ class Simulation:
                 cf[c] = "f"
                 self.plans_v.append(cans.Plan(n, self.dli, self.dzci_h, self.dzfi_h, self.cbcvel[6 * c:6 * c + 6],
                                               self.bcvel[6 * c:6 * c + 6], "".join(cf)))
-        self.u, self.v, self.w, self.p, self.pp = [cans.field(n, device) for _ in range(5)]
-        self.dudtrko, self.dvdtrko, self.dwdtrko = [torch.zeros((n[2], n[1], n[0]), dtype=torch.float64,
+        fdt = torch.float32 if self.fp32 else torch.float64
+        self.u, self.v, self.w, self.p = [cans.field(n, device, fdt) for _ in range(4)]
+        self.pp = cans.field(n, device)
+        self.dudtrko, self.dvdtrko, self.dwdtrko = [torch.zeros((n[2], n[1], n[0]), dtype=fdt,
                                                                 device=device) for _ in range(3)]
+        if self.fp32:
+            # second velocity buffer: rk writes the new velocity there and the two are swapped
+            self.unew, self.vnew, self.wnew = [cans.field(n, device, fdt) for _ in range(3)]
+            t32 = lambda a: torch.tensor(a, dtype=torch.float32, device=device)
+            self.dzci32, self.dzfi32 = t32(self.dzci_h), t32(self.dzfi_h)
+            self.gvr_c32, self.gvr_f32 = t32(gvr_c), t32(gvr_f)
+            self.rk_work = cans.rk_f32_work(n, False, device)
         self.time, self.istep, self.dt, self.dti = 0., 0, 0., 0.
         self.divtot = self.divmax = 0.
         self.dpdl = np.zeros(3)
@@ -134,7 +155,8 @@ class Simulation:
         """Fortran-indexed host arrays (n1+2, n2+2, n3+2) -> device fields."""
         for name, a in (("u", u), ("v", v), ("w", w), ("p", p)):
             if a is not None:
-                getattr(self, name).copy_(cans.to_device(a, self.device))
+                fld = getattr(self, name)
+                fld.copy_(cans.to_device(a, self.device, fld.dtype))
         for sc, a in zip(self.scalars, scalars):
             if a is not None:
                 sc["val"].copy_(cans.to_device(a, self.device))
@@ -153,10 +175,15 @@ class Simulation:
         if restart:
             import os
             for name, fld in self._io_vars():
-                self.time, self.istep = cans.load_field(os.path.join(restart_dir, f"fld_{name}.bin"), n, fld)
-        cans.bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
-                      self.w, restart)
-        cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
+                tmp = fld if fld.dtype == self.pp.dtype else cans.field(n, self.device)
+                self.time, self.istep = cans.load_field(os.path.join(restart_dir, f"fld_{name}.bin"), n, tmp)
+                if tmp is not fld:
+                    fld.copy_(tmp)
+        bounduvw = cans.bounduvw_f32 if self.fp32 else cans.bounduvw
+        boundp = cans.boundp_f32 if self.fp32 else cans.boundp
+        bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v, self.w,
+                 restart)
+        boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
         for sc in self.scalars:
             cans.boundp(sc["cbc"], n, sc["bc"], self.is_bound, self.dl, self.dzc, sc["val"])
         self._new_dt()
@@ -166,7 +193,8 @@ class Simulation:
         fld_s_001.bin ... for the scalars."""
         import os
         for name, fld in self._io_vars():
-            cans.save_field(os.path.join(datadir, f"fld_{name}.bin"), self.n, fld, self.time, self.istep)
+            # the FP32 run writes the reference's FP64 file layout (values widened exactly)
+            cans.save_field(os.path.join(datadir, f"fld_{name}.bin"), self.n, fld.double(), self.time, self.istep)
 
     # ------------------------------------------------------------------ text output
     def out0d(self, datadir):
@@ -177,7 +205,7 @@ class Simulation:
             mean = [0., 0., 0.]
             for d, (fld, gvr) in enumerate(((self.u, self.gvr_f), (self.v, self.gvr_f), (self.w, self.gvr_c))):
                 if self.is_forced[d] or abs(self.bforce[d]) > 0.:
-                    mean[d] = cans.bulk_mean(self.n, gvr, fld)
+                    mean[d] = cans.bulk_mean(self.n, gvr, fld.double())
             dpdl = list(self.dpdl) if any(self.is_forced) else [-b for b in self.bforce]
             output.out0d(os.path.join(datadir, "forcing.out"), [self.time] + dpdl + mean)
         for i, sc in enumerate(self.scalars):
@@ -199,21 +227,55 @@ class Simulation:
         if self.scalars:
             items.append(("scal_01_mean", self.zc, dzc, self.scalars[0]["val"]))
         for name, z_g, dz, f in items:
-            p1d = cans.out1d(n, self.l, self.dl, 3, dz, f).cpu().numpy()
+            p1d = cans.out1d(n, self.l, self.dl, 3, dz, f.double()).cpu().numpy()
             output.write_out1d(path(name), 3, n, self.dl, z_g, p1d)
         if velstats:
-            st = cans.out1d_chan(n, self.l, self.dl, self.u, self.v, self.w).cpu().numpy()
+            st = cans.out1d_chan(n, self.l, self.dl, self.u.double(), self.v.double(), self.w.double()).cpu().numpy()
             output.write_out1d_chan(path("velstats"), n, self.zc, st)
         torch.cuda.synchronize()
 
     def _new_dt(self):
-        dt_cfl = cans.chkdt(self.n, self.dl, self.dzci, self.dzfi, self.visc, self.alpha_max, self.is_impdiff, 0,
-                            self.u, self.v, self.w)
+        if self.fp32:
+            dt_cfl = cans.chkdt_f32(self.n, self.dl, self.dzci32, self.dzfi32, self.visc, self.alpha_max, 0, 0,
+                                    self.u, self.v, self.w)
+        else:
+            dt_cfl = cans.chkdt(self.n, self.dl, self.dzci, self.dzfi, self.visc, self.alpha_max, self.is_impdiff,
+                                0, self.u, self.v, self.w)
         self.dt = self.dt_f if self.dt_f > 0. else min(self.cfl * dt_cfl, self.dtmax)
         self.dti = 1. / self.dt
         return dt_cfl
 
+    def _substep_fp32(self, irk):
+        """One RK3 substep of the FP32 run, in the order of substep(): rk writes the new
+        velocity into the second buffer and the two buffers are swapped (the reference updates
+        u, v, w in place; every later call reads the new velocity, so the results agree)."""
+        n = self.n
+        dtrk = (RKCOEFF[irk][0] + RKCOEFF[irk][1]) * self.dt
+        dtrki = 1. / dtrk
+        f = cans.rk_f32(RKCOEFF[irk], n, self.dli, self.dzci32, self.dzfi32, self.gvr_c32, self.gvr_f32, self.dt,
+                        self.visc, self.p, self.is_forced, self.velf, self.bforce, self.dudtrko, self.dvdtrko,
+                        self.dwdtrko, self.u, self.v, self.w, self.unew, self.vnew, self.wnew, self.rk_work)
+        self.u, self.unew = self.unew, self.u
+        self.v, self.vnew = self.vnew, self.v
+        self.w, self.wnew = self.wnew, self.w
+        self.dpdl += f
+        cans.bounduvw_f32(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
+                          self.w, False, cans.HALO_LOWER)
+        cans.fillps_f32(n, self.dli, self.dzfi32, dtrki, self.u, self.v, self.w, self.pp)
+        cans.updt_rhs_b("ccc", self.cbcpre, n, self.is_bound, self.plan_p.rhsb, self.pp)
+        it, _ = self.plan_p.solve_refined(self.pp, self.dli, self.dzci, self.dzfi,
+                                          rtol=self.p_refine.get("rtol", 0.), max_iter=self.p_refine["max_iter"])
+        self.p_refine_iters = max(self.p_refine_iters, it)
+        cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.pp)
+        cans.correc_f32(n, self.dli, self.dzci32, dtrk, self.pp, self.u, self.v, self.w)
+        cans.bounduvw_f32(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
+                          self.w, True, cans.HALO_UPPER, cans.HALO_NONE)
+        cans.updatep_f32(n, self.dli, self.dzci32, self.dzfi32, 0., 0, self.pp, self.p)
+        cans.boundp_f32(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
+
     def substep(self, irk):
+        if self.fp32:
+            return self._substep_fp32(irk)
         n = self.n
         dtrk = (RKCOEFF[irk][0] + RKCOEFF[irk][1]) * self.dt
         dtrki = 1. / dtrk
@@ -265,11 +327,15 @@ class Simulation:
         small), then chkdiv (abort when divmax > small or divtot is NaN, unless
         is_mask_divergence_check)."""
         dt_cfl = self._new_dt()
-        if dt_cfl < SMALL:
+        if dt_cfl < self.small:
             self._abort(f"time step is too small (dt_cfl = {dt_cfl:.3e})")
-        self.divtot, self.divmax = cans.chkdiv(self.n, self.l, self.dli, self.dzfi, self.u, self.v, self.w,
-                                               allow_nonfinite=True)
-        if not self.is_mask_divergence_check and (self.divmax > SMALL or np.isnan(self.divtot)):
+        if self.fp32:
+            self.divtot, self.divmax = cans.chkdiv_f32(self.n, self.l, self.dli, self.dzfi32, self.u, self.v, self.w,
+                                                       allow_nonfinite=True)
+        else:
+            self.divtot, self.divmax = cans.chkdiv(self.n, self.l, self.dli, self.dzfi, self.u, self.v, self.w,
+                                                   allow_nonfinite=True)
+        if not self.is_mask_divergence_check and (self.divmax > self.small or np.isnan(self.divtot)):
             self._abort(f"maximum divergence is too large (divtot = {self.divtot:.3e}, "
                         f"divmax = {self.divmax:.3e})")
 

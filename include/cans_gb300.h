@@ -149,6 +149,53 @@ int cans_rk_scal(const double rkpar[2], const int n[3], const double dli[3], con
 size_t cans_rk_scal_work_doubles(const int n[3], int is_impdiff);
 /* bulk_forcing_s (src/scal.f90:301): s += f on the interior when is_forced */
 int cans_bulk_forcing_s(const int n[3], int is_forced, double f, double *s, void *stream);
+/* ---- the FP32 run ------------------------------------------------------------------------
+ * The routines above with FP32 fields u, v, w, p and FP32 device grid arrays (dzci, dzfi,
+ * grid_vol_ratio), the form of the reference's single-precision build (src/types.f90:12-18,
+ * rp = sp) except that the pressure correction pp stays FP64: it is the right-hand side and
+ * solution of the FP64-accurate refined solve (cans_solver_refined on a CANS_FP32 plan).
+ * Arithmetic per cell is the FP64 routines' in FP32, in the same order; global sums add
+ * per-warp FP32 partial sums in FP64.  Explicit diffusion only (is_impdiff != 0 returns
+ * CANS_ENOTSUP). */
+/* fillps (src/fillps.f90:13): FP32 divergence of u, v, w written to the FP64 p */
+int cans_fillps_f32(const int n[3], const double dli[3], const float *dzfi, double dti,
+                    const float *u, const float *v, const float *w, double *p, void *stream);
+/* correc (src/correc.f90:13): gradient of the FP64 p (differences of hi/lo float pairs) */
+int cans_correc_f32(const int n[3], const double dli[3], const float *dzci, double dt,
+                    const double *p, float *u, float *v, float *w, void *stream);
+/* updatep (src/updatep.f90:14), explicit form: p += pp rounded to FP32 */
+int cans_updatep_f32(const int n[3], const double dli[3], const float *dzci, const float *dzfi,
+                     double alpha, int is_impdiff, const double *pp, float *p, void *stream);
+/* rk (src/rk.f90:24) with mom_xyz_ad (src/mom.f90:771): out of place when unew != u (the new
+ * velocity goes to the interior of the haloed unew, vnew, wnew -- a second velocity buffer the
+ * caller swaps with u, v, w afterwards; its ghost cells are left for the following bounduvw),
+ * in place when unew == u, vnew == v, wnew == w.  dudtrko..: FP32 halo-free.  work: device
+ * scratch of cans_rk_f32_work_bytes(n, in_place) bytes.  f[3] (host): the forcing velf - mean
+ * (FP64 means); synchronises `stream` when any is_forced is set. */
+int cans_rk_f32(const double rkpar[2], const int n[3], const double dli[3], const float *dzci,
+                const float *dzfi, const float *grid_vol_ratio_c, const float *grid_vol_ratio_f,
+                double dt, double visc, const float *p, const int is_forced[3], const double velf[3],
+                const double bforce[3], int is_impdiff, float *dudtrko, float *dvdtrko, float *dwdtrko,
+                float *u, float *v, float *w, float *unew, float *vnew, float *wnew, double f[3],
+                void *work, void *stream);
+size_t cans_rk_f32_work_bytes(const int n[3], int in_place);
+/* bounduvw / boundp (src/bound.f90:17,124) on FP32 fields (same arguments) */
+int cans_bounduvw_f32(const char cbc[18], const int n[3], const double bc[18], const int is_bound[6],
+                      const double dl[3], const double *dzc, const double *dzf, float *u, float *v,
+                      float *w, int keep_norm, int halos_norm, int halos_tang, void *stream);
+int cans_boundp_f32(const char cbc[6], const int n[3], const double bc[6], const int is_bound[6],
+                    const double dl[3], const double *dzc, float *p, int halo_side, void *stream);
+/* chkdiv / chkdt / bulk_mean (src/chkdiv.f90:15, src/chkdt.f90:16, src/utils.f90:15) on FP32
+ * fields; FP32 per-cell arithmetic, FP64 sums; synchronise `stream` */
+int cans_chkdiv_f32(const int n[3], const double l[3], const double dli[3], const float *dzfi,
+                    const float *u, const float *v, const float *w, double *divtot, double *divmax,
+                    void *stream);
+int cans_chkdt_f32(const int n[3], const double dl[3], const float *dzci, const float *dzfi,
+                   double visc, double alpha, int is_impdiff, int is_impdiff_1d, const float *u,
+                   const float *v, const float *w, double *dtmax, void *stream);
+int cans_bulk_mean_f32(const int n[3], const float *grid_vol_ratio, const float *p, double *mean,
+                       void *stream);
+
 /* bounduvw (src/bound.f90:17), one GPU: halos_* are -1 lower, 0 none, 1 upper, 2 both
  * (argument absent in the reference).  dl: host; dzc, dzf: HOST arrays 0..n3+1
  * (only dzc(0), dzc(n3), dzf(0), dzf(n3) are read). */

@@ -14,6 +14,7 @@ def _bare_sim(monkeypatch, dt_cfl, divtot, divmax, masked=False):
     sim.visc, sim.alpha_max, sim.is_impdiff = 1e-3, 0., 0
     sim.cfl, sim.dtmax, sim.dt_f = 0.95, 1e5, -1.
     sim.icheck, sim.istep, sim.kill = 1, 7, False
+    sim.fp32, sim.small = False, driver.SMALL
     sim.is_mask_divergence_check = masked
     monkeypatch.setattr(cans, "chkdt", lambda *a, **k: dt_cfl)
     monkeypatch.setattr(cans, "chkdiv", lambda *a, **k: (divtot, divmax))
