@@ -203,7 +203,7 @@ def bench_ours(args, rank, world):
     if args.only == "rk3":
         return {"rk3_step": bench_rk3(args.size, dev, 20)}
     if args.only == "rk3-fp32":  # profiling aid: the FP32 run of the TGV only
-        return {"rk3_step_fp32": bench_rk3(args.size, dev, max(1, args.steps), legs=("fp32",))}
+        return {"rk3_step_fp32": bench_rk3(args.size, dev, max(1, args.steps), legs=("fp32_run",))}
     if args.only == "fp32-solve":  # profiling aid: plain FP32 solves (the passes of the refinement)
         return {"fp32_solve": bench_fp32_solve(args, n, dli, dzc, dzf, dev)}
     if args.only == "mx":

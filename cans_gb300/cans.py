@@ -137,6 +137,9 @@ def _setup(L):
     L.cans_chkdiv_f32.argtypes = L.cans_chkdiv.argtypes
     L.cans_chkdt_f32.argtypes = L.cans_chkdt.argtypes
     L.cans_bulk_mean_f32.argtypes = L.cans_bulk_mean.argtypes
+    L.cans_correc_updatep_f32.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V, _V]
+    L.cans_plan_set_zpass.argtypes = [_V, C.c_int]
+    L.cans_plan_get_zpass.argtypes = [_V, _I]
 
 
 def _check(rc, where):
@@ -261,6 +264,17 @@ class Plan:
         ms = (C.c_double * 2)()
         _check(lib().cans_plan_autotune(self._h, int(force), ms), "cans_plan_autotune")
         return list(ms)
+
+    @property
+    def zpass(self):
+        """z pass of an FP32 plan: 0 column sweep, 1 partitioned (cans_plan_get_zpass)"""
+        m = C.c_int()
+        _check(lib().cans_plan_get_zpass(self._h, C.byref(m)), "cans_plan_get_zpass")
+        return m.value
+
+    def set_zpass(self, mode):
+        """cans_plan_set_zpass: 0 column sweep, 1 partitioned, -1 automatic"""
+        _check(lib().cans_plan_set_zpass(self._h, int(mode)), "cans_plan_set_zpass")
 
     def shape(self, d):
         """(radix order, lines per CTA, compile-time length or 0) of direction d"""
@@ -602,3 +616,9 @@ def bulk_mean_f32(n, gvr, p, stream=None):
     r = C.c_double()
     _check(lib().cans_bulk_mean_f32(_ints(n), _ptr(gvr), _ptr(p), C.byref(r), _stream(stream)), "cans_bulk_mean_f32")
     return r.value
+
+
+def correc_updatep_f32(n, dli, dzci, dt, pp, u, v, w, p, stream=None):
+    """correc + the explicit updatep in one pass over pp (cans_correc_updatep_f32)"""
+    _check(lib().cans_correc_updatep_f32(_ints(n), _dbls(dli), _ptr(dzci), float(dt), _ptr(pp), _ptr(u), _ptr(v),
+                                         _ptr(w), _ptr(p), _stream(stream)), "cans_correc_updatep_f32")

@@ -43,6 +43,13 @@ struct cans_plan {
   double *a_d = nullptr, *b_d = nullptr, *c_d = nullptr, *bb_d = nullptr;
   float *a32 = nullptr;       // a_k rounded to FP32 (FP32 z columns: no FP64 conversions in the sweep)
   int *zorder = nullptr;      // FP32 plans: z column groups, those with FP64 columns first
+  float4 *coef4 = nullptr;    // FP32 plans: (a_k, b_k, c_k, 0) rounded to FP32 (partitioned z pass)
+  int *col64 = nullptr;       // FP32 plans: the columns eliminated in FP64 (|lambda| < lam32)
+  float *lamf = nullptr;      // FP32 plans: lambda per column in FP32, NaN for the FP64 columns
+  int n64 = 0;
+  int zpart_L = 0;            // FP32 plans: rows per segment of the partitioned z pass (0: not used)
+  int zpart_mode = 0;         // 1: the partitioned z pass (when zpart_L != 0), 0: the column-sweep kernel
+
   void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)
   double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
   float *R32 = nullptr;        // refinement: FP32 haloed residual (high part)

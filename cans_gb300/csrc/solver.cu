@@ -314,6 +314,82 @@ __global__ void k_factor_to_f32(const double *__restrict__ a, float *__restrict_
   if (t < n) b[t] = (float)a[t];
 }
 
+// FP64 elimination of one spectral column of an FP32 plan (the low-wavenumber columns with
+// |lambda_xy| < lam32, incl. the singular one): FP64 factors, the forward sweep into the FP64
+// scratch W, software-pipelined loads of U rows; overwrites the FP32 column of S
+__device__ __forceinline__ void zsolve_hyb64_col(float *__restrict__ S, double *__restrict__ W,
+                                                 const double *__restrict__ zinv, const double *__restrict__ dd,
+                                                 const double *__restrict__ p2, const double *__restrict__ dcl,
+                                                 const double *__restrict__ a, const double *__restrict__ c,
+                                                 long ncol, int nn, int zper, double norm, long col) {
+  constexpr int U = 8;
+  double y = 0.;
+  int k = 0;
+  for (; k + U <= nn; k += U) {
+    float sv[U];
+    double zv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const size_t idx = (size_t)(k + u) * ncol + col;
+      sv[u] = S[idx];
+      zv[u] = zinv[idx];
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      y = ((double)sv[u] * norm - a[k + u] * y) * zv[u];
+      W[(size_t)(k + u) * ncol + col] = y;
+    }
+  }
+  for (; k < nn; k++) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = ((double)S[idx] * norm - a[k] * y) * zinv[idx];
+    W[idx] = y;
+  }
+  const double sn = y;
+  k = nn - 2;
+  for (; k - U + 1 >= 0; k -= U) {
+    double wv[U], dv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const size_t idx = (size_t)(k - u) * ncol + col;
+      wv[u] = W[idx];
+      dv[u] = dd[idx];
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      y = wv[u] - dv[u] * y;
+      W[(size_t)(k - u) * ncol + col] = y;
+    }
+  }
+  for (; k >= 0; k--) {
+    const size_t idx = (size_t)k * ncol + col;
+    y = W[idx] - dd[idx] * y;
+    W[idx] = y;
+  }
+  if (zper) {
+    const size_t iN = (size_t)nn * ncol + col;
+    const double den = dcl[col];
+    const double pN = den == 0. ? 0. : ((double)S[iN] * norm - c[nn] * y - a[nn] * sn) / den;
+    S[iN] = (float)pN;
+    for (int k = 0; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      S[idx] = (float)(W[idx] + p2[idx] * pN);
+    }
+  } else {
+    for (k = 0; k + U <= nn; k += U) {
+      double wv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) wv[u] = W[(size_t)(k + u) * ncol + col];
+#pragma unroll
+      for (int u = 0; u < U; u++) S[(size_t)(k + u) * ncol + col] = (float)wv[u];
+    }
+    for (; k < nn; k++) {
+      const size_t idx = (size_t)k * ncol + col;
+      S[idx] = (float)W[idx];
+    }
+  }
+}
+
 // z solve on FP32 spectral data (FP32 plans).  Columns with |lambda_xy| >= lam32 are
 // eliminated in FP32 with the FP32-rounded factors (their system has condition number below
 // ~300, so FP32 gives ~1e-5 or better and the refinement contracts by that per step); the
@@ -429,72 +505,192 @@ __global__ void __launch_bounds__(128) k_zsolve_hyb(float *__restrict__ S, doubl
     }
     return;
   }
-  // FP64 columns: same prefetch structure
-  constexpr int U = 8;
-  double y = 0.;
-  int k = 0;
-  for (; k + U <= nn; k += U) {
-    float sv[U];
-    double zv[U];
+  // FP64 columns: the FP64 factors and an FP64 scratch for the forward sweep
+  zsolve_hyb64_col(S, W, zinv, dd, p2, dcl, a, c, ncol, nn, zper, norm, col);
+}
+
+// ---- z elimination of FP32 plans, partitioned along z (non-periodic z, nn <= kZW kZL).
+// One launch, two roles.  The first n64b CTAs eliminate the FP64 columns (|lambda| < lam32,
+// incl. the singular mode), one thread per column from the list col64, with the FP64 factors
+// (zsolve_hyb64_col); they are scheduled first, so their long FP64 sweeps overlap the rest.
+// Every other CTA owns kZC consecutive spectral columns, eliminated in FP32 with the
+// factors formed on the fly from a, b, c and lambda; its threads are (column c, segment s):
+// segment s holds rows [s kZL, s kZL + kZL) of its column in registers (loaded once,
+// coalesced across the columns), so each value is read from and written to HBM once
+// (8 B/cell).  Every segment but the last ends with a separator row; the rows before it
+// ("inner") are eliminated locally by two register sweeps run together:
+//   top-down (LU): the inner last row's values of Y = T_s^-1 r, G (left coupling
+//     -a_first e_first) and H (right coupling -c_last e_last), keeping 1/den per row;
+//   bottom-up (UL): the inner first row's values of Y, G, H;
+// which give the tridiagonal system of the W - 1 separator values (diagonally dominant like
+// the column's: |lambda| >= lam32 > 0), solved by parallel cyclic reduction across the
+// segments; then each segment solves its inner rows with the separators as boundary values
+// (LU forward with the kept 1/den, back substitution) and writes the column back.  Full
+// segments run a predicate-free path; the last (ragged) segment a predicated one.
+constexpr int kZL = 16;              // rows per segment
+constexpr int kZC = 8;               // spectral columns per CTA
+constexpr int kZW = 32;              // segments per column at most: nn <= kZW * kZL
+constexpr int kZT = kZC * kZW;       // threads per CTA at most
+
+// the local sweeps of one segment with NI inner rows of its first NR rows (templated: full
+// segments have NI = kZL - 1, NR = kZL and no predicates)
+template <bool FULL>
+__device__ __forceinline__ void zpart_sweeps(const float (&r)[kZL], float (&zz)[kZL], const float (&A)[kZL],
+                                             const float (&Bl)[kZL], const float (&C)[kZL], int ni, float &y,
+                                             float &gy, float &hl, float &yu, float &gf, float &hu) {
+  float dprev = 0.f, zl = 0.f, ep = 0.f;
+  y = 0.f; gy = 0.f; yu = 0.f; hu = 0.f;
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      const size_t idx = (size_t)(k + u) * ncol + col;
-      sv[u] = S[idx];
-      zv[u] = zinv[idx];
+  for (int t = 0; t < kZL; t++) {
+    if (FULL ? t < kZL - 1 : t < ni) {  // top-down, row t
+      const float z = __fdividef(1.f, Bl[t] - A[t] * dprev);
+      zz[t] = z;
+      dprev = C[t] * z;
+      y = (r[t] - A[t] * y) * z;
+      gy = (t == 0 ? -A[t] : -A[t] * gy) * z;
+      zl = z;
     }
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      y = ((double)sv[u] * norm - a[k + u] * y) * zv[u];
-      W[(size_t)(k + u) * ncol + col] = y;
+    const int u = kZL - 1 - t;
+    if (FULL ? u < kZL - 1 : u < ni) {  // bottom-up, row u
+      const float zu = __fdividef(1.f, Bl[u] - C[u] * ep);
+      const bool bottom = FULL ? u == kZL - 2 : u == ni - 1;
+      yu = (r[u] - C[u] * yu) * zu;
+      hu = (bottom ? -C[u] : -C[u] * hu) * zu;
+      ep = A[u] * zu;
     }
   }
-  for (; k < nn; k++) {
-    const size_t idx = (size_t)k * ncol + col;
-    y = ((double)S[idx] * norm - a[k] * y) * zinv[idx];
-    W[idx] = y;
-  }
-  const double sn = y;
-  k = nn - 2;
-  for (; k - U + 1 >= 0; k -= U) {
-    double wv[U], dv[U];
+  gf = -ep;
+  const int il = FULL ? kZL - 2 : ni - 1;
+  float cl = 0.f;
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      const size_t idx = (size_t)(k - u) * ncol + col;
-      wv[u] = W[idx];
-      dv[u] = dd[idx];
-    }
+  for (int t = 0; t < kZL; t++)
+    if (t == il) cl = C[t];
+  hl = -cl * zl;
+}
+
+// the inner rows with the boundary values XL (left) and XR (right), in place in r
+template <bool FULL>
+__device__ __forceinline__ void zpart_final(float (&r)[kZL], const float (&zz)[kZL], const float (&A)[kZL],
+                                            const float (&C)[kZL], int ni, float XL, float XR) {
+  float yv = 0.f;
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      y = wv[u] - dv[u] * y;
-      W[(size_t)(k - u) * ncol + col] = y;
+  for (int t = 0; t < kZL; t++) {
+    if (FULL ? t < kZL - 1 : t < ni) {
+      float rk = r[t];
+      if (t == 0) rk -= A[t] * XL;
+      if (FULL ? t == kZL - 2 : t == ni - 1) rk -= C[t] * XR;
+      yv = (rk - A[t] * yv) * zz[t];
+      r[t] = yv;
     }
   }
-  for (; k >= 0; k--) {
-    const size_t idx = (size_t)k * ncol + col;
-    y = W[idx] - dd[idx] * y;
-    W[idx] = y;
-  }
-  if (zper) {
-    const size_t iN = (size_t)nn * ncol + col;
-    const double den = dcl[col];
-    const double pN = den == 0. ? 0. : ((double)S[iN] * norm - c[nn] * y - a[nn] * sn) / den;
-    S[iN] = (float)pN;
-    for (int k = 0; k < nn; k++) {
-      const size_t idx = (size_t)k * ncol + col;
-      S[idx] = (float)(W[idx] + p2[idx] * pN);
+  float x = 0.f;
+#pragma unroll
+  for (int t = kZL - 1; t >= 0; t--) {
+    if (FULL ? t < kZL - 2 : t < ni - 1) {
+      x = r[t] - C[t] * zz[t] * x;
+      r[t] = x;
+    } else if (FULL ? t == kZL - 2 : t == ni - 1) {
+      x = r[t];
     }
+  }
+}
+
+__global__ void __launch_bounds__(kZT, 2) k_zsolve_part(float *__restrict__ S, double *__restrict__ Wsc,
+                                                         const float *__restrict__ lamf,
+                                                         const float4 *__restrict__ coef, long ncol, int nn, int W,
+                                                         float normf, const int *__restrict__ col64, int n64,
+                                                         int n64b, const double *__restrict__ zinv,
+                                                         const double *__restrict__ dd,
+                                                         const double *__restrict__ a64,
+                                                         const double *__restrict__ c64, double norm) {
+  if ((int)blockIdx.x < n64b) {  // FP64 role
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n64)
+      zsolve_hyb64_col(S, Wsc, zinv, dd, nullptr, nullptr, a64, c64, ncol, nn, 0, norm, (long)col64[t]);
+    return;
+  }
+  // exchange Yf Gf Hf Yl Gl Hl [W][kZC]; then, in the same memory, the reduced rows
+  // alpha beta gamma delta [W][kZC] twice (ping-pong of the cyclic reduction)
+  __shared__ float xbuf[8 * kZW * kZC];
+  __shared__ float4 sco[kZW * kZL];  // (a_k (0 at row 0), b_k, c_k, -)
+  float(*xs)[kZW][kZC] = reinterpret_cast<float(*)[kZW][kZC]>(xbuf);
+  float(*red)[4][kZW][kZC] = reinterpret_cast<float(*)[4][kZW][kZC]>(xbuf);
+  for (int k = threadIdx.x; k < nn; k += blockDim.x) sco[k] = coef[k];
+  __syncthreads();
+  const int c = threadIdx.x % kZC, s = threadIdx.x / kZC;
+  const long col = (long)(blockIdx.x - n64b) * kZC + c;
+  const float lam = col < ncol ? lamf[col] : __int_as_float(0x7fc00000);
+  const bool on = lam == lam;  // NaN: an FP64 column (or past the end)
+  const int b = s * kZL;
+  const bool lastseg = s == W - 1;
+  const int rows = lastseg ? nn - b : kZL;  // rows of the segment
+  const int ni = lastseg ? rows : kZL - 1;  // inner rows (the rest is the separator)
+  float *base = S + (size_t)b * ncol + col;
+  const int stride = (int)ncol;
+  float r[kZL], zz[kZL], A[kZL], Bl[kZL], C[kZL];
+#pragma unroll
+  for (int t = 0; t < kZL; t++) {
+    const bool in = on && t < rows;
+    const float4 q = sco[b + (t < rows ? t : 0)];
+    r[t] = in ? base[t * stride] * normf : 0.f;
+    A[t] = in ? q.x : 0.f;
+    Bl[t] = in ? q.y + lam : 1.f;
+    C[t] = in ? q.z : 0.f;
+    zz[t] = 0.f;
+  }
+  float y, gy, hl, yu, gf, hu;
+  if (lastseg) zpart_sweeps<false>(r, zz, A, Bl, C, ni, y, gy, hl, yu, gf, hu);
+  else zpart_sweeps<true>(r, zz, A, Bl, C, ni, y, gy, hl, yu, gf, hu);
+  xs[0][s][c] = yu; xs[1][s][c] = gf; xs[2][s][c] = lastseg ? 0.f : hu;
+  xs[3][s][c] = y; xs[4][s][c] = gy; xs[5][s][c] = lastseg ? 0.f : hl;
+  __syncthreads();
+  // the separator rows: segment s < W-1 owns row b + kZL - 1 and its equation
+  const int nr = W - 1;
+  int pp = 0;
+  float al = 0.f, be = 1.f, ga = 0.f, de = 0.f;
+  if (s < nr && on) {
+    const float Am = A[kZL - 1], Bm = Bl[kZL - 1], Cm = C[kZL - 1];
+    al = s > 0 ? Am * xs[4][s][c] : 0.f;
+    be = Bm + Am * xs[5][s][c] + Cm * xs[1][s + 1][c];
+    ga = s + 1 < nr ? Cm * xs[2][s + 1][c] : 0.f;
+    de = r[kZL - 1] - Am * xs[3][s][c] - Cm * xs[0][s + 1][c];
+  }
+  __syncthreads();  // xs is read; its memory now holds the reduced rows
+  if (s < nr) {
+    red[0][0][s][c] = al; red[0][1][s][c] = be; red[0][2][s][c] = ga; red[0][3][s][c] = de;
+  }
+  __syncthreads();
+  // parallel cyclic reduction of the separator system (identity rows outside 0..nr-1)
+  for (int h = 1; h < nr; h <<= 1) {
+    if (s < nr) {
+      float alm = 0.f, bem = 1.f, gam = 0.f, dem = 0.f, alp = 0.f, bep = 1.f, gap = 0.f, dep = 0.f;
+      if (s - h >= 0) {
+        alm = red[pp][0][s - h][c]; bem = red[pp][1][s - h][c]; gam = red[pp][2][s - h][c]; dem = red[pp][3][s - h][c];
+      }
+      if (s + h < nr) {
+        alp = red[pp][0][s + h][c]; bep = red[pp][1][s + h][c]; gap = red[pp][2][s + h][c]; dep = red[pp][3][s + h][c];
+      }
+      const float k1 = al / bem, k2 = ga / bep;
+      const float al2 = -alm * k1, be2 = be - gam * k1 - alp * k2, ga2 = -gap * k2, de2 = de - dem * k1 - dep * k2;
+      al = al2; be = be2; ga = ga2; de = de2;
+      red[pp ^ 1][0][s][c] = al; red[pp ^ 1][1][s][c] = be; red[pp ^ 1][2][s][c] = ga; red[pp ^ 1][3][s][c] = de;
+    }
+    pp ^= 1;
+    __syncthreads();
+  }
+  if (!on) return;
+  const float XL = s > 0 ? red[pp][3][s - 1][c] / red[pp][1][s - 1][c] : 0.f;
+  const float XR = s < nr ? de / be : 0.f;
+  if (lastseg) {
+    zpart_final<false>(r, zz, A, C, ni, XL, XR);
+#pragma unroll
+    for (int t = 0; t < kZL; t++)
+      if (t < rows) base[t * stride] = r[t];
   } else {
-    for (k = 0; k + U <= nn; k += U) {
-      double wv[U];
+    zpart_final<true>(r, zz, A, C, ni, XL, XR);
+    r[kZL - 1] = XR;  // the separator row
 #pragma unroll
-      for (int u = 0; u < U; u++) wv[u] = W[(size_t)(k + u) * ncol + col];
-#pragma unroll
-      for (int u = 0; u < U; u++) S[(size_t)(k + u) * ncol + col] = (float)wv[u];
-    }
-    for (; k < nn; k++) {
-      const size_t idx = (size_t)k * ncol + col;
-      S[idx] = (float)W[idx];
-    }
+    for (int t = 0; t < kZL; t++) base[t * stride] = r[t];
   }
 }
 
@@ -546,6 +742,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
   cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->a32); cudaFree(P->zorder); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
+  cudaFree(P->coef4); cudaFree(P->col64); cudaFree(P->lamf);
   cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->E32b); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
   for (auto &e : P->rev) cudaEventDestroy(e);
@@ -757,6 +954,17 @@ template <typename T> static int launch_y(cans_plan *P, int fwd) {
   return CANS_OK;
 }
 
+// The z pass of FP32 plans without a measurement: the column sweep (one thread per column,
+// precomputed factors) is bandwidth-bound once the columns fill the GPU; below that (fewer
+// than ~1.3 columns per thread slot of the SMs, e.g. 256^2 columns) the partitioned pass's
+// parallelism along z wins (measured on GB300: 256^3 0.09 vs 0.34 ms; 512^3 0.95 vs 0.55 ms).
+static int zpass_auto(const cans_plan *P) {
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long ncol = (long)P->n[0] * P->n[1];
+  return ncol < (long)nsm * 1280 ? 1 : 0;
+}
+
 static int launch_z(cans_plan *P, const Factor *F, double norm, bool f32) {
   const long ncol = (long)P->n[0] * P->n[1];
   const int nn = P->zper ? P->nn - 1 : P->nn;
@@ -765,7 +973,17 @@ static int launch_z(cans_plan *P, const Factor *F, double norm, bool f32) {
   if (!f32)
     k_zsolve64<<<grid, tpb, 0, P->stream>>>((double *)P->S, F->zinv, F->dd, F->p2, F->dcl, P->a_d, P->c_d, ncol,
                                             nn, P->zper, norm);
-  else
+  else if (P->zpart_L && !P->zper && P->zpart_mode) {
+    const int W = (nn + kZL - 1) / kZL;  // <= kZW (zpart_L is set only then)
+    const int tb = W * kZC;
+    const int n64b = (P->n64 + tb - 1) / tb;
+    const unsigned g = (unsigned)(n64b + (ncol + kZC - 1) / kZC);
+    k_zsolve_part<<<g, (unsigned)tb, 0, P->stream>>>((float *)P->S, P->R64, P->lamf, P->coef4, ncol, nn, W,
+                                                      (float)norm, P->col64, P->n64, n64b, F->zinv, F->dd, P->a_d,
+                                                      P->c_d, norm);
+    CANS_LAUNCH_CHECK();
+    return CANS_OK;
+  } else
     k_zsolve_hyb<<<grid, tpb, 0, P->stream>>>((float *)P->S, P->R64, P->lamcol, P->lam32, F->zinv, F->dd, F->p2,
                                               F->dcl, F->zinv32, F->dd32, F->p232, P->a_d, P->c_d, P->a32, P->zorder,
                                               ncol, nn, P->zper, norm);
@@ -962,6 +1180,36 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
       cans_set_last_cuda_error(e);
       return fail(CANS_ECUDA);
     }
+    // partitioned z pass (non-periodic z): segment length L, the FP64 column list, FP32 rows
+    const int nnz = P->nn;
+    if (!P->zper && nnz >= 1 && nnz <= kZW * kZL) {
+      P->zpart_L = kZL;
+      std::vector<int> c64;
+      for (long c = 0; c < (long)n1 * n2; c++)
+        if (fabs(lamcol[c]) < P->lam32) c64.push_back((int)c);
+      P->n64 = (int)c64.size();
+      std::vector<float4> coefh(n3);
+      for (int k = 0; k < n3; k++)
+        coefh[k] = make_float4(k > 0 ? (float)P->a_h[k] : 0.f, (float)P->b_h[k], (float)P->c_h[k], 0.f);
+      // lambda per column in FP32, NaN where the column is eliminated in FP64
+      std::vector<float> lamfh(lamcol.size());
+      for (size_t c = 0; c < lamcol.size(); c++)
+        lamfh[c] = fabs(lamcol[c]) < P->lam32 ? nanf("") : (float)lamcol[c];
+      if ((e = cudaMalloc(&P->coef4, n3 * sizeof(float4))) != cudaSuccess ||
+          (e = cudaMemcpy(P->coef4, coefh.data(), n3 * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess ||
+          (e = cudaMalloc(&P->col64, std::max<size_t>(c64.size(), 1) * sizeof(int))) != cudaSuccess ||
+          (e = cudaMalloc(&P->lamf, lamfh.size() * sizeof(float))) != cudaSuccess ||
+          (e = cudaMemcpy(P->lamf, lamfh.data(), lamfh.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+
+          (!c64.empty() &&
+           (e = cudaMemcpy(P->col64, c64.data(), c64.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess) ||
+          false) {
+        cans_set_last_cuda_error(e);
+        return fail(e == cudaErrorMemoryAllocation ? CANS_ENOMEM : CANS_ECUDA);
+      }
+      P->bytes += (long long)(n3 * sizeof(float4) + c64.size() * sizeof(int) + lamfh.size() * sizeof(float));
+      P->zpart_mode = zpass_auto(P);
+    }
   }
   if (cudaMemcpy(P->a32, a32h.data(), n3 * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(P->zw, zw_h, (n3 + 2) * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1116,6 +1364,43 @@ template <typename T> int tune_dir(cans_plan *P, int d, const void *pin, int for
 }
 }  // namespace
 
+extern "C" int cans_plan_set_zpass(cans_plan *P, int mode) {
+  if (!P || mode < -1 || mode > 1) return CANS_EINVAL;
+  if (mode == 1 && !P->zpart_L) return CANS_ENOTSUP;
+  P->zpart_mode = mode == -1 ? (P->zpart_L ? zpass_auto(P) : 0) : mode;
+  return CANS_OK;
+}
+
+extern "C" int cans_plan_get_zpass(const cans_plan *P, int *mode) {
+  if (!P || !mode) return CANS_EINVAL;
+  *mode = P->zpart_L ? P->zpart_mode : 0;
+  return CANS_OK;
+}
+
+// mean ms of the plan's z pass (Poisson factors) in z mode `mode`, over a few launches
+static int time_zpass(cans_plan *P, int mode, float *ms) {
+  Factor *F;
+  int rc = get_factor(P, 0., false, &F);
+  if (rc) return rc;
+  const int keep = P->zpart_mode;
+  P->zpart_mode = mode;
+  cudaEvent_t e0, e1;
+  CANS_CUDA_TRY(cudaEventCreate(&e0));
+  CANS_CUDA_TRY(cudaEventCreate(&e1));
+  rc = launch_z(P, F, P->normfft, true);  // warm-up
+  const int reps = 5;
+  cudaEventRecord(e0, P->stream);
+  for (int i = 0; i < reps && !rc; i++) rc = launch_z(P, F, P->normfft, true);
+  cudaEventRecord(e1, P->stream);
+  cudaEventSynchronize(e1);
+  cudaEventElapsedTime(ms, e0, e1);
+  *ms /= reps;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  P->zpart_mode = keep;
+  return rc;
+}
+
 extern "C" int cans_plan_autotune(cans_plan *P, int force, double ms_out[2]) {
   if (!P) return CANS_EINVAL;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1132,6 +1417,13 @@ extern "C" int cans_plan_autotune(cans_plan *P, int force, double ms_out[2]) {
                : CANS_ECUDA;
   for (int d = 0; d < 2 && !rc; d++)
     rc = P->precision == CANS_FP64 ? tune_dir<double>(P, d, pin, force) : tune_dir<float>(P, d, pin, force);
+  // FP32 plans: the faster of the two z passes (on the zeroed spectral buffer)
+  if (!rc && P->precision == CANS_FP32 && P->zpart_L) {
+    float t0 = 0.f, t1 = 0.f;
+    rc = time_zpass(P, 0, &t0);
+    if (!rc) rc = time_zpass(P, 1, &t1);
+    if (!rc) P->zpart_mode = t1 < t0 ? 1 : 0;
+  }
   cudaStreamSynchronize(P->stream);
   cudaFree(pin);
   if (rc) return rc;

@@ -26,23 +26,45 @@ namespace {
 constexpr int kTB = 256;
 unsigned blocks_for(long count, int tb = kTB) { return (unsigned)((count + tb - 1) / tb); }
 
-// FP64 sum over a block of per-thread FP32 values: FP32 warp sums, widened exactly, then
-// added in FP64 by warp 0 (the block total in lane 0 of warp 0)
-template <int NC> __device__ __forceinline__ void block_sum_f64(float (&v)[NC], double (&out)[NC]) {
+// FP64 sum over a block of kTB threads of per-thread FP32 values v (+ optional compensation
+// terms e, the low parts of per-thread Kahan sums): FP32 warp sums, widened exactly and added
+// in FP64 by thread 0 (the block total is valid in thread 0 only).  tid: linear thread index.
+template <int NC>
+__device__ __forceinline__ void block_sum_f64(float (&v)[NC], float (&e)[NC], double (&out)[NC], int tid) {
   __shared__ double red[NC][kTB / 32];
   for (int c = 0; c < NC; c++)
-    for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
-  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int o = 16; o > 0; o >>= 1) {
+      v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+      e[c] += __shfl_down_sync(0xffffffffu, e[c], o);
+    }
+  const int wid = tid >> 5, lane = tid & 31;
   if (lane == 0)
-    for (int c = 0; c < NC; c++) red[c][wid] = f2d(v[c]);
+    for (int c = 0; c < NC; c++) red[c][wid] = f2d(v[c]) + f2d(e[c]);
   __syncthreads();
   for (int c = 0; c < NC; c++) {
     double s = 0.;
-    if (threadIdx.x == 0)
+    if (tid == 0)
       for (int q = 0; q < kTB / 32; q++) s += red[c][q];
     out[c] = s;
   }
 }
+template <int NC> __device__ __forceinline__ void block_sum_f64(float (&v)[NC], double (&out)[NC], int tid) {
+  float e[NC];
+  for (int c = 0; c < NC; c++) e[c] = 0.f;
+  block_sum_f64<NC>(v, e, out, tid);
+}
+
+// Kahan-compensated running FP32 sum: s + e carries the total
+__device__ __forceinline__ void kahan_add(float &s, float &e, float x) {
+  const float y = x - e;
+  const float t = s + y;
+  e = (t - s) - y;
+  s = t;
+}
+
+// 2D thread blocks over (i, j) with an interior plane per blockIdx.z (no index division)
+constexpr int kBX = 32, kBY = 8;
+__device__ __forceinline__ int tid2() { return threadIdx.y * kBX + threadIdx.x; }
 }  // namespace
 
 // ------------------------------------------------------------------------------ fillps
@@ -50,13 +72,20 @@ __global__ void __launch_bounds__(kTB) k_fillps32(Dims d, float dti, float dtidx
                                                   const float *__restrict__ dzfi, const float *__restrict__ u,
                                                   const float *__restrict__ v, const float *__restrict__ w,
                                                   double *__restrict__ p) {
-  int i, j, k;
-  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
-  const int n1 = d.n1, n2 = d.n2;
-  const size_t c = hidx(i, j, k, n1, n2);
-  const float r = ((w[c] - w[hidx(i, j, k - 1, n1, n2)]) * dti * dzfi[k] + (v[c] - v[hidx(i, j - 1, k, n1, n2)]) * dtidyi) +
-                  (u[c] - u[hidx(i - 1, j, k, n1, n2)]) * dtidxi;
+  const int i = blockIdx.x * kBX + threadIdx.x + 1, j = blockIdx.y * kBY + threadIdx.y + 1, k = blockIdx.z + 1;
+  if (i > d.n1 || j > d.n2) return;
+  const int sy = d.n1 + 2;
+  const size_t sz = (size_t)sy * (d.n2 + 2);
+  const size_t c = (size_t)k * sz + (size_t)(j * sy + i);
+  const float r = ((w[c] - w[c - sz]) * dti * dzfi[k] + (v[c] - v[c - sy]) * dtidyi) + (u[c] - u[c - 1]) * dtidxi;
   p[c] = f2d(r);
+}
+
+inline dim3 grid_interior(const int n[3]) {
+  return dim3((unsigned)((n[0] + kBX - 1) / kBX), (unsigned)((n[1] + kBY - 1) / kBY), (unsigned)n[2]);
+}
+inline dim3 grid_haloed(const int n[3]) {
+  return dim3((unsigned)((n[0] + 2 + kBX - 1) / kBX), (unsigned)((n[1] + 2 + kBY - 1) / kBY), (unsigned)(n[2] + 2));
 }
 
 extern "C" int cans_fillps_f32(const int n[3], const double dli[3], const float *dzfi, double dti, const float *u,
@@ -64,8 +93,9 @@ extern "C" int cans_fillps_f32(const int n[3], const double dli[3], const float 
   if (!n || !dli || !dzfi || !u || !v || !w || !p || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   Dims d{n[0], n[1], n[2]};
   const long cnt = (long)n[0] * n[1] * n[2];
-  k_fillps32<<<blocks_for(cnt), kTB, 0, as_stream(stream)>>>(d, (float)dti, (float)(dti * dli[0]),
-                                                              (float)(dti * dli[1]), dzfi, u, v, w, p);
+  (void)cnt;
+  k_fillps32<<<grid_interior(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(d, (float)dti, (float)(dti * dli[0]),
+                                                                        (float)(dti * dli[1]), dzfi, u, v, w, p);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
@@ -80,39 +110,52 @@ __device__ __forceinline__ float ddiff(double a, float bh, float bl) {
   return (ah - bh) + (al - bl);
 }
 
+// one thread per haloed cell (the reference's ranges: u for i <= n1, v for j <= n2, w for
+// k <= n3); with pres != nullptr also updatep's explicit p += pp on the interior (the two
+// calls read the same pp and touch disjoint fields, so one pass serves both)
 __global__ void __launch_bounds__(kTB) k_correc32(Dims d, float fi, float fj, float dt,
                                                   const float *__restrict__ dzci, const double *__restrict__ p,
                                                   float *__restrict__ u, float *__restrict__ v,
-                                                  float *__restrict__ w) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long nx = d.n1 + 2, ny = d.n2 + 2;
-  if (t >= nx * ny * (d.n3 + 2)) return;
-  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / (nx * ny));
-  const int n1 = d.n1, n2 = d.n2;
-  const size_t c = (size_t)t;
+                                                  float *__restrict__ w, float *__restrict__ pres) {
+  const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y, k = blockIdx.z;
+  if (i > d.n1 + 1 || j > d.n2 + 1) return;
+  const int sy = d.n1 + 2;
+  const size_t sz = (size_t)sy * (d.n2 + 2);
+  const size_t c = (size_t)k * sz + (size_t)(j * sy + i);
   float ph, pl;
   d2f_split(p[c], ph, pl);
   if (i <= d.n1) u[c] = u[c] - fi * ddiff(p[c + 1], ph, pl);
-  if (j <= d.n2) v[c] = v[c] - fj * ddiff(p[hidx(i, j + 1, k, n1, n2)], ph, pl);
-  if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * ddiff(p[hidx(i, j, k + 1, n1, n2)], ph, pl);
+  if (j <= d.n2) v[c] = v[c] - fj * ddiff(p[c + sy], ph, pl);
+  if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * ddiff(p[c + sz], ph, pl);
+  if (pres && i >= 1 && i <= d.n1 && j >= 1 && j <= d.n2 && k >= 1 && k <= d.n3) pres[c] = pres[c] + ph;
 }
 
 extern "C" int cans_correc_f32(const int n[3], const double dli[3], const float *dzci, double dt, const double *p,
                                float *u, float *v, float *w, void *stream) {
   if (!n || !dli || !dzci || !p || !u || !v || !w || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   Dims d{n[0], n[1], n[2]};
-  const long cnt = (long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
-  k_correc32<<<blocks_for(cnt), kTB, 0, as_stream(stream)>>>(d, (float)(dt * dli[0]), (float)(dt * dli[1]),
-                                                              (float)dt, dzci, p, u, v, w);
+  k_correc32<<<grid_haloed(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(d, (float)(dt * dli[0]), (float)(dt * dli[1]),
+                                                                        (float)dt, dzci, p, u, v, w, nullptr);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
+extern "C" int cans_correc_updatep_f32(const int n[3], const double dli[3], const float *dzci, double dt,
+                                       const double *pp, float *u, float *v, float *w, float *p, void *stream) {
+  if (!n || !dli || !dzci || !pp || !u || !v || !w || !p || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
+  Dims d{n[0], n[1], n[2]};
+  k_correc32<<<grid_haloed(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(d, (float)(dt * dli[0]), (float)(dt * dli[1]),
+                                                                        (float)dt, dzci, pp, u, v, w, p);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
 
 // ------------------------------------------------------------------------------ updatep
 __global__ void __launch_bounds__(kTB) k_updatep32(Dims d, const double *__restrict__ pp, float *__restrict__ p) {
-  int i, j, k;
-  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
-  const size_t c = hidx(i, j, k, d.n1, d.n2);
+  const int i = blockIdx.x * kBX + threadIdx.x + 1, j = blockIdx.y * kBY + threadIdx.y + 1, k = blockIdx.z + 1;
+  if (i > d.n1 || j > d.n2) return;
+  const int sy = d.n1 + 2;
+  const size_t c = (size_t)k * sy * (d.n2 + 2) + (size_t)(j * sy + i);
   p[c] = p[c] + d2f_rn(pp[c]);
 }
 
@@ -122,17 +165,32 @@ extern "C" int cans_updatep_f32(const int n[3], const double dli[3], const float
   if (!n || !dli || !dzci || !dzfi || !pp || !p || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   if (is_impdiff) return CANS_ENOTSUP;  // the FP32 run has explicit diffusion only
   Dims d{n[0], n[1], n[2]};
-  k_updatep32<<<blocks_for((long)n[0] * n[1] * n[2]), kTB, 0, as_stream(stream)>>>(d, pp, p);
+  k_updatep32<<<grid_interior(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(d, pp, p);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
 
 // ------------------------------------------------------------------------------ momentum
-// mom_xyz_ad + RK update with the new velocity written to haloed arrays (the second velocity
-// buffer, or the library scratch of the in-place call); with `partials` each block also
-// writes the FP64 sums of gvr_f*u_new, gvr_f*v_new, gvr_c*w_new (the bulk means of
-// src/utils.f90:15-42) to partials[3*block + c]
-__global__ void __launch_bounds__(kTB) k_mom_rk32(Dims d, float dxi, float dyi, float visc, float f1, float f2,
+// mom_xyz_ad + RK update (mom_rk_point, the FP64 kernels' arithmetic in FP32) with the new
+// velocity written to haloed arrays (the second velocity buffer, or the library scratch of the
+// in-place call).  A 32 x 8 thread block owns an (i, j) tile and marches up kMomK planes of k:
+// the values of planes k-1 and k that plane k+1's cells need again (u, v, w, p at (i, j) and
+// the few in-plane neighbours the z terms use) stay in registers, so each step loads the 6
+// new plane-(k+1) values and the 14 in-plane neighbours (L1 hits: the warp's own rows), with
+// 32-bit in-plane offsets and no index division.  With `partials` each block also writes the
+// FP64 sums of gvr_f u_new, gvr_f v_new, gvr_c w_new (the bulk means of src/utils.f90:15-42;
+// Kahan sums per thread, FP32 warp sums, FP64 across warps) to partials[3*block + c].
+constexpr int kMomK = 16;
+inline dim3 grid_mom(const int n[3]) {
+  return dim3((unsigned)((n[0] + kBX - 1) / kBX), (unsigned)((n[1] + kBY - 1) / kBY),
+              (unsigned)((n[2] + kMomK - 1) / kMomK));
+}
+inline size_t mom_blocks(const int n[3]) {
+  const dim3 g = grid_mom(n);
+  return (size_t)g.x * g.y * g.z;
+}
+
+__global__ void __launch_bounds__(kTB, 3) k_mom_rk32(Dims d, float dxi, float dyi, float visc, float f1, float f2,
                                                   float f12, float bfx, float bfy, float bfz,
                                                   const float *__restrict__ dzci, const float *__restrict__ dzfi,
                                                   const float *__restrict__ u, const float *__restrict__ v,
@@ -142,23 +200,57 @@ __global__ void __launch_bounds__(kTB) k_mom_rk32(Dims d, float dxi, float dyi, 
                                                   float *__restrict__ vn, float *__restrict__ wn,
                                                   const float *__restrict__ gvr_c, const float *__restrict__ gvr_f,
                                                   double *__restrict__ partials) {
-  float nv[3] = {0.f, 0.f, 0.f};
-  int k = 0;
-  const bool in = mom_rk_cell<float, true>(d, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, 0, dzci, dzfi, u, v, w, p,
-                                           dudtrko, dvdtrko, dwdtrko, un, vn, wn, nullptr,
-                                           (long)blockIdx.x * blockDim.x + threadIdx.x, nullptr, 0.f, 0.f, 0.f,
-                                           0.f, nv, &k);
-  if (!partials) return;  // uniform over the grid
-  float s[3] = {0.f, 0.f, 0.f};
-  if (in) {
-    s[0] = nv[0] * gvr_f[k];
-    s[1] = nv[1] * gvr_f[k];
-    s[2] = nv[2] * gvr_c[k];
+  const int i = blockIdx.x * kBX + threadIdx.x + 1, j = blockIdx.y * kBY + threadIdx.y + 1;
+  const int k0 = blockIdx.z * kMomK + 1, k1 = min(k0 + kMomK - 1, d.n3);
+  float s[3] = {0.f, 0.f, 0.f}, e[3] = {0.f, 0.f, 0.f};
+  if (i <= d.n1 && j <= d.n2) {
+    const int sy = d.n1 + 2;
+    const size_t sz = (size_t)sy * (d.n2 + 2);
+    const size_t nxy = (size_t)d.n1 * d.n2;
+    const size_t o = (size_t)(j * sy + i);
+    MomIn<float> m;
+    // window at k0: planes k0 - 1 and k0
+    {
+      const size_t cm = (size_t)(k0 - 1) * sz + o, c = cm + sz;
+      m.u_ccc = u[cm]; m.v_ccc = v[cm]; m.w_ccc = w[cm]; m.w_pcc = w[cm + 1]; m.w_cpc = w[cm + sy];
+      m.u_ccp = u[c]; m.u_mcp = u[c - 1]; m.v_ccp = v[c]; m.v_cmp = v[c - sy]; m.w_ccp = w[c]; m.p_ccp = p[c];
+    }
+    size_t h = (size_t)(i - 1) + (size_t)d.n1 * (size_t)(j - 1) + nxy * (size_t)(k0 - 1);
+    for (int k = k0; k <= k1; k++, h += nxy) {
+      const size_t c = (size_t)k * sz + o, cp = c + sz;
+      // roll the window: plane k becomes the centre, plane k-1 the lower neighbour
+      m.u_ccm = m.u_ccc; m.v_ccm = m.v_ccc; m.w_ccm = m.w_ccc; m.w_pcm = m.w_pcc; m.w_cpm = m.w_cpc;
+      m.u_ccc = m.u_ccp; m.u_mcc = m.u_mcp; m.v_ccc = m.v_ccp; m.v_cmc = m.v_cmp; m.w_ccc = m.w_ccp;
+      m.p_ccc = m.p_ccp;
+      // plane k+1
+      m.u_ccp = u[cp]; m.u_mcp = u[cp - 1]; m.v_ccp = v[cp]; m.v_cmp = v[cp - sy]; m.w_ccp = w[cp]; m.p_ccp = p[cp];
+      // in-plane neighbours at plane k
+      m.u_pcc = u[c + 1]; m.u_cmc = u[c - sy]; m.u_cpc = u[c + sy]; m.u_mpc = u[c - 1 + sy];
+      m.v_mcc = v[c - 1]; m.v_pcc = v[c + 1]; m.v_cpc = v[c + sy]; m.v_pmc = v[c + 1 - sy];
+      m.w_mcc = w[c - 1]; m.w_pcc = w[c + 1]; m.w_cmc = w[c - sy]; m.w_cpc = w[c + sy];
+      m.p_pcc = p[c + 1]; m.p_cpc = p[c + sy];
+      m.dzci_k = dzci[k]; m.dzci_km = dzci[k - 1]; m.dzfi_k = dzfi[k]; m.dzfi_kp = dzfi[k + 1];
+      float dudt, dvdt, dwdt, nu, nv, nw, dud, dvd, dwd;
+      mom_rk_point<float>(m, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, 0, dudtrko[h], dvdtrko[h], dwdtrko[h],
+                          dudt, dvdt, dwdt, nu, nv, nw, dud, dvd, dwd);
+      dudtrko[h] = dudt; dvdtrko[h] = dvdt; dwdtrko[h] = dwdt;
+      un[c] = nu; vn[c] = nv; wn[c] = nw;
+      if (partials) {
+        kahan_add(s[0], e[0], nu * gvr_f[k]);
+        kahan_add(s[1], e[1], nv * gvr_f[k]);
+        kahan_add(s[2], e[2], nw * gvr_c[k]);
+      }
+      // the window keeps w(i+1, j, k) and w(i, j+1, k) for the next plane's w_pcm, w_cpm
+    }
   }
+  if (!partials) return;  // uniform over the grid
+  for (int c = 0; c < 3; c++) e[c] = -e[c];  // Kahan: the total is s - e
   double tot[3];
-  block_sum_f64<3>(s, tot);
-  if (threadIdx.x == 0)
-    for (int c = 0; c < 3; c++) partials[(size_t)blockIdx.x * 3 + c] = tot[c];
+  block_sum_f64<3>(s, e, tot, tid2());
+  if (tid2() == 0) {
+    const size_t b = ((size_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    for (int c = 0; c < 3; c++) partials[b * 3 + c] = tot[c];
+  }
 }
 
 // bulk means (FP64 sums of the block partials) and the forcing f_c = velf_c - mean_c of
@@ -190,8 +282,8 @@ __global__ void k_rk_means32(const double *__restrict__ partials, long nblk, dou
 __global__ void __launch_bounds__(kTB) k_rk_forcing32(Dims d, const double *__restrict__ fout, int fx, int fy, int fz,
                                                       float *__restrict__ u, float *__restrict__ v,
                                                       float *__restrict__ w) {
-  int i, j, k;
-  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const int i = blockIdx.x * kBX + threadIdx.x + 1, j = blockIdx.y * kBY + threadIdx.y + 1, k = blockIdx.z + 1;
+  if (i > d.n1 || j > d.n2) return;
   const float *ff = reinterpret_cast<const float *>(fout + 3);
   const size_t c = hidx(i, j, k, d.n1, d.n2);
   if (fx) u[c] = u[c] + ff[0];
@@ -204,8 +296,8 @@ __global__ void __launch_bounds__(kTB) k_copy_interior32(Dims d, const float *__
                                                          const float *__restrict__ vn, const float *__restrict__ wn,
                                                          float *__restrict__ u, float *__restrict__ v,
                                                          float *__restrict__ w) {
-  int i, j, k;
-  if (!cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const int i = blockIdx.x * kBX + threadIdx.x + 1, j = blockIdx.y * kBY + threadIdx.y + 1, k = blockIdx.z + 1;
+  if (i > d.n1 || j > d.n2) return;
   const size_t c = hidx(i, j, k, d.n1, d.n2);
   u[c] = un[c]; v[c] = vn[c]; w[c] = wn[c];
 }
@@ -213,7 +305,7 @@ __global__ void __launch_bounds__(kTB) k_copy_interior32(Dims d, const float *__
 extern "C" size_t cans_rk_f32_work_bytes(const int n[3], int in_place) {
   if (!n) return 0;
   const size_t nh = (size_t)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
-  const size_t nblk = blocks_for((long)n[0] * n[1] * n[2]);
+  const size_t nblk = mom_blocks(n);
   size_t b = (3 * nblk + 8) * sizeof(double);
   b = (b + 255) & ~(size_t)255;
   return b + (in_place ? 3 * nh * sizeof(float) : 0);
@@ -233,8 +325,7 @@ extern "C" int cans_rk_f32(const double rkpar[2], const int n[3], const double d
   if (in_place != (vnew == v) || in_place != (wnew == w)) return CANS_EINVAL;
   cudaStream_t st = as_stream(stream);
   Dims d{n[0], n[1], n[2]};
-  const long np = (long)n[0] * n[1] * n[2];
-  const unsigned nblk = blocks_for(np);
+  const size_t nblk = mom_blocks(n);
   const bool forced = is_forced[0] || is_forced[1] || is_forced[2];
   // work: partials (3 nblk) + f (3 doubles + 3 floats) doubles, then (in place) three haloed buffers
   double *partials = static_cast<double *>(work), *fdev = partials + 3 * (size_t)nblk;
@@ -247,19 +338,22 @@ extern "C" int cans_rk_f32(const double rkpar[2], const int n[3], const double d
     wn = vn + nh;
   }
   const float f1 = (float)(rkpar[0] * dt), f2 = (float)(rkpar[1] * dt), f12 = (float)((rkpar[0] + rkpar[1]) * dt);
-  k_mom_rk32<<<nblk, kTB, 0, st>>>(d, (float)dli[0], (float)dli[1], (float)visc, f1, f2, f12, (float)bforce[0],
-                                    (float)bforce[1], (float)bforce[2], dzci, dzfi, u, v, w, p, dudtrko, dvdtrko,
-                                    dwdtrko, un, vn, wn, gvr_c, gvr_f, forced ? partials : nullptr);
+  const dim3 blk(kBX, kBY);
+  k_mom_rk32<<<grid_mom(n), blk, 0, st>>>(d, (float)dli[0], (float)dli[1], (float)visc, f1, f2, f12,
+                                           (float)bforce[0], (float)bforce[1], (float)bforce[2], dzci, dzfi, u, v, w,
+                                           p, dudtrko, dvdtrko, dwdtrko, un, vn, wn, gvr_c, gvr_f,
+                                           forced ? partials : nullptr);
   CANS_LAUNCH_CHECK();
   if (in_place) {
-    k_copy_interior32<<<nblk, kTB, 0, st>>>(d, un, vn, wn, u, v, w);
+    k_copy_interior32<<<grid_interior(n), blk, 0, st>>>(d, un, vn, wn, u, v, w);
     CANS_LAUNCH_CHECK();
   }
   if (forced) {
-    k_rk_means32<<<1, kTB, 0, st>>>(partials, nblk, velf[0], velf[1], velf[2], is_forced[0], is_forced[1],
+    k_rk_means32<<<1, kTB, 0, st>>>(partials, (long)nblk, velf[0], velf[1], velf[2], is_forced[0], is_forced[1],
                                      is_forced[2], fdev);
     CANS_LAUNCH_CHECK();
-    k_rk_forcing32<<<nblk, kTB, 0, st>>>(d, fdev, is_forced[0], is_forced[1], is_forced[2], unew, vnew, wnew);
+    k_rk_forcing32<<<grid_interior(n), blk, 0, st>>>(d, fdev, is_forced[0], is_forced[1], is_forced[2], unew, vnew,
+                                                      wnew);
     CANS_LAUNCH_CHECK();
   }
   if (f) {
@@ -353,7 +447,7 @@ __global__ void __launch_bounds__(kTB) k_chkdiv32(Dims d, float dxi, float dyi, 
   }
   block_max_f32(mx, part_max);
   double tot[1];
-  block_sum_f64<1>(s, tot);
+  block_sum_f64<1>(s, tot, threadIdx.x);
   if (threadIdx.x == 0) part_sum[blockIdx.x] = tot[0];
 }
 
@@ -453,7 +547,7 @@ __global__ void __launch_bounds__(kTB) k_bulk_mean32(Dims d, const float *__rest
   float s[1] = {0.f};
   if (cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) s[0] = p[hidx(i, j, k, d.n1, d.n2)] * gvr[k];
   double tot[1];
-  block_sum_f64<1>(s, tot);
+  block_sum_f64<1>(s, tot, threadIdx.x);
   if (threadIdx.x == 0) part[blockIdx.x] = tot[0];
 }
 

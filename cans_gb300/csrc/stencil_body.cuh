@@ -69,12 +69,77 @@ __device__ __forceinline__ void updatep_cell(const Dims &d, double dxi, double d
   }
 }
 
-// mom_xyz_ad (src/mom.f90:771-1019) fused with the RK update of src/rk.f90:155-186 at
-// interior cell t, in the field precision T (double; float for the FP32 run, the reference's
-// single-precision build of src/types.f90:12-18).  The new velocity goes to un/vn/wn: halo-free
-// index (HALO_OUT false: the FP64 kernels' scratch) or haloed index (HALO_OUT true: the
-// out-of-place FP32 kernel writing the second velocity buffer); dudtrko in place, dudtd to
-// dtd (impdiff, halo-free, 3 fields).  Returns false past the end.
+// The 27 velocity values, 4 pressure values and 4 grid factors the fused momentum update of
+// one cell reads: name suffix = offset in (x, y, z), m = -1, c = 0, p = +1.
+template <typename T> struct MomIn {
+  T u_ccm, u_cmc, u_mcc, u_ccc, u_pcc, u_mpc, u_cpc, u_mcp, u_ccp;
+  T v_ccm, v_cmc, v_pmc, v_mcc, v_ccc, v_pcc, v_cpc, v_ccp, v_cmp;
+  T w_ccm, w_pcm, w_cpm, w_cmc, w_mcc, w_ccc, w_pcc, w_cpc, w_ccp;
+  T p_ccc, p_pcc, p_cpc, p_ccp;
+  T dzci_k, dzci_km, dzfi_k, dzfi_kp;
+};
+
+// mom_xyz_ad (src/mom.f90:771-1019) and the RK update of src/rk.f90:155-186 on the values of
+// one cell, in the field precision T (double; float for the FP32 run, the reference's
+// single-precision build of src/types.f90:12-18): returns the new dudtrko (dudt...), the
+// updated velocity before buoyancy and implicit-diffusion terms (un...) and the implicit part
+// (dud..., zero unless impdiff).  dto_*: the old dudtrko.
+template <typename T>
+__device__ __forceinline__ void mom_rk_point(const MomIn<T> &m, T dxi, T dyi, T visc, T f1, T f2, T f12, T bfx,
+                                             T bfy, T bfz, int impdiff, T dto_u, T dto_v, T dto_w, T &dudt, T &dvdt,
+                                             T &dwdt, T &un, T &vn, T &wn, T &dud, T &dvd, T &dwd) {
+  const T q = T(0.25);
+  const T dzci_k = m.dzci_k, dzci_km = m.dzci_km, dzfi_k = m.dzfi_k, dzfi_kp = m.dzfi_kp;
+  const T rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
+  // x
+  const T dudxp = (m.u_pcc - m.u_ccc) * dxi, dudxm = (m.u_ccc - m.u_mcc) * dxi;
+  const T dudyp = (m.u_cpc - m.u_ccc) * dyi, dudym = (m.u_ccc - m.u_cmc) * dyi;
+  const T dudzp = (m.u_ccp - m.u_ccc) * dzci_k, dudzm = (m.u_ccc - m.u_ccm) * dzci_km;
+  const T uuip = q * (m.u_ccc + m.u_pcc) * m.u_pcc, uuim = q * (m.u_ccc + m.u_mcc) * m.u_mcc;
+  const T vujp = q * (m.v_ccc + m.v_pcc) * m.u_cpc, vujm = q * (m.v_cmc + m.v_pmc) * m.u_cmc;
+  const T wukp = q * (m.w_ccc + m.w_pcc) * m.u_ccp, wukm = q * (m.w_ccm + m.w_pcm) * m.u_ccm;
+  const T dudtd_xy = visc * (dudxp - dudxm) * dxi + visc * (dudyp - dudym) * dyi;
+  const T dudtd_z = visc * (dudzp - dudzm) * dzfi_k;
+  dudt = -(uuip - uuim) * dxi - (vujp - vujm) * dyi - (wukp - wukm) * dzfi_k;
+  // y
+  const T dvdxp = (m.v_pcc - m.v_ccc) * dxi, dvdxm = (m.v_ccc - m.v_mcc) * dxi;
+  const T dvdyp = (m.v_cpc - m.v_ccc) * dyi, dvdym = (m.v_ccc - m.v_cmc) * dyi;
+  const T dvdzp = (m.v_ccp - m.v_ccc) * dzci_k, dvdzm = (m.v_ccc - m.v_ccm) * dzci_km;
+  const T uvip = q * (m.u_ccc + m.u_cpc) * m.v_pcc, uvim = q * (m.u_mcc + m.u_mpc) * m.v_mcc;
+  const T vvjp = q * (m.v_ccc + m.v_cpc) * m.v_cpc, vvjm = q * (m.v_ccc + m.v_cmc) * m.v_cmc;
+  const T wvkp = q * (m.w_ccc + m.w_cpc) * m.v_ccp, wvkm = q * (m.w_ccm + m.w_cpm) * m.v_ccm;
+  const T dvdtd_xy = visc * (dvdxp - dvdxm) * dxi + visc * (dvdyp - dvdym) * dyi;
+  const T dvdtd_z = visc * (dvdzp - dvdzm) * dzfi_k;
+  dvdt = -(uvip - uvim) * dxi - (vvjp - vvjm) * dyi - (wvkp - wvkm) * dzfi_k;
+  // z
+  const T dwdxp = (m.w_pcc - m.w_ccc) * dxi, dwdxm = (m.w_ccc - m.w_mcc) * dxi;
+  const T dwdyp = (m.w_cpc - m.w_ccc) * dyi, dwdym = (m.w_ccc - m.w_cmc) * dyi;
+  const T dwdzp = (m.w_ccp - m.w_ccc) * dzfi_kp, dwdzm = (m.w_ccc - m.w_ccm) * dzfi_k;
+  const T uwip = q * (rdzm * m.u_ccc + rdzp * m.u_ccp) * m.w_pcc;
+  const T uwim = q * (rdzm * m.u_mcc + rdzp * m.u_mcp) * m.w_mcc;
+  const T vwjp = q * (rdzm * m.v_ccc + rdzp * m.v_ccp) * m.w_cpc;
+  const T vwjm = q * (rdzm * m.v_cmc + rdzp * m.v_cmp) * m.w_cmc;
+  const T wwkp = q * (m.w_ccc + m.w_ccp) * m.w_ccp, wwkm = q * (m.w_ccc + m.w_ccm) * m.w_ccm;
+  const T dwdtd_xy = visc * (dwdxp - dwdxm) * dxi + visc * (dwdyp - dwdym) * dyi;
+  const T dwdtd_z = visc * (dwdzp - dwdzm) * dzci_k;
+  dwdt = -(uwip - uwim) * dxi - (vwjp - vwjm) * dyi - (wwkp - wwkm) * dzci_k;
+  dud = T(0); dvd = T(0); dwd = T(0);
+  if (impdiff) {
+    dud = dudtd_xy + dudtd_z; dvd = dvdtd_xy + dvdtd_z; dwd = dwdtd_xy + dwdtd_z;
+  } else {
+    dudt = dudt + dudtd_xy + dudtd_z;
+    dvdt = dvdt + dvdtd_xy + dvdtd_z;
+    dwdt = dwdt + dwdtd_xy + dwdtd_z;
+  }
+  un = m.u_ccc + f1 * dudt + f2 * dto_u + f12 * (bfx - dxi * (m.p_pcc - m.p_ccc));
+  vn = m.v_ccc + f1 * dvdt + f2 * dto_v + f12 * (bfy - dyi * (m.p_cpc - m.p_ccc));
+  wn = m.w_ccc + f1 * dwdt + f2 * dto_w + f12 * (bfz - dzci_k * (m.p_ccp - m.p_ccc));
+}
+
+// mom_xyz_ad fused with the RK update (mom_rk_point) at interior cell t, loading the values
+// from the haloed fields.  The new velocity goes to un/vn/wn: halo-free index (HALO_OUT
+// false: the FP64 kernels' scratch) or haloed index (HALO_OUT true); dudtrko in place, dudtd
+// to dtd (impdiff, halo-free, 3 fields).  Returns false past the end.
 template <typename T, bool HALO_OUT = false>
 __device__ __forceinline__ bool mom_rk_cell(const Dims &d, T dxi, T dyi, T visc, T f1, T f2, T f12, T bfx, T bfy,
                                             T bfz, int impdiff, const T *__restrict__ dzci,
@@ -84,66 +149,26 @@ __device__ __forceinline__ bool mom_rk_cell(const Dims &d, T dxi, T dyi, T visc,
                                             T *__restrict__ dvdtrko, T *__restrict__ dwdtrko, T *__restrict__ un_out,
                                             T *__restrict__ vn_out, T *__restrict__ wn_out, T *__restrict__ dtd,
                                             long t, const T *__restrict__ sb = nullptr, T gbx = T(0),
-                                            T gby = T(0), T gbz = T(0), T beta = T(0), T *newvel = nullptr,
-                                            int *kout = nullptr) {
+                                            T gby = T(0), T gbz = T(0), T beta = T(0)) {
   int i, j, k;
   if (!cell3(t, d, i, j, k)) return false;
   const int n1 = d.n1, n2 = d.n2;
   const size_t np = (size_t)d.n1 * d.n2 * d.n3;
   const size_t sx = 1, sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
   const size_t c = hidx(i, j, k, n1, n2);
-  const T q = T(0.25);
-  const T dzci_k = dzci[k], dzci_km = dzci[k - 1], dzfi_k = dzfi[k], dzfi_kp = dzfi[k + 1];
-  const T rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
-  const T u_ccm = u[c - sz], u_cmc = u[c - sy], u_mcc = u[c - sx], u_ccc = u[c], u_pcc = u[c + sx],
-          u_mpc = u[c - sx + sy], u_cpc = u[c + sy], u_mcp = u[c - sx + sz], u_ccp = u[c + sz];
-  const T v_ccm = v[c - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx],
-          v_ccc = v[c], v_pcc = v[c + sx], v_cpc = v[c + sy], v_ccp = v[c + sz], v_cmp = v[c - sy + sz];
-  const T w_ccm = w[c - sz], w_pcm = w[c + sx - sz], w_cpm = w[c + sy - sz], w_cmc = w[c - sy], w_mcc = w[c - sx],
-          w_ccc = w[c], w_pcc = w[c + sx], w_cpc = w[c + sy], w_ccp = w[c + sz];
-  // x
-  const T dudxp = (u_pcc - u_ccc) * dxi, dudxm = (u_ccc - u_mcc) * dxi;
-  const T dudyp = (u_cpc - u_ccc) * dyi, dudym = (u_ccc - u_cmc) * dyi;
-  const T dudzp = (u_ccp - u_ccc) * dzci_k, dudzm = (u_ccc - u_ccm) * dzci_km;
-  const T uuip = q * (u_ccc + u_pcc) * u_pcc, uuim = q * (u_ccc + u_mcc) * u_mcc;
-  const T vujp = q * (v_ccc + v_pcc) * u_cpc, vujm = q * (v_cmc + v_pmc) * u_cmc;
-  const T wukp = q * (w_ccc + w_pcc) * u_ccp, wukm = q * (w_ccm + w_pcm) * u_ccm;
-  const T dudtd_xy = visc * (dudxp - dudxm) * dxi + visc * (dudyp - dudym) * dyi;
-  const T dudtd_z = visc * (dudzp - dudzm) * dzfi_k;
-  T dudt = -(uuip - uuim) * dxi - (vujp - vujm) * dyi - (wukp - wukm) * dzfi_k;
-  // y
-  const T dvdxp = (v_pcc - v_ccc) * dxi, dvdxm = (v_ccc - v_mcc) * dxi;
-  const T dvdyp = (v_cpc - v_ccc) * dyi, dvdym = (v_ccc - v_cmc) * dyi;
-  const T dvdzp = (v_ccp - v_ccc) * dzci_k, dvdzm = (v_ccc - v_ccm) * dzci_km;
-  const T uvip = q * (u_ccc + u_cpc) * v_pcc, uvim = q * (u_mcc + u_mpc) * v_mcc;
-  const T vvjp = q * (v_ccc + v_cpc) * v_cpc, vvjm = q * (v_ccc + v_cmc) * v_cmc;
-  const T wvkp = q * (w_ccc + w_cpc) * v_ccp, wvkm = q * (w_ccm + w_cpm) * v_ccm;
-  const T dvdtd_xy = visc * (dvdxp - dvdxm) * dxi + visc * (dvdyp - dvdym) * dyi;
-  const T dvdtd_z = visc * (dvdzp - dvdzm) * dzfi_k;
-  T dvdt = -(uvip - uvim) * dxi - (vvjp - vvjm) * dyi - (wvkp - wvkm) * dzfi_k;
-  // z
-  const T dwdxp = (w_pcc - w_ccc) * dxi, dwdxm = (w_ccc - w_mcc) * dxi;
-  const T dwdyp = (w_cpc - w_ccc) * dyi, dwdym = (w_ccc - w_cmc) * dyi;
-  const T dwdzp = (w_ccp - w_ccc) * dzfi_kp, dwdzm = (w_ccc - w_ccm) * dzfi_k;
-  const T uwip = q * (rdzm * u_ccc + rdzp * u_ccp) * w_pcc, uwim = q * (rdzm * u_mcc + rdzp * u_mcp) * w_mcc;
-  const T vwjp = q * (rdzm * v_ccc + rdzp * v_ccp) * w_cpc, vwjm = q * (rdzm * v_cmc + rdzp * v_cmp) * w_cmc;
-  const T wwkp = q * (w_ccc + w_ccp) * w_ccp, wwkm = q * (w_ccc + w_ccm) * w_ccm;
-  const T dwdtd_xy = visc * (dwdxp - dwdxm) * dxi + visc * (dwdyp - dwdym) * dyi;
-  const T dwdtd_z = visc * (dwdzp - dwdzm) * dzci_k;
-  T dwdt = -(uwip - uwim) * dxi - (vwjp - vwjm) * dyi - (wwkp - wwkm) * dzci_k;
-  T dud = T(0), dvd = T(0), dwd = T(0);
-  if (impdiff) {
-    dud = dudtd_xy + dudtd_z; dvd = dvdtd_xy + dvdtd_z; dwd = dwdtd_xy + dwdtd_z;
-  } else {
-    dudt = dudt + dudtd_xy + dudtd_z;
-    dvdt = dvdt + dvdtd_xy + dvdtd_z;
-    dwdt = dwdt + dwdtd_xy + dwdtd_z;
-  }
+  MomIn<T> m;
+  m.dzci_k = dzci[k]; m.dzci_km = dzci[k - 1]; m.dzfi_k = dzfi[k]; m.dzfi_kp = dzfi[k + 1];
+  m.u_ccm = u[c - sz]; m.u_cmc = u[c - sy]; m.u_mcc = u[c - sx]; m.u_ccc = u[c]; m.u_pcc = u[c + sx];
+  m.u_mpc = u[c - sx + sy]; m.u_cpc = u[c + sy]; m.u_mcp = u[c - sx + sz]; m.u_ccp = u[c + sz];
+  m.v_ccm = v[c - sz]; m.v_cmc = v[c - sy]; m.v_pmc = v[c + sx - sy]; m.v_mcc = v[c - sx]; m.v_ccc = v[c];
+  m.v_pcc = v[c + sx]; m.v_cpc = v[c + sy]; m.v_ccp = v[c + sz]; m.v_cmp = v[c - sy + sz];
+  m.w_ccm = w[c - sz]; m.w_pcm = w[c + sx - sz]; m.w_cpm = w[c + sy - sz]; m.w_cmc = w[c - sy]; m.w_mcc = w[c - sx];
+  m.w_ccc = w[c]; m.w_pcc = w[c + sx]; m.w_cpc = w[c + sy]; m.w_ccp = w[c + sz];
+  m.p_ccc = p[c]; m.p_pcc = p[c + sx]; m.p_cpc = p[c + sy]; m.p_ccp = p[c + sz];
   const size_t h = (size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (size_t)(k - 1));
-  const T pc = p[c];
-  T un = u_ccc + f1 * dudt + f2 * dudtrko[h] + f12 * (bfx - dxi * (p[c + sx] - pc));
-  T vn = v_ccc + f1 * dvdt + f2 * dvdtrko[h] + f12 * (bfy - dyi * (p[c + sy] - pc));
-  T wn = w_ccc + f1 * dwdt + f2 * dwdtrko[h] + f12 * (bfz - dzci_k * (p[c + sz] - pc));
+  T dudt, dvdt, dwdt, un, vn, wn, dud, dvd, dwd;
+  mom_rk_point<T>(m, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, impdiff, dudtrko[h], dvdtrko[h], dwdtrko[h], dudt,
+                  dvdt, dwdt, un, vn, wn, dud, dvd, dwd);
   if (sb) {
     // Boussinesq buoyancy of the first scalar (src/rk.f90:163-177), gacc * beta
     const T sc = sb[c];
@@ -158,8 +183,6 @@ __device__ __forceinline__ bool mom_rk_cell(const Dims &d, T dxi, T dyi, T visc,
   dudtrko[h] = dudt; dvdtrko[h] = dvdt; dwdtrko[h] = dwdt;
   const size_t o = HALO_OUT ? c : h;
   un_out[o] = un; vn_out[o] = vn; wn_out[o] = wn;
-  if (newvel) { newvel[0] = un; newvel[1] = vn; newvel[2] = wn; }
-  if (kout) *kout = k;
   return true;
 }
 

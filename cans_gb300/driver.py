@@ -267,10 +267,11 @@ class Simulation:
                                           rtol=self.p_refine.get("rtol", 0.), max_iter=self.p_refine["max_iter"])
         self.p_refine_iters = max(self.p_refine_iters, it)
         cans.boundp(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.pp)
-        cans.correc_f32(n, self.dli, self.dzci32, dtrk, self.pp, self.u, self.v, self.w)
+        # correc and updatep in one pass over pp (they write disjoint fields), then the two
+        # boundary calls of src/main.f90:470,472
+        cans.correc_updatep_f32(n, self.dli, self.dzci32, dtrk, self.pp, self.u, self.v, self.w, self.p)
         cans.bounduvw_f32(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v,
                           self.w, True, cans.HALO_UPPER, cans.HALO_NONE)
-        cans.updatep_f32(n, self.dli, self.dzci32, self.dzfi32, 0., 0, self.pp, self.p)
         cans.boundp_f32(self.cbcpre, n, self.bcpre, self.is_bound, self.dl, self.dzc, self.p, cans.HALO_UPPER)
 
     def substep(self, irk):

@@ -166,6 +166,11 @@ int cans_correc_f32(const int n[3], const double dli[3], const float *dzci, doub
 /* updatep (src/updatep.f90:14), explicit form: p += pp rounded to FP32 */
 int cans_updatep_f32(const int n[3], const double dli[3], const float *dzci, const float *dzfi,
                      double alpha, int is_impdiff, const double *pp, float *p, void *stream);
+/* correc (src/correc.f90:13) and the explicit updatep (src/updatep.f90:14) in one pass over
+ * pp: the two read the same pp and write disjoint fields, so the host may call this in place
+ * of correc, bounduvw, updatep (src/main.f90:469-471), followed by bounduvw and boundp */
+int cans_correc_updatep_f32(const int n[3], const double dli[3], const float *dzci, double dt,
+                            const double *pp, float *u, float *v, float *w, float *p, void *stream);
 /* rk (src/rk.f90:24) with mom_xyz_ad (src/mom.f90:771): out of place when unew != u (the new
  * velocity goes to the interior of the haloed unew, vnew, wnew -- a second velocity buffer the
  * caller swaps with u, v, w afterwards; its ghost cells are left for the following bounduvw),
@@ -339,6 +344,15 @@ int cans_plan_autotune(cans_plan *plan, int force, double ms[2]);
  * (0: generic kernel) */
 int cans_plan_get_shape(const cans_plan *plan, int d, int radix[12], int *nstages, int *ncx,
                         int *spec);
+/* z pass of an FP32 plan (no counterpart in the reference; the elimination of
+ * src/solver_gpu.f90:278-428): mode 0 = one thread per spectral column sweeping all rows with
+ * precomputed factors; 1 = the column split into 16-row segments held in registers, factors
+ * formed on the fly, the segments joined by a cyclic reduction of their separator rows (non-
+ * periodic z with at most 512 rows; CANS_ENOTSUP otherwise); -1 = the automatic choice (by the
+ * number of columns; the default).  cans_plan_autotune measures both and keeps the faster.
+ * Results differ between the modes only by FP32 rounding of the correction solve. */
+int cans_plan_set_zpass(cans_plan *plan, int mode);
+int cans_plan_get_zpass(const cans_plan *plan, int *mode);
 int cans_batch_create(int nsys, cans_plan *const *plans, void *stream, cans_batch **batch);
 int cans_batch_destroy(cans_batch *batch);
 /* System s, on the field p[s] (device, haloed):

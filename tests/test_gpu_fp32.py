@@ -228,3 +228,21 @@ def test_fp32_run_forced_channel(require_gpu):
     print("FP32 channel after 6 steps, rel L2 vs oracle:", errs, "divmax", sim.divmax)
     assert errs["u"] <= 1e-6 and errs["v"] <= 1e-4 and errs["w"] <= 1e-4, errs
     assert not sim.kill
+
+
+def test_correc_updatep_fused_equals_separate(require_gpu):
+    """cans_correc_updatep_f32 writes exactly what correc_f32 + updatep_f32 write."""
+    import torch
+    from cans_gb300 import cans
+    n = (14, 12, 10)
+    dl, dli, dzc, dzf, dzci, dzfi, dzci_d, dzfi_d = _setup(n)
+    u, v, w, p = _fields32(n, 12)
+    pp = np.asfortranarray(_fields32(n, 13, 1)[0] * 1e-3 + 1e-12)
+    a = [_dev32(x) for x in (u, v, w, p)]
+    b = [x.clone() for x in a]
+    ppd = cans.to_device(pp)
+    cans.correc_f32(n, dli, dzci_d, 0.013, ppd, *a[:3])
+    cans.updatep_f32(n, dli, dzci_d, dzfi_d, 0., 0, ppd, a[3])
+    cans.correc_updatep_f32(n, dli, dzci_d, 0.013, ppd, *b)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)

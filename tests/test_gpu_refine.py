@@ -17,6 +17,13 @@ CASES = [
     ((10, 512, 12), (1.0, 4.0, 2.0), "NNPPNN", 1.3),           # FP32 register-FFT y pass
     ((256, 12, 10), (2.0, 1.0, 2.0), "NNPPNN", 1.3),           # FP32 persistent passes, 256
     ((12, 1024, 6), (1.0, 4.0, 2.0), "PPDDNN", 1.3),           # FP32 persistent passes, 1024
+    # the partitioned z pass (the default for few columns): 16-row segments, ragged last
+    # segment (37 = 2*16 + 5, 129 = 8*16 + 1), 24 and 32 segments (384, 512 rows: the
+    # benchmark grids), Dirichlet z
+    ((16, 12, 37), (4.0, 2.0, 2.0), "PPPPNN", 1.4),
+    ((8, 8, 129), (4.0, 2.0, 2.0), "PPPPNN", 1.3),
+    ((16, 16, 384), (4.0, 2.0, 2.0), "PPNNDD", 1.2),
+    ((24, 20, 512), (12.566, 6.283, 2.0), "PPPPNN", 1.4),
 ]
 
 
@@ -28,7 +35,15 @@ def _setup(n, l, cbc, gr, seed=2):
     ref = O.initsolver(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc")
     p = random_field(n, seed, zero_mean=singular(cbc), dzf=dzf)
     want = p.copy(order="F")
-    O.solver(n, ref["normfft"], ref["lambdaxy"], ref["a"], ref["b"], ref["c"], cbc, "ccc", want)
+    solve = lambda x: O.solver(n, ref["normfft"], ref["lambdaxy"], ref["a"], ref["b"], ref["c"], cbc, "ccc", x)
+    solve(want)
+    # accuracy reference: the oracle's FP64 solve plus one refinement step with an
+    # extended-precision residual (the FP64 solve alone carries ~1e-11 of rounding error on
+    # the ill-conditioned 512-row stretched columns)
+    e = O.field(n)
+    e[1:-1, 1:-1, 1:-1] = O.poisson_residual_ld(n, dli, cbc, ref["a"], ref["b"], ref["c"], want, p)
+    solve(e)
+    want[1:-1, 1:-1, 1:-1] += e[1:-1, 1:-1, 1:-1]
     return dl, dli, dzc, dzf, dzci, dzfi, p, want
 
 
@@ -58,8 +73,8 @@ def test_refined_reaches_fp64_accuracy(require_gpu, n, l, cbc, gr):
     got = cans.fview(d)[1:-1, 1:-1, 1:-1]
     w = want[1:-1, 1:-1, 1:-1]
     err = gauge_rel_l2(got, w, dzf) if singular(cbc) else rel_l2(got, w)
-    # the oracle is itself an FP64 solve: its rounding grows with the line length
-    assert err <= 1e-12 * max(1.0, max(n) / 256), (err, it, rr)
+    # against the extended-precision reference: the benchmark spec's flat 1e-12
+    assert err <= 1e-12, (err, it, rr)
     assert it <= 4 and rr <= 1e-14, (it, rr)
     # ghost cells untouched
     g = cans.fview(d)
@@ -158,3 +173,29 @@ def test_two_corrections_at_least_as_accurate_as_fp64_path(require_gpu):
     e2 = gauge_rel_l2(cans.fview(k2)[i3], r, dzf)
     e64 = gauge_rel_l2(cans.fview(x64)[i3], r, dzf)
     assert e2 <= e64, (e2, e64)
+
+
+@pytest.mark.parametrize("n,l,cbc,gr", [CASES[0], CASES[2], CASES[9], CASES[10], CASES[12]])
+def test_both_z_passes(require_gpu, n, l, cbc, gr):
+    """The column-sweep and the partitioned z pass of an FP32 plan: both FP32-accurate, and the
+    refined solves of both reach the same FP64 accuracy."""
+    import torch
+    from cans_gb300 import cans
+    dl, dli, dzc, dzf, dzci, dzfi, p, want = _setup(n, l, cbc, gr, seed=17)
+    plan = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc", precision=cans.FP32)
+    T = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
+    w = want[1:-1, 1:-1, 1:-1]
+    cmp = (lambda a: gauge_rel_l2(a, w, dzf)) if singular(cbc) else (lambda a: rel_l2(a, w))
+    errs = {}
+    for mode in (0, 1):
+        plan.set_zpass(mode)
+        assert plan.zpass == mode
+        d32 = cans.to_device(p, dtype=torch.float32)
+        plan.solve(d32)
+        d = cans.to_device(p)
+        plan.solve_refined(d, dli, T(dzci), T(dzfi), rtol=0.0, max_iter=3)
+        errs[mode] = (cmp(cans.fview(d32).astype(np.float64)[1:-1, 1:-1, 1:-1]), cmp(cans.fview(d)[1:-1, 1:-1, 1:-1]))
+    print("z passes (fp32 error, refined error):", errs)
+    for mode in (0, 1):
+        assert errs[mode][0] < 1e-5 and errs[mode][1] <= 1e-12, errs
+    plan.set_zpass(-1)
