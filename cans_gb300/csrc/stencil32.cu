@@ -68,24 +68,38 @@ __device__ __forceinline__ int tid2() { return threadIdx.y * kBX + threadIdx.x; 
 }  // namespace
 
 // ------------------------------------------------------------------------------ fillps
+// 32 x 8 tiles of (i, j) marching kMarch planes of k: w(i, j, k-1) is the previous plane's
+// w(i, j, k), kept in a register
+constexpr int kMarch = 16;
 __global__ void __launch_bounds__(kTB) k_fillps32(Dims d, float dti, float dtidxi, float dtidyi,
                                                   const float *__restrict__ dzfi, const float *__restrict__ u,
                                                   const float *__restrict__ v, const float *__restrict__ w,
                                                   double *__restrict__ p) {
-  const int i = blockIdx.x * kBX + threadIdx.x + 1, j = blockIdx.y * kBY + threadIdx.y + 1, k = blockIdx.z + 1;
+  const int i = blockIdx.x * kBX + threadIdx.x + 1, j = blockIdx.y * kBY + threadIdx.y + 1;
   if (i > d.n1 || j > d.n2) return;
+  const int k0 = blockIdx.z * kMarch + 1, k1 = min(k0 + kMarch - 1, d.n3);
   const int sy = d.n1 + 2;
   const size_t sz = (size_t)sy * (d.n2 + 2);
-  const size_t c = (size_t)k * sz + (size_t)(j * sy + i);
-  const float r = ((w[c] - w[c - sz]) * dti * dzfi[k] + (v[c] - v[c - sy]) * dtidyi) + (u[c] - u[c - 1]) * dtidxi;
-  p[c] = f2d(r);
+  size_t c = (size_t)k0 * sz + (size_t)(j * sy + i);
+  float wm = w[c - sz];
+  for (int k = k0; k <= k1; k++, c += sz) {
+    const float wc = w[c];
+    const float r = ((wc - wm) * dti * dzfi[k] + (v[c] - v[c - sy]) * dtidyi) + (u[c] - u[c - 1]) * dtidxi;
+    p[c] = f2d(r);
+    wm = wc;
+  }
 }
 
 inline dim3 grid_interior(const int n[3]) {
   return dim3((unsigned)((n[0] + kBX - 1) / kBX), (unsigned)((n[1] + kBY - 1) / kBY), (unsigned)n[2]);
 }
-inline dim3 grid_haloed(const int n[3]) {
-  return dim3((unsigned)((n[0] + 2 + kBX - 1) / kBX), (unsigned)((n[1] + 2 + kBY - 1) / kBY), (unsigned)(n[2] + 2));
+inline dim3 grid_march(const int n[3]) {
+  return dim3((unsigned)((n[0] + kBX - 1) / kBX), (unsigned)((n[1] + kBY - 1) / kBY),
+              (unsigned)((n[2] + kMarch - 1) / kMarch));
+}
+inline dim3 grid_march_haloed(const int n[3]) {
+  return dim3((unsigned)((n[0] + 2 + kBX - 1) / kBX), (unsigned)((n[1] + 2 + kBY - 1) / kBY),
+              (unsigned)((n[2] + 2 + kMarch - 1) / kMarch));
 }
 
 extern "C" int cans_fillps_f32(const int n[3], const double dli[3], const float *dzfi, double dti, const float *u,
@@ -94,48 +108,73 @@ extern "C" int cans_fillps_f32(const int n[3], const double dli[3], const float 
   Dims d{n[0], n[1], n[2]};
   const long cnt = (long)n[0] * n[1] * n[2];
   (void)cnt;
-  k_fillps32<<<grid_interior(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(d, (float)dti, (float)(dti * dli[0]),
+  k_fillps32<<<grid_march(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(d, (float)dti, (float)(dti * dli[0]),
                                                                         (float)(dti * dli[1]), dzfi, u, v, w, p);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
 
 // ------------------------------------------------------------------------------ correc
-// u -= dt*dxi*(pp(i+1) - pp(i)) with the FP64 difference taken on hi/lo float pairs: the hi
-// parts of neighbouring values differ by far less than a factor 2 on a resolved field, so
-// their difference is exact and the result matches the rounded FP64 difference to ~1 ulp
-__device__ __forceinline__ float ddiff(double a, float bh, float bl) {
-  float ah, al;
-  d2f_split(a, ah, al);
-  return (ah - bh) + (al - bl);
-}
-
-// one thread per haloed cell (the reference's ranges: u for i <= n1, v for j <= n2, w for
-// k <= n3); with pres != nullptr also updatep's explicit p += pp on the interior (the two
-// calls read the same pp and touch disjoint fields, so one pass serves both)
+// correc computes u -= dt*dxi*(pp(i+1) - pp(i)) with the FP64 difference taken on hi/lo float
+// pairs: the hi parts of neighbouring values differ by far less than a factor 2 on a resolved
+// field, so their difference is exact and the result matches the rounded FP64 difference to
+// ~1 ulp.
+// One thread per haloed (i, j) column of a 32 x 8 tile, marching kMarch planes of k (the
+// reference's ranges: u for i <= n1, v for j <= n2, w for k <= n3, over the haloed box); with
+// pres != nullptr also updatep's explicit p += pp on the interior (the two calls read the same
+// pp and touch disjoint fields, so one pass serves both).  Every pp value is split into its
+// hi/lo float pair once: the thread splits pp(i, j, k+1) (its next plane, also the +z
+// neighbour), takes the +x neighbour's split from the next lane and the +y neighbour's from
+// shared memory (edge lanes / rows split their extra neighbour themselves).
 __global__ void __launch_bounds__(kTB) k_correc32(Dims d, float fi, float fj, float dt,
                                                   const float *__restrict__ dzci, const double *__restrict__ p,
                                                   float *__restrict__ u, float *__restrict__ v,
                                                   float *__restrict__ w, float *__restrict__ pres) {
-  const int i = blockIdx.x * kBX + threadIdx.x, j = blockIdx.y * kBY + threadIdx.y, k = blockIdx.z;
-  if (i > d.n1 + 1 || j > d.n2 + 1) return;
+  __shared__ float2 sp[2][kBY][kBX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = blockIdx.x * kBX + tx, j = blockIdx.y * kBY + ty;
+  const bool act = i <= d.n1 + 1 && j <= d.n2 + 1;
+  const int k0 = blockIdx.z * kMarch, k1 = min(k0 + kMarch - 1, d.n3 + 1);
   const int sy = d.n1 + 2;
   const size_t sz = (size_t)sy * (d.n2 + 2);
-  const size_t c = (size_t)k * sz + (size_t)(j * sy + i);
-  float ph, pl;
-  d2f_split(p[c], ph, pl);
-  if (i <= d.n1) u[c] = u[c] - fi * ddiff(p[c + 1], ph, pl);
-  if (j <= d.n2) v[c] = v[c] - fj * ddiff(p[c + sy], ph, pl);
-  if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * ddiff(p[c + sz], ph, pl);
-  if (pres && i >= 1 && i <= d.n1 && j >= 1 && j <= d.n2 && k >= 1 && k <= d.n3) pres[c] = pres[c] + ph;
+  size_t c = (size_t)k0 * sz + (size_t)(j * sy + i);
+  const bool xin = i >= 1 && i <= d.n1, yin = j >= 1 && j <= d.n2;
+  float ph = 0.f, pl = 0.f;
+  if (act) d2f_split(p[c], ph, pl);
+  int buf = 0;
+  for (int k = k0; k <= k1; k++, c += sz) {
+    // plane k+1 of this column (the +z neighbour, and the next plane's own value)
+    float nh = 0.f, nl = 0.f;
+    if (act && k <= d.n3) d2f_split(p[c + sz], nh, nl);
+    sp[buf][ty][tx] = make_float2(ph, pl);
+    __syncthreads();
+    // +x from the next lane, +y from the next row (edges split it themselves)
+    float xh = __shfl_down_sync(0xffffffffu, ph, 1), xl = __shfl_down_sync(0xffffffffu, pl, 1);
+    float yh = 0.f, yl = 0.f;
+    if (act) {
+      if (tx == kBX - 1 && i <= d.n1) d2f_split(p[c + 1], xh, xl);
+      if (ty < kBY - 1) {
+        const float2 q = sp[buf][ty + 1][tx];
+        yh = q.x; yl = q.y;
+      } else if (j <= d.n2) {
+        d2f_split(p[c + sy], yh, yl);
+      }
+      if (i <= d.n1) u[c] = u[c] - fi * ((xh - ph) + (xl - pl));
+      if (j <= d.n2) v[c] = v[c] - fj * ((yh - ph) + (yl - pl));
+      if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * ((nh - ph) + (nl - pl));
+      if (pres && xin && yin && k >= 1 && k <= d.n3) pres[c] = pres[c] + ph;
+    }
+    ph = nh; pl = nl;
+    buf ^= 1;  // the next plane writes the other buffer: one barrier per plane
+  }
 }
 
 extern "C" int cans_correc_f32(const int n[3], const double dli[3], const float *dzci, double dt, const double *p,
                                float *u, float *v, float *w, void *stream) {
   if (!n || !dli || !dzci || !p || !u || !v || !w || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   Dims d{n[0], n[1], n[2]};
-  k_correc32<<<grid_haloed(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(d, (float)(dt * dli[0]), (float)(dt * dli[1]),
-                                                                        (float)dt, dzci, p, u, v, w, nullptr);
+  k_correc32<<<grid_march_haloed(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(
+      d, (float)(dt * dli[0]), (float)(dt * dli[1]), (float)dt, dzci, p, u, v, w, nullptr);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
@@ -144,8 +183,8 @@ extern "C" int cans_correc_updatep_f32(const int n[3], const double dli[3], cons
                                        const double *pp, float *u, float *v, float *w, float *p, void *stream) {
   if (!n || !dli || !dzci || !pp || !u || !v || !w || !p || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   Dims d{n[0], n[1], n[2]};
-  k_correc32<<<grid_haloed(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(d, (float)(dt * dli[0]), (float)(dt * dli[1]),
-                                                                        (float)dt, dzci, pp, u, v, w, p);
+  k_correc32<<<grid_march_haloed(n), dim3(kBX, kBY), 0, as_stream(stream)>>>(
+      d, (float)(dt * dli[0]), (float)(dt * dli[1]), (float)dt, dzci, pp, u, v, w, p);
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
