@@ -139,6 +139,9 @@ def _setup(L):
     L.cans_bulk_mean_f32.argtypes = L.cans_bulk_mean.argtypes
     L.cans_correc_updatep_f32.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V, _V]
     L.cans_plan_set_zpass.argtypes = [_V, C.c_int]
+    L.cans_plan_check.argtypes = [_V]
+    L.cans_initflow.argtypes = [C.c_char_p, _D, _I, _D, _D, _D, _D, _D, _D, C.c_double, _I, _D, _D, C.c_int,
+                                _V, _V, _V, _V, _V]
     L.cans_plan_get_zpass.argtypes = [_V, _I]
 
 
@@ -264,6 +267,14 @@ class Plan:
         ms = (C.c_double * 2)()
         _check(lib().cans_plan_autotune(self._h, int(force), ms), "cans_plan_autotune")
         return list(ms)
+
+    def check(self):
+        """cans_plan_check: True when the solves since the last check were all finite"""
+        rc = lib().cans_plan_check(self._h)
+        if rc == ENONFINITE:
+            return False
+        _check(rc, "cans_plan_check")
+        return True
 
     @property
     def zpass(self):
@@ -622,3 +633,15 @@ def correc_updatep_f32(n, dli, dzci, dt, pp, u, v, w, p, stream=None):
     """correc + the explicit updatep in one pass over pp (cans_correc_updatep_f32)"""
     _check(lib().cans_correc_updatep_f32(_ints(n), _dbls(dli), _ptr(dzci), float(dt), _ptr(pp), _ptr(u), _ptr(v),
                                          _ptr(w), _ptr(p), _stream(stream)), "cans_correc_updatep_f32")
+
+
+def initflow(inivel, bcvel, n, l, dl, zc, zf, dzc, dzf, visc, is_forced, velf, bforce, is_wallturb, u, v, w, p,
+             stream=None):
+    """initflow (src/initflow.f90:16): interiors of the FP64 device fields u, v, w, p"""
+    zc, pzc = _hp(zc)
+    zf, pzf = _hp(zf)
+    dzc, pdc = _hp(dzc)
+    dzf, pdf = _hp(dzf)
+    _check(lib().cans_initflow(_chars(inivel), _dbls(bcvel), _ints(n), _dbls(l), _dbls(dl), pzc, pzf, pdc, pdf,
+                               float(visc), _ints(is_forced), _dbls(velf), _dbls(bforce), int(bool(is_wallturb)),
+                               _ptr(u), _ptr(v), _ptr(w), _ptr(p), _stream(stream)), "cans_initflow")

@@ -62,6 +62,7 @@ struct cans_plan {
   unsigned long long clock = 0;
   long long bytes = 0;
   void *red = nullptr;        // reduction scratch
+  int *status = nullptr;      // device word: 1 once a z pass has seen a non-finite spectral value
   // optional per-pass timing: events recorded between the passes of each solve
   bool timing = false;
   std::vector<cudaEvent_t> ev;  // kTimedSolves x (kPasses + 1)

@@ -742,7 +742,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
   cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->a32); cudaFree(P->zorder); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
-  cudaFree(P->coef4); cudaFree(P->col64); cudaFree(P->lamf);
+  cudaFree(P->coef4); cudaFree(P->col64); cudaFree(P->lamf); cudaFree(P->status);
   cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->E32b); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
   for (auto &e : P->rev) cudaEventDestroy(e);
@@ -965,7 +965,30 @@ static int zpass_auto(const cans_plan *P) {
   return ncol < (long)nsm * 1280 ? 1 : 0;
 }
 
+static int launch_z_pass(cans_plan *P, const Factor *F, double norm, bool f32);
+
+// Non-finite detection of the solves: a NaN or Inf anywhere in the right-hand side reaches
+// every column after the two transforms (each transform output sums its whole line) and the
+// whole column after the elimination, so the first spectral row after the z pass carries it.
+template <typename T> __global__ void k_check_nonfinite(const T *__restrict__ S, long n, int *__restrict__ status) {
+  const long t = threadIdx.x;
+  if (t < n && !isfinite(S[t])) atomicOr(status, 1);
+}
+
+static int check_z(cans_plan *P, bool f32) {
+  const long ncol = (long)P->n[0] * P->n[1];
+  if (f32) k_check_nonfinite<float><<<1, 256, 0, P->stream>>>((const float *)P->S, ncol, P->status);
+  else k_check_nonfinite<double><<<1, 256, 0, P->stream>>>((const double *)P->S, ncol, P->status);
+  CANS_LAUNCH_CHECK();
+  return CANS_OK;
+}
+
 static int launch_z(cans_plan *P, const Factor *F, double norm, bool f32) {
+  const int rc = launch_z_pass(P, F, norm, f32);
+  return rc ? rc : check_z(P, f32);
+}
+
+static int launch_z_pass(cans_plan *P, const Factor *F, double norm, bool f32) {
   const long ncol = (long)P->n[0] * P->n[1];
   const int nn = P->zper ? P->nn - 1 : P->nn;
   const int tpb = kZGroup;
@@ -1150,7 +1173,9 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
       (e = cudaMalloc(&P->c_d, n3 * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->bb_d, n3 * sizeof(double))) != cudaSuccess ||
       (e = cudaMalloc(&P->S, ncell * esz)) != cudaSuccess ||
-      (e = cudaMalloc(&P->red, 4096)) != cudaSuccess) {
+      (e = cudaMalloc(&P->red, 4096)) != cudaSuccess ||
+      (e = cudaMalloc(&P->status, sizeof(int))) != cudaSuccess ||
+      (e = cudaMemset(P->status, 0, sizeof(int))) != cudaSuccess) {
     cans_set_last_cuda_error(e);
     return fail(e == cudaErrorMemoryAllocation ? CANS_ENOMEM : CANS_ECUDA);
   }
@@ -1363,6 +1388,15 @@ template <typename T> int tune_dir(cans_plan *P, int d, const void *pin, int for
   return CANS_OK;
 }
 }  // namespace
+
+extern "C" int cans_plan_check(cans_plan *P) {
+  if (!P) return CANS_EINVAL;
+  int h = 0;
+  CANS_CUDA_TRY(cudaMemcpyAsync(&h, P->status, sizeof(int), cudaMemcpyDeviceToHost, P->stream));
+  CANS_CUDA_TRY(cudaMemsetAsync(P->status, 0, sizeof(int), P->stream));
+  CANS_CUDA_TRY(cudaStreamSynchronize(P->stream));
+  return h ? CANS_ENONFINITE : CANS_OK;
+}
 
 extern "C" int cans_plan_set_zpass(cans_plan *P, int mode) {
   if (!P || mode < -1 || mode > 1) return CANS_EINVAL;

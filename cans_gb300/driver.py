@@ -179,6 +179,8 @@ class Simulation:
                 self.time, self.istep = cans.load_field(os.path.join(restart_dir, f"fld_{name}.bin"), n, tmp)
                 if tmp is not fld:
                     fld.copy_(tmp)
+        elif self.case.get("inivel"):
+            self._initflow()
         bounduvw = cans.bounduvw_f32 if self.fp32 else cans.bounduvw
         boundp = cans.boundp_f32 if self.fp32 else cans.boundp
         bounduvw(self.cbcvel, n, self.bcvel, self.is_bound, self.dl, self.dzc, self.dzf, self.u, self.v, self.w,
@@ -187,6 +189,18 @@ class Simulation:
         for sc in self.scalars:
             cans.boundp(sc["cbc"], n, sc["bc"], self.is_bound, self.dl, self.dzc, sc["val"])
         self._new_dt()
+
+    def _initflow(self):
+        """initflow (src/initflow.f90:16-259, src/main.f90:375) from the case's inivel and
+        is_wallturb keys, on the device (FP64, rounded into the fields of the FP32 run)."""
+        n = self.n
+        flds = [cans.field(n, self.device) for _ in range(4)] if self.fp32 else [self.u, self.v, self.w, self.p]
+        cans.initflow(self.case["inivel"], self.bcvel, n, self.l, self.dl, self.zc, self.zf, self.dzc, self.dzf,
+                      self.visc, self.is_forced, self.velf, self.bforce, bool(self.case.get("is_wallturb", False)),
+                      *flds)
+        if self.fp32:
+            for dst, src in zip((self.u, self.v, self.w, self.p), flds):
+                dst[1:-1, 1:-1, 1:-1] = src[1:-1, 1:-1, 1:-1]
 
     def save(self, datadir):
         """Checkpoint (src/main.f90:578-616 with is_overwrite_save): fld_u/v/w/p.bin and
@@ -339,6 +353,9 @@ class Simulation:
         if not self.is_mask_divergence_check and (self.divmax > self.small or np.isnan(self.divtot)):
             self._abort(f"maximum divergence is too large (divtot = {self.divtot:.3e}, "
                         f"divmax = {self.divmax:.3e})")
+        # the library's own record of the pressure solves (no counterpart in the reference)
+        if not self.plan_p.check():
+            self._abort("the pressure solve met a non-finite right-hand side")
 
     def step(self, nsteps=1):
         if self.kill:

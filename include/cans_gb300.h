@@ -63,6 +63,18 @@ int cans_initsolver(const int ng[3], const double dli[3], const double *dzci_g, 
                     const char cbc[6], const double bc[6], const char c_or_f[3], int precision,
                     void *stream, cans_plan **plan,
                     double *lambdaxy, double *a, double *b, double *c, double *normfft, double rhsb[6]);
+/* initflow (src/initflow.f90:16-259), one GPU: the initial u, v, w, p (device, haloed, FP64;
+ * interiors written, ghosts untouched) for inivel 'cou' 'poi' 'tbl' 'iop' 'zer' 'uni' 'log'
+ * 'hcl' 'hcp' 'tgv' 'tgw' 'ant' 'pdc' 'hdc' (CANS_EINVAL otherwise), with the reference's noise
+ * amplitudes, seeds (123, 456, 789), bulk-velocity rescaling and, with is_wallturb, the
+ * cross-stream vortex pair.  zc, zf, dzc, dzf: HOST arrays 0..n3+1 (cans_initgrid).  The
+ * noise is splitmix64 of (seed, global cell index): the reference's gfortran random_number
+ * stream cannot be reproduced.  Synchronises `stream`. */
+int cans_initflow(const char inivel[3], const double bcvel[18], const int n[3], const double l[3],
+                  const double dl[3], const double *zc, const double *zf, const double *dzc,
+                  const double *dzf, double visc, const int is_forced[3], const double velf[3],
+                  const double bforce[3], int is_wallturb, double *u, double *v, double *w, double *p,
+                  void *stream);
 /* fftend (src/fft.f90:210-246): releases the plan and its device memory */
 int cans_plan_destroy(cans_plan *plan);
 /* device bytes held by the plan (work space + factorisations) */
@@ -344,6 +356,12 @@ int cans_plan_autotune(cans_plan *plan, int force, double ms[2]);
  * (0: generic kernel) */
 int cans_plan_get_shape(const cans_plan *plan, int d, int radix[12], int *nstages, int *ncx,
                         int *spec);
+/* Non-finite check of the plan's solves (the reference tests only the divergence for NaN,
+ * src/main.f90:503-509): every z pass records whether its spectral data held a NaN or Inf
+ * (a non-finite right-hand side value reaches all of it).  Synchronises the plan's stream;
+ * returns CANS_ENONFINITE when a solve since the last check saw one (and clears the record),
+ * CANS_OK otherwise. */
+int cans_plan_check(cans_plan *plan);
 /* z pass of an FP32 plan (no counterpart in the reference; the elimination of
  * src/solver_gpu.f90:278-428): mode 0 = one thread per spectral column sweeping all rows with
  * precomputed factors; 1 = the column split into 16-row segments held in registers, factors

@@ -1035,6 +1035,194 @@ void orc_add_noise(const int n[3], unsigned long long seed, double norm, double 
       }
 }
 
+/* ============================== initflow ============================== */
+/* the 1D profile of src/initflow.f90:46-101,156-184 (cases that set u = u1d(k)); returns
+ * 1 when the case is a 3D analytic field (tgv, tgw, ant), -1 for an unknown name.  The
+ * single-precision literals of the reference (built without -fdefault-real-8) are kept:
+ * 0.09, 0.88, 11.6, 1./.88, sqrt(2.), sqrt(3.).  Also returns ubulk, is_noise, is_mean. */
+int orc_initflow_profile(const char *inivel, const double bcvel[18], int n3, const double l[3], const double *zc,
+                         double visc, const int is_forced[3], const double velf[3], const double bforce[3],
+                         int is_wallturb, double *u1d, double *ubulk_out, int *is_noise, int *is_mean) {
+  double uref = 1., ubulk = 1.;
+  if (is_forced[0]) ubulk = velf[0];
+  *is_noise = 0; *is_mean = 0;
+  /* bcvel(0:1,3,1): bottom/top z values of u -> bcvel[0 + 2*2 + 6*0], bcvel[1 + 2*2] */
+  const double bz0 = bcvel[4], bz1 = bcvel[5];
+  const double f009 = (double)0.09f, f088 = (double)0.88f, f116 = (double)11.6f;
+  int rc = 0;
+  if (!strncmp(inivel, "cou", 3)) {
+    for (int k = 1; k <= n3; k++) {
+      const double z = zc[k] / l[2];
+      double v = .5 * (1. - 2. * z) * 1.;
+      v = v + 0.5;
+      u1d[k - 1] = bz0 * v + bz1 * (1. - v);
+    }
+    uref = fabs(bz1 - bz0);
+  } else if (!strncmp(inivel, "poi", 3) || !strncmp(inivel, "hcp", 3) || !strncmp(inivel, "iop", 3)) {
+    const double lz = !strncmp(inivel, "hcp", 3) ? 2. * l[2] : l[2];
+    if (!strncmp(inivel, "iop", 3)) ubulk = 0.5 * fabs(bz0 + bz1);
+    for (int k = 1; k <= n3; k++) {
+      const double z = zc[k] / lz;
+      u1d[k - 1] = 6. * z * (1. - z) * ubulk;
+      if (!strncmp(inivel, "iop", 3)) u1d[k - 1] = u1d[k - 1] - ubulk;
+    }
+    *is_mean = 1;
+  } else if (!strncmp(inivel, "tbl", 3)) {
+    const double d = 1., theta = 54. * visc / uref;
+    for (int k = 1; k <= n3; k++) u1d[k - 1] = (0.5 + (0.5) * tanh((d / (2. * theta)) * (1. - zc[k] / d))) * uref;
+    *is_noise = 1;
+  } else if (!strncmp(inivel, "zer", 3)) {
+    for (int k = 0; k < n3; k++) u1d[k] = 0.;
+  } else if (!strncmp(inivel, "uni", 3)) {
+    for (int k = 0; k < n3; k++) u1d[k] = uref;
+  } else if (!strncmp(inivel, "log", 3) || !strncmp(inivel, "hcl", 3)) {
+    const double lz = !strncmp(inivel, "hcl", 3) ? 2. * l[2] : l[2];
+    const double reb = ubulk * lz / visc;
+    const double retau = f009 * pow(reb, f088);
+    for (int k = 1; k <= n3; k++) {
+      double z = zc[k] / lz * 2. * retau;
+      if (z >= retau) z = 2. * retau - z;
+      u1d[k - 1] = 2.5 * log(z) + 5.5;
+      if (z <= f116) u1d[k - 1] = z;
+    }
+    *is_noise = 1; *is_mean = 1;
+  } else if (!strncmp(inivel, "pdc", 3) || !strncmp(inivel, "hdc", 3)) {
+    double lref = l[2] / 2.;
+    if (strncmp(inivel, "pdc", 3)) lref = 2. * lref;
+    if (is_wallturb) {
+      uref = pow(bforce[0] * lref, 0.5);
+      const double retau = uref * lref / visc;
+      const double reb = pow(retau / f009, (double)(1.f / .88f));
+      ubulk = reb * visc / (2 * lref);
+    } else {
+      ubulk = (bforce[0] * lref * lref / (3. * visc));
+    }
+    const double lz = !strncmp(inivel, "pdc", 3) ? l[2] : 2. * l[2];
+    for (int k = 1; k <= n3; k++) {
+      const double z = zc[k] / lz;
+      u1d[k - 1] = 6. * z * (1. - z) * ubulk;
+    }
+    *is_mean = 1;
+  } else if (!strncmp(inivel, "tgv", 3) || !strncmp(inivel, "tgw", 3) || !strncmp(inivel, "ant", 3)) {
+    rc = 1;
+  } else {
+    rc = -1;
+  }
+  *ubulk_out = ubulk;
+  return rc;
+}
+
+/* src/initflow.f90:16-259 on one rank (lo = 1): interiors of u, v, w, p; the noise of
+ * add_noise is this project's generator (orc_add_noise, seeds 123, 456, 789), not gfortran's
+ * random_number.  Returns -1 for an unknown case name. */
+int orc_initflow(const char *inivel, const double bcvel[18], const int n[3], const double l[3], const double dl[3],
+                 const double *zc, const double *zf, const double *dzc, const double *dzf, double visc,
+                 const int is_forced[3], const double velf[3], const double bforce[3], int is_wallturb, double *u,
+                 double *v, double *w, double *p) {
+  const int n1 = n[0], n2 = n[1], n3 = n[2];
+  const double pi = acos(-1.);
+  double *u1d = malloc(sizeof(double) * (size_t)(n3 > 0 ? n3 : 1));
+  double ubulk;
+  int is_noise, is_mean;
+  const int rc = orc_initflow_profile(inivel, bcvel, n3, l, zc, visc, is_forced, velf, bforce, is_wallturb, u1d,
+                                      &ubulk, &is_noise, &is_mean);
+  if (rc < 0) { free(u1d); return -1; }
+  const double uref = 1.;
+  if (rc == 0) {
+    for (int k = 1; k <= n3; k++)
+      for (int j = 1; j <= n2; j++)
+        for (int i = 1; i <= n1; i++) {
+          u[IX(i, j, k)] = u1d[k - 1];
+          v[IX(i, j, k)] = 0.; w[IX(i, j, k)] = 0.; p[IX(i, j, k)] = 0.;
+        }
+  } else if (!strncmp(inivel, "tgv", 3)) {
+    for (int k = 1; k <= n3; k++) {
+      const double zcc = zc[k] / l[2] * 2. * pi;
+      for (int j = 1; j <= n2; j++) {
+        const double yc = (double)((float)j - .5f) * dl[1] / l[1] * 2. * pi;
+        const double yf = (double)((float)j - .0f) * dl[1] / l[1] * 2. * pi;
+        for (int i = 1; i <= n1; i++) {
+          const double xc = (double)((float)i - .5f) * dl[0] / l[0] * 2. * pi;
+          const double xf = (double)((float)i - .0f) * dl[0] / l[0] * 2. * pi;
+          u[IX(i, j, k)] = sin(xf) * cos(yc) * cos(zcc) * uref;
+          v[IX(i, j, k)] = -cos(xc) * sin(yf) * cos(zcc) * uref;
+          w[IX(i, j, k)] = 0.;
+          p[IX(i, j, k)] = 0.;
+        }
+      }
+    }
+  } else if (!strncmp(inivel, "tgw", 3)) {
+    for (int k = 1; k <= n3; k++)
+      for (int j = 1; j <= n2; j++) {
+        const double yc = (double)((float)j - .5f) * dl[1], yf = (double)((float)j - .0f) * dl[1];
+        for (int i = 1; i <= n1; i++) {
+          const double xc = (double)((float)i - .5f) * dl[0], xf = (double)((float)i - .0f) * dl[0];
+          u[IX(i, j, k)] = cos(xf) * sin(yc) * uref;
+          v[IX(i, j, k)] = -sin(xc) * cos(yf) * uref;
+          w[IX(i, j, k)] = 0.;
+          p[IX(i, j, k)] = -(cos(2. * xc) + cos(2. * yc)) / 4. * uref * uref;
+        }
+      }
+  } else {  /* ant */
+    const double a = (double)(4.f * sqrtf(2.f) / 3.f / sqrtf(3.f));
+    for (int k = 1; k <= n3; k++) {
+      const double zcc = zc[k] / l[2] * 2. * pi + 0.5 * pi, zff = zf[k] / l[2] * 2. * pi + 0.5 * pi;
+      for (int j = 1; j <= n2; j++) {
+        const double yc = (double)((float)j - .5f) * dl[1] / l[1] * 2. * pi + 0.5 * pi;
+        const double yf = (double)((float)j - .0f) * dl[1] / l[1] * 2. * pi + 0.5 * pi;
+        for (int i = 1; i <= n1; i++) {
+          const double xc = (double)((float)i - .5f) * dl[0] / l[0] * 2. * pi + 0.5 * pi;
+          const double xf = (double)((float)i - .0f) * dl[0] / l[0] * 2. * pi + 0.5 * pi;
+          const double uu = a * (sin(xf - 5. * pi / 6.) * cos(yc - 1. * pi / 6.) * sin(zcc) -
+                                 sin(xf - 1. * pi / 6.) * sin(yc) * cos(zcc - 5. * pi / 6.)) * uref;
+          const double vv = a * (sin(xc) * sin(yf - 5. * pi / 6.) * sin(zcc - 1. * pi / 6.) -
+                                 cos(xc - 5. * pi / 6.) * sin(yf - 1. * pi / 6.) * sin(zcc)) * uref;
+          const double ww = a * (cos(xc - 1. * pi / 6.) * sin(yc) * sin(zff - 5. * pi / 6.) -
+                                 sin(xc) * cos(yc - 5. * pi / 6.) * sin(zff - 1. * pi / 6.)) * uref;
+          u[IX(i, j, k)] = uu; v[IX(i, j, k)] = vv; w[IX(i, j, k)] = ww;
+          p[IX(i, j, k)] = -(uu * uu + vv * vv + ww * ww) / 2.;
+        }
+      }
+    }
+  }
+  if (is_noise) {
+    orc_add_noise(n, 123, .05, u);
+    orc_add_noise(n, 456, .05, v);
+    orc_add_noise(n, 789, .05, w);
+  }
+  if (is_mean && strncmp(inivel, "iop", 3)) {
+    /* set_mean (src/initflow.f90:379-403) with grid_vol_ratio = dzf/l3*(dl1/l1)*(dl2/l2) */
+    double meanold = 0.;
+    for (int k = 1; k <= n3; k++) {
+      const double g = dzf[k] / l[2] * (dl[0] / l[0]) * (dl[1] / l[1]);
+      for (int j = 1; j <= n2; j++)
+        for (int i = 1; i <= n1; i++) meanold = meanold + u[IX(i, j, k)] * g;
+    }
+    if (fabs(meanold) > DBL_EPSILON)
+      for (int k = 1; k <= n3; k++)
+        for (int j = 1; j <= n2; j++)
+          for (int i = 1; i <= n1; i++) u[IX(i, j, k)] = u[IX(i, j, k)] / meanold * ubulk;
+  }
+  if (is_wallturb) {
+    /* the Taylor-Green cross-stream pair of src/initflow.f90:227-245 */
+    for (int k = 1; k <= n3; k++) {
+      const double zcc = (zc[k] / l[2]) * 2. * pi, zff = (zc[k] / l[2] + 0.5 * dzc[k] / l[2]) * 2. * pi;
+      for (int j = 1; j <= n2; j++) {
+        const double yc = (double)((float)j - .5f) * dl[1] / l[1] * 2. * pi;
+        const double yf = (double)((float)j - .0f) * dl[1] / l[1] * 2. * pi;
+        for (int i = 1; i <= n1; i++) {
+          const double xc = (double)((float)i - .5f) * dl[0] / l[0] * 2. * pi;
+          v[IX(i, j, k)] = sin(xc) * cos(yf) * cos(zcc) * ubulk;
+          w[IX(i, j, k)] = -cos(xc) * sin(yc) * cos(zff) * ubulk;
+          p[IX(i, j, k)] = 0.;
+        }
+      }
+    }
+  }
+  free(u1d);
+  return 0;
+}
+
 /* ============================== whole-run driver ============================== */
 struct orc_state {
   orc_case cs;

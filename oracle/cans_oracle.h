@@ -133,6 +133,17 @@ void orc_poisson_residual_ld(const int n[3], const double dli[3], const char cbc
  * p(i,j,k) += 2*(r-0.5)*norm over the interior, r = splitmix64 of (seed, global index) */
 void orc_add_noise(const int n[3], unsigned long long seed, double norm, double *p);
 
+/* initflow (src/initflow.f90:16-259), one rank: interiors of u, v, w, p (HOST grid arrays
+ * 0..n3+1); noise from orc_add_noise (seeds 123, 456, 789).  -1 for an unknown case. */
+int orc_initflow(const char *inivel, const double bcvel[18], const int n[3], const double l[3], const double dl[3],
+                 const double *zc, const double *zf, const double *dzc, const double *dzf, double visc,
+                 const int is_forced[3], const double velf[3], const double bforce[3], int is_wallturb, double *u,
+                 double *v, double *w, double *p);
+/* its 1D profile part: 1 for the 3D analytic cases (tgv, tgw, ant), -1 unknown */
+int orc_initflow_profile(const char *inivel, const double bcvel[18], int n3, const double l[3], const double *zc,
+                         double visc, const int is_forced[3], const double velf[3], const double bforce[3],
+                         int is_wallturb, double *u1d, double *ubulk, int *is_noise, int *is_mean);
+
 /* ---------- whole-run driver (src/main.f90:144-520, single rank, no I/O) ---------- */
 /* profile statistics of src/output.f90 (out1d 56-157, out1d_chan 327-393, out2d_duct 395-529) */
 void orc_out1d(const int n[3], const double l[3], const double dl[3], int idir, const double *dz, const double *p,

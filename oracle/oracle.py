@@ -68,6 +68,9 @@ def _setup(L):
     L.orc_chkdiv.argtypes = [_I, _D, _D, _D, _D, _D, _D, _D, _D]
     L.orc_add_noise.argtypes = [_I, C.c_ulonglong, C.c_double, _D]
     L.orc_poisson_residual_ld.argtypes = [_I, _D, C.c_char_p, _D, _D, _D, _D, _D, _D]
+    L.orc_initflow.argtypes = [C.c_char_p, _D, _I, _D, _D, _D, _D, _D, _D, C.c_double, _I, _D, _D, C.c_int,
+                               _D, _D, _D, _D]
+    L.orc_initflow.restype = C.c_int
     L.orc_state_new.argtypes = [C.c_void_p]
     L.orc_state_new.restype = C.c_void_p
     L.orc_state_free.argtypes = [C.c_void_p]
@@ -284,6 +287,16 @@ def poisson_residual_ld(n, dli, cbc, a, b, c, x, rhs):
     a, b, c = (np.ascontiguousarray(v, dtype=np.float64) for v in (a, b, c))
     lib().orc_poisson_residual_ld(_ip(n), _dp(dli), _cs(cbc), _p(a), _p(b), _p(c), _p(x), _p(rhs), _p(r))
     return r
+
+
+def initflow(inivel, bcvel, n, l, dl, zc, zf, dzc, dzf, visc, is_forced, velf, bforce, is_wallturb, u, v, w, p):
+    """initflow (src/initflow.f90:16-259) into the interiors of the Fortran-ordered u, v, w, p"""
+    rc = lib().orc_initflow(_cs(inivel), _dp(bcvel), _ip(n), _dp(l), _dp(dl), _p(np.ascontiguousarray(zc)),
+                            _p(np.ascontiguousarray(zf)), _p(np.ascontiguousarray(dzc)),
+                            _p(np.ascontiguousarray(dzf)), float(visc), _ip(is_forced), _dp(velf), _dp(bforce),
+                            int(bool(is_wallturb)), _p(u), _p(v), _p(w), _p(p))
+    if rc != 0:
+        raise ValueError(f"initflow: unknown initial condition {inivel!r}")
 
 
 def add_noise(n, seed, norm, p):

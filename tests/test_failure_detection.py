@@ -15,6 +15,11 @@ def _bare_sim(monkeypatch, dt_cfl, divtot, divmax, masked=False):
     sim.cfl, sim.dtmax, sim.dt_f = 0.95, 1e5, -1.
     sim.icheck, sim.istep, sim.kill = 1, 7, False
     sim.fp32, sim.small = False, driver.SMALL
+
+    class _Plan:
+        def check(self):
+            return True
+    sim.plan_p = _Plan()
     sim.is_mask_divergence_check = masked
     monkeypatch.setattr(cans, "chkdt", lambda *a, **k: dt_cfl)
     monkeypatch.setattr(cans, "chkdiv", lambda *a, **k: (divtot, divmax))
@@ -74,3 +79,27 @@ def test_nan_velocity_stops_gpu_run(require_gpu):
     with pytest.raises(cans.CansError) as e:
         cans.chkdiv(n, sim.l, sim.dli, sim.dzfi, sim.u, sim.v, sim.w)
     assert e.value.status == cans.ENONFINITE
+
+
+@pytest.mark.gpu
+def test_solver_reports_nonfinite_rhs(require_gpu):
+    """A NaN (and an Inf) written into the right-hand side: the solve itself stays
+    asynchronous, cans_plan_check reports CANS_ENONFINITE once and clears the record."""
+    import torch
+    from cans_gb300 import cans
+    n = [16, 12, 10]
+    dli = [8., 12., 10.]
+    dzci = dzfi = np.full(n[2] + 2, 10.)
+    for prec in (cans.FP64, cans.FP32):
+        plan = cans.Plan(n, dli, dzci, dzfi, "PPPPNN", [0.] * 6, "ccc", precision=prec)
+        p = cans.field(n)
+        p[1:-1, 1:-1, 1:-1] = torch.randn((n[2], n[1], n[0]), dtype=torch.float64, device="cuda")
+        p[1:-1, 1:-1, 1:-1] -= p[1:-1, 1:-1, 1:-1].mean()
+        plan.solve(p) if prec == cans.FP64 else plan.solve(p.float())
+        assert plan.check()
+        for bad in (float("nan"), float("inf")):
+            q = p.clone()
+            q[5, 6, 7] = bad
+            plan.solve(q) if prec == cans.FP64 else plan.solve(q.float())
+            assert not plan.check()
+            assert plan.check()  # the record was cleared
