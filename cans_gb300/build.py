@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 SRC_DIR = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libcans_gb300.so")
-SOURCES = ["solver.cu", "stencil.cu", "stencil32.cu", "refine.cu", "batch.cu", "boxes.cu", "adjoint.cu", "io.cu", "stats.cu", "initflow.cu"]
+SOURCES = ["solver.cu", "stencil.cu", "stencil32.cu", "refine.cu", "batch.cu", "boxes.cu", "adjoint.cu", "io.cu", "stats.cu", "initflow.cu", "ztile.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-I" + os.path.join(ROOT, "include")]

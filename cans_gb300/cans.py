@@ -278,13 +278,13 @@ class Plan:
 
     @property
     def zpass(self):
-        """z pass of an FP32 plan: 0 column sweep, 1 partitioned (cans_plan_get_zpass)"""
+        """z pass of an FP32 plan: 0 column sweep, 1 partitioned, 2 TMA-tiled (cans_plan_get_zpass)"""
         m = C.c_int()
         _check(lib().cans_plan_get_zpass(self._h, C.byref(m)), "cans_plan_get_zpass")
         return m.value
 
     def set_zpass(self, mode):
-        """cans_plan_set_zpass: 0 column sweep, 1 partitioned, -1 automatic"""
+        """cans_plan_set_zpass: 0 column sweep, 1 partitioned, 2 TMA-tiled, -1 automatic"""
         _check(lib().cans_plan_set_zpass(self._h, int(mode)), "cans_plan_set_zpass")
 
     def shape(self, d):

@@ -7,6 +7,7 @@
 #include "cans_internal.cuh"
 #include "fft_smem.cuh"
 #include "fpconv.cuh"
+#include "tma.cuh"
 
 struct DirTables {
   void *tw = nullptr, *post = nullptr, *pre = nullptr;  // device, precision of the plan
@@ -48,7 +49,16 @@ struct cans_plan {
   float *lamf = nullptr;      // FP32 plans: lambda per column in FP32, NaN for the FP64 columns
   int n64 = 0;
   int zpart_L = 0;            // FP32 plans: rows per segment of the partitioned z pass (0: not used)
-  int zpart_mode = 0;         // 1: the partitioned z pass (when zpart_L != 0), 0: the column-sweep kernel
+  int zpart_mode = 0;         // 0: the column-sweep kernel, 1: the partitioned z pass (zpart_L != 0),
+                              // 2: the TMA-tiled z pass (zt.ok)
+  struct {                    // FP32 plans: the TMA-tiled z pass (ztile.cu)
+    bool ok = false;          // usable: ncol % 4 == 0 and the row count fits a tile
+    CUtensorMap map;          // S as [rows][ncol] FP32, boxes of 32 columns x boxrows rows
+    int W = 0, L = 0;         // segments per column (power of two) and rows per segment
+    int ni = 0;               // inner rows of every segment when all are full (kernel variant), else 0
+    int nbox = 0, boxrows = 0, nbuf = 0, grid = 0, threads = 0;
+    size_t smem = 0;
+  } zt;
 
   void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)
   double *R64 = nullptr;      // refinement residual / rhs copies (FP64) when needed
@@ -62,7 +72,8 @@ struct cans_plan {
   unsigned long long clock = 0;
   long long bytes = 0;
   void *red = nullptr;        // reduction scratch
-  int *status = nullptr;      // device word: 1 once a z pass has seen a non-finite spectral value
+  int *status = nullptr;      // device word: bit 0 once a z pass has seen a non-finite spectral
+                              // value, bit 1 once a bounded wait of the tiled z pass expired
   // optional per-pass timing: events recorded between the passes of each solve
   bool timing = false;
   std::vector<cudaEvent_t> ev;  // kTimedSolves x (kPasses + 1)
@@ -71,6 +82,10 @@ struct cans_plan {
   int nres = 0;
 };
 static const int kPasses = 5, kTimedSolves = 256, kTimedResiduals = 512;
+
+// the TMA-tiled z pass of FP32 plans (ztile.cu)
+int cans_ztile_setup(cans_plan *P);
+int cans_ztile_launch(cans_plan *P, const Factor *F, double norm);
 
 // complex sequences per CTA: the largest power of two (<= 16) keeping the two FFT buffers
 // within a budget, so several CTAs share an SM and the transposed x stores are runs of
@@ -681,6 +696,123 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
       __syncthreads();
     }
   });
+}
+
+// FP64 elimination of one spectral column of an FP32 plan (the low-wavenumber columns with
+// |lambda_xy| < lam32, incl. the singular one) with the FP64 factors.  The column is solved
+// unscaled (x' = T^-1 s) and the FFT normalisation applied to the result; FP32 <-> FP64
+// conversions are integer operations (fpconv.cuh), so the FP64 pipe runs only the recurrence
+// (forward: one FMA and one product per row; backward: one FMA, one product).  The loads of the
+// next U rows are issued before the recurrence runs over the current U rows.  The forward
+// values go to the FP64 scratch W; non-periodic z writes the result to S during the backward
+// sweep, periodic z adds the closure (auxiliary vector p2) in a last pass.
+__device__ __forceinline__ void zsolve_hyb64_col(float *__restrict__ S, double *__restrict__ W,
+                                                 const double *__restrict__ zinv, const double *__restrict__ dd,
+                                                 const double *__restrict__ p2, const double *__restrict__ dcl,
+                                                 const double *__restrict__ a, const double *__restrict__ c,
+                                                 long ncol, int nn, int zper, double norm, long col) {
+  constexpr int U = 4, kPD = 32;  // rows per register chunk; L2 prefetch distance in rows
+  const size_t P = (size_t)ncol;
+  const float normf = (float)norm;
+  float *Sc = S + col;
+  double *Wc = W + col;
+  const double *zc = zinv + col, *dc = dd + col;
+  double y = 0.;
+  const int nf = nn / U;
+  {
+    float sv[U];
+    double zv[U];
+    if (nf > 0) {
+#pragma unroll
+      for (int u = 0; u < U; u++) { sv[u] = Sc[u * P]; zv[u] = zc[u * P]; }
+    }
+    for (int ch = 0; ch < nf; ch++) {
+      const int k = ch * U;
+      float sn[U];
+      double zn[U];
+      const bool more = ch + 1 < nf;
+      if (k + kPD < nn) {  // L2 prefetch kPD rows ahead: the loads below then wait on L2, not DRAM
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (k + kPD + u < nn) { tma::prefetch_l2(Sc + (k + kPD + u) * P); tma::prefetch_l2(zc + (k + kPD + u) * P); }
+      }
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < U; u++) { sn[u] = Sc[(k + U + u) * P]; zn[u] = zc[(k + U + u) * P]; }
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        y = (f2d(sv[u]) - a[k + u] * y) * zv[u];
+        Wc[(k + u) * P] = y;
+      }
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < U; u++) { sv[u] = sn[u]; zv[u] = zn[u]; }
+      }
+    }
+  }
+  for (int k = nf * U; k < nn; k++) {
+    y = (f2d(Sc[k * P]) - a[k] * y) * zc[k * P];
+    Wc[k * P] = y;
+  }
+  const double sl = y;  // forward value of the last row = its solution
+  if (!zper) Sc[(nn - 1) * P] = d2f_rn(y) * normf;
+  const int bf = (nn - 1) / U;
+  {
+    double wv[U], dv[U];
+    if (bf > 0) {
+#pragma unroll
+      for (int u = 0; u < U; u++) { wv[u] = Wc[(nn - 2 - u) * P]; dv[u] = dc[(nn - 2 - u) * P]; }
+    }
+    for (int ch = 0; ch < bf; ch++) {
+      const int k = nn - 2 - ch * U;
+      double wn[U], dn[U];
+      const bool more = ch + 1 < bf;
+      if (k - kPD >= 0) {
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (k - kPD - u >= 0) { tma::prefetch_l2(Wc + (k - kPD - u) * P); tma::prefetch_l2(dc + (k - kPD - u) * P); }
+      }
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < U; u++) { wn[u] = Wc[(k - U - u) * P]; dn[u] = dc[(k - U - u) * P]; }
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        y = wv[u] - dv[u] * y;
+        if (zper) Wc[(k - u) * P] = y;
+        else Sc[(k - u) * P] = d2f_rn(y) * normf;
+      }
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < U; u++) { wv[u] = wn[u]; dv[u] = dn[u]; }
+      }
+    }
+  }
+  for (int k = nn - 2 - bf * U; k >= 0; k--) {
+    y = Wc[k * P] - dc[k * P] * y;
+    if (zper) Wc[k * P] = y;
+    else Sc[k * P] = d2f_rn(y) * normf;
+  }
+  if (zper) {
+    const double den = dcl[col];
+    const double pN = den == 0. ? 0. : (f2d(Sc[nn * P]) - c[nn] * y - a[nn] * sl) / den;
+    Sc[nn * P] = d2f_rn(pN) * normf;
+    const double *pc = p2 + col;
+    // independent rows: U-row batches of loads, the rows kPD ahead prefetched into L2
+    for (int k = 0; k < nn; k += U) {
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (k + kPD + u < nn) { tma::prefetch_l2(Wc + (k + kPD + u) * P); tma::prefetch_l2(pc + (k + kPD + u) * P); }
+      double wv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (k + u < nn) wv[u] = fma(pc[(k + u) * P], pN, Wc[(k + u) * P]);
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (k + u < nn) Sc[(k + u) * P] = d2f_rn(wv[u]) * normf;
+    }
+  }
 }
 
 // z solve, FP64 spectral data, in place (one spectral column)

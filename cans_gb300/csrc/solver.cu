@@ -314,82 +314,6 @@ __global__ void k_factor_to_f32(const double *__restrict__ a, float *__restrict_
   if (t < n) b[t] = (float)a[t];
 }
 
-// FP64 elimination of one spectral column of an FP32 plan (the low-wavenumber columns with
-// |lambda_xy| < lam32, incl. the singular one): FP64 factors, the forward sweep into the FP64
-// scratch W, software-pipelined loads of U rows; overwrites the FP32 column of S
-__device__ __forceinline__ void zsolve_hyb64_col(float *__restrict__ S, double *__restrict__ W,
-                                                 const double *__restrict__ zinv, const double *__restrict__ dd,
-                                                 const double *__restrict__ p2, const double *__restrict__ dcl,
-                                                 const double *__restrict__ a, const double *__restrict__ c,
-                                                 long ncol, int nn, int zper, double norm, long col) {
-  constexpr int U = 8;
-  double y = 0.;
-  int k = 0;
-  for (; k + U <= nn; k += U) {
-    float sv[U];
-    double zv[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const size_t idx = (size_t)(k + u) * ncol + col;
-      sv[u] = S[idx];
-      zv[u] = zinv[idx];
-    }
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      y = ((double)sv[u] * norm - a[k + u] * y) * zv[u];
-      W[(size_t)(k + u) * ncol + col] = y;
-    }
-  }
-  for (; k < nn; k++) {
-    const size_t idx = (size_t)k * ncol + col;
-    y = ((double)S[idx] * norm - a[k] * y) * zinv[idx];
-    W[idx] = y;
-  }
-  const double sn = y;
-  k = nn - 2;
-  for (; k - U + 1 >= 0; k -= U) {
-    double wv[U], dv[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const size_t idx = (size_t)(k - u) * ncol + col;
-      wv[u] = W[idx];
-      dv[u] = dd[idx];
-    }
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      y = wv[u] - dv[u] * y;
-      W[(size_t)(k - u) * ncol + col] = y;
-    }
-  }
-  for (; k >= 0; k--) {
-    const size_t idx = (size_t)k * ncol + col;
-    y = W[idx] - dd[idx] * y;
-    W[idx] = y;
-  }
-  if (zper) {
-    const size_t iN = (size_t)nn * ncol + col;
-    const double den = dcl[col];
-    const double pN = den == 0. ? 0. : ((double)S[iN] * norm - c[nn] * y - a[nn] * sn) / den;
-    S[iN] = (float)pN;
-    for (int k = 0; k < nn; k++) {
-      const size_t idx = (size_t)k * ncol + col;
-      S[idx] = (float)(W[idx] + p2[idx] * pN);
-    }
-  } else {
-    for (k = 0; k + U <= nn; k += U) {
-      double wv[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) wv[u] = W[(size_t)(k + u) * ncol + col];
-#pragma unroll
-      for (int u = 0; u < U; u++) S[(size_t)(k + u) * ncol + col] = (float)wv[u];
-    }
-    for (; k < nn; k++) {
-      const size_t idx = (size_t)k * ncol + col;
-      S[idx] = (float)W[idx];
-    }
-  }
-}
-
 // z solve on FP32 spectral data (FP32 plans).  Columns with |lambda_xy| >= lam32 are
 // eliminated in FP32 with the FP32-rounded factors (their system has condition number below
 // ~300, so FP32 gives ~1e-5 or better and the refinement contracts by that per step); the
@@ -598,7 +522,7 @@ __device__ __forceinline__ void zpart_final(float (&r)[kZL], const float (&zz)[k
 __global__ void __launch_bounds__(kZT, 2) k_zsolve_part(float *__restrict__ S, double *__restrict__ Wsc,
                                                          const float *__restrict__ lamf,
                                                          const float4 *__restrict__ coef, long ncol, int nn, int W,
-                                                         float normf, const int *__restrict__ col64, int n64,
+                                                         float normf, float bshift, const int *__restrict__ col64, int n64,
                                                          int n64b, const double *__restrict__ zinv,
                                                          const double *__restrict__ dd,
                                                          const double *__restrict__ a64,
@@ -619,8 +543,9 @@ __global__ void __launch_bounds__(kZT, 2) k_zsolve_part(float *__restrict__ S, d
   __syncthreads();
   const int c = threadIdx.x % kZC, s = threadIdx.x / kZC;
   const long col = (long)(blockIdx.x - n64b) * kZC + c;
-  const float lam = col < ncol ? lamf[col] : __int_as_float(0x7fc00000);
-  const bool on = lam == lam;  // NaN: an FP64 column (or past the end)
+  const float lam0 = col < ncol ? lamf[col] : __int_as_float(0x7fc00000);
+  const bool on = lam0 == lam0;  // NaN: an FP64 column (or past the end)
+  const float lam = lam0 + bshift;  // Helmholtz: the diagonal shift of the factors
   const int b = s * kZL;
   const bool lastseg = s == W - 1;
   const int rows = lastseg ? nn - b : kZL;  // rows of the segment
@@ -954,11 +879,14 @@ template <typename T> static int launch_y(cans_plan *P, int fwd) {
   return CANS_OK;
 }
 
-// The z pass of FP32 plans without a measurement: the column sweep (one thread per column,
-// precomputed factors) is bandwidth-bound once the columns fill the GPU; below that (fewer
-// than ~1.3 columns per thread slot of the SMs, e.g. 256^2 columns) the partitioned pass's
-// parallelism along z wins (measured on GB300: 256^3 0.09 vs 0.34 ms; 512^3 0.95 vs 0.55 ms).
+// The z pass of FP32 plans without a measurement: the TMA-tiled pass where the plan's shape
+// allows it (each value read and written once, measured fastest on GB300 at 256^3 and 512^3);
+// otherwise the column sweep (one thread per column, precomputed factors), which is
+// bandwidth-bound once the columns fill the GPU, or below that (fewer than ~1.3 columns per
+// thread slot of the SMs) the register-partitioned pass.
 static int zpass_auto(const cans_plan *P) {
+  if (P->zt.ok) return 2;
+  if (!P->zpart_L) return 0;
   int dev = 0, nsm = 152;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const long ncol = (long)P->n[0] * P->n[1];
@@ -996,14 +924,16 @@ static int launch_z_pass(cans_plan *P, const Factor *F, double norm, bool f32) {
   if (!f32)
     k_zsolve64<<<grid, tpb, 0, P->stream>>>((double *)P->S, F->zinv, F->dd, F->p2, F->dcl, P->a_d, P->c_d, ncol,
                                             nn, P->zper, norm);
-  else if (P->zpart_L && !P->zper && P->zpart_mode) {
+  else if (P->zt.ok && P->zpart_mode == 2)
+    return cans_ztile_launch(P, F, norm);
+  else if (P->zpart_L && !P->zper && P->zpart_mode == 1) {
     const int W = (nn + kZL - 1) / kZL;  // <= kZW (zpart_L is set only then)
     const int tb = W * kZC;
     const int n64b = (P->n64 + tb - 1) / tb;
     const unsigned g = (unsigned)(n64b + (ncol + kZC - 1) / kZC);
     k_zsolve_part<<<g, (unsigned)tb, 0, P->stream>>>((float *)P->S, P->R64, P->lamf, P->coef4, ncol, nn, W,
-                                                      (float)norm, P->col64, P->n64, n64b, F->zinv, F->dd, P->a_d,
-                                                      P->c_d, norm);
+                                                      (float)norm, (float)F->key, P->col64, P->n64, n64b, F->zinv,
+                                                      F->dd, P->a_d, P->c_d, norm);
     CANS_LAUNCH_CHECK();
     return CANS_OK;
   } else
@@ -1205,18 +1135,20 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
       cans_set_last_cuda_error(e);
       return fail(CANS_ECUDA);
     }
-    // partitioned z pass (non-periodic z): segment length L, the FP64 column list, FP32 rows
+    // the FP64 column list, FP32 rows (a_k, b_k, c_k) with the wrap couplings a_0 and c_last
+    // zeroed when z is not periodic, and lambda per column in FP32 (NaN for the FP64 columns):
+    // the partitioned (non-periodic z, <= kZW kZL rows) and the TMA-tiled z passes
     const int nnz = P->nn;
-    if (!P->zper && nnz >= 1 && nnz <= kZW * kZL) {
-      P->zpart_L = kZL;
+    {
       std::vector<int> c64;
       for (long c = 0; c < (long)n1 * n2; c++)
         if (fabs(lamcol[c]) < P->lam32) c64.push_back((int)c);
       P->n64 = (int)c64.size();
       std::vector<float4> coefh(n3);
-      for (int k = 0; k < n3; k++)
-        coefh[k] = make_float4(k > 0 ? (float)P->a_h[k] : 0.f, (float)P->b_h[k], (float)P->c_h[k], 0.f);
-      // lambda per column in FP32, NaN where the column is eliminated in FP64
+      for (int k = 0; k < n3; k++) {
+        const bool a0 = k == 0 && !P->zper, clast = k == nnz - 1 && !P->zper;
+        coefh[k] = make_float4(a0 ? 0.f : (float)P->a_h[k], (float)P->b_h[k], clast ? 0.f : (float)P->c_h[k], 0.f);
+      }
       std::vector<float> lamfh(lamcol.size());
       for (size_t c = 0; c < lamcol.size(); c++)
         lamfh[c] = fabs(lamcol[c]) < P->lam32 ? nanf("") : (float)lamcol[c];
@@ -1225,14 +1157,14 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
           (e = cudaMalloc(&P->col64, std::max<size_t>(c64.size(), 1) * sizeof(int))) != cudaSuccess ||
           (e = cudaMalloc(&P->lamf, lamfh.size() * sizeof(float))) != cudaSuccess ||
           (e = cudaMemcpy(P->lamf, lamfh.data(), lamfh.size() * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
-
           (!c64.empty() &&
-           (e = cudaMemcpy(P->col64, c64.data(), c64.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess) ||
-          false) {
+           (e = cudaMemcpy(P->col64, c64.data(), c64.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)) {
         cans_set_last_cuda_error(e);
         return fail(e == cudaErrorMemoryAllocation ? CANS_ENOMEM : CANS_ECUDA);
       }
       P->bytes += (long long)(n3 * sizeof(float4) + c64.size() * sizeof(int) + lamfh.size() * sizeof(float));
+      if (!P->zper && nnz >= 1 && nnz <= kZW * kZL) P->zpart_L = kZL;
+      if ((rc = cans_ztile_setup(P))) return fail(rc);
       P->zpart_mode = zpass_auto(P);
     }
   }
@@ -1395,19 +1327,20 @@ extern "C" int cans_plan_check(cans_plan *P) {
   CANS_CUDA_TRY(cudaMemcpyAsync(&h, P->status, sizeof(int), cudaMemcpyDeviceToHost, P->stream));
   CANS_CUDA_TRY(cudaMemsetAsync(P->status, 0, sizeof(int), P->stream));
   CANS_CUDA_TRY(cudaStreamSynchronize(P->stream));
-  return h ? CANS_ENONFINITE : CANS_OK;
+  return (h & 2) ? CANS_ETIMEOUT : (h & 1) ? CANS_ENONFINITE : CANS_OK;
 }
 
 extern "C" int cans_plan_set_zpass(cans_plan *P, int mode) {
-  if (!P || mode < -1 || mode > 1) return CANS_EINVAL;
-  if (mode == 1 && !P->zpart_L) return CANS_ENOTSUP;
-  P->zpart_mode = mode == -1 ? (P->zpart_L ? zpass_auto(P) : 0) : mode;
+  if (!P || mode < -1 || mode > 2) return CANS_EINVAL;
+  if (P->precision != CANS_FP32 && mode > 0) return CANS_ENOTSUP;
+  if ((mode == 1 && !P->zpart_L) || (mode == 2 && !P->zt.ok)) return CANS_ENOTSUP;
+  P->zpart_mode = mode == -1 ? (P->precision == CANS_FP32 ? zpass_auto(P) : 0) : mode;
   return CANS_OK;
 }
 
 extern "C" int cans_plan_get_zpass(const cans_plan *P, int *mode) {
   if (!P || !mode) return CANS_EINVAL;
-  *mode = P->zpart_L ? P->zpart_mode : 0;
+  *mode = P->zpart_mode;
   return CANS_OK;
 }
 
@@ -1452,11 +1385,16 @@ extern "C" int cans_plan_autotune(cans_plan *P, int force, double ms_out[2]) {
   for (int d = 0; d < 2 && !rc; d++)
     rc = P->precision == CANS_FP64 ? tune_dir<double>(P, d, pin, force) : tune_dir<float>(P, d, pin, force);
   // FP32 plans: the faster of the two z passes (on the zeroed spectral buffer)
-  if (!rc && P->precision == CANS_FP32 && P->zpart_L) {
-    float t0 = 0.f, t1 = 0.f;
-    rc = time_zpass(P, 0, &t0);
-    if (!rc) rc = time_zpass(P, 1, &t1);
-    if (!rc) P->zpart_mode = t1 < t0 ? 1 : 0;
+  if (!rc && P->precision == CANS_FP32) {
+    float best = 0.f;
+    int pick = 0;
+    for (int mode = 0; mode <= 2 && !rc; mode++) {
+      if ((mode == 1 && !P->zpart_L) || (mode == 2 && !P->zt.ok)) continue;
+      float t = 0.f;
+      rc = time_zpass(P, mode, &t);
+      if (!rc && (mode == 0 || t < best)) { best = t; pick = mode; }
+    }
+    if (!rc) P->zpart_mode = pick;
   }
   cudaStreamSynchronize(P->stream);
   cudaFree(pin);

@@ -101,8 +101,9 @@ __global__ void __launch_bounds__(kTB) k_mom_rk(Dims d, double dxi, double dyi, 
                       (long)blockIdx.x * blockDim.x + threadIdx.x, sb, gbx, gby, gbz, beta);
 }
 
-// copy-back of the new velocity with the per-block partial sums of the bulk means
-// (grid_vol_ratio weighted, src/utils.f90:15-42); partials[blk*3 + c]
+// copy-back of the new velocity with (partials != nullptr, the forced or implicit-diffusion
+// substep) the per-block partial sums of the bulk means (grid_vol_ratio weighted,
+// src/utils.f90:15-42); partials[blk*3 + c]
 __global__ void __launch_bounds__(kTB) k_rk_writeback(Dims d, const double *__restrict__ unew,
                                                       const double *__restrict__ gvr_c,
                                                       const double *__restrict__ gvr_f, double *__restrict__ u,
@@ -117,8 +118,9 @@ __global__ void __launch_bounds__(kTB) k_rk_writeback(Dims d, const double *__re
     const size_t c = hidx(i, j, k, d.n1, d.n2);
     const double un = unew[t], vn = unew[t + np], wn = unew[t + 2 * np];
     u[c] = un; v[c] = vn; w[c] = wn;
-    s0 = un * gvr_f[k]; s1 = vn * gvr_f[k]; s2 = wn * gvr_c[k];
+    if (partials) { s0 = un * gvr_f[k]; s1 = vn * gvr_f[k]; s2 = wn * gvr_c[k]; }
   }
+  if (!partials) return;  // no forcing: the bulk means are not needed (uniform over the grid)
   for (int o = 16; o > 0; o >>= 1) {
     s0 += __shfl_down_sync(0xffffffffu, s0, o);
     s1 += __shfl_down_sync(0xffffffffu, s1, o);
@@ -260,9 +262,9 @@ static int rk_impl(const double rkpar[2], const int n[3], const double dli[3], c
                                   is_impdiff ? 1 : 0, dzci, dzfi, u, v, w, p, dudtrko, dvdtrko, dwdtrko, unew, dtd,
                                   sb, sb ? gacc[0] : 0., sb ? gacc[1] : 0., sb ? gacc[2] : 0., beta);
   CANS_LAUNCH_CHECK();
-  k_rk_writeback<<<nblk, kTB, 0, st>>>(d, unew, gvr_c, gvr_f, u, v, w, partials);
-  CANS_LAUNCH_CHECK();
   const bool forced = is_forced[0] || is_forced[1] || is_forced[2];
+  k_rk_writeback<<<nblk, kTB, 0, st>>>(d, unew, gvr_c, gvr_f, u, v, w, (forced || is_impdiff) ? partials : nullptr);
+  CANS_LAUNCH_CHECK();
   if (forced || is_impdiff) {
     k_sum_partials<<<1, kTB, 0, st>>>(partials, nblk, 3, 3, means);
     CANS_LAUNCH_CHECK();

@@ -1,0 +1,98 @@
+// Tensor-memory-accelerator (TMA) tile loads and shared-memory mbarriers for sm_103a, as
+// inline PTX, plus the host-side encoding of a 2-D tensor map.
+//
+// Every wait on an mbarrier is bounded in time (%globaltimer): a wait that has not completed
+// after kWaitLimitNs returns false and the caller records the failure instead of spinning.
+#pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tma {
+
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // one second
+constexpr uint32_t kSuspendHintNs = 20000;  // a waiting thread sleeps up to this long per try (woken on completion)
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// make initialised barriers visible to the async (TMA) proxy before first use
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendHintNs)
+      : "memory");
+  return ok != 0;
+}
+
+// wait for the phase of parity `parity` to complete; false after kWaitLimitNs
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  while (!mbar_try_wait(bar, parity))
+    if (globaltimer() - t0 > kWaitLimitNs) return false;
+  return true;
+}
+
+// 2-D tiled TMA load of the box at (x, y) (x innermost, in elements) into shared memory;
+// completion is signalled on `bar` as transaction bytes
+__device__ __forceinline__ void load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_map(const CUtensorMap *map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// hint: bring the 128-byte line holding `p` into L2 (no register, no completion)
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// named barrier over `nthreads` threads (a multiple of 32) of the CTA
+__device__ __forceinline__ void bar_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+}  // namespace tma
+
+// host: a 2-D FP32 tensor map over a row-major [rows][cols] array (cols innermost) with
+// boxes of box_cols x box_rows; out-of-range elements of a box read as zero.  Returns
+// false when the driver entry point is unavailable or the encoding is rejected
+// (base not 16-byte aligned, row pitch not a multiple of 16 bytes, box too large).
+bool cans_encode_map_2d_f32(CUtensorMap *map, const void *base, uint64_t cols, uint64_t rows, uint32_t box_cols,
+                            uint32_t box_rows);

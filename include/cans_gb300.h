@@ -359,16 +359,21 @@ int cans_plan_get_shape(const cans_plan *plan, int d, int radix[12], int *nstage
 /* Non-finite check of the plan's solves (the reference tests only the divergence for NaN,
  * src/main.f90:503-509): every z pass records whether its spectral data held a NaN or Inf
  * (a non-finite right-hand side value reaches all of it).  Synchronises the plan's stream;
- * returns CANS_ENONFINITE when a solve since the last check saw one (and clears the record),
- * CANS_OK otherwise. */
+ * returns CANS_ENONFINITE when a solve since the last check saw one, CANS_ETIMEOUT when a
+ * bounded wait of the TMA-tiled z pass expired (its results are then not valid), CANS_OK
+ * otherwise; clears the record. */
 int cans_plan_check(cans_plan *plan);
 /* z pass of an FP32 plan (no counterpart in the reference; the elimination of
  * src/solver_gpu.f90:278-428): mode 0 = one thread per spectral column sweeping all rows with
  * precomputed factors; 1 = the column split into 16-row segments held in registers, factors
  * formed on the fly, the segments joined by a cyclic reduction of their separator rows (non-
- * periodic z with at most 512 rows; CANS_ENOTSUP otherwise); -1 = the automatic choice (by the
- * number of columns; the default).  cans_plan_autotune measures both and keeps the faster.
- * Results differ between the modes only by FP32 rounding of the correction solve. */
+ * periodic z with at most 512 rows); 2 = tiles of 32 columns x all rows moved into shared
+ * memory by TMA (each value read and written once), factors formed on the fly, up to 16
+ * segments per column joined by a cyclic reduction that also closes periodic z (n1 n2 a
+ * multiple of 4, at most 512 rows); -1 = the automatic choice (mode 2 where it applies; the
+ * default).  CANS_ENOTSUP for a mode the plan's shape does not allow (and for FP64 plans,
+ * which have mode 0 only).  cans_plan_autotune measures the available modes and keeps the
+ * fastest.  Results differ between the modes only by FP32 rounding. */
 int cans_plan_set_zpass(cans_plan *plan, int mode);
 int cans_plan_get_zpass(const cans_plan *plan, int *mode);
 int cans_batch_create(int nsys, cans_plan *const *plans, void *stream, cans_batch **batch);

@@ -175,27 +175,81 @@ def test_two_corrections_at_least_as_accurate_as_fp64_path(require_gpu):
     assert e2 <= e64, (e2, e64)
 
 
-@pytest.mark.parametrize("n,l,cbc,gr", [CASES[0], CASES[2], CASES[9], CASES[10], CASES[12]])
-def test_both_z_passes(require_gpu, n, l, cbc, gr):
-    """The column-sweep and the partitioned z pass of an FP32 plan: both FP32-accurate, and the
-    refined solves of both reach the same FP64 accuracy."""
+Z_CASES = [CASES[0], CASES[2], CASES[3], CASES[4], CASES[9], CASES[10], CASES[12],
+           # many tiles per CTA of the tiled z pass (its buffers cycle through several phases)
+           ((256, 128, 16), (4.0, 2.0, 2.0), "PPPPNN", 1.2),
+           ((128, 128, 24), (6.2831853, 6.2831853, 6.2831853), "PPPPPP", 0.0)]
+
+
+def _zmodes(plan):
+    """the z passes the plan offers: 0 column sweep, 1 partitioned (registers), 2 TMA-tiled"""
+    from cans_gb300 import cans
+    modes = []
+    for mode in (0, 1, 2):
+        try:
+            plan.set_zpass(mode)
+        except cans.CansError as e:
+            assert e.status == cans.ENOTSUP
+            continue
+        assert plan.zpass == mode
+        modes.append(mode)
+    plan.set_zpass(-1)
+    return modes
+
+
+@pytest.mark.parametrize("n,l,cbc,gr", Z_CASES)
+def test_all_z_passes(require_gpu, n, l, cbc, gr):
+    """Every z pass of an FP32 plan (column sweep, partitioned, TMA-tiled): each FP32-accurate,
+    and the refined solves of each reach the same FP64 accuracy; no bounded wait expires."""
     import torch
     from cans_gb300 import cans
     dl, dli, dzc, dzf, dzci, dzfi, p, want = _setup(n, l, cbc, gr, seed=17)
     plan = cans.Plan(n, dli, dzci, dzfi, cbc, [0.] * 6, "ccc", precision=cans.FP32)
+    modes = _zmodes(plan)
+    assert 0 in modes and 2 in modes  # every case here has a column count divisible by 4
+    assert plan.zpass == 2  # the automatic choice
     T = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
     w = want[1:-1, 1:-1, 1:-1]
     cmp = (lambda a: gauge_rel_l2(a, w, dzf)) if singular(cbc) else (lambda a: rel_l2(a, w))
     errs = {}
-    for mode in (0, 1):
+    for mode in modes:
         plan.set_zpass(mode)
-        assert plan.zpass == mode
         d32 = cans.to_device(p, dtype=torch.float32)
         plan.solve(d32)
         d = cans.to_device(p)
         plan.solve_refined(d, dli, T(dzci), T(dzfi), rtol=0.0, max_iter=3)
         errs[mode] = (cmp(cans.fview(d32).astype(np.float64)[1:-1, 1:-1, 1:-1]), cmp(cans.fview(d)[1:-1, 1:-1, 1:-1]))
+        assert plan.check()
     print("z passes (fp32 error, refined error):", errs)
-    for mode in (0, 1):
+    for mode in modes:
         assert errs[mode][0] < 1e-5 and errs[mode][1] <= 1e-12, errs
     plan.set_zpass(-1)
+
+
+@pytest.mark.parametrize("cbc,c_or_f", [("PPNNNN", "ccc"), ("PPPPPP", "ccc"), ("PPPPDD", "ccf")])
+def test_fp32_helmholtz_all_z_passes(require_gpu, cbc, c_or_f):
+    """solve_helmholtz (src/solve_helmholtz.f90:28) on an FP32 plan against the FP64 oracle,
+    through every z pass: the shift 1/alpha enters the on-the-fly factors of the partitioned
+    and tiled passes (FP32 tolerance 1e-5)."""
+    from cans_gb300 import cans
+    from gpu_common import is_bound_for
+    n, l = (12, 10, 14), (1.0, 1.0, 1.0)
+    dl = [l[d] / n[d] for d in range(3)]
+    dli = [1 / x for x in dl]
+    dzc, dzf, dzci, dzfi = grid_for(n, l, cbc, 1.2 if cbc[4] != "P" else 0.0)
+    bc = [0.3, -0.2, 0.5, 1.0, -0.7, 0.25]
+    ref = O.initsolver(n, dli, dzci, dzfi, cbc, bc, c_or_f)
+    plan = cans.Plan(n, dli, dzci, dzfi, cbc, bc, c_or_f, precision=cans.FP32)
+    is_bound = is_bound_for(cbc)
+    modes = _zmodes(plan)
+    assert 2 in modes
+    for mode in modes:
+        plan.set_zpass(mode)
+        for alpha in (-0.013, -0.021):
+            p = random_field(n, 7)
+            d = cans.to_device(p)
+            O.solve_helmholtz(n, ref["normfft"], alpha, ref["lambdaxy"], ref["a"], ref["b"], ref["c"], ref["rhsb"],
+                              is_bound, cbc, c_or_f, p)
+            plan.solve_helmholtz(alpha, is_bound, d)
+            got = cans.fview(d)
+            assert rel_l2(got[1:-1, 1:-1, 1:-1], p[1:-1, 1:-1, 1:-1]) <= 1e-5, (mode, alpha)
