@@ -63,14 +63,6 @@ struct OpParams {
   int zper;
 };
 
-// exact difference e_nb - e_c of two FP32 values; at a boundary the ghost rule applies:
-// periodic (enb is the wrapped value), Neumann (ghost = e_c: 0), Dirichlet (ghost = -e_c)
-__device__ __forceinline__ df diff_nb(bool inside, int rule, float enb, float ec) {
-  if (inside || rule == 0) return two_sum(enb, -ec);
-  if (rule > 0) return {0.f, 0.f};
-  return {-2.f * ec, 0.f};  // exact
-}
-
 // block sum of a per-thread FP32 value: warp shuffles in FP32 (the FP64 pipe is 58x slower),
 // per-warp partials accumulated in FP64 by one thread
 __device__ __forceinline__ void block_reduce_to(float v, double *out) {
@@ -109,23 +101,31 @@ struct Dot2 {
 };
 
 // (R, Rlo) -= L e ;  ||R||^2 partials ;  folding of pending corrections into x (FP64), in the
-// order x = e0 + e1 + ... : xmode 0 none, 1 x = eprev + e, 2 x = (x + eprev) + e.
-// Work unit: one (j, k) row; the CTA strides over rows and its threads run along i.  Row
-// pointers (with the y/z ghost rules resolved per row) keep the per-cell work to loads and
-// the double-float arithmetic.
-__global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, float *__restrict__ R,
-                                               float *__restrict__ Rlo, const float *__restrict__ Eprev,
-                                               double *__restrict__ x, int xmode,
-                                               const float2 *__restrict__ a2, const float2 *__restrict__ c2,
-                                               const float2 *__restrict__ s2, OpParams o,
-                                               double *__restrict__ part, const double *__restrict__ rhs,
-                                               double *__restrict__ part0) {
-  // rhs != nullptr (first residual): the current residual is the FP64 right-hand side itself,
-  // split into (hi, lo) here, and part0 receives the partial sums of ||rhs||^2
+// order x = e0 + e1 + ... : XMODE 0 none, 1 x = eprev + e, 2 x = (x + eprev) + e.
+// FIRST (first residual): the current residual is the FP64 right-hand side itself, split
+// into (hi, lo) here, and part0 receives the partial sums of ||rhs||^2.
+// Work unit: one (j, k) row; the CTA strides over rows and its kDfTB threads run along i.
+// The boundary rules are resolved once per row, as neighbour row pointers and multipliers:
+// a y or z neighbour outside the box reads the centre row (a ghost equal to the centre value
+// gives an exact zero difference: Neumann, and the z walls whose rule is folded into b), with
+// multiplier -1 for a Dirichlet ghost (difference -2 e_c, exact); the x ends take the wrapped
+// value or the ghost by a per-cell select.  So the cell loop has no branches and every
+// difference goes through the same exact two-sum.
+constexpr int kDfTB = 64;
+template <bool FIRST, int XMODE>
+__global__ void __launch_bounds__(kDfTB) k_dfres(const float *__restrict__ E, float *__restrict__ R,
+                                                 float *__restrict__ Rlo, const float *__restrict__ Eprev,
+                                                 double *__restrict__ x, const float2 *__restrict__ a2,
+                                                 const float2 *__restrict__ c2, const float2 *__restrict__ s2,
+                                                 OpParams o, double *__restrict__ part,
+                                                 const double *__restrict__ rhs, double *__restrict__ part0) {
   const int n1 = o.n1, n2 = o.n2, n3 = o.n3;
   const long sy = n1 + 2, sz = (long)(n1 + 2) * (n2 + 2);
   const long nrows = (long)n2 * n3;
   const float2 mcx = make_float2(-o.cx.x, -o.cx.y), mcy = make_float2(-o.cy.x, -o.cy.y);
+  // x ends: wrapped neighbour index, or the ghost as a multiple of the centre value
+  const float gw = o.gx0 > 0 ? 1.f : -1.f, ge = o.gx1 > 0 ? 1.f : -1.f;
+  const bool wrapw = o.gx0 == 0, wrape = o.gx1 == 0;
   float sq = 0.f, sq0 = 0.f;
   for (long u = blockIdx.x; u < nrows; u += gridDim.x) {
     const int j = (int)(u % n2) + 1, k = (int)(u / n2) + 1;
@@ -133,56 +133,51 @@ __global__ void __launch_bounds__(kTB) k_dfres(const float *__restrict__ E, floa
     const float2 mav = make_float2(-av.x, -av.y), mcv = make_float2(-cv.x, -cv.y), msv = make_float2(-sv.x, -sv.y);
     const long c0 = (long)hidx(0, j, k, n1, n2);
     const float *Ec = E + c0;
-    // neighbour rows: inside the box, the periodic wrap, or none (Neumann/Dirichlet rule)
-    const float *Es = j > 1 ? Ec - sy : (o.gy0 == 0 ? Ec + (long)(n2 - 1) * sy : nullptr);
-    const float *En = j < n2 ? Ec + sy : (o.gy1 == 0 ? Ec - (long)(n2 - 1) * sy : nullptr);
-    const bool hasb = k > 1 || o.zper, hast = k < n3 || o.zper;
-    const float *Eb = k > 1 ? Ec - sz : Ec + (long)(n3 - 1) * sz;
-    const float *Et = k < n3 ? Ec + sz : Ec - (long)(n3 - 1) * sz;
+    const bool sin = j > 1 || o.gy0 == 0, nin = j < n2 || o.gy1 == 0;
+    const float *Es = j > 1 ? Ec - sy : (o.gy0 == 0 ? Ec + (long)(n2 - 1) * sy : Ec);
+    const float *En = j < n2 ? Ec + sy : (o.gy1 == 0 ? Ec - (long)(n2 - 1) * sy : Ec);
+    const float ms = sin || o.gy0 > 0 ? 1.f : -1.f, mn = nin || o.gy1 > 0 ? 1.f : -1.f;
+    const float *Eb = k > 1 ? Ec - sz : (o.zper ? Ec + (long)(n3 - 1) * sz : Ec);
+    const float *Et = k < n3 ? Ec + sz : (o.zper ? Ec - (long)(n3 - 1) * sz : Ec);
     float *Rr = R + c0;
     float *Lr = Rlo + (long)n1 * u;  // low parts of the row: Lr[i - 1], i = 1..n1
-    for (int i = threadIdx.x + 1; i <= n1; i += blockDim.x) {
+    for (int i = threadIdx.x + 1; i <= n1; i += kDfTB) {
       const float ec = Ec[i];
-      const float ew = i > 1 ? Ec[i - 1] : (o.gx0 == 0 ? Ec[n1] : 0.f);
-      const float ee = i < n1 ? Ec[i + 1] : (o.gx1 == 0 ? Ec[1] : 0.f);
-      const float es = Es ? Es[i] : 0.f, en = En ? En[i] : 0.f;
-      const float eb = hasb ? Eb[i] : 0.f, et = hast ? Et[i] : 0.f;
+      float ew = Ec[i == 1 && wrapw ? n1 : i - 1];
+      float ee = Ec[i == n1 && wrape ? 1 : i + 1];
+      if (i == 1 && !wrapw) ew = gw * ec;
+      if (i == n1 && !wrape) ee = ge * ec;
+      const float es = ms * Es[i], en = mn * En[i];
+      const float eb = Eb[i], et = Et[i];
       float rh, rl;
-      if (rhs) {
+      if (FIRST) {
         d2f_split(rhs[c0 + i], rh, rl);
         sq0 = __fmaf_rn(rh, rh, sq0);
       } else {
         rh = Rr[i];
         rl = Lr[i - 1];
       }
-      const df dw = diff_nb(i > 1, o.gx0, ew, ec);
-      const df de = diff_nb(i < n1, o.gx1, ee, ec);
-      const df ds = diff_nb(j > 1, o.gy0, es, ec);
-      const df dn = diff_nb(j < n2, o.gy1, en, ec);
+      const df dw = two_sum(ew, -ec), de = two_sum(ee, -ec);
+      const df ds = two_sum(es, -ec), dn = two_sum(en, -ec);
+      const df db = two_sum(eb, -ec), dt = two_sum(et, -ec);
       Dot2 acc{rh, rl};
       acc.add_prod(mcx, de.h, de.l);
       acc.add_prod(mcx, dw.h, dw.l);
       acc.add_prod(mcy, dn.h, dn.l);
       acc.add_prod(mcy, ds.h, ds.l);
-      if (hasb) {
-        const df db = two_sum(eb, -ec);
-        acc.add_prod(mav, db.h, db.l);
-      }
-      if (hast) {
-        const df dt = two_sum(et, -ec);
-        acc.add_prod(mcv, dt.h, dt.l);
-      }
+      acc.add_prod(mav, db.h, db.l);
+      acc.add_prod(mcv, dt.h, dt.l);
       acc.add_prod(msv, ec, 0.f);
       const df r = two_sum(acc.s, acc.err);  // |err| may exceed |s| after cancellation
       Rr[i] = r.h;
       Lr[i - 1] = r.l;
-      if (xmode == 1) x[c0 + i] = f2d(Eprev[c0 + i]) + f2d(ec);
-      else if (xmode == 2) x[c0 + i] = (x[c0 + i] + f2d(Eprev[c0 + i])) + f2d(ec);
+      if (XMODE == 1) x[c0 + i] = f2d(Eprev[c0 + i]) + f2d(ec);
+      if (XMODE == 2) x[c0 + i] = (x[c0 + i] + f2d(Eprev[c0 + i])) + f2d(ec);
       sq = __fmaf_rn(r.h, r.h, sq);
     }
   }
   block_reduce_to(sq, &part[blockIdx.x]);
-  if (rhs) {
+  if (FIRST) {
     __syncthreads();  // block_reduce_to's shared array is reused
     block_reduce_to(sq0, &part0[blockIdx.x]);
   }
@@ -250,7 +245,6 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const unsigned nblk_r = (unsigned)std::min<long>((long)o.n2 * o.n3, (long)kResidualCtasPerSM * nsm);
-  const int tpb = 64;  // several cells per thread and row amortise the per-row set-up
   cudaStream_t st = b.st;
   double nrhs = 0., nr = 0.;
   double *part0 = b.part + 2 * (size_t)nblk_r + 16;  // ||rhs||^2 partials of the first residual pass
@@ -282,8 +276,15 @@ extern "C" int cans_solver_refined(cans_plan *P, double *p, const double dli[3],
       const int xmode = npend == 2 ? (has_x ? 2 : 1) : 0;
       const bool timed = P->timing && P->nres < kTimedResiduals;
       if (timed) cudaEventRecord(P->rev[2 * (size_t)P->nres], st);
-      k_dfres<<<nblk_r, tpb, 0, st>>>(pend[npend - 1], b.R, b.Rlo, npend == 2 ? pend[0] : nullptr, p, xmode, b.a2,
-                                      b.c2, b.s2, o, b.part, first ? p : nullptr, part0);
+      const float *ek = pend[npend - 1], *ep = npend == 2 ? pend[0] : nullptr;
+      if (first && xmode == 0)
+        k_dfres<true, 0><<<nblk_r, kDfTB, 0, st>>>(ek, b.R, b.Rlo, ep, p, b.a2, b.c2, b.s2, o, b.part, p, part0);
+      else if (xmode == 0)
+        k_dfres<false, 0><<<nblk_r, kDfTB, 0, st>>>(ek, b.R, b.Rlo, ep, p, b.a2, b.c2, b.s2, o, b.part, nullptr, part0);
+      else if (xmode == 1)
+        k_dfres<false, 1><<<nblk_r, kDfTB, 0, st>>>(ek, b.R, b.Rlo, ep, p, b.a2, b.c2, b.s2, o, b.part, nullptr, part0);
+      else
+        k_dfres<false, 2><<<nblk_r, kDfTB, 0, st>>>(ek, b.R, b.Rlo, ep, p, b.a2, b.c2, b.s2, o, b.part, nullptr, part0);
       CANS_LAUNCH_CHECK();
       if (timed) cudaEventRecord(P->rev[2 * (size_t)P->nres++ + 1], st);
       first = false;

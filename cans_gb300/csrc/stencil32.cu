@@ -122,15 +122,15 @@ extern "C" int cans_fillps_f32(const int n[3], const double dli[3], const float 
 // One thread per haloed (i, j) column of a 32 x 8 tile, marching kMarch planes of k (the
 // reference's ranges: u for i <= n1, v for j <= n2, w for k <= n3, over the haloed box); with
 // pres != nullptr also updatep's explicit p += pp on the interior (the two calls read the same
-// pp and touch disjoint fields, so one pass serves both).  Every pp value is split into its
-// hi/lo float pair once: the thread splits pp(i, j, k+1) (its next plane, also the +z
-// neighbour), takes the +x neighbour's split from the next lane and the +y neighbour's from
-// shared memory (edge lanes / rows split their extra neighbour themselves).
+// pp and touch disjoint fields, so one pass serves both).  The thread splits pp(i, j, k+1)
+// (its next plane, also the +z neighbour) and pp(i, j+1, k) into hi/lo float pairs and takes
+// the +x neighbour's split from the next lane (the edge lane splits its own).  No barrier: all
+// operands of plane k+1 (pp, u, v, w, p) are loaded while plane k is computed, so each thread
+// keeps a plane of loads in flight.
 __global__ void __launch_bounds__(kTB) k_correc32(Dims d, float fi, float fj, float dt,
                                                   const float *__restrict__ dzci, const double *__restrict__ p,
                                                   float *__restrict__ u, float *__restrict__ v,
                                                   float *__restrict__ w, float *__restrict__ pres) {
-  __shared__ float2 sp[2][kBY][kBX];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i = blockIdx.x * kBX + tx, j = blockIdx.y * kBY + ty;
   const bool act = i <= d.n1 + 1 && j <= d.n2 + 1;
@@ -139,33 +139,39 @@ __global__ void __launch_bounds__(kTB) k_correc32(Dims d, float fi, float fj, fl
   const size_t sz = (size_t)sy * (d.n2 + 2);
   size_t c = (size_t)k0 * sz + (size_t)(j * sy + i);
   const bool xin = i >= 1 && i <= d.n1, yin = j >= 1 && j <= d.n2;
+  const bool ux = act && i <= d.n1, vy = act && j <= d.n2, edge = tx == kBX - 1;
+  const bool pin = pres && xin && yin;
+  // plane-k operands
+  const double p0 = act ? p[c] : 0.;
+  double pn = act && k0 <= d.n3 ? p[c + sz] : 0.;
+  double py = vy ? p[c + sy] : 0.;
+  double px = ux && edge ? p[c + 1] : 0.;
+  float uu = ux ? u[c] : 0.f, vv = vy ? v[c] : 0.f, ww = act && k0 <= d.n3 ? w[c] : 0.f;
+  float pr = pin && k0 >= 1 && k0 <= d.n3 ? pres[c] : 0.f;
   float ph = 0.f, pl = 0.f;
-  if (act) d2f_split(p[c], ph, pl);
-  int buf = 0;
+  if (act) d2f_split(p0, ph, pl);
   for (int k = k0; k <= k1; k++, c += sz) {
-    // plane k+1 of this column (the +z neighbour, and the next plane's own value)
-    float nh = 0.f, nl = 0.f;
-    if (act && k <= d.n3) d2f_split(p[c + sz], nh, nl);
-    sp[buf][ty][tx] = make_float2(ph, pl);
-    __syncthreads();
-    // +x from the next lane, +y from the next row (edges split it themselves)
+    // plane k+1's operands, in flight while plane k is computed
+    const size_t cn = c + sz;
+    const bool nx = k < k1;
+    const double pn2 = act && nx && k + 1 <= d.n3 ? p[cn + sz] : 0.;
+    const double py2 = vy && nx ? p[cn + sy] : 0.;
+    const double px2 = ux && edge && nx ? p[cn + 1] : 0.;
+    const float uu2 = ux && nx ? u[cn] : 0.f, vv2 = vy && nx ? v[cn] : 0.f;
+    const float ww2 = act && nx && k + 1 <= d.n3 ? w[cn] : 0.f;
+    const float pr2 = pin && nx && k + 1 >= 1 && k + 1 <= d.n3 ? pres[cn] : 0.f;
+    float nh = 0.f, nl = 0.f, yh = 0.f, yl = 0.f;
+    if (act && k <= d.n3) d2f_split(pn, nh, nl);
+    if (vy) d2f_split(py, yh, yl);
     float xh = __shfl_down_sync(0xffffffffu, ph, 1), xl = __shfl_down_sync(0xffffffffu, pl, 1);
-    float yh = 0.f, yl = 0.f;
-    if (act) {
-      if (tx == kBX - 1 && i <= d.n1) d2f_split(p[c + 1], xh, xl);
-      if (ty < kBY - 1) {
-        const float2 q = sp[buf][ty + 1][tx];
-        yh = q.x; yl = q.y;
-      } else if (j <= d.n2) {
-        d2f_split(p[c + sy], yh, yl);
-      }
-      if (i <= d.n1) u[c] = u[c] - fi * ((xh - ph) + (xl - pl));
-      if (j <= d.n2) v[c] = v[c] - fj * ((yh - ph) + (yl - pl));
-      if (k <= d.n3) w[c] = w[c] - dt * dzci[k] * ((nh - ph) + (nl - pl));
-      if (pres && xin && yin && k >= 1 && k <= d.n3) pres[c] = pres[c] + ph;
-    }
+    if (ux && edge) d2f_split(px, xh, xl);
+    if (ux) u[c] = uu - fi * ((xh - ph) + (xl - pl));
+    if (vy) v[c] = vv - fj * ((yh - ph) + (yl - pl));
+    if (act && k <= d.n3) w[c] = ww - dt * dzci[k] * ((nh - ph) + (nl - pl));
+    if (pin && k >= 1 && k <= d.n3) pres[c] = pr + ph;
     ph = nh; pl = nl;
-    buf ^= 1;  // the next plane writes the other buffer: one barrier per plane
+    pn = pn2; py = py2; px = px2;
+    uu = uu2; vv = vv2; ww = ww2; pr = pr2;
   }
 }
 
