@@ -58,6 +58,7 @@ struct cans_plan {
     int ni = 0;               // inner rows of every segment when all are full (kernel variant), else 0
     int nbox = 0, boxrows = 0, nbuf = 0, grid = 0, threads = 0;
     size_t smem = 0;
+    unsigned char *pure = nullptr;  // device, per tile: all columns eliminated in FP32
   } zt;
 
   void *S = nullptr;          // spectral work buffer n1*n2*n3 (plan precision)

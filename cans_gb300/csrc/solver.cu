@@ -667,7 +667,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   for (int d = 0; d < 2; d++) { cudaFree(P->tab[d].tw); cudaFree(P->tab[d].post); cudaFree(P->tab[d].pre); }
   for (auto &f : P->fac) free_factor(f);
   cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->a32); cudaFree(P->zorder); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
-  cudaFree(P->coef4); cudaFree(P->col64); cudaFree(P->lamf); cudaFree(P->status);
+  cudaFree(P->coef4); cudaFree(P->col64); cudaFree(P->lamf); cudaFree(P->status); cudaFree(P->zt.pure);
   cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->E32b); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
   for (auto &e : P->rev) cudaEventDestroy(e);

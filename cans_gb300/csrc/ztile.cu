@@ -26,6 +26,7 @@
 // plan's status word (reported by cans_plan_check) and the CTA stops issuing and returns
 // after its copies in flight have landed.
 #include <algorithm>
+#include <vector>
 
 #include "plan.cuh"
 
@@ -37,12 +38,15 @@ constexpr int kTWmax = 16;  // segments (consumer warps) at most
 constexpr int kT64 = 3;     // FP64-column warps per CTA (idle where there are fewer columns): 20 warps
                             // in all, five per scheduler, leave 96 registers a thread
 constexpr int kTThreads = 32 * (kTWmax + 1 + kT64);
+constexpr int kRU = 8, kRN = 4;                       // FP64 rings: rows per chunk, chunks
+constexpr int kRingBytes = 2 * kRN * kRU * 32 * 8;   // per FP64 warp
 
 struct ZTileArgs {
   float *S;
   double *Wsc;
   const float *lamf;    // lambda_xy per column in FP32; NaN: an FP64 column
   const float4 *coef;   // (a_k, b_k, c_k, -), a_0 = c_last = 0 when z is not periodic
+  const unsigned char *tilepure;  // per tile: 1 when all its 32 columns are FP32 columns
   float bshift, normf;  // diagonal shift (Helmholtz) and the FFT normalisation
   long ncol;
   int rows, W, L, nbox, boxrows, nbuf, ntiles;
@@ -54,7 +58,7 @@ struct ZTileArgs {
 };
 
 struct ZTileSmem {
-  size_t tile_floats, co, xch, xs, bars, flags, total;
+  size_t tile_floats, co, xch, xs, bars, flags, ring, total;
 };
 
 __host__ __device__ inline ZTileSmem ztile_layout(int rows, int W, int nbox, int boxrows, int nbuf) {
@@ -65,8 +69,123 @@ __host__ __device__ inline ZTileSmem ztile_layout(int rows, int W, int nbox, int
   L.xs = L.xch + (size_t)8 * W * kTC * 4;            // float[W][32]
   L.bars = L.xs + (size_t)W * kTC * 4;               // uint64 full[nbuf], empty[nbuf]
   L.flags = L.bars + (size_t)2 * nbuf * 8;           // int consumer abort, int producer abort
-  L.total = L.flags + 16;
+  L.ring = L.flags + 16;                             // the FP64 warps' copy rings
+  L.total = L.ring + (size_t)kT64 * kRingBytes;
   return L;
+}
+
+// FP64 elimination of one spectral column (zsolve_hyb64_col's arithmetic) fed by a per-thread
+// ring of kRN chunks of kRU rows in shared memory, filled by cp.async kRN - 1 chunks ahead of
+// the recurrence, so a column's sweeps wait on FP64 latency rather than on memory: forward
+// (S, zinv) -> W; backward (W, dd) -> S, or -> W for periodic z, whose closure pass streams
+// (W, p2) -> S the same way.  ring: this warp's kRingBytes (two arrays of kRN kRU 32 doubles).
+__device__ __forceinline__ void zsolve64_col_ring(const ZTileArgs &A, long col, int lane, unsigned char *ring) {
+  double *r0 = reinterpret_cast<double *>(ring);                   // zinv / W
+  double *r1 = r0 + kRN * kRU * 32;                                 // S (as float) / dd / p2
+  float *r1f = reinterpret_cast<float *>(r1);
+  const int nn = A.nn64;
+  const size_t P = (size_t)A.ncol;
+  float *Sc = A.S + col;
+  double *Wc = A.Wsc + col;
+  const double *zc = A.zinv + col, *dc = A.dd + col;
+  const float normf = (float)A.norm;
+  auto slot = [&](int q, int u) { return (q * kRU + u) * 32 + lane; };
+  const int nf = (nn + kRU - 1) / kRU;
+  auto issue_f = [&](int ch) {
+    if (ch < nf) {
+      const int q = ch % kRN;
+#pragma unroll
+      for (int u = 0; u < kRU; u++) {
+        const int k = ch * kRU + u;
+        if (k < nn) {
+          tma::cp_async4(r1f + slot(q, u), Sc + k * P);
+          tma::cp_async8(r0 + slot(q, u), zc + k * P);
+        }
+      }
+    }
+    tma::cp_async_commit();
+  };
+  double y = 0.;
+  for (int c = 0; c < kRN - 1; c++) issue_f(c);
+  for (int ch = 0; ch < nf; ch++) {
+    issue_f(ch + kRN - 1);
+    tma::cp_async_wait<kRN - 1>();
+    const int q = ch % kRN;
+#pragma unroll
+    for (int u = 0; u < kRU; u++) {
+      const int k = ch * kRU + u;
+      if (k < nn) {
+        y = (f2d(r1f[slot(q, u)]) - A.a64[k] * y) * r0[slot(q, u)];
+        Wc[k * P] = y;
+      }
+    }
+  }
+  tma::cp_async_wait<0>();
+  const double sl = y;
+  if (!A.zper) Sc[(nn - 1) * P] = d2f_rn(y) * normf;
+  // backward over rows nn-2 .. 0
+  const int nbk = nn - 1, nfb = (nbk + kRU - 1) / kRU;
+  auto issue_b = [&](int ch) {
+    if (ch < nfb) {
+      const int q = ch % kRN;
+#pragma unroll
+      for (int u = 0; u < kRU; u++) {
+        const int k = nn - 2 - ch * kRU - u;
+        if (k >= 0) {
+          tma::cp_async8(r0 + slot(q, u), Wc + k * P);
+          tma::cp_async8(r1 + slot(q, u), dc + k * P);
+        }
+      }
+    }
+    tma::cp_async_commit();
+  };
+  for (int c = 0; c < kRN - 1; c++) issue_b(c);
+  for (int ch = 0; ch < nfb; ch++) {
+    issue_b(ch + kRN - 1);
+    tma::cp_async_wait<kRN - 1>();
+    const int q = ch % kRN;
+#pragma unroll
+    for (int u = 0; u < kRU; u++) {
+      const int k = nn - 2 - ch * kRU - u;
+      if (k >= 0) {
+        y = r0[slot(q, u)] - r1[slot(q, u)] * y;
+        if (A.zper) Wc[k * P] = y;
+        else Sc[k * P] = d2f_rn(y) * normf;
+      }
+    }
+  }
+  tma::cp_async_wait<0>();
+  if (!A.zper) return;
+  const double den = A.dcl[col];
+  const double pN = den == 0. ? 0. : (f2d(Sc[nn * P]) - A.c64[nn] * y - A.a64[nn] * sl) / den;
+  Sc[nn * P] = d2f_rn(pN) * normf;
+  const double *pc = A.p2 + col;
+  auto issue_c = [&](int ch) {
+    if (ch < nf) {
+      const int q = ch % kRN;
+#pragma unroll
+      for (int u = 0; u < kRU; u++) {
+        const int k = ch * kRU + u;
+        if (k < nn) {
+          tma::cp_async8(r0 + slot(q, u), Wc + k * P);
+          tma::cp_async8(r1 + slot(q, u), pc + k * P);
+        }
+      }
+    }
+    tma::cp_async_commit();
+  };
+  for (int c = 0; c < kRN - 1; c++) issue_c(c);
+  for (int ch = 0; ch < nf; ch++) {
+    issue_c(ch + kRN - 1);
+    tma::cp_async_wait<kRN - 1>();
+    const int q = ch % kRN;
+#pragma unroll
+    for (int u = 0; u < kRU; u++) {
+      const int k = ch * kRU + u;
+      if (k < nn) Sc[k * P] = d2f_rn(fma(r1[slot(q, u)], pN, r0[slot(q, u)])) * normf;
+    }
+  }
+  tma::cp_async_wait<0>();
 }
 
 }  // namespace
@@ -81,8 +200,8 @@ __device__ __forceinline__ float rcpf(float x) {  // reciprocal, MUFU approximat
 // inner rows (rows = W (NI + 1)), so the sweeps are straight-line code; NI = 0: the inner row
 // count ni is a run-time value <= kTL - 1 (ragged last segment) and the rows are predicated.
 template <int NI>
-__device__ __forceinline__ void ztile_consume(const ZTileArgs &A, float *__restrict__ T, const float4 *__restrict__ co,
-                                              float *__restrict__ xch, float *__restrict__ Xs, int s, int lane,
+__device__ __forceinline__ void ztile_consume(const ZTileArgs &A, float *T, const float4 *co,
+                                              float *xch, float *Xs, int s, int lane,
                                               int b0, int ni_rt, int W, int tile, volatile int *cabort, bool &stop) {
   constexpr int NMAX = NI ? NI : kTL - 1;
   const int ni = NI ? NI : ni_rt;
@@ -123,6 +242,8 @@ __device__ __forceinline__ void ztile_consume(const ZTileArgs &A, float *__restr
     } else {
       zz[t] = 0.f;
     }
+    // let the scheduler run loads at most 8 rows ahead (bounded register use)
+    if ((t & 7) == 7) asm volatile("" ::: "memory");
   }
   const float hl = -co[m - 1].z * zl;  // H at the last inner row
   X6(0, s) = yf;  // first inner row: Y, G, H
@@ -173,21 +294,28 @@ __device__ __forceinline__ void ztile_consume(const ZTileArgs &A, float *__restr
       yv = (rk - q.x * yv) * zz[t];
       Ts[t * kTC] = yv;
     }
+    if ((t & 7) == 7) asm volatile("" ::: "memory");
   }
-  const size_t pitch = (size_t)A.ncol;
+  // back substitution in place; the tile's rows (scaled) then leave by a TMA store issued by
+  // the producer, or (tiles holding FP64 columns or columns past the end) by this warp's row
+  // stores of its FP32 columns
   const float normf = A.normf;
-  float *Sc = A.S + col + (size_t)b0 * pitch;
-  if (on) {
-    Sc[(size_t)ni * pitch] = XR * normf;
-    Sc[(size_t)(ni - 1) * pitch] = yv * normf;
-  }
+  Ts[(size_t)ni * kTC] = XR * normf;
+  Ts[(size_t)(ni - 1) * kTC] = yv * normf;
   float x = yv;
 #pragma unroll
   for (int t = NMAX - 2; t >= 0; t--) {
     if (NI || t < ni - 1) {
       x = Ts[t * kTC] - cs[t].z * zz[t] * x;
-      if (on) Sc[(size_t)t * pitch] = x * normf;
+      Ts[t * kTC] = x * normf;
     }
+    if ((t & 7) == 0) asm volatile("" ::: "memory");
+  }
+  if (!A.tilepure[tile]) {
+    const size_t pitch = (size_t)A.ncol;
+    float *Sc = A.S + col + (size_t)b0 * pitch;
+    if (on)
+      for (int t = 0; t <= ni; t++) Sc[(size_t)t * pitch] = Ts[t * kTC];
   }
 }
 
@@ -223,27 +351,47 @@ __global__ void __launch_bounds__(kTThreads, 1) k_zsolve_tile(const __grid_const
   for (int k = threadIdx.x; k < A.rows; k += blockDim.x) co[k] = A.coef[k];
   __syncthreads();
 
-  if (warp == W) {  // ---- producer
+  if (warp == W) {  // ---- producer: loads of the next tiles, stores of the solved ones
     if (lane != 0) return;
     tma::prefetch_map(&map);
     const uint32_t bytes = (uint32_t)(lay.tile_floats * 4);
-    int j = 0;
+    // tile j's buffer, once its consumers are done: TMA store (all-FP32 tiles), then free
+    auto retire = [&](int jj) -> bool {
+      const int b = jj % nbuf;
+      if (!tma::mbar_wait(&empty[b], (uint32_t)((jj / nbuf) & 1))) return false;
+      const int tile = blockIdx.x + jj * gridDim.x;
+      if (A.tilepure[tile]) {
+        const float *src = tiles + (size_t)b * lay.tile_floats;
+        for (int q = 0; q < A.nbox; q++)
+          tma::store_2d(&map, tile * kTC, q * A.boxrows, src + (size_t)q * A.boxrows * kTC);
+        tma::bulk_commit();
+        tma::bulk_wait_read();
+      }
+      return true;
+    };
+    int j = 0, nret = 0;
+    bool ok = true;
     for (int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x, j++) {
       const int b = j % nbuf;
-      if (j >= nbuf && !tma::mbar_wait(&empty[b], (uint32_t)((j / nbuf - 1) & 1))) {
-        *pabort = 1;
-        atomicOr(A.status, 2);
-        break;
+      if (j >= nbuf) {
+        if (!(ok = retire(j - nbuf))) break;
+        nret++;
       }
-      if (*cabort) break;
+      if (*cabort) { ok = false; break; }
       tma::mbar_arrive_expect_tx(&full[b], bytes);
       float *dst = tiles + (size_t)b * lay.tile_floats;
       for (int q = 0; q < A.nbox; q++)
         tma::load_2d(dst + (size_t)q * A.boxrows * kTC, &map, tile * kTC, q * A.boxrows, &full[b]);
     }
-    // the last load issued into each buffer has landed before the CTA may exit
-    for (int i = std::max(0, j - nbuf); i < j; i++)
-      if (!tma::mbar_wait(&full[i % nbuf], (uint32_t)((i / nbuf) & 1))) atomicOr(A.status, 2);
+    for (; ok && nret < j; nret++) ok = retire(nret);
+    if (!ok) {
+      *pabort = 1;
+      atomicOr(A.status, 2);
+      // the last load issued into each buffer has landed before the CTA may exit
+      for (int i = std::max(0, j - nbuf); i < j; i++)
+        if (!tma::mbar_wait(&full[i % nbuf], (uint32_t)((i / nbuf) & 1))) atomicOr(A.status, 2);
+    }
+    tma::bulk_wait();
     return;
   }
 
@@ -251,8 +399,7 @@ __global__ void __launch_bounds__(kTThreads, 1) k_zsolve_tile(const __grid_const
     // column groups of 32 dealt round-robin over the CTAs first, then over their FP64 warps
     for (long t = ((long)(warp - W - 1) * gridDim.x + blockIdx.x) * 32 + lane; t < A.n64;
          t += (long)gridDim.x * kT64 * 32)
-      zsolve_hyb64_col(A.S, A.Wsc, A.zinv, A.dd, A.p2, A.dcl, A.a64, A.c64, A.ncol, A.nn64, A.zper, A.norm,
-                       (long)A.col64[t]);
+      zsolve64_col_ring(A, (long)A.col64[t], lane, sm + lay.ring + (size_t)(warp - W - 1) * kRingBytes);
     return;
   }
 
@@ -325,16 +472,31 @@ int cans_ztile_setup(cans_plan *P) {
   if (nbuf < 2) return CANS_OK;
   if (!cans_encode_map_2d_f32(&P->zt.map, P->S, (uint64_t)ncol, (uint64_t)rows, kTC, (uint32_t)boxrows))
     return CANS_OK;
+  // per tile: all 32 columns in range and eliminated in FP32 (lambda not NaN in lamf)
+  {
+    const long nt = (ncol + kTC - 1) / kTC;
+    std::vector<float> lf((size_t)ncol);
+    CANS_CUDA_TRY(cudaMemcpy(lf.data(), P->lamf, lf.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    std::vector<unsigned char> pure((size_t)nt, 1);
+    for (long c = 0; c < nt * kTC; c++)
+      if (c >= ncol || lf[(size_t)c] != lf[(size_t)c]) pure[(size_t)(c / kTC)] = 0;
+    if (!P->zt.pure) {
+      CANS_CUDA_TRY(cudaMalloc(&P->zt.pure, (size_t)nt));
+      P->bytes += nt;
+    }
+    CANS_CUDA_TRY(cudaMemcpy(P->zt.pure, pure.data(), (size_t)nt, cudaMemcpyHostToDevice));
+  }
   const size_t smem = ztile_layout(rows, W, nbox, boxrows, nbuf).total;
   CANS_CUDA_TRY(cudaFuncSetAttribute(k_zsolve_tile<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
   CANS_CUDA_TRY(cudaFuncSetAttribute(k_zsolve_tile<15>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
   CANS_CUDA_TRY(cudaFuncSetAttribute(k_zsolve_tile<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+  CANS_CUDA_TRY(cudaFuncSetAttribute(k_zsolve_tile<31>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+  CANS_CUDA_TRY(cudaFuncSetAttribute(k_zsolve_tile<23>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
   const long ntiles = (ncol + kTC - 1) / kTC;
   P->zt.W = W;
   P->zt.L = L;
-  // straight-line variants where all segments are full and the unrolled sweeps fit the
-  // registers (16 and 8 rows; the longer segments run the predicated variant)
-  P->zt.ni = rows == W * L && (L == 16 || L == 8) ? L - 1 : 0;
+  // straight-line variants where all segments are full (the predicated variant otherwise)
+  P->zt.ni = rows == W * L && (L == 32 || L == 24 || L == 16 || L == 8) ? L - 1 : 0;
   P->zt.nbox = nbox;
   P->zt.boxrows = boxrows;
   P->zt.nbuf = nbuf;
@@ -353,6 +515,7 @@ int cans_ztile_launch(cans_plan *P, const Factor *F, double norm) {
   A.Wsc = P->R64;
   A.lamf = P->lamf;
   A.coef = P->coef4;
+  A.tilepure = P->zt.pure;
   A.bshift = (float)F->key;
   A.normf = (float)norm;
   A.ncol = (long)P->n[0] * P->n[1];
@@ -377,6 +540,8 @@ int cans_ztile_launch(cans_plan *P, const Factor *F, double norm) {
   A.status = P->status;
   const dim3 g(P->zt.grid), t(P->zt.threads);
   switch (P->zt.ni) {
+    case 31: k_zsolve_tile<31><<<g, t, P->zt.smem, P->stream>>>(P->zt.map, A); break;
+    case 23: k_zsolve_tile<23><<<g, t, P->zt.smem, P->stream>>>(P->zt.map, A); break;
     case 15: k_zsolve_tile<15><<<g, t, P->zt.smem, P->stream>>>(P->zt.map, A); break;
     case 7: k_zsolve_tile<7><<<g, t, P->zt.smem, P->stream>>>(P->zt.map, A); break;
     default: k_zsolve_tile<0><<<g, t, P->zt.smem, P->stream>>>(P->zt.map, A); break;
