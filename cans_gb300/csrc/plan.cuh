@@ -18,6 +18,7 @@ struct Factor {
   bool valid = false;
   double *zinv = nullptr, *dd = nullptr, *p2 = nullptr, *dcl = nullptr;  // device, FP64
   float *zinv32 = nullptr, *dd32 = nullptr, *p232 = nullptr;             // FP32 copies (FP32 plans)
+  float2 *zdf = nullptr, *ddf = nullptr, *p2df = nullptr;  // FP64 columns, double-float, [row][n64]
   unsigned long long stamp = 0;
 };
 
@@ -48,6 +49,8 @@ struct cans_plan {
   int *col64 = nullptr;       // FP32 plans: the columns eliminated in FP64 (|lambda| < lam32)
   float *lamf = nullptr;      // FP32 plans: lambda per column in FP32, NaN for the FP64 columns
   int n64 = 0;
+  float2 *adf = nullptr;      // FP32 plans: a_k as double-float pairs (FP64 columns of the tiled z pass)
+  float2 *wdf = nullptr;      // FP32 plans: double-float scratch [row][n64] of the tiled z pass
   int zpart_L = 0;            // FP32 plans: rows per segment of the partitioned z pass (0: not used)
   int zpart_mode = 0;         // 0: the column-sweep kernel, 1: the partitioned z pass (zpart_L != 0),
                               // 2: the TMA-tiled z pass (zt.ok)

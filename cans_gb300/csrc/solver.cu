@@ -309,6 +309,24 @@ __global__ void k_zfactor(const double *__restrict__ lamcol, const double *__res
   dcl[col] = (fabs(den) <= pt || structural) ? 0. : den;
 }
 
+// the FP64 columns' factors as double-float pairs in column-list order [row][n64]
+__global__ void k_factor_dfl(const double *__restrict__ zinv, const double *__restrict__ dd,
+                             const double *__restrict__ p2, const int *__restrict__ col64, int n64, long ncol,
+                             int nn, float2 *__restrict__ zdf, float2 *__restrict__ ddf, float2 *__restrict__ p2df) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)n64 * nn) return;
+  const size_t k = t / n64, q = t % n64, src = k * ncol + col64[q];
+  float h, l;
+  d2f_split(zinv[src], h, l);
+  zdf[t] = make_float2(h, l);
+  d2f_split(dd[src], h, l);
+  ddf[t] = make_float2(h, l);
+  if (p2) {
+    d2f_split(p2[src], h, l);
+    p2df[t] = make_float2(h, l);
+  }
+}
+
 __global__ void k_factor_to_f32(const double *__restrict__ a, float *__restrict__ b, size_t n) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) b[t] = (float)a[t];
@@ -659,6 +677,7 @@ template <typename T> static int upload_tables(cans_plan *P, int d) {
 static void free_factor(Factor &f) {
   cudaFree(f.zinv); cudaFree(f.dd); cudaFree(f.p2); cudaFree(f.dcl);
   cudaFree(f.zinv32); cudaFree(f.dd32); cudaFree(f.p232);
+  cudaFree(f.zdf); cudaFree(f.ddf); cudaFree(f.p2df);
   f = Factor();
 }
 
@@ -668,6 +687,7 @@ extern "C" int cans_plan_destroy(cans_plan *P) {
   for (auto &f : P->fac) free_factor(f);
   cudaFree(P->lamcol); cudaFree(P->zw); cudaFree(P->a_d); cudaFree(P->a32); cudaFree(P->zorder); cudaFree(P->b_d); cudaFree(P->c_d); cudaFree(P->bb_d);
   cudaFree(P->coef4); cudaFree(P->col64); cudaFree(P->lamf); cudaFree(P->status); cudaFree(P->zt.pure);
+  cudaFree(P->adf); cudaFree(P->wdf);
   cudaFree(P->S); cudaFree(P->R64); cudaFree(P->R32); cudaFree(P->red); cudaFree(P->E32); cudaFree(P->E32b); cudaFree(P->Rlo); cudaFree(P->rpart); cudaFree(P->coef2);
   for (auto &e : P->ev) cudaEventDestroy(e);
   for (auto &e : P->rev) cudaEventDestroy(e);
@@ -733,6 +753,22 @@ int get_factor(cans_plan *P, double key, bool helm, Factor **out) {
     CANS_LAUNCH_CHECK();
     if (P->zper) {
       k_factor_to_f32<<<g, 256, 0, P->stream>>>(slot->p2, slot->p232, cells);
+      CANS_LAUNCH_CHECK();
+    }
+    if (P->zt.ok && P->n64 > 0) {  // the FP64 columns' factors for the tiled z pass
+      const size_t c64 = (size_t)P->n64 * std::max(nn, 1);
+      if (!slot->zdf) {
+        CANS_CUDA_TRY(cudaMalloc(&slot->zdf, c64 * sizeof(float2)));
+        CANS_CUDA_TRY(cudaMalloc(&slot->ddf, c64 * sizeof(float2)));
+        P->bytes += (long long)(2 * c64 * sizeof(float2));
+        if (P->zper) {
+          CANS_CUDA_TRY(cudaMalloc(&slot->p2df, c64 * sizeof(float2)));
+          P->bytes += (long long)(c64 * sizeof(float2));
+        }
+      }
+      k_factor_dfl<<<(unsigned)((c64 + 255) / 256), 256, 0, P->stream>>>(slot->zinv, slot->dd, P->zper ? slot->p2 : nullptr,
+                                                                          P->col64, P->n64, ncol, nn, slot->zdf,
+                                                                          slot->ddf, slot->p2df);
       CANS_LAUNCH_CHECK();
     }
   }
@@ -1165,6 +1201,21 @@ extern "C" int cans_initsolver(const int ng[3], const double dli[3], const doubl
       P->bytes += (long long)(n3 * sizeof(float4) + c64.size() * sizeof(int) + lamfh.size() * sizeof(float));
       if (!P->zper && nnz >= 1 && nnz <= kZW * kZL) P->zpart_L = kZL;
       if ((rc = cans_ztile_setup(P))) return fail(rc);
+      if (P->zt.ok && P->n64 > 0) {  // double-float a_k and scratch of the tiled pass's FP64 columns
+        std::vector<float2> adh(n3);
+        for (int k = 0; k < n3; k++) {
+          const float h = (float)P->a_h[k];
+          adh[k] = make_float2(h, (float)(P->a_h[k] - (double)h));
+        }
+        const size_t c64 = (size_t)P->n64 * std::max(P->zper ? P->nn - 1 : P->nn, 1);
+        if ((e = cudaMalloc(&P->adf, n3 * sizeof(float2))) != cudaSuccess ||
+            (e = cudaMemcpy(P->adf, adh.data(), n3 * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMalloc(&P->wdf, c64 * sizeof(float2))) != cudaSuccess) {
+          cans_set_last_cuda_error(e);
+          return fail(e == cudaErrorMemoryAllocation ? CANS_ENOMEM : CANS_ECUDA);
+        }
+        P->bytes += (long long)(n3 * sizeof(float2) + c64 * sizeof(float2));
+      }
       P->zpart_mode = zpass_auto(P);
     }
   }

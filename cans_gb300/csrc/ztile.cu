@@ -39,7 +39,7 @@ constexpr int kT64 = 3;     // FP64-column warps per CTA (idle where there are f
                             // in all, five per scheduler, leave 96 registers a thread
 constexpr int kTThreads = 32 * (kTWmax + 1 + kT64);
 constexpr int kRU = 8, kRN = 4;                       // FP64 rings: rows per chunk, chunks
-constexpr int kRingBytes = 2 * kRN * kRU * 32 * 8;   // per FP64 warp
+constexpr int kRingBytes = 2 * kRN * kRU * 32 * 8;   // per FP64 warp (two float2 arrays)
 
 struct ZTileArgs {
   float *S;
@@ -53,6 +53,8 @@ struct ZTileArgs {
   const int *col64;
   int n64, nn64, zper;
   const double *zinv, *dd, *p2, *dcl, *a64, *c64;
+  const float2 *zdf, *ddf, *p2df, *adf;  // FP64-column factors and a_k as double-float pairs
+  float2 *wdf;                           // double-float scratch [row][n64]
   double norm;
   int *status;
 };
@@ -74,20 +76,45 @@ __host__ __device__ inline ZTileSmem ztile_layout(int rows, int W, int nbox, int
   return L;
 }
 
-// FP64 elimination of one spectral column (zsolve_hyb64_col's arithmetic) fed by a per-thread
-// ring of kRN chunks of kRU rows in shared memory, filled by cp.async kRN - 1 chunks ahead of
-// the recurrence, so a column's sweeps wait on FP64 latency rather than on memory: forward
-// (S, zinv) -> W; backward (W, dd) -> S, or -> W for periodic z, whose closure pass streams
-// (W, p2) -> S the same way.  ring: this warp's kRingBytes (two arrays of kRN kRU 32 doubles).
-__device__ __forceinline__ void zsolve64_col_ring(const ZTileArgs &A, long col, int lane, unsigned char *ring) {
-  double *r0 = reinterpret_cast<double *>(ring);                   // zinv / W
-  double *r1 = r0 + kRN * kRU * 32;                                 // S (as float) / dd / p2
+// double-float (hi + lo FP32 pair, ~48-bit significand) arithmetic for the FP64 columns: GB300
+// runs FP64 at a small fraction of its FP32 rate and a dependent chain of FP64 operations at a
+// long latency, so the column sweeps use error-free FP32 transformations (two-sum, FMA
+// two-product) instead.  Operand order is kept: no contraction changes the rounding.
+__device__ __forceinline__ float2 dfl_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = __fmaf_rn(a.x, b.x, -p);
+  e = __fmaf_rn(a.x, b.y, e);
+  e = __fmaf_rn(a.y, b.x, e);
+  const float s = __fadd_rn(p, e);
+  return make_float2(s, __fsub_rn(e, __fsub_rn(s, p)));
+}
+__device__ __forceinline__ float2 dfl_add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  const float r = __fadd_rn(s, e);
+  return make_float2(r, __fsub_rn(e, __fsub_rn(r, s)));
+}
+__device__ __forceinline__ float2 dfl_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+// Elimination of one FP64 column (list index t, spectral column col) with the plan's FP64
+// factors held as double-float pairs in column-list order ([row][n64]: a warp's 32 columns
+// are contiguous): forward y_k = (s_k - a_k y_{k-1}) z_k into the double-float scratch,
+// backward x_k = y_k - d_k x_{k+1}, the periodic closure x += p2 x_N (x_N from the FP64
+// formula of the sweep kernels).  Operands stream through a per-thread ring of kRN chunks of
+// kRU rows in shared memory, filled by cp.async kRN - 1 chunks ahead.  ring: this warp's
+// kRingBytes.
+__device__ __forceinline__ void zsolve_dfl_col_ring(const ZTileArgs &A, long t, long col, int lane,
+                                                    unsigned char *ring) {
+  float2 *r0 = reinterpret_cast<float2 *>(ring);      // zdf / W / W
+  float2 *r1 = r0 + kRN * kRU * 32;                    // S (as float) / ddf / p2df
   float *r1f = reinterpret_cast<float *>(r1);
   const int nn = A.nn64;
-  const size_t P = (size_t)A.ncol;
+  const size_t P = (size_t)A.ncol, Q = (size_t)A.n64;
   float *Sc = A.S + col;
-  double *Wc = A.Wsc + col;
-  const double *zc = A.zinv + col, *dc = A.dd + col;
+  float2 *Wt = A.wdf + t;
+  const float2 *zt = A.zdf + t, *dt = A.ddf + t;
   const float normf = (float)A.norm;
   auto slot = [&](int q, int u) { return (q * kRU + u) * 32 + lane; };
   const int nf = (nn + kRU - 1) / kRU;
@@ -99,13 +126,13 @@ __device__ __forceinline__ void zsolve64_col_ring(const ZTileArgs &A, long col, 
         const int k = ch * kRU + u;
         if (k < nn) {
           tma::cp_async4(r1f + slot(q, u), Sc + k * P);
-          tma::cp_async8(r0 + slot(q, u), zc + k * P);
+          tma::cp_async8(r0 + slot(q, u), zt + k * Q);
         }
       }
     }
     tma::cp_async_commit();
   };
-  double y = 0.;
+  float2 y = make_float2(0.f, 0.f);
   for (int c = 0; c < kRN - 1; c++) issue_f(c);
   for (int ch = 0; ch < nf; ch++) {
     issue_f(ch + kRN - 1);
@@ -115,15 +142,15 @@ __device__ __forceinline__ void zsolve64_col_ring(const ZTileArgs &A, long col, 
     for (int u = 0; u < kRU; u++) {
       const int k = ch * kRU + u;
       if (k < nn) {
-        y = (f2d(r1f[slot(q, u)]) - A.a64[k] * y) * r0[slot(q, u)];
-        Wc[k * P] = y;
+        const float2 rhs = make_float2(r1f[slot(q, u)], 0.f);
+        y = dfl_mul(dfl_add(rhs, dfl_neg(dfl_mul(A.adf[k], y))), r0[slot(q, u)]);
+        Wt[k * Q] = y;
       }
     }
   }
   tma::cp_async_wait<0>();
-  const double sl = y;
-  if (!A.zper) Sc[(nn - 1) * P] = d2f_rn(y) * normf;
-  // backward over rows nn-2 .. 0
+  const float2 sl = y;
+  if (!A.zper) Sc[(nn - 1) * P] = __fadd_rn(y.x, y.y) * normf;
   const int nbk = nn - 1, nfb = (nbk + kRU - 1) / kRU;
   auto issue_b = [&](int ch) {
     if (ch < nfb) {
@@ -132,8 +159,8 @@ __device__ __forceinline__ void zsolve64_col_ring(const ZTileArgs &A, long col, 
       for (int u = 0; u < kRU; u++) {
         const int k = nn - 2 - ch * kRU - u;
         if (k >= 0) {
-          tma::cp_async8(r0 + slot(q, u), Wc + k * P);
-          tma::cp_async8(r1 + slot(q, u), dc + k * P);
+          tma::cp_async8(r0 + slot(q, u), Wt + k * Q);
+          tma::cp_async8(r1 + slot(q, u), dt + k * Q);
         }
       }
     }
@@ -148,18 +175,22 @@ __device__ __forceinline__ void zsolve64_col_ring(const ZTileArgs &A, long col, 
     for (int u = 0; u < kRU; u++) {
       const int k = nn - 2 - ch * kRU - u;
       if (k >= 0) {
-        y = r0[slot(q, u)] - r1[slot(q, u)] * y;
-        if (A.zper) Wc[k * P] = y;
-        else Sc[k * P] = d2f_rn(y) * normf;
+        y = dfl_add(r0[slot(q, u)], dfl_neg(dfl_mul(r1[slot(q, u)], y)));
+        if (A.zper) Wt[k * Q] = y;
+        else Sc[k * P] = __fadd_rn(y.x, y.y) * normf;
       }
     }
   }
   tma::cp_async_wait<0>();
   if (!A.zper) return;
+  // closure row N = nn (FP64, once per column): x_N = (s_N - c_N x_0 - a_N y_{nn-1}) / dcl
   const double den = A.dcl[col];
-  const double pN = den == 0. ? 0. : (f2d(Sc[nn * P]) - A.c64[nn] * y - A.a64[nn] * sl) / den;
-  Sc[nn * P] = d2f_rn(pN) * normf;
-  const double *pc = A.p2 + col;
+  const double x0 = (double)y.x + (double)y.y, yl = (double)sl.x + (double)sl.y;
+  const double pN = den == 0. ? 0. : ((double)Sc[nn * P] - A.c64[nn] * x0 - A.a64[nn] * yl) / den;
+  Sc[nn * P] = (float)pN * normf;
+  const float pNh = (float)pN;
+  const float2 pNd = make_float2(pNh, (float)(pN - (double)pNh));
+  const float2 *pt = A.p2df + t;
   auto issue_c = [&](int ch) {
     if (ch < nf) {
       const int q = ch % kRN;
@@ -167,8 +198,8 @@ __device__ __forceinline__ void zsolve64_col_ring(const ZTileArgs &A, long col, 
       for (int u = 0; u < kRU; u++) {
         const int k = ch * kRU + u;
         if (k < nn) {
-          tma::cp_async8(r0 + slot(q, u), Wc + k * P);
-          tma::cp_async8(r1 + slot(q, u), pc + k * P);
+          tma::cp_async8(r0 + slot(q, u), Wt + k * Q);
+          tma::cp_async8(r1 + slot(q, u), pt + k * Q);
         }
       }
     }
@@ -182,7 +213,10 @@ __device__ __forceinline__ void zsolve64_col_ring(const ZTileArgs &A, long col, 
 #pragma unroll
     for (int u = 0; u < kRU; u++) {
       const int k = ch * kRU + u;
-      if (k < nn) Sc[k * P] = d2f_rn(fma(r1[slot(q, u)], pN, r0[slot(q, u)])) * normf;
+      if (k < nn) {
+        const float2 x = dfl_add(r0[slot(q, u)], dfl_mul(r1[slot(q, u)], pNd));
+        Sc[k * P] = __fadd_rn(x.x, x.y) * normf;
+      }
     }
   }
   tma::cp_async_wait<0>();
@@ -399,7 +433,7 @@ __global__ void __launch_bounds__(kTThreads, 1) k_zsolve_tile(const __grid_const
     // column groups of 32 dealt round-robin over the CTAs first, then over their FP64 warps
     for (long t = ((long)(warp - W - 1) * gridDim.x + blockIdx.x) * 32 + lane; t < A.n64;
          t += (long)gridDim.x * kT64 * 32)
-      zsolve64_col_ring(A, (long)A.col64[t], lane, sm + lay.ring + (size_t)(warp - W - 1) * kRingBytes);
+      zsolve_dfl_col_ring(A, t, (long)A.col64[t], lane, sm + lay.ring + (size_t)(warp - W - 1) * kRingBytes);
     return;
   }
 
@@ -530,6 +564,11 @@ int cans_ztile_launch(cans_plan *P, const Factor *F, double norm) {
   A.n64 = P->n64;
   A.zper = P->zper;
   A.nn64 = P->zper ? P->nn - 1 : P->nn;
+  A.zdf = F->zdf;
+  A.ddf = F->ddf;
+  A.p2df = F->p2df;
+  A.adf = P->adf;
+  A.wdf = P->wdf;
   A.zinv = F->zinv;
   A.dd = F->dd;
   A.p2 = F->p2;
