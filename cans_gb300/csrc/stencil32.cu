@@ -524,33 +524,43 @@ extern "C" int cans_chkdiv_f32(const int n[3], const double l[3], const double d
 }
 
 // chkdt (src/chkdt.f90:16-78) in FP32
+// one thread per interior cell of a 32 x 8 (i, j) tile of plane k (no index division; the
+// neighbours at fixed offsets from the cell's address); the block's max goes to part[block]
 __global__ void __launch_bounds__(kTB) k_chkdt32(Dims d, float dxi, float dyi, const float *__restrict__ dzci,
                                                  const float *__restrict__ dzfi, const float *__restrict__ u,
                                                  const float *__restrict__ v, const float *__restrict__ w,
                                                  float *__restrict__ part) {
-  int i, j, k;
+  const int i = blockIdx.x * kBX + threadIdx.x + 1, j = blockIdx.y * kBY + threadIdx.y + 1, k = blockIdx.z + 1;
   float mx = 0.f;
-  if (cell3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) {
-    const int n1 = d.n1, n2 = d.n2;
-    auto U = [&](int a, int b, int cc) { return u[hidx(a, b, cc, n1, n2)]; };
-    auto V = [&](int a, int b, int cc) { return v[hidx(a, b, cc, n1, n2)]; };
-    auto W = [&](int a, int b, int cc) { return w[hidx(a, b, cc, n1, n2)]; };
+  if (i <= d.n1 && j <= d.n2) {
+    const long sy = d.n1 + 2, sz = sy * (d.n2 + 2);
+    const size_t c = (size_t)k * sz + (size_t)j * sy + i;
+    const float *U = u + c, *V = v + c, *W = w + c;
     const float q = 0.25f;
-    const float ux = fabsf(U(i, j, k));
-    const float vx = q * fabsf(V(i, j, k) + V(i, j - 1, k) + V(i + 1, j, k) + V(i + 1, j - 1, k));
-    const float wx = q * fabsf(W(i, j, k) + W(i, j, k - 1) + W(i + 1, j, k) + W(i + 1, j, k - 1));
+    const float ux = fabsf(U[0]);
+    const float vx = q * fabsf(V[0] + V[-sy] + V[1] + V[1 - sy]);
+    const float wx = q * fabsf(W[0] + W[-sz] + W[1] + W[1 - sz]);
     const float dtix = ux * dxi + vx * dyi + wx * dzfi[k];
-    const float uy = q * fabsf(U(i, j, k) + U(i, j + 1, k) + U(i - 1, j + 1, k) + U(i - 1, j, k));
-    const float vy = fabsf(V(i, j, k));
-    const float wy = q * fabsf(W(i, j, k) + W(i, j + 1, k) + W(i, j + 1, k - 1) + W(i, j, k - 1));
+    const float uy = q * fabsf(U[0] + U[sy] + U[sy - 1] + U[-1]);
+    const float vy = fabsf(V[0]);
+    const float wy = q * fabsf(W[0] + W[sy] + W[sy - sz] + W[-sz]);
     const float dtiy = uy * dxi + vy * dyi + wy * dzfi[k];
-    const float uz = q * fabsf(U(i, j, k) + U(i - 1, j, k) + U(i - 1, j, k + 1) + U(i, j, k + 1));
-    const float vz = q * fabsf(V(i, j, k) + V(i, j - 1, k) + V(i, j - 1, k + 1) + V(i, j, k + 1));
-    const float wz = fabsf(W(i, j, k));
+    const float uz = q * fabsf(U[0] + U[-1] + U[sz - 1] + U[sz]);
+    const float vz = q * fabsf(V[0] + V[-sy] + V[sz - sy] + V[sz]);
+    const float wz = fabsf(W[0]);
     const float dtiz = uz * dxi + vz * dyi + wz * dzci[k];
     mx = fmaxf(fmaxf(dtix, dtiy), dtiz);
   }
-  block_max_f32(mx, part);
+  __shared__ float rm[kTB / 32];
+  const int tid = threadIdx.y * kBX + threadIdx.x;
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((tid & 31) == 0) rm[tid >> 5] = mx;
+  __syncthreads();
+  if (tid == 0) {
+    float b = 0.f;
+    for (int qq = 0; qq < kTB / 32; qq++) b = fmaxf(b, rm[qq]);
+    part[blockIdx.x + gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z)] = b;
+  }
 }
 
 extern "C" int cans_chkdt_f32(const int n[3], const double dl[3], const float *dzci, const float *dzfi, double visc,
@@ -560,13 +570,14 @@ extern "C" int cans_chkdt_f32(const int n[3], const double dl[3], const float *d
   if (n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
   cudaStream_t st = as_stream(stream);
   Dims d{n[0], n[1], n[2]};
-  const unsigned nblk = blocks_for((long)n[0] * n[1] * n[2]);
+  const dim3 g = grid_interior(n);
+  const unsigned nblk = g.x * g.y * g.z;
   std::lock_guard<std::mutex> lk(g_red32_mu);
   double *s;
   int rc = red32_scratch((size_t)nblk + 4, &s);
   if (rc) return rc;
   float *pm = reinterpret_cast<float *>(s + 2);
-  k_chkdt32<<<nblk, kTB, 0, st>>>(d, (float)(1. / dl[0]), (float)(1. / dl[1]), dzci, dzfi, u, v, w, pm);
+  k_chkdt32<<<g, dim3(kBX, kBY), 0, st>>>(d, (float)(1. / dl[0]), (float)(1. / dl[1]), dzci, dzfi, u, v, w, pm);
   CANS_LAUNCH_CHECK();
   k_max1<<<1, kTB, 0, st>>>(pm, nblk, s);
   CANS_LAUNCH_CHECK();
