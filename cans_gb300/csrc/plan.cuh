@@ -245,6 +245,11 @@ template <typename T, int M> struct PassGeo {
 // conversion instructions: there the FP64 pipe is otherwise idle and the integer versions'
 // ALU work measured slower (x-forward from FP64 0.56 -> 0.87 ms at 512^3).
 template <typename T, typename TF> __device__ __forceinline__ T cvt_to(TF v) { return (T)v; }
+// exact widening into the x-backward pass's output type: FP32 -> FP64 by integer operations
+// (fpconv.cuh), which keeps the conversion off GB300's FP64 pipe where the pass also adds in
+// FP64 (the accumulating pass of the refinement: two FP64-pipe operations per value otherwise)
+template <typename TF, typename T> __device__ __forceinline__ TF widen(T v) { return (TF)v; }
+template <> __device__ __forceinline__ double widen<double, float>(float v) { return f2d(v); }
 
 // 16-byte vector of T (global loads of contiguous rows in the compile-time path)
 template <typename T> struct Vec16;
@@ -462,11 +467,11 @@ __device__ __forceinline__ void ylines_persist(T *__restrict__ S, long nlines, c
 template <typename T, typename TF>
 __device__ __forceinline__ TF xbwd_value(const TF *__restrict__ p, size_t idx, int acc, T v, const T *add0,
                                          const T *add1) {
-  if (acc == 0) return cvt_to<TF, T>(v);
-  if (acc == 1) return (TF)(p[idx] + cvt_to<TF, T>(v));
-  TF x = cvt_to<TF, T>(add0[idx]);
-  if (add1) x = x + cvt_to<TF, T>(add1[idx]);
-  return x + cvt_to<TF, T>(v);
+  if (acc == 0) return widen<TF, T>(v);
+  if (acc == 1) return (TF)(p[idx] + widen<TF, T>(v));
+  TF x = widen<TF, T>(add0[idx]);
+  if (add1) x = x + widen<TF, T>(add1[idx]);
+  return x + widen<TF, T>(v);
 }
 
 // 5. x-backward: S[k][i][j] -> haloed rows p(1:n1, j, k) (see xbwd_value)
@@ -691,10 +696,10 @@ __device__ __forceinline__ void xbwd_persist(const T *__restrict__ S, TF *__rest
         T v0, v1;
         r2r_post2<T, M, kLay<M>, KD>(P, Z, q, i, post, v0, v1);
         const size_t idx = (size_t)(row0 - p) + (size_t)(2 * q) * (n1 + 2) + i;
-        p[idx] = acc == 1 ? (TF)(old0[u] + cvt_to<TF, T>(v0)) : xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
+        p[idx] = acc == 1 ? (TF)(old0[u] + widen<TF, T>(v0)) : xbwd_value<T, TF>(p, idx, acc, v0, add0, add1);
         if (j + 1 < n2) {
           const size_t idx1 = idx + (size_t)(n1 + 2);
-          p[idx1] = acc == 1 ? (TF)(old1[u] + cvt_to<TF, T>(v1)) : xbwd_value<T, TF>(p, idx1, acc, v1, add0, add1);
+          p[idx1] = acc == 1 ? (TF)(old1[u] + widen<TF, T>(v1)) : xbwd_value<T, TF>(p, idx1, acc, v1, add0, add1);
         }
       }
       __syncthreads();
