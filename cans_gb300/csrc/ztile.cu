@@ -47,7 +47,7 @@ struct ZTileArgs {
   const float *lamf;    // lambda_xy per column in FP32; NaN: an FP64 column
   const float4 *coef;   // (a_k, b_k, c_k, -), a_0 = c_last = 0 when z is not periodic
   const unsigned char *tilepure;  // per tile: 1 when all its 32 columns are FP32 columns
-  float bshift, normf;  // diagonal shift (Helmholtz) and the FFT normalisation
+  float bshift, normi;  // diagonal shift (Helmholtz) and 1 / the FFT normalisation
   long ncol;
   int rows, W, L, nbox, boxrows, nbuf, ntiles;
   const int *col64;
@@ -236,7 +236,8 @@ __device__ __forceinline__ float rcpf(float x) {  // reciprocal, MUFU approximat
 template <int NI>
 __device__ __forceinline__ void ztile_consume(const ZTileArgs &A, float *T, const float4 *co,
                                               float *xch, float *Xs, int s, int lane,
-                                              int b0, int ni_rt, int W, int tile, volatile int *cabort, bool &stop) {
+                                              int b0, int ni_rt, int W, int tile, float lam0, volatile int *cabort,
+                                              bool &stop) {
   constexpr int NMAX = NI ? NI : kTL - 1;
   const int ni = NI ? NI : ni_rt;
   const int m = b0 + ni;
@@ -245,9 +246,8 @@ __device__ __forceinline__ void ztile_consume(const ZTileArgs &A, float *T, cons
   auto X6 = [&](int v, int seg) -> float & { return xch[((size_t)v * W + seg) * kTC + lane]; };
   auto R = [&](int pp, int v, int seg) -> float & { return xch[(((size_t)pp * 4 + v) * W + seg) * kTC + lane]; };
   const long col = (long)tile * kTC + lane;
-  float lam = col < A.ncol ? A.lamf[col] : __int_as_float(0x7fc00000);
-  const bool on = lam == lam;  // NaN: an FP64 column or past the last column
-  lam = on ? lam + A.bshift : -1.0e30f;
+  const bool on = lam0 == lam0;  // NaN: an FP64 column or past the last column
+  const float lam = on ? (lam0 + A.bshift) * A.normi : -1.0e30f;
   const float4 *cs = co + b0;
   float *Ts = T + (size_t)b0 * kTC + lane;
 
@@ -330,22 +330,21 @@ __device__ __forceinline__ void ztile_consume(const ZTileArgs &A, float *T, cons
     }
     if ((t & 7) == 7) asm volatile("" ::: "memory");
   }
-  // back substitution in place; the tile's rows (scaled) then leave by a TMA store issued by
-  // the producer, or (tiles holding FP64 columns or columns past the end) by this warp's row
+  // back substitution in place; the tile's rows then leave by a TMA store issued by the
+  // producer, or (tiles holding FP64 columns or columns past the end) by this warp's row
   // stores of its FP32 columns
-  const float normf = A.normf;
-  Ts[(size_t)ni * kTC] = XR * normf;
-  Ts[(size_t)(ni - 1) * kTC] = yv * normf;
+  Ts[(size_t)ni * kTC] = XR;
+  Ts[(size_t)(ni - 1) * kTC] = yv;
   float x = yv;
 #pragma unroll
   for (int t = NMAX - 2; t >= 0; t--) {
     if (NI || t < ni - 1) {
       x = Ts[t * kTC] - cs[t].z * zz[t] * x;
-      Ts[t * kTC] = x * normf;
+      Ts[t * kTC] = x;
     }
     if ((t & 7) == 0) asm volatile("" ::: "memory");
   }
-  if (!A.tilepure[tile]) {
+  if (!__all_sync(0xffffffffu, on)) {  // the tile holds an FP64 column or columns past the end
     const size_t pitch = (size_t)A.ncol;
     float *Sc = A.S + col + (size_t)b0 * pitch;
     if (on)
@@ -382,7 +381,11 @@ __global__ void __launch_bounds__(kTThreads, 1) k_zsolve_tile(const __grid_const
     *pabort = 0;
     tma::mbar_fence_init();
   }
-  for (int k = threadIdx.x; k < A.rows; k += blockDim.x) co[k] = A.coef[k];
+  // the operator divided by the FFT normalisation: the solution comes out normalised
+  for (int k = threadIdx.x; k < A.rows; k += blockDim.x) {
+    const float4 c = A.coef[k];
+    co[k] = make_float4(c.x * A.normi, c.y * A.normi, c.z * A.normi, 0.f);
+  }
   __syncthreads();
 
   if (warp == W) {  // ---- producer: loads of the next tiles, stores of the solved ones
@@ -392,9 +395,10 @@ __global__ void __launch_bounds__(kTThreads, 1) k_zsolve_tile(const __grid_const
     // tile j's buffer, once its consumers are done: TMA store (all-FP32 tiles), then free
     auto retire = [&](int jj) -> bool {
       const int b = jj % nbuf;
-      if (!tma::mbar_wait(&empty[b], (uint32_t)((jj / nbuf) & 1))) return false;
       const int tile = blockIdx.x + jj * gridDim.x;
-      if (A.tilepure[tile]) {
+      const bool pure = A.tilepure[tile] != 0;  // loaded before the wait: its latency overlaps it
+      if (!tma::mbar_wait(&empty[b], (uint32_t)((jj / nbuf) & 1))) return false;
+      if (pure) {
         const float *src = tiles + (size_t)b * lay.tile_floats;
         for (int q = 0; q < A.nbox; q++)
           tma::store_2d(&map, tile * kTC, q * A.boxrows, src + (size_t)q * A.boxrows * kTC);
@@ -443,14 +447,22 @@ __global__ void __launch_bounds__(kTThreads, 1) k_zsolve_tile(const __grid_const
   const int ni = (s == W - 1 ? A.rows - b0 : A.L) - 1;  // inner rows; row b0 + ni is the separator
   int j = 0;
   bool stop = false;
+  // lambda of the column in the next tile, loaded one tile ahead (off the sweeps' critical path)
+  auto lam_of = [&](int tile) {
+    const long col = (long)tile * kTC + lane;
+    return tile < A.ntiles && col < A.ncol ? A.lamf[col] : __int_as_float(0x7fc00000);
+  };
+  float lam_nx = lam_of(blockIdx.x);
   for (int tile = blockIdx.x; tile < A.ntiles && !stop; tile += gridDim.x, j++) {
     const int b = j % nbuf;
+    const float lam0 = lam_nx;
+    lam_nx = lam_of(tile + gridDim.x);
     if (!tma::mbar_wait(&full[b], (uint32_t)((j / nbuf) & 1))) {
       *cabort = 1;
       atomicOr(A.status, 2);
     }
     float *T = tiles + (size_t)b * lay.tile_floats;
-    ztile_consume<NI>(A, T, co, xch, Xs, s, lane, b0, ni, W, tile, cabort, stop);
+    ztile_consume<NI>(A, T, co, xch, Xs, s, lane, b0, ni, W, tile, lam0, cabort, stop);
     if (stop) break;
     // order this thread's generic shared-memory accesses before the next TMA write of the buffer
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -551,7 +563,7 @@ int cans_ztile_launch(cans_plan *P, const Factor *F, double norm) {
   A.coef = P->coef4;
   A.tilepure = P->zt.pure;
   A.bshift = (float)F->key;
-  A.normf = (float)norm;
+  A.normi = (float)(1. / norm);
   A.ncol = (long)P->n[0] * P->n[1];
   A.rows = P->nn;
   A.W = P->zt.W;
