@@ -138,6 +138,7 @@ def _setup(L):
     L.cans_chkdt_f32.argtypes = L.cans_chkdt.argtypes
     L.cans_bulk_mean_f32.argtypes = L.cans_bulk_mean.argtypes
     L.cans_correc_updatep_f32.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V, _V]
+    L.cans_selftest_wait_timeout.argtypes = [C.c_int, _I]
     L.cans_plan_set_zpass.argtypes = [_V, C.c_int]
     L.cans_plan_check.argtypes = [_V]
     L.cans_initflow.argtypes = [C.c_char_p, _D, _I, _D, _D, _D, _D, _D, _D, C.c_double, _I, _D, _D, C.c_int,
@@ -645,3 +646,11 @@ def initflow(inivel, bcvel, n, l, dl, zc, zf, dzc, dzf, visc, is_forced, velf, b
     _check(lib().cans_initflow(_chars(inivel), _dbls(bcvel), _ints(n), _dbls(l), _dbls(dl), pzc, pzf, pdc, pdf,
                                float(visc), _ints(is_forced), _dbls(velf), _dbls(bforce), int(bool(is_wallturb)),
                                _ptr(u), _ptr(v), _ptr(w), _ptr(p), _stream(stream)), "cans_initflow")
+
+
+def selftest_wait_timeout(limit_us=20000):
+    """cans_selftest_wait_timeout: True when a bounded device wait that nothing releases gave up
+    after limit_us and the kernel returned (the context stays usable)"""
+    r = C.c_int(0)
+    _check(lib().cans_selftest_wait_timeout(int(limit_us), C.byref(r)), "cans_selftest_wait_timeout")
+    return bool(r.value)

@@ -55,12 +55,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// wait for the phase of parity `parity` to complete; false after kWaitLimitNs
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// wait for the phase of parity `parity` to complete; false after limit_ns
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned long long limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = globaltimer();
   while (!mbar_try_wait(bar, parity))
-    if (globaltimer() - t0 > kWaitLimitNs) return false;
+    if (globaltimer() - t0 > limit_ns) return false;
   return true;
 }
 

@@ -600,3 +600,36 @@ int cans_ztile_launch(cans_plan *P, const Factor *F, double norm) {
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
+
+// Self-test of the bounded wait used by the tiled z pass: one CTA waits on an mbarrier that no
+// thread arrives on, with a limit of limit_us microseconds.  The wait must give up, the kernel
+// records that in *result (1: the wait expired and returned, 2: it completed, which would
+// be an error) and returns; the context stays usable.
+__global__ void k_selftest_wait(unsigned long long limit_ns, int *result) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tma::mbar_init(&bar, 1);
+    tma::mbar_fence_init();
+  }
+  __syncthreads();
+  const bool done = tma::mbar_wait(&bar, 0, limit_ns);
+  if (threadIdx.x == 0) *result = done ? 2 : 1;
+}
+
+extern "C" int cans_selftest_wait_timeout(int limit_us, int *expired) {
+  if (!expired || limit_us < 1 || limit_us > 100000) return CANS_EINVAL;
+  int *d = nullptr;
+  CANS_CUDA_TRY(cudaMalloc(&d, sizeof(int)));
+  k_selftest_wait<<<1, 32>>>((unsigned long long)limit_us * 1000ull, d);
+  cans_count_launch();
+  int h = 0;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    cans_set_last_cuda_error(e);
+    return CANS_ECUDA;
+  }
+  *expired = h == 1;
+  return CANS_OK;
+}

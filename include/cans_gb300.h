@@ -363,6 +363,11 @@ int cans_plan_get_shape(const cans_plan *plan, int d, int radix[12], int *nstage
  * bounded wait of the TMA-tiled z pass expired (its results are then not valid), CANS_OK
  * otherwise; clears the record. */
 int cans_plan_check(cans_plan *plan);
+/* Self-test of the bounded device waits (no counterpart in the reference): launches one CTA
+ * that waits on an mbarrier nothing arrives on, with a limit of limit_us microseconds
+ * (1..100000); *expired = 1 when the wait gave up and the kernel returned normally, as the
+ * tiled z pass's waits do before reporting CANS_ETIMEOUT.  Synchronises the device. */
+int cans_selftest_wait_timeout(int limit_us, int *expired);
 /* z pass of an FP32 plan (no counterpart in the reference; the elimination of
  * src/solver_gpu.f90:278-428): mode 0 = one thread per spectral column sweeping all rows with
  * precomputed factors; 1 = the column split into 16-row segments held in registers, factors

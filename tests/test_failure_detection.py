@@ -103,3 +103,22 @@ def test_solver_reports_nonfinite_rhs(require_gpu):
             plan.solve(q) if prec == cans.FP64 else plan.solve(q.float())
             assert not plan.check()
             assert plan.check()  # the record was cleared
+
+
+@pytest.mark.gpu
+def test_bounded_device_wait_expires(require_gpu):
+    """A device wait that nothing releases (an mbarrier no thread arrives on) gives up after
+    its limit and the kernel returns; the context stays usable for the next solve.  This is
+    the wait of the TMA-tiled z pass, which then reports CANS_ETIMEOUT through
+    cans_plan_check; no GPU fault is involved."""
+    import torch
+    from cans_gb300 import cans
+    assert cans.selftest_wait_timeout(20000)
+    n = [16, 12, 10]
+    plan = cans.Plan(n, [8., 12., 10.], np.full(n[2] + 2, 10.), np.full(n[2] + 2, 10.), "PPPPNN", [0.] * 6,
+                     "ccc", precision=cans.FP32)
+    p = cans.field(n).float()
+    p[1:-1, 1:-1, 1:-1] = torch.randn((n[2], n[1], n[0]), device="cuda")
+    p[1:-1, 1:-1, 1:-1] -= p[1:-1, 1:-1, 1:-1].mean()
+    plan.solve(p)
+    assert plan.check()
