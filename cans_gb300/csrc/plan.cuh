@@ -54,6 +54,7 @@ struct cans_plan {
   int zpart_L = 0;            // FP32 plans: rows per segment of the partitioned z pass (0: not used)
   int zpart_mode = 0;         // 0: the column-sweep kernel, 1: the partitioned z pass (zpart_L != 0),
                               // 2: the TMA-tiled z pass (zt.ok)
+  int ytma = 1;               // FP32 plans: y passes fed by TMA bulk copies (k_ylines_pt)
   struct {                    // FP32 plans: the TMA-tiled z pass (ztile.cu)
     bool ok = false;          // usable: ncol % 4 == 0 and the row count fits a tile
     CUtensorMap map;          // S as [rows][ncol] FP32, boxes of 32 columns x boxrows rows
@@ -458,6 +459,69 @@ __device__ __forceinline__ void ylines_persist(T *__restrict__ S, long nlines, c
       if (tile + gridDim.x < ntiles) load(tile + gridDim.x);
       ylines_fft_store<T, M, decltype(K)::value>(S, nlines, M, P, tile * G::LPB, A, B, stg, tw, post, pre);
       __syncthreads();  // the next tile's staging overwrites B, its first step A
+    }
+  });
+}
+
+// persistent FP32 y pass fed by TMA: each CTA loops over tiles tile0, tile0 + gridDim.x, ...;
+// the LPB contiguous lines of the next tile are brought into one of two landing buffers (rows
+// of the staging pitch SLD) by bulk TMA copies, one per line, issued by one thread while the
+// current tile is transformed, with completion on the buffer's mbarrier.  The transform reads
+// its first step straight from the landing buffer.  Lines past the end of the last tile are
+// zeroed (two lines share one complex sequence).  Waits are bounded; an expired wait sets
+// bit 1 of *status (the transform then runs on whatever the buffer holds).
+template <int M>
+__device__ __forceinline__ void ylines_persist_tma(float *__restrict__ S, long nlines, const DirParams &P, long ntiles,
+                                                   unsigned char *smem, int *status) {
+  static_assert(M > 0, "compile-time lengths only");
+  using T = float;
+  using T2 = cplx_t<T>;
+  using G = PassGeo<T, M>;
+  T2 *A = reinterpret_cast<T2 *>(smem);
+  T2 *B = A + (size_t)G::NCX * G::LD;
+  const size_t toff = tile_tables_offset<T>(G::NCX, G::LD, G::LPB, G::SLD);
+  T2 *stw = reinterpret_cast<T2 *>(smem + toff);
+  const size_t loff = (toff + (size_t)3 * M * sizeof(T2) + 127) & ~(size_t)127;
+  T *L0 = reinterpret_cast<T *>(smem + loff);
+  T *L1 = L0 + (size_t)G::LPB * G::SLD;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(L1 + (size_t)G::LPB * G::SLD);
+  const T2 *tw = stw, *post = stw + M, *pre = stw + 2 * M;
+  auto issue = [&](long tile, T *dst, uint64_t *b) {
+    const long rows = nlines - tile * G::LPB < G::LPB ? nlines - tile * G::LPB : G::LPB;
+    tma::mbar_arrive_expect_tx(b, (uint32_t)(rows * M * sizeof(T)));
+    const T *src = S + (size_t)tile * G::LPB * M;
+    for (int r = 0; r < rows; r++) tma::bulk_load(dst + (size_t)r * G::SLD, src + (size_t)r * M, M * sizeof(T), b);
+  };
+  long tile = blockIdx.x;
+  if (threadIdx.x == 0) {
+    tma::mbar_init(&bar[0], 1);
+    tma::mbar_init(&bar[1], 1);
+    tma::mbar_fence_init();
+    if (tile < ntiles) issue(tile, L0, &bar[0]);
+  }
+  copy_tables<T, M>(P, M, M, stw, stw + M, stw + 2 * M);
+  __syncthreads();
+  int j = 0;
+  with_kind<M, 2>(P.kind, [&](auto K) {
+    for (; tile < ntiles; tile += gridDim.x, j++) {
+      const int b = j & 1;
+      T *L = b ? L1 : L0;
+      if (threadIdx.x == 0 && tile + gridDim.x < ntiles) {
+        // the other buffer was last read by the previous tile's transform (barrier below)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(tile + gridDim.x, b ? L0 : L1, &bar[b ^ 1]);
+      }
+      if (!tma::mbar_wait(&bar[b], (uint32_t)((j >> 1) & 1))) {
+        if (threadIdx.x == 0 && status) atomicOr(status, 2);
+        tma::mbar_wait(&bar[b], (uint32_t)((j >> 1) & 1));  // once more for the copies in flight
+      }
+      const long rows = nlines - tile * G::LPB;
+      if (rows < G::LPB) {  // zero the lines past the end (they share sequences with real lines)
+        for (int e = threadIdx.x; e < (G::LPB - (int)rows) * G::SLD; e += blockDim.x) L[rows * G::SLD + e] = 0.f;
+        __syncthreads();
+      }
+      ylines_fft_store<T, M, decltype(K)::value>(S, nlines, M, P, tile * G::LPB, A, B, L, tw, post, pre);
+      __syncthreads();  // the landing buffer and A/B are free for the next tiles
     }
   });
 }

@@ -237,6 +237,22 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_ylines_p(T *__r
   ylines_persist<T, M>(S, nlines, P, ntiles, smem);
 }
 
+// FP32 y pass fed by TMA bulk copies (two landing buffers: two CTAs per SM at 512)
+template <int M>
+__global__ void __launch_bounds__(256, 2) k_ylines_pt(float *__restrict__ S, long nlines, long ntiles, DirParams P,
+                                                      int *status) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  ylines_persist_tma<M>(S, nlines, P, ntiles, smem, status);
+}
+// its shared memory: the pass layout, the tables, two landing buffers, two mbarriers
+template <int M> static size_t smem_bytes_pt(const DirParams &q) {
+  using G = PassGeo<float, M>;
+  const size_t toff = tile_tables_offset<float>(G::NCX, G::LD, G::LPB, G::SLD);
+  const size_t loff = (toff + (size_t)3 * M * sizeof(float2) + 127) & ~(size_t)127;
+  (void)q;
+  return loff + (size_t)2 * G::LPB * G::SLD * sizeof(float) + 2 * sizeof(uint64_t) + 16;
+}
+
 template <typename T, typename TF, int M>
 __global__ void __launch_bounds__(256) k_xbwd(const T *__restrict__ S, TF *__restrict__ p, int n1, int n2, DirParams P,
                                               int acc, const T *add0, const T *add1) {
@@ -895,6 +911,15 @@ template <typename T> static int launch_y(cans_plan *P, int fwd) {
     unsigned pg = 0;
 #define CALL_YP(MM)                                                                              \
   do {                                                                                           \
+    if constexpr (sizeof(T) == 4) {                                                              \
+      if (P->ytma) {                                                                             \
+        const size_t smt = smem_bytes_pt<MM>(q);                                                 \
+        if ((rc = set_smem<T>((const void *)k_ylines_pt<MM>, smt))) return rc;                   \
+        if ((rc = resident_grid((const void *)k_ylines_pt<MM>, smt, ntiles, &pg))) return rc;    \
+        k_ylines_pt<MM><<<pg, 256, smt, P->stream>>>((float *)P->S, nlines, ntiles, q, P->status); \
+        break;                                                                                   \
+      }                                                                                          \
+    }                                                                                            \
     if ((rc = set_smem<T>((const void *)k_ylines_p<T, MM>, sm))) return rc;                      \
     if ((rc = resident_grid((const void *)k_ylines_p<T, MM>, sm, ntiles, &pg))) return rc;       \
     k_ylines_p<T, MM><<<pg, 256, sm, P->stream>>>((T *)P->S, nlines, ntiles, q);                  \

@@ -75,6 +75,15 @@ __device__ __forceinline__ void load_2d(void *dst, const CUtensorMap *map, int x
       : "memory");
 }
 
+// bulk (non-tensor) TMA copy of `bytes` contiguous bytes global -> shared, completion as
+// transaction bytes on `bar`; both addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
 // 2-D tiled TMA store of the box at (x, y) from shared memory (bulk-group completion)
 __device__ __forceinline__ void store_2d(const CUtensorMap *map, int x, int y, const void *src) {
   asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
