@@ -25,6 +25,7 @@
 #include <mutex>
 #include <tuple>
 #include <cfloat>
+#include <unordered_map>
 #include <vector>
 
 #include "cans_internal.cuh"
@@ -795,8 +796,27 @@ int get_factor(cans_plan *P, double key, bool helm, Factor **out) {
   return CANS_OK;
 }
 
+// The dynamic shared-memory limit of a pass kernel, raised once per (device, kernel) to the
+// largest size asked for so far: the per-launch path then makes no attribute call
+struct SmemKey {
+  int dev;
+  const void *fn;
+  bool operator==(const SmemKey &o) const { return dev == o.dev && fn == o.fn; }
+};
+struct SmemKeyHash {
+  size_t operator()(const SmemKey &k) const { return std::hash<const void *>()(k.fn) ^ (size_t)k.dev; }
+};
+static std::mutex g_smem_mu;
+static std::unordered_map<SmemKey, size_t, SmemKeyHash> g_smem_set;
+
 template <typename T> static int set_smem(const void *fn, size_t bytes) {
+  int dev = 0;
+  CANS_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> g(g_smem_mu);
+  size_t &cur = g_smem_set[SmemKey{dev, fn}];
+  if (bytes <= cur) return CANS_OK;
   CANS_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
   return CANS_OK;
 }
 
@@ -820,8 +840,20 @@ static int resident_grid(const void *fn, size_t smem, long tiles, unsigned *grid
     CANS_CUDA_TRY(cudaGetDevice(&dev));
     CANS_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   }
+  // resident CTAs per SM of (kernel, shared memory), computed once
+  static std::mutex mu;
+  static std::unordered_map<const void *, std::vector<std::pair<size_t, int>>> memo;
   int per = 0;
-  CANS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, smem));
+  {
+    std::lock_guard<std::mutex> g(mu);
+    for (const auto &e : memo[fn])
+      if (e.first == smem) per = e.second;
+  }
+  if (!per) {
+    CANS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, smem));
+    std::lock_guard<std::mutex> g(mu);
+    memo[fn].push_back({smem, per});
+  }
   if (per < 1) return CANS_ENOTSUP;
   *grid = (unsigned)std::max(1L, std::min<long>(tiles, (long)per * nsm));
   return CANS_OK;
