@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(kDfTB) k_dfres(const float *__restrict__ E, fl
     const float *Et = k < n3 ? Ec + sz : (o.zper ? Ec - (long)(n3 - 1) * sz : Ec);
     float *Rr = R + c0;
     float *Lr = Rlo + (long)n1 * u;  // low parts of the row: Lr[i - 1], i = 1..n1
-#pragma unroll 4
+#pragma unroll 8
     for (int i = threadIdx.x + 1; i <= n1; i += kDfTB) {
       const float ec = Ec[i];
       float ew = Ec[i == 1 && wrapw ? n1 : i - 1];
