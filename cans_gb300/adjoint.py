@@ -1,7 +1,8 @@
 """Reverse-mode gradients of a CaNS run through the library's hand-written adjoint kernels.
 
-`AdjointRun(case)` wraps `driver.Simulation` for explicit diffusion, a fixed time step
-(`dt_f`) and no flow-rate forcing.  `forward(u0, v0, w0, bforce, nsteps)` runs the model
+`AdjointRun(case)` wraps `driver.Simulation` for explicit or implicit diffusion
+(`is_impdiff`: the three velocity Helmholtz solves of src/main.f90:455-463 and updatep's
+alpha lap(pp) term are reversed too), a fixed time step (`dt_f`) and no flow-rate forcing.  `forward(u0, v0, w0, bforce, nsteps)` runs the model
 from the given interior initial velocity and uniform body force and returns
 
     J = 1/2 sum over interior cells of (u^2 dx dy dzf + v^2 dx dy dzf + w^2 dx dy dzc),
@@ -11,7 +12,8 @@ every `ckpt_every` steps.  `backward()` returns dJ/d(u0, v0, w0) (interior array
 dJ/d(bforce): it walks the segments between checkpoints backwards, recomputes each
 segment's substep inputs from its checkpoint, and applies the adjoint of every substep
 (src/main.f90:452-472 in reverse: boundp, updatep, bounduvw, correc, boundp, solver,
-fillps, bounduvw, rk) and finally that of the initial boundary fills
+fillps, bounduvw, the Helmholtz solves when diffusion is implicit, rk) and finally that of
+the initial boundary fills
 (src/main.f90:388-418).  Device memory: one checkpoint per `ckpt_every` steps plus
 3 x 3 x ckpt_every velocity fields of the segment being reversed.
 """
@@ -23,8 +25,8 @@ from .driver import RKCOEFF, Simulation
 
 class AdjointRun:
     def __init__(self, case, device="cuda", ckpt_every=10):
-        if int(case.get("is_impdiff", 0)) or any(int(x) for x in case.get("is_forced", [0, 0, 0])):
-            raise ValueError("adjoint: explicit diffusion and no flow-rate forcing only")
+        if any(int(x) for x in case.get("is_forced", [0, 0, 0])):
+            raise ValueError("adjoint: no flow-rate forcing")
         if not case.get("dt_f", -1.) > 0.:
             raise ValueError("adjoint: fixed time step (dt_f > 0) required")
         self.case = dict(case)
@@ -92,10 +94,11 @@ class AdjointRun:
         s = self.sim
         n = s.n
         dtrk = (RKCOEFF[irk][0] + RKCOEFF[irk][1]) * s.dt
+        alpha = -.5 * s.visc * dtrk if s.is_impdiff else 0.
         gu, gv, gw, gp = g["gu"], g["gv"], g["gw"], g["gp"]
         cans.boundp_adjoint(s.cbcpre, n, s.bcpre, s.is_bound, s.dl, s.dzc, gp, cans.HALO_UPPER)
         gpp = torch.zeros_like(gp)
-        cans.updatep_adjoint(n, 0, gp, gpp)
+        cans.updatep_adjoint(n, s.is_impdiff, gp, gpp, s.dli, s.dzci, s.dzfi, alpha)
         cans.bounduvw_adjoint(s.cbcvel, n, s.bcvel, s.is_bound, s.dl, s.dzc, s.dzf, gu, gv, gw, True, cans.HALO_UPPER,
                               cans.HALO_NONE)
         cans.correc_adjoint(n, s.dli, s.dzci, dtrk, gu, gv, gw, gpp)
@@ -104,8 +107,11 @@ class AdjointRun:
         cans.fillps_adjoint(n, s.dli, s.dzfi, 1. / dtrk, gpp, gu, gv, gw)
         cans.bounduvw_adjoint(s.cbcvel, n, s.bcvel, s.is_bound, s.dl, s.dzc, s.dzf, gu, gv, gw, False,
                               cans.HALO_LOWER)
+        if s.is_impdiff:  # the velocity Helmholtz solves (their boundary terms are constants)
+            for c, gf in enumerate((gu, gv, gw)):
+                s.plans_v[c].solve_helmholtz_adjoint(alpha, gf)
         gbf = cans.rk_adjoint(RKCOEFF[irk], n, s.dli, s.dzci, s.dzfi, s.dt, s.visc, u_in[0], u_in[1], u_in[2], gu, gv,
-                              gw, g["gdu"], g["gdv"], g["gdw"], gp, self.work)
+                              gw, g["gdu"], g["gdv"], g["gdw"], gp, self.work, is_impdiff=s.is_impdiff)
         g["gbf"] += gbf
 
     def backward(self):

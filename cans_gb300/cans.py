@@ -110,11 +110,11 @@ def _setup(L):
     L.cans_solve_helmholtz_adjoint.argtypes = [_V, C.c_double, _V]
     L.cans_fillps_adjoint.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
     L.cans_correc_adjoint.argtypes = [_I, _D, _V, C.c_double, _V, _V, _V, _V, _V]
-    L.cans_updatep_adjoint.argtypes = [_I, C.c_int, _V, _V, _V]
+    L.cans_updatep_adjoint.argtypes = [_I, _D, _V, _V, C.c_double, C.c_int, _V, _V, _V]
     L.cans_bounduvw_adjoint.argtypes = [C.c_char_p, _I, _D, _I, _D, _D, _D, _V, _V, _V, C.c_int, C.c_int, C.c_int, _V]
     L.cans_boundp_adjoint.argtypes = [C.c_char_p, _I, _D, _I, _D, _D, _V, C.c_int, _V]
-    L.cans_rk_adjoint.argtypes = [_D, _I, _D, _V, _V, C.c_double, C.c_double, _V, _V, _V, _V, _V, _V, _V, _V, _V,
-                                  _V, _D, _V, _V]
+    L.cans_rk_adjoint.argtypes = [_D, _I, _D, _V, _V, C.c_double, C.c_double, C.c_int, _V, _V, _V, _V, _V, _V, _V,
+                                  _V, _V, _V, _D, _V, _V]
     L.cans_rk_adjoint_work_doubles.argtypes = [_I]
     L.cans_rk_adjoint_work_doubles.restype = C.c_size_t
     L.cans_plan_get_shape.argtypes = [_V, C.c_int, _I, _I, _I, _I]
@@ -428,9 +428,13 @@ def correc_adjoint(n, dli, dzci, dt, gu, gv, gw, gp, stream=None):
                                      _ptr(gp), _stream(stream)), "cans_correc_adjoint")
 
 
-def updatep_adjoint(n, is_impdiff, gp, gpp, stream=None):
-    _check(lib().cans_updatep_adjoint(_ints(n), int(is_impdiff), _ptr(gp), _ptr(gpp), _stream(stream)),
-           "cans_updatep_adjoint")
+def updatep_adjoint(n, is_impdiff, gp, gpp, dli=None, dzci=None, dzfi=None, alpha=0., stream=None):
+    """updatep^T: gpp += gp (explicit) or gpp += (I + alpha lap)^T gp (is_impdiff; needs dli,
+    dzci, dzfi and alpha as given to updatep)"""
+    _check(lib().cans_updatep_adjoint(_ints(n), _dbls(dli) if dli is not None else None,
+                                      _ptr(dzci) if dzci is not None else None,
+                                      _ptr(dzfi) if dzfi is not None else None, float(alpha), int(is_impdiff),
+                                      _ptr(gp), _ptr(gpp), _stream(stream)), "cans_updatep_adjoint")
 
 
 def bounduvw_adjoint(cbc, n, bc, is_bound, dl, dzc_h, dzf_h, gu, gv, gw, keep_norm=False, halos_norm=HALO_BOTH,
@@ -454,11 +458,11 @@ def rk_adjoint_work(n, device="cuda"):
 
 
 def rk_adjoint(rkpar, n, dli, dzci, dzfi, dt, visc, u, v, w, gu, gv, gw, gdu, gdv, gdw, gp, work, want_gbf=True,
-               stream=None):
+               stream=None, is_impdiff=0):
     """returns the body-force adjoint increment (3,) when want_gbf"""
     gbf = (C.c_double * 3)()
     _check(lib().cans_rk_adjoint(_dbls(rkpar), _ints(n), _dbls(dli), _ptr(dzci), _ptr(dzfi), float(dt), float(visc),
-                                 _ptr(u), _ptr(v), _ptr(w), _ptr(gu), _ptr(gv), _ptr(gw), _ptr(gdu), _ptr(gdv),
+                                 int(is_impdiff), _ptr(u), _ptr(v), _ptr(w), _ptr(gu), _ptr(gv), _ptr(gw), _ptr(gdu), _ptr(gdv),
                                  _ptr(gdw), _ptr(gp), gbf if want_gbf else None, _ptr(work), _stream(stream)),
            "cans_rk_adjoint")
     return np.array(list(gbf))

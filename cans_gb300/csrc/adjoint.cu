@@ -154,6 +154,7 @@ __constant__ int c_slot_off[27][3] = {
 // cb[s][cell] = sum over components of lambda_R * dR/d(input slot s); also the adjoint of
 // the previous dudtrko (f2 * lambda_unew) in place of lambda_dudtrko_new
 __global__ void __launch_bounds__(kTB) k_mom_vjp(Dims d, double dxi, double dyi, double visc, double f1, double f2,
+                                                  double f12, int impdiff,
                                                   const double *__restrict__ dzci, const double *__restrict__ dzfi,
                                                   const double *__restrict__ u, const double *__restrict__ v,
                                                   const double *__restrict__ w, const double *__restrict__ gu1,
@@ -177,42 +178,48 @@ __global__ void __launch_bounds__(kTB) k_mom_vjp(Dims d, double dxi, double dyi,
                w_mcc = w[c - sx], w_ccc = w[c], w_pcc = w[c + sx], w_cpc = w[c + sy], w_ccp = w[c + sz];
   const double u_mpc = u[c - sx + sy];
   const double lu = gu1[c], lv = gv1[c], lw = gw1[c];
+  // weights of the advection terms (f1 u_new + dudtrko adjoint) and of the diffusion terms:
+  // the same with explicit diffusion; with impdiff the diffusion is not part of dudtrko and
+  // enters u_new with the explicit half of the Crank-Nicolson split, f12 dud - f12/2 dud
+  // (src/rk.f90:155-186)
   const double a = f1 * lu + gdu[t], b = f1 * lv + gdv[t], g = f1 * lw + gdw[t];
+  const double hf = 0.5 * f12;
+  const double ad = impdiff ? hf * lu : a, bd = impdiff ? hf * lv : b, gd = impdiff ? hf * lw : g;
   gdu[t] = f2 * lu; gdv[t] = f2 * lv; gdw[t] = f2 * lw;
   const double q = 0.25;
   const double dx2 = visc * dxi * dxi, dy2 = visc * dyi * dyi;
   double s[27];
   // u slots
-  s[0] = a * (-dxi * q * u_pcc + dxi * q * u_mcc - 2. * dx2 - 2. * dy2 - visc * (dzci_k + dzci_km) * dzfi_k) +
+  s[0] = a * (-dxi * q * u_pcc + dxi * q * u_mcc) + ad * (-2. * dx2 - 2. * dy2 - visc * (dzci_k + dzci_km) * dzfi_k) +
          b * (-dxi * q * v_pcc) + g * (-dxi * q * rdzm * w_pcc);
-  s[1] = a * (-dxi * q * (u_ccc + 2. * u_pcc) + dx2);
-  s[2] = a * (dxi * q * (u_ccc + 2. * u_mcc) + dx2) + b * (dxi * q * v_mcc) + g * (dxi * q * rdzm * w_mcc);
-  s[3] = a * (-dyi * q * (v_ccc + v_pcc) + dy2) + b * (-dxi * q * v_pcc);
-  s[4] = a * (dyi * q * (v_cmc + v_pmc) + dy2);
-  s[5] = a * (-dzfi_k * q * (w_ccc + w_pcc) + visc * dzci_k * dzfi_k) + g * (-dxi * q * rdzp * w_pcc);
-  s[6] = a * (dzfi_k * q * (w_ccm + w_pcm) + visc * dzci_km * dzfi_k);
+  s[1] = a * (-dxi * q * (u_ccc + 2. * u_pcc)) + ad * dx2;
+  s[2] = a * (dxi * q * (u_ccc + 2. * u_mcc)) + ad * dx2 + b * (dxi * q * v_mcc) + g * (dxi * q * rdzm * w_mcc);
+  s[3] = a * (-dyi * q * (v_ccc + v_pcc)) + ad * dy2 + b * (-dxi * q * v_pcc);
+  s[4] = a * (dyi * q * (v_cmc + v_pmc)) + ad * dy2;
+  s[5] = a * (-dzfi_k * q * (w_ccc + w_pcc)) + ad * (visc * dzci_k * dzfi_k) + g * (-dxi * q * rdzp * w_pcc);
+  s[6] = a * (dzfi_k * q * (w_ccm + w_pcm)) + ad * (visc * dzci_km * dzfi_k);
   s[7] = b * (dxi * q * v_mcc);
   s[8] = g * (dxi * q * rdzp * w_mcc);
   // v slots
-  s[9] = b * (-dyi * q * v_cpc + dyi * q * v_cmc - 2. * dx2 - 2. * dy2 - visc * (dzci_k + dzci_km) * dzfi_k) +
+  s[9] = b * (-dyi * q * v_cpc + dyi * q * v_cmc) + bd * (-2. * dx2 - 2. * dy2 - visc * (dzci_k + dzci_km) * dzfi_k) +
          a * (-dyi * q * u_cpc) + g * (-dyi * q * rdzm * w_cpc);
-  s[10] = b * (-dxi * q * (u_ccc + u_cpc) + dx2) + a * (-dyi * q * u_cpc);
-  s[11] = b * (dxi * q * (u_mcc + u_mpc) + dx2);
-  s[12] = b * (-dyi * q * (v_ccc + 2. * v_cpc) + dy2);
-  s[13] = b * (dyi * q * (v_ccc + 2. * v_cmc) + dy2) + a * (dyi * q * u_cmc) + g * (dyi * q * rdzm * w_cmc);
-  s[14] = b * (-dzfi_k * q * (w_ccc + w_cpc) + visc * dzci_k * dzfi_k) + g * (-dyi * q * rdzp * w_cpc);
-  s[15] = b * (dzfi_k * q * (w_ccm + w_cpm) + visc * dzci_km * dzfi_k);
+  s[10] = b * (-dxi * q * (u_ccc + u_cpc)) + bd * dx2 + a * (-dyi * q * u_cpc);
+  s[11] = b * (dxi * q * (u_mcc + u_mpc)) + bd * dx2;
+  s[12] = b * (-dyi * q * (v_ccc + 2. * v_cpc)) + bd * dy2;
+  s[13] = b * (dyi * q * (v_ccc + 2. * v_cmc)) + bd * dy2 + a * (dyi * q * u_cmc) + g * (dyi * q * rdzm * w_cmc);
+  s[14] = b * (-dzfi_k * q * (w_ccc + w_cpc)) + bd * (visc * dzci_k * dzfi_k) + g * (-dyi * q * rdzp * w_cpc);
+  s[15] = b * (dzfi_k * q * (w_ccm + w_cpm)) + bd * (visc * dzci_km * dzfi_k);
   s[16] = a * (dyi * q * u_cmc);
   s[17] = g * (dyi * q * rdzp * w_cmc);
   // w slots
-  s[18] = g * (-dzci_k * q * w_ccp + dzci_k * q * w_ccm - 2. * dx2 - 2. * dy2 - visc * (dzfi_kp + dzfi_k) * dzci_k) +
+  s[18] = g * (-dzci_k * q * w_ccp + dzci_k * q * w_ccm) + gd * (-2. * dx2 - 2. * dy2 - visc * (dzfi_kp + dzfi_k) * dzci_k) +
           a * (-dzfi_k * q * u_ccp) + b * (-dzfi_k * q * v_ccp);
-  s[19] = g * (-dxi * q * (rdzm * u_ccc + rdzp * u_ccp) + dx2) + a * (-dzfi_k * q * u_ccp);
-  s[20] = g * (dxi * q * (rdzm * u_mcc + rdzp * u_mcp) + dx2);
-  s[21] = g * (-dyi * q * (rdzm * v_ccc + rdzp * v_ccp) + dy2) + b * (-dzfi_k * q * v_ccp);
-  s[22] = g * (dyi * q * (rdzm * v_cmc + rdzp * v_cmp) + dy2);
-  s[23] = g * (-dzci_k * q * (w_ccc + 2. * w_ccp) + visc * dzfi_kp * dzci_k);
-  s[24] = g * (dzci_k * q * (w_ccc + 2. * w_ccm) + visc * dzfi_k * dzci_k) + a * (dzfi_k * q * u_ccm) +
+  s[19] = g * (-dxi * q * (rdzm * u_ccc + rdzp * u_ccp)) + gd * dx2 + a * (-dzfi_k * q * u_ccp);
+  s[20] = g * (dxi * q * (rdzm * u_mcc + rdzp * u_mcp)) + gd * dx2;
+  s[21] = g * (-dyi * q * (rdzm * v_ccc + rdzp * v_ccp)) + gd * dy2 + b * (-dzfi_k * q * v_ccp);
+  s[22] = g * (dyi * q * (rdzm * v_cmc + rdzp * v_cmp)) + gd * dy2;
+  s[23] = g * (-dzci_k * q * (w_ccc + 2. * w_ccp)) + gd * (visc * dzfi_kp * dzci_k);
+  s[24] = g * (dzci_k * q * (w_ccc + 2. * w_ccm)) + gd * (visc * dzfi_k * dzci_k) + a * (dzfi_k * q * u_ccm) +
           b * (dzfi_k * q * v_ccm);
   s[25] = a * (dzfi_k * q * u_ccm);
   s[26] = b * (dzfi_k * q * v_ccm);
@@ -301,11 +308,43 @@ extern "C" int cans_correc_adjoint(const int n[3], const double dli[3], const do
   return CANS_OK;
 }
 
-extern "C" int cans_updatep_adjoint(const int n[3], int is_impdiff, const double *gp, double *gpp, void *stream) {
+// transpose of updatep with implicit diffusion, p += pp + alpha lap(pp) on the interior
+// (src/updatep.f90), gathered per haloed cell x of gpp: gpp(x) += gp(x) + alpha * the sum over
+// the interior cells c whose 7-point Laplacian reads x of the coefficient of x times gp(c)
+__global__ void __launch_bounds__(kTB) k_updatep_impl_adj(Dims d, double dxi, double dyi, double alpha,
+                                                          const double *__restrict__ dzci,
+                                                          const double *__restrict__ dzfi,
+                                                          const double *__restrict__ gp, double *__restrict__ gpp) {
+  int i, j, k;
+  if (!haloed3((long)blockIdx.x * blockDim.x + threadIdx.x, d, i, j, k)) return;
+  const int n1 = d.n1, n2 = d.n2;
+  const double cx = dxi * dxi, cy = dyi * dyi;
+  double acc = 0.;
+  auto G = [&](int a, int b, int c) { return gp[hidx(a, b, c, n1, n2)]; };
+  if (inside(d, i, j, k)) {
+    const double diag = -2. * cx - 2. * cy - (dzci[k] + dzci[k - 1]) * dzfi[k];
+    acc += G(i, j, k) * (1. + alpha * diag);
+  }
+  if (inside(d, i - 1, j, k)) acc += alpha * cx * G(i - 1, j, k);
+  if (inside(d, i + 1, j, k)) acc += alpha * cx * G(i + 1, j, k);
+  if (inside(d, i, j - 1, k)) acc += alpha * cy * G(i, j - 1, k);
+  if (inside(d, i, j + 1, k)) acc += alpha * cy * G(i, j + 1, k);
+  if (inside(d, i, j, k - 1)) acc += alpha * dzci[k - 1] * dzfi[k - 1] * G(i, j, k - 1);  // its +z neighbour
+  if (inside(d, i, j, k + 1)) acc += alpha * dzci[k] * dzfi[k + 1] * G(i, j, k + 1);      // its -z neighbour
+  gpp[hidx(i, j, k, n1, n2)] += acc;
+}
+
+extern "C" int cans_updatep_adjoint(const int n[3], const double dli[3], const double *dzci, const double *dzfi,
+                                    double alpha, int is_impdiff, const double *gp, double *gpp, void *stream) {
   if (!n || !gp || !gpp || n[0] < 1 || n[1] < 1 || n[2] < 1) return CANS_EINVAL;
-  if (is_impdiff) return CANS_ENOTSUP;
   Dims d{n[0], n[1], n[2]};
-  k_updatep_adj<<<nblk((long)n[0] * n[1] * n[2]), kTB, 0, as_stream(stream)>>>(d, gp, gpp);
+  if (is_impdiff) {
+    if (!dli || !dzci || !dzfi) return CANS_EINVAL;
+    const long cnt = (long)(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+    k_updatep_impl_adj<<<nblk(cnt), kTB, 0, as_stream(stream)>>>(d, dli[0], dli[1], alpha, dzci, dzfi, gp, gpp);
+  } else {
+    k_updatep_adj<<<nblk((long)n[0] * n[1] * n[2]), kTB, 0, as_stream(stream)>>>(d, gp, gpp);
+  }
   CANS_LAUNCH_CHECK();
   return CANS_OK;
 }
@@ -336,14 +375,15 @@ extern "C" size_t cans_rk_adjoint_work_doubles(const int n[3]) {
   return (size_t)27 * np + 3 * (size_t)nblk(nh) + 8;
 }
 
-// adjoint of cans_rk with explicit diffusion and no flow-rate forcing.  In: the forward
+// adjoint of cans_rk (explicit or implicit diffusion; no flow-rate forcing).  In: the forward
 // substep's input velocity u, v, w (haloed, as rk read it), the adjoints gu, gv, gw of the
 // velocity after rk (haloed; the ghosts rk left untouched) and gdu, gdv, gdw of the
 // dudtrko it wrote.  Out, in place: gu, gv, gw become the adjoints of the input velocity,
 // gdu, gdv, gdw those of the input dudtrko; gp (haloed) accumulates the pressure's and
 // gbf[3] (host) the uniform body force's.  work: cans_rk_adjoint_work_doubles(n) doubles.
 extern "C" int cans_rk_adjoint(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
-                               const double *dzfi, double dt, double visc, const double *u, const double *v,
+                               const double *dzfi, double dt, double visc, int is_impdiff, const double *u,
+                               const double *v,
                                const double *w, double *gu, double *gv, double *gw, double *gdu, double *gdv,
                                double *gdw, double *gp, double gbf[3], double *work, void *stream) {
   if (!rkpar || !n || !dli || !dzci || !dzfi || !u || !v || !w || !gu || !gv || !gw || !gdu || !gdv || !gdw || !gp ||
@@ -359,8 +399,8 @@ extern "C" int cans_rk_adjoint(const double rkpar[2], const int n[3], const doub
   const unsigned gh = nblk(nh);
   k_rk_pgrad_adj<<<gh, kTB, 0, st>>>(d, dli[0], dli[1], f12, dzci, gu, gv, gw, gp, partials);
   CANS_LAUNCH_CHECK();
-  k_mom_vjp<<<nblk(np), kTB, 0, st>>>(d, dli[0], dli[1], visc, f1, f2, dzci, dzfi, u, v, w, gu, gv, gw, gdu, gdv,
-                                       gdw, cb);
+  k_mom_vjp<<<nblk(np), kTB, 0, st>>>(d, dli[0], dli[1], visc, f1, f2, f12, is_impdiff ? 1 : 0, dzci, dzfi, u, v, w,
+                                       gu, gv, gw, gdu, gdv, gdw, cb);
   CANS_LAUNCH_CHECK();
   k_mom_gather<<<gh, kTB, 0, st>>>(d, cb, gu, gv, gw);
   CANS_LAUNCH_CHECK();

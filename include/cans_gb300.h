@@ -309,9 +309,11 @@ int cans_fillps_adjoint(const int n[3], const double dli[3], const double *dzfi,
 int cans_correc_adjoint(const int n[3], const double dli[3], const double *dzci, double dt,
                         const double *gu, const double *gv, const double *gw, double *gp,
                         void *stream);
-/* updatep^T (explicit: p += pp): gpp += gp on the interior; is_impdiff != 0: CANS_ENOTSUP */
-int cans_updatep_adjoint(const int n[3], int is_impdiff, const double *gp, double *gpp,
-                         void *stream);
+/* updatep^T (same arguments as cans_updatep): explicit (p += pp): gpp += gp on the interior;
+ * is_impdiff (p += pp + alpha lap(pp), src/updatep.f90): gpp += (I + alpha lap)^T gp, which
+ * also reaches the ghost cells of gpp that lap read (folded back by cans_boundp_adjoint) */
+int cans_updatep_adjoint(const int n[3], const double dli[3], const double *dzci, const double *dzfi,
+                         double alpha, int is_impdiff, const double *gp, double *gpp, void *stream);
 /* transposes of bounduvw / boundp (same arguments): ghost adjoints go back to the
  * interior cells the ghosts were filled from, in reverse order, and are zeroed */
 int cans_bounduvw_adjoint(const char cbc[18], const int n[3], const double bc[18],
@@ -328,9 +330,9 @@ int cans_boundp_adjoint(const char cbc[6], const int n[3], const double bc[6],
  * may be NULL) += the uniform body force's (synchronises the stream).  work: device
  * scratch of cans_rk_adjoint_work_doubles(n) doubles. */
 int cans_rk_adjoint(const double rkpar[2], const int n[3], const double dli[3], const double *dzci,
-                    const double *dzfi, double dt, double visc, const double *u, const double *v,
-                    const double *w, double *gu, double *gv, double *gw, double *gdu, double *gdv,
-                    double *gdw, double *gp, double gbf[3], double *work, void *stream);
+                    const double *dzfi, double dt, double visc, int is_impdiff, const double *u,
+                    const double *v, const double *w, double *gu, double *gv, double *gw, double *gdu,
+                    double *gdv, double *gdw, double *gp, double gbf[3], double *work, void *stream);
 size_t cans_rk_adjoint_work_doubles(const int n[3]);
 
 /* ---------------------------------------------------------------- batched solves
