@@ -143,6 +143,44 @@ __device__ __forceinline__ void fft_stage(const T2 *__restrict__ src, T2 *__rest
   }
 }
 
+// one Stockham stage of a prime radix R > 8 known only at run time (lengths with prime factors
+// 11 .. kMaxPrimeRadix): the R-point DFT directly (R^2 complex products), its roots read from
+// the m-point twiddle table (R divides m)
+constexpr int kMaxPrimeRadix = 61;
+template <int SIGN, typename T2>
+__device__ __forceinline__ void fft_stage_prime(const T2 *__restrict__ src, T2 *__restrict__ dst, int m, int nlines,
+                                                int ld, int Ns, const T2 *__restrict__ tw, int R) {
+  const int nb = m / R, total = nb * nlines, tws = m / (Ns * R), rs = m / R;
+  for (int b = threadIdx.x; b < total; b += blockDim.x) {
+    const int line = b / nb, jb = b - line * nb;
+    const T2 *s = src + line * ld;
+    T2 *d = dst + line * ld;
+    const int k = jb % Ns;
+    T2 v[kMaxPrimeRadix];
+    for (int r = 0; r < R; ++r) {
+      v[r] = s[jb + r * nb];
+      if (r > 0 && Ns > 1) {
+        T2 w = tw[r * k * tws];
+        if (SIGN > 0) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    const int idxD = (jb / Ns) * Ns * R + k;
+    for (int q = 0; q < R; ++q) {
+      T2 acc = v[0];
+      int e = 0;  // (r q) mod R
+      for (int r = 1; r < R; ++r) {
+        e += q;
+        if (e >= R) e -= R;
+        T2 w = tw[e * rs];
+        if (SIGN > 0) w.y = -w.y;
+        acc = cadd(acc, cmul(v[r], w));
+      }
+      d[idxD + q * Ns] = acc;
+    }
+  }
+}
+
 // batched complex FFT of the CTA's lines; data starts in A; returns the buffer holding the result
 template <int SIGN, typename T2>
 __device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P, const T2 *__restrict__ tw) {
@@ -156,7 +194,8 @@ __device__ T2 *fft_lines(T2 *A, T2 *B, const DirParams &P, const T2 *__restrict_
       case 4: fft_stage<4, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
       case 5: fft_stage<5, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
       case 7: fft_stage<7, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
-      default: fft_stage<8, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
+      case 8: fft_stage<8, SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw); break;
+      default: fft_stage_prime<SIGN>(src, dst, P.m, P.ncx, P.ld, Ns, tw, R); break;
     }
     __syncthreads();
     Ns *= R;

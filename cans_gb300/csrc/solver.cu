@@ -147,7 +147,13 @@ bool factor_radices(int m, int *radix, int *ns) {
   while (m % 8 == 0 && m != 16) { radix[(*ns)++] = 8; m /= 8; }
   while (m % 4 == 0) { radix[(*ns)++] = 4; m /= 4; }
   while (m % 2 == 0) { radix[(*ns)++] = 2; m /= 2; }
-  for (int r : {3, 5, 7}) while (m % r == 0) { radix[(*ns)++] = r; m /= r; }
+  for (int r : {3, 5, 7}) while (m % r == 0 && *ns < 12) { radix[(*ns)++] = r; m /= r; }
+  // prime factors 11 .. kMaxPrimeRadix: a direct DFT stage (fft_stage_prime)
+  for (int r = 11; r <= kMaxPrimeRadix && m > 1; r += 2) {
+    bool prime = true;
+    for (int q = 3; q * q <= r; q += 2) prime = prime && r % q != 0;
+    while (prime && m % r == 0 && *ns < 12) { radix[(*ns)++] = r; m /= r; }
+  }
   return m == 1 && *ns <= 12;
 }
 

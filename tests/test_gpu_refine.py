@@ -24,6 +24,7 @@ CASES = [
     ((8, 8, 129), (4.0, 2.0, 2.0), "PPPPNN", 1.3),
     ((16, 16, 384), (4.0, 2.0, 2.0), "PPNNDD", 1.2),
     ((24, 20, 512), (12.566, 6.283, 2.0), "PPPPNN", 1.4),
+    ((22, 26, 16), (1.0, 1.0, 1.0), "PPNNNN", 1.2),           # prime factors 11, 13 (direct-DFT stages)
 ]
 
 

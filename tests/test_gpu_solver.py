@@ -37,6 +37,13 @@ CASES = [
     ((10, 256, 6), (1.0, 1.0, 1.0), "DDNNNN", "ccc", 1.2),
     ((1024, 4, 5), (2.0, 1.0, 1.0), "NNPPNN", "ccc", 1.2),
     ((4, 1024, 5), (1.0, 2.0, 1.0), "PPDDNN", "ccc", 1.2),
+    # prime factors above 7 (direct-DFT stages): 11, 13, 2*17, 3*23, 61 (the largest), in every
+    # kind family
+    ((22, 13, 9), (1.0, 1.0, 1.0), "PPPPNN", "ccc", 1.2),
+    ((34, 11, 8), (1.0, 1.0, 1.0), "NNDDNN", "ccc", 1.2),
+    ((69, 26, 7), (2.0, 1.0, 1.0), "DDNNNN", "ccc", 1.1),
+    ((61, 11, 6), (1.0, 1.0, 1.0), "PPNNPP", "ccc", 0.0),
+    ((12, 13, 9), (1.0, 1.0, 1.0), "DDDDDD", "fcc", 1.2),      # face-centred: m = 2 (n - 1) = 22
 ]
 
 
@@ -149,5 +156,5 @@ def test_invalid_arguments_raise(require_gpu):
         cans.Plan(n, [8, 8, 8], dzci, dzfi, "PXPPNN", [0.] * 6, "ccc")
     assert e.value.status == cans.EINVAL
     with pytest.raises(cans.CansError) as e:
-        cans.Plan((11, 8, 8), [8, 8, 8], dzci, dzfi, "PPPPNN", [0.] * 6, "ccc")  # length 11: prime radix
+        cans.Plan((67, 8, 8), [8, 8, 8], dzci, dzfi, "PPPPNN", [0.] * 6, "ccc")  # length 67: prime above 61
     assert e.value.status == cans.ENOTSUP
