@@ -33,7 +33,7 @@ extern "C" {
 #define CANS_EINVAL 1      /* bad argument (sizes, BC characters, NULL pointers) */
 #define CANS_ENOMEM 2      /* device allocation failed */
 #define CANS_ECUDA 3       /* a CUDA call or kernel launch failed */
-#define CANS_ENOTSUP 4     /* transform length or BC combination not supported */
+#define CANS_ENOTSUP 4     /* transform length (a prime factor above 61) or BC combination not supported */
 #define CANS_ETIMEOUT 5    /* a bounded device wait expired */
 #define CANS_ENONFINITE 6  /* non-finite value detected in a checked result */
 #define CANS_EIO 7         /* a checkpoint file could not be opened, read or written */
