@@ -261,14 +261,28 @@ __global__ void __launch_bounds__(kTB, 3) k_mom_rk32(Dims d, float dxi, float dy
       m.u_ccp = u[c]; m.u_mcp = u[c - 1]; m.v_ccp = v[c]; m.v_cmp = v[c - sy]; m.w_ccp = w[c]; m.p_ccp = p[c];
     }
     size_t h = (size_t)(i - 1) + (size_t)d.n1 * (size_t)(j - 1) + nxy * (size_t)(k0 - 1);
+    // plane k+1's six values and the RK tendencies of plane k are loaded one iteration ahead
+    // (the plane after the last one of the march is a halo plane: always in bounds)
+    float q_u, q_um, q_v, q_vm, q_w, q_p, r_u, r_v, r_w;
+    {
+      const size_t cp = (size_t)(k0 + 1) * sz + o;
+      q_u = u[cp]; q_um = u[cp - 1]; q_v = v[cp]; q_vm = v[cp - sy]; q_w = w[cp]; q_p = p[cp];
+      r_u = dudtrko[h]; r_v = dvdtrko[h]; r_w = dwdtrko[h];
+    }
     for (int k = k0; k <= k1; k++, h += nxy) {
       const size_t c = (size_t)k * sz + o, cp = c + sz;
       // roll the window: plane k becomes the centre, plane k-1 the lower neighbour
       m.u_ccm = m.u_ccc; m.v_ccm = m.v_ccc; m.w_ccm = m.w_ccc; m.w_pcm = m.w_pcc; m.w_cpm = m.w_cpc;
       m.u_ccc = m.u_ccp; m.u_mcc = m.u_mcp; m.v_ccc = m.v_ccp; m.v_cmc = m.v_cmp; m.w_ccc = m.w_ccp;
       m.p_ccc = m.p_ccp;
-      // plane k+1
-      m.u_ccp = u[cp]; m.u_mcp = u[cp - 1]; m.v_ccp = v[cp]; m.v_cmp = v[cp - sy]; m.w_ccp = w[cp]; m.p_ccp = p[cp];
+      // plane k+1 (loaded last iteration) and the loads of plane k+2 / the next tendencies
+      m.u_ccp = q_u; m.u_mcp = q_um; m.v_ccp = q_v; m.v_cmp = q_vm; m.w_ccp = q_w; m.p_ccp = q_p;
+      const float o_u = r_u, o_v = r_v, o_w = r_w;
+      if (k < k1) {
+        const size_t cq = cp + sz;
+        q_u = u[cq]; q_um = u[cq - 1]; q_v = v[cq]; q_vm = v[cq - sy]; q_w = w[cq]; q_p = p[cq];
+        r_u = dudtrko[h + nxy]; r_v = dvdtrko[h + nxy]; r_w = dwdtrko[h + nxy];
+      }
       // in-plane neighbours at plane k
       m.u_pcc = u[c + 1]; m.u_cmc = u[c - sy]; m.u_cpc = u[c + sy]; m.u_mpc = u[c - 1 + sy];
       m.v_mcc = v[c - 1]; m.v_pcc = v[c + 1]; m.v_cpc = v[c + sy]; m.v_pmc = v[c + 1 - sy];
@@ -276,8 +290,8 @@ __global__ void __launch_bounds__(kTB, 3) k_mom_rk32(Dims d, float dxi, float dy
       m.p_pcc = p[c + 1]; m.p_cpc = p[c + sy];
       m.dzci_k = dzci[k]; m.dzci_km = dzci[k - 1]; m.dzfi_k = dzfi[k]; m.dzfi_kp = dzfi[k + 1];
       float dudt, dvdt, dwdt, nu, nv, nw, dud, dvd, dwd;
-      mom_rk_point<float>(m, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, 0, dudtrko[h], dvdtrko[h], dwdtrko[h],
-                          dudt, dvdt, dwdt, nu, nv, nw, dud, dvd, dwd);
+      mom_rk_point<float>(m, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, 0, o_u, o_v, o_w, dudt, dvdt, dwdt, nu,
+                          nv, nw, dud, dvd, dwd);
       dudtrko[h] = dudt; dvdtrko[h] = dvdt; dwdtrko[h] = dwdt;
       un[c] = nu; vn[c] = nv; wn[c] = nw;
       if (partials) {
