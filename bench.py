@@ -240,7 +240,7 @@ def bench_ours(args, rank, world):
             "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
             "peak_source": kind, "traffic": traffic_for("residual", workload + "_fp32"),
             "algorithmic_bytes_per_launch": int(res_bytes), "kernel_ms": ref["residual_ms"],
-            "next_kernel": {"kernel": "k_ylines_p<float,512> (FP32 y transform, in place)",
+            "next_kernel": {"kernel": "k_ylines_pt<512> (FP32 y transform, TMA-fed, in place)",
                             "achieved": round(8 * ncell / (y_ms * 1e-3) / 1e9, 1), "kernel_ms": round(y_ms, 4),
                             "algorithmic_bytes_per_launch": 8 * ncell,
                             "traffic": traffic_for("solve_y_fp32", workload + "_fp32")},
