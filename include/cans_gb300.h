@@ -58,7 +58,9 @@ int cans_initgrid(int gtype, int n, double gr, double lz, int is_periodic, doubl
  * values and the transform plans on the device.  Optional HOST outputs (NULL
  * to skip) return what the reference returns:
  *   lambdaxy[ng1*ng2] (Fortran order), a,b,c[ng3], *normfft,
- *   rhsb[6] = the constant face values of rhsb{x,y,z}(:,:,0:1), rhsb[ibound+2*idir]. */
+ *   rhsb[6] = the constant face values of rhsb{x,y,z}(:,:,0:1), rhsb[ibound+2*idir].
+ * ng[0], ng[1]: any length whose prime factors are at most 61 (the reference takes any
+ * length through FFTW/cuFFT); a larger prime factor returns CANS_ENOTSUP. */
 int cans_initsolver(const int ng[3], const double dli[3], const double *dzci_g, const double *dzfi_g,
                     const char cbc[6], const double bc[6], const char c_or_f[3], int precision,
                     void *stream, cans_plan **plan,
