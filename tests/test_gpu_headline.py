@@ -92,7 +92,7 @@ def test_channel_poisson_at_benchmark_size(require_gpu, n):
     # Thomas recursion on the ill-conditioned columns, so they agree far below their error
     # (measured on GB300: 2.9e-14 at 512^3, 9.5e-16 at 1024x512x384)
     assert r["fp64_vs_oracle"] <= 1e-12, r
-    # the benchmark spec's bound against an accurate solution of the same discrete operator
+    # the refined path's 1e-12 bound against an accurate solution of the same discrete operator
     assert r["refined_vs_ref"] <= 1e-12, r
     # the FP64 path is as accurate as the oracle's (the reference's) own FP64 solve
     assert r["fp64_vs_ref"] <= max(2.0 * r["oracle_vs_ref"], 1e-12), r

@@ -74,7 +74,7 @@ def test_refined_reaches_fp64_accuracy(require_gpu, n, l, cbc, gr):
     got = cans.fview(d)[1:-1, 1:-1, 1:-1]
     w = want[1:-1, 1:-1, 1:-1]
     err = gauge_rel_l2(got, w, dzf) if singular(cbc) else rel_l2(got, w)
-    # against the extended-precision reference: the benchmark spec's flat 1e-12
+    # against the extended-precision reference: the flat 1e-12 target of the refined path
     assert err <= 1e-12, (err, it, rr)
     assert it <= 4 and rr <= 1e-14, (it, rr)
     # ghost cells untouched
