@@ -179,7 +179,11 @@ def test_two_corrections_at_least_as_accurate_as_fp64_path(require_gpu):
 Z_CASES = [CASES[0], CASES[2], CASES[3], CASES[4], CASES[9], CASES[10], CASES[12],
            # many tiles per CTA of the tiled z pass (its buffers cycle through several phases)
            ((256, 128, 16), (4.0, 2.0, 2.0), "PPPPNN", 1.2),
-           ((128, 128, 24), (6.2831853, 6.2831853, 6.2831853), "PPPPPP", 0.0)]
+           ((128, 128, 24), (6.2831853, 6.2831853, 6.2831853), "PPPPPP", 0.0),
+           # the shapes of the reference's two-dimensional examples: ny = 2 (differentially
+           # heated cavity) and nz = 4 (2-D Taylor-Green vortex: two-row z tiles)
+           ((128, 2, 128), (1.0, 0.015625, 1.0), "NNPPNN", 0.0),
+           ((32, 32, 4), (6.2831853, 6.2831853, 0.125), "PPPPPP", 0.0)]
 
 
 def _zmodes(plan):

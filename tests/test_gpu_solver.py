@@ -25,6 +25,9 @@ CASES = [
     ((12, 10, 9), (1.0, 1.0, 1.0), "DDDDDD", "ccf", 1.2),      # face-centred Dirichlet top in z
     ((9, 10, 8), (1.0, 1.0, 1.0), "NNNNDD", "fcc", 0.0),       # face-centred NN (REDFT00)
     ((64, 48, 32), (4.0, 2.0, 2.0), "PPPPNN", "ccc", 1.4),
+    # the shapes of the reference's two-dimensional examples (ny = 2, nz = 4)
+    ((128, 2, 128), (1.0, 0.015625, 1.0), "NNPPNN", "ccc", 0.0),
+    ((32, 32, 4), (6.2831853, 6.2831853, 0.125), "PPPPPP", "ccc", 0.0),
     # 512-point lines: the register-FFT tiles and the persistent pass kernels, every kind
     ((512, 8, 6), (2.0, 1.0, 1.0), "PPNNNN", "ccc", 1.2),      # x R2HC / HC2R
     ((512, 6, 6), (2.0, 1.0, 1.0), "NNDDNN", "ccc", 1.2),      # x REDFT10 / REDFT01
