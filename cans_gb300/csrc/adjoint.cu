@@ -161,6 +161,9 @@ __global__ void __launch_bounds__(kTB) k_mom_vjp(Dims d, double dxi, double dyi,
                                                   const double *__restrict__ gv1, const double *__restrict__ gw1,
                                                   double *__restrict__ gdu, double *__restrict__ gdv,
                                                   double *__restrict__ gdw, double *__restrict__ cb) {
+  __shared__ double rdz[2 * 8];
+  int k0;
+  const bool table = mom_rdz_table<8>(d, dzci, dzfi, rdz, k0);
   int i, j, k;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (!cell3(t, d, i, j, k)) return;
@@ -169,7 +172,8 @@ __global__ void __launch_bounds__(kTB) k_mom_vjp(Dims d, double dxi, double dyi,
   const size_t sx = 1, sy = (size_t)(n1 + 2), sz = (size_t)(n1 + 2) * (n2 + 2);
   const size_t c = hidx(i, j, k, n1, n2);
   const double dzci_k = dzci[k], dzci_km = dzci[k - 1], dzfi_k = dzfi[k], dzfi_kp = dzfi[k + 1];
-  const double rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
+  const double rdzm = table ? rdz[2 * (k - k0)] : mom_rdz(dzci, dzfi, k, 0);
+  const double rdzp = table ? rdz[2 * (k - k0) + 1] : mom_rdz(dzci, dzfi, k, 1);
   const double u_ccm = u[c - sz], u_cmc = u[c - sy], u_mcc = u[c - sx], u_ccc = u[c], u_pcc = u[c + sx],
                u_cpc = u[c + sy], u_mcp = u[c - sx + sz], u_ccp = u[c + sz];
   const double v_ccm = v[c - sz], v_cmc = v[c - sy], v_pmc = v[c + sx - sy], v_mcc = v[c - sx], v_ccc = v[c],

@@ -77,7 +77,35 @@ template <typename T> struct MomIn {
   T w_ccm, w_pcm, w_cpm, w_cmc, w_mcc, w_ccc, w_pcc, w_cpc, w_ccp;
   T p_ccc, p_pcc, p_cpc, p_ccp;
   T dzci_k, dzci_km, dzfi_k, dzfi_kp;
+  T rdzm, rdzp;  // dzci_k / dzfi_k and dzci_k / dzfi_kp (per plane: see mom_rdz)
 };
+
+// the two per-plane ratios of mom_xyz_ad's z interpolation (src/mom.f90, the w-momentum
+// advection), the same IEEE division wherever it is evaluated
+template <typename T> __device__ __forceinline__ T mom_rdz(const T *__restrict__ dzci, const T *__restrict__ dzfi,
+                                                           int k, int which) {
+  return dzci[k] / dzfi[k + which];
+}
+
+// the plane ratios of the planes that a CTA of flat interior cells [blockIdx.x * blockDim.x,
+// + blockDim.x) lies in, rdz[2 (k - k0) + 0/1]: one division per plane and ratio instead of
+// two per cell (GB300 divides FP64 on its 1/58-rate unit).  False when the CTA spans more
+// than P planes (grids with n1 n2 < blockDim / (P - 1)): the caller divides per cell.  Every
+// thread of the CTA calls it (it synchronises the CTA).
+template <int P, typename T>
+__device__ __forceinline__ bool mom_rdz_table(const Dims &d, const T *__restrict__ dzci, const T *__restrict__ dzfi,
+                                              T (&rdz)[2 * P], int &k0) {
+  const long np = (long)d.n1 * d.n2 * d.n3, nxy = (long)d.n1 * d.n2;
+  const long t0 = (long)blockIdx.x * blockDim.x;
+  const long tl = (t0 + (long)blockDim.x < np ? t0 + (long)blockDim.x : np) - 1;
+  k0 = (int)(t0 / nxy) + 1;
+  const int nk = t0 < np ? (int)(tl / nxy) + 2 - k0 : 0;
+  const bool ok = nk >= 1 && nk <= P;
+  if (ok && (int)threadIdx.x < 2 * nk)
+    rdz[threadIdx.x] = mom_rdz(dzci, dzfi, k0 + (int)(threadIdx.x >> 1), (int)(threadIdx.x & 1));
+  __syncthreads();
+  return ok;
+}
 
 // mom_xyz_ad (src/mom.f90:771-1019) and the RK update of src/rk.f90:155-186 on the values of
 // one cell, in the field precision T (double; float for the FP32 run, the reference's
@@ -90,7 +118,7 @@ __device__ __forceinline__ void mom_rk_point(const MomIn<T> &m, T dxi, T dyi, T 
                                              T &dwdt, T &un, T &vn, T &wn, T &dud, T &dvd, T &dwd) {
   const T q = T(0.25);
   const T dzci_k = m.dzci_k, dzci_km = m.dzci_km, dzfi_k = m.dzfi_k, dzfi_kp = m.dzfi_kp;
-  const T rdzm = dzci_k / dzfi_k, rdzp = dzci_k / dzfi_kp;
+  const T rdzm = m.rdzm, rdzp = m.rdzp;
   // x
   const T dudxp = (m.u_pcc - m.u_ccc) * dxi, dudxm = (m.u_ccc - m.u_mcc) * dxi;
   const T dudyp = (m.u_cpc - m.u_ccc) * dyi, dudym = (m.u_ccc - m.u_cmc) * dyi;
@@ -139,7 +167,8 @@ __device__ __forceinline__ void mom_rk_point(const MomIn<T> &m, T dxi, T dyi, T 
 // mom_xyz_ad fused with the RK update (mom_rk_point) at interior cell t, loading the values
 // from the haloed fields.  The new velocity goes to un/vn/wn: halo-free index (HALO_OUT
 // false: the FP64 kernels' scratch) or haloed index (HALO_OUT true); dudtrko in place, dudtd
-// to dtd (impdiff, halo-free, 3 fields).  Returns false past the end.
+// to dtd (impdiff, halo-free, 3 fields).  rdz: the plane ratios of mom_rdz precomputed for
+// planes rdz_k0.. (else divided here).  Returns false past the end.
 template <typename T, bool HALO_OUT = false>
 __device__ __forceinline__ bool mom_rk_cell(const Dims &d, T dxi, T dyi, T visc, T f1, T f2, T f12, T bfx, T bfy,
                                             T bfz, int impdiff, const T *__restrict__ dzci,
@@ -149,7 +178,8 @@ __device__ __forceinline__ bool mom_rk_cell(const Dims &d, T dxi, T dyi, T visc,
                                             T *__restrict__ dvdtrko, T *__restrict__ dwdtrko, T *__restrict__ un_out,
                                             T *__restrict__ vn_out, T *__restrict__ wn_out, T *__restrict__ dtd,
                                             long t, const T *__restrict__ sb = nullptr, T gbx = T(0),
-                                            T gby = T(0), T gbz = T(0), T beta = T(0)) {
+                                            T gby = T(0), T gbz = T(0), T beta = T(0),
+                                            const T *rdz = nullptr, int rdz_k0 = 0) {
   int i, j, k;
   if (!cell3(t, d, i, j, k)) return false;
   const int n1 = d.n1, n2 = d.n2;
@@ -158,6 +188,11 @@ __device__ __forceinline__ bool mom_rk_cell(const Dims &d, T dxi, T dyi, T visc,
   const size_t c = hidx(i, j, k, n1, n2);
   MomIn<T> m;
   m.dzci_k = dzci[k]; m.dzci_km = dzci[k - 1]; m.dzfi_k = dzfi[k]; m.dzfi_kp = dzfi[k + 1];
+  if (rdz) {  // the CTA's table of planes rdz_k0.. (mom_rdz), rdz[2 (k - rdz_k0) + 0/1]
+    m.rdzm = rdz[2 * (k - rdz_k0)]; m.rdzp = rdz[2 * (k - rdz_k0) + 1];
+  } else {
+    m.rdzm = mom_rdz(dzci, dzfi, k, 0); m.rdzp = mom_rdz(dzci, dzfi, k, 1);
+  }
   m.u_ccm = u[c - sz]; m.u_cmc = u[c - sy]; m.u_mcc = u[c - sx]; m.u_ccc = u[c]; m.u_pcc = u[c + sx];
   m.u_mpc = u[c - sx + sy]; m.u_cpc = u[c + sy]; m.u_mcp = u[c - sx + sz]; m.u_ccp = u[c + sz];
   m.v_ccm = v[c - sz]; m.v_cmc = v[c - sy]; m.v_pmc = v[c + sx - sy]; m.v_mcc = v[c - sx]; m.v_ccc = v[c];
