@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kTB) k_mom_vjp(Dims d, double dxi, double dyi,
                                                   double *__restrict__ gdw, double *__restrict__ cb) {
   __shared__ double rdz[2 * 8];
   int k0;
-  const bool table = mom_rdz_table<8>(d, dzci, dzfi, rdz, k0);
+  const bool table = mom_rdz_table<8>(d, dzci, dzfi, rdz, k0, (long)blockIdx.x * blockDim.x);
   int i, j, k;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (!cell3(t, d, i, j, k)) return;

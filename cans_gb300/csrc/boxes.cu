@@ -62,15 +62,19 @@ enum CellOp { OP_MOM = 0, OP_WRITEBACK = 1, OP_FILLPS = 2, OP_CORREC = 3, OP_UPD
 template <int OP>
 __global__ void __launch_bounds__(kTB) k_boxes_cells(const BoxK *__restrict__ box, const long *__restrict__ start,
                                                       int nbox, long total, int irk) {
+  __shared__ double rdz[2 * 8];  // OP_MOM: the block's plane ratios (mom_rdz_table)
   for (long blk = blockIdx.x; blk < total; blk += gridDim.x) {
     const int s = find_item(start, nbox, blk);
     const BoxK &b = box[s];
-    const long t = (blk - __ldg(&start[s])) * kTB + threadIdx.x;
+    const long t0 = (blk - __ldg(&start[s])) * kTB, t = t0 + threadIdx.x;
     if (OP == OP_MOM) {
       const size_t np = (size_t)b.d.n1 * b.d.n2 * b.d.n3;
+      int k0;
+      const bool table = mom_rdz_table<8>(b.d, b.dzci, b.dzfi, rdz, k0, t0);
       mom_rk_cell<double>(b.d, b.dxi, b.dyi, b.visc, b.f1[irk], b.f2[irk], b.f12[irk], b.bf[0], b.bf[1], b.bf[2],
                           b.impdiff, b.dzci, b.dzfi, b.u, b.v, b.w, b.p, b.dudtrko, b.dvdtrko, b.dwdtrko, b.unew,
-                          b.unew + np, b.unew + 2 * np, b.dtd, t);
+                          b.unew + np, b.unew + 2 * np, b.dtd, t, nullptr, 0., 0., 0., 0., table ? rdz : nullptr, k0);
+      __syncthreads();  // the next block's table overwrites rdz
     } else if (OP == OP_WRITEBACK) {
       // rk.f90 write-back, then (implicit diffusion) u = (u - f12/2 dudtd) + f with f = 0
       // (no forcing): the expressions of k_rk_writeback and k_rk_forcing, fused

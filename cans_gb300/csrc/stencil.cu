@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kTB) k_mom_rk(Dims d, double dxi, double dyi, 
   const size_t np = (size_t)d.n1 * d.n2 * d.n3;
   __shared__ double rdz[2 * 8];
   int k0;
-  const bool table = mom_rdz_table<8>(d, dzci, dzfi, rdz, k0);
+  const bool table = mom_rdz_table<8>(d, dzci, dzfi, rdz, k0, (long)blockIdx.x * blockDim.x);
   mom_rk_cell<double>(d, dxi, dyi, visc, f1, f2, f12, bfx, bfy, bfz, impdiff, dzci, dzfi, u, v, w, p, dudtrko,
                       dvdtrko, dwdtrko, unew, unew + np, unew + 2 * np, dtd,
                       (long)blockIdx.x * blockDim.x + threadIdx.x, sb, gbx, gby, gbz, beta, table ? rdz : nullptr,

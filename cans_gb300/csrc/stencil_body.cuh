@@ -87,16 +87,15 @@ template <typename T> __device__ __forceinline__ T mom_rdz(const T *__restrict__
   return dzci[k] / dzfi[k + which];
 }
 
-// the plane ratios of the planes that a CTA of flat interior cells [blockIdx.x * blockDim.x,
-// + blockDim.x) lies in, rdz[2 (k - k0) + 0/1]: one division per plane and ratio instead of
-// two per cell (GB300 divides FP64 on its 1/58-rate unit).  False when the CTA spans more
-// than P planes (grids with n1 n2 < blockDim / (P - 1)): the caller divides per cell.  Every
-// thread of the CTA calls it (it synchronises the CTA).
+// the plane ratios of the planes that a CTA's flat interior cells [t0, t0 + blockDim.x) lie
+// in, rdz[2 (k - k0) + 0/1]: one division per plane and ratio instead of two per cell (GB300
+// divides FP64 on its 1/58-rate unit).  False when the CTA spans more than P planes (grids
+// with n1 n2 < blockDim / (P - 1)): the caller divides per cell.  Every thread of the CTA
+// calls it (it synchronises the CTA).
 template <int P, typename T>
 __device__ __forceinline__ bool mom_rdz_table(const Dims &d, const T *__restrict__ dzci, const T *__restrict__ dzfi,
-                                              T (&rdz)[2 * P], int &k0) {
+                                              T (&rdz)[2 * P], int &k0, long t0) {
   const long np = (long)d.n1 * d.n2 * d.n3, nxy = (long)d.n1 * d.n2;
-  const long t0 = (long)blockIdx.x * blockDim.x;
   const long tl = (t0 + (long)blockDim.x < np ? t0 + (long)blockDim.x : np) - 1;
   k0 = (int)(t0 / nxy) + 1;
   const int nk = t0 < np ? (int)(tl / nxy) + 2 - k0 : 0;
