@@ -150,31 +150,31 @@ constexpr int kMaxPrimeRadix = 61;
 template <int SIGN, typename T2>
 __device__ __forceinline__ void fft_stage_prime(const T2 *__restrict__ src, T2 *__restrict__ dst, int m, int nlines,
                                                 int ld, int Ns, const T2 *__restrict__ tw, int R) {
+  // no per-thread array of the R inputs (it would give every runtime-length transform
+  // kernel a stack frame): each output re-reads its inputs from shared memory and
+  // re-applies the stage twiddle, the same products in the same order
   const int nb = m / R, total = nb * nlines, tws = m / (Ns * R), rs = m / R;
   for (int b = threadIdx.x; b < total; b += blockDim.x) {
     const int line = b / nb, jb = b - line * nb;
     const T2 *s = src + line * ld;
     T2 *d = dst + line * ld;
     const int k = jb % Ns;
-    T2 v[kMaxPrimeRadix];
-    for (int r = 0; r < R; ++r) {
-      v[r] = s[jb + r * nb];
-      if (r > 0 && Ns > 1) {
-        T2 w = tw[r * k * tws];
-        if (SIGN > 0) w.y = -w.y;
-        v[r] = cmul(v[r], w);
-      }
-    }
     const int idxD = (jb / Ns) * Ns * R + k;
     for (int q = 0; q < R; ++q) {
-      T2 acc = v[0];
+      T2 acc = s[jb];
       int e = 0;  // (r q) mod R
       for (int r = 1; r < R; ++r) {
         e += q;
         if (e >= R) e -= R;
+        T2 x = s[jb + r * nb];
+        if (Ns > 1) {
+          T2 w1 = tw[r * k * tws];
+          if (SIGN > 0) w1.y = -w1.y;
+          x = cmul(x, w1);
+        }
         T2 w = tw[e * rs];
         if (SIGN > 0) w.y = -w.y;
-        acc = cadd(acc, cmul(v[r], w));
+        acc = cadd(acc, cmul(x, w));
       }
       d[idxD + q * Ns] = acc;
     }
