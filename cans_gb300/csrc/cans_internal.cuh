@@ -46,6 +46,19 @@ template <int SIGN, typename T2> __device__ __forceinline__ T2 cmul_i(T2 a) {
   return SIGN < 0 ? cmk<T2>(a.y, -a.x) : cmk<T2>(-a.y, a.x);
 }
 
+// x / 2^S, exactly.  For FP64 the exponent field is lowered by S on the integer pipe (GB300
+// issues FP64 multiplies at 1/58 of its FP32 rate); zero, results that would be subnormal,
+// infinities and NaNs take the multiply, out of line so that it is not issued for the rest.
+// FP32: the multiply.
+template <int S> static __device__ __noinline__ double pow2_scale_mul(double x) { return (1.0 / (1 << S)) * x; }
+template <int S> __device__ __forceinline__ float pow2_scale(float x) { return (1.0f / (1 << S)) * x; }
+template <int S> __device__ __forceinline__ double pow2_scale(double x) {
+  const long long b = __double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e > (unsigned)S && e < 0x7ffu) return __longlong_as_double(b - ((long long)S << 52));
+  return pow2_scale_mul<S>(x);
+}
+
 // haloed field index, Fortran order, extents (n1+2,n2+2,n3+2)
 __host__ __device__ __forceinline__ size_t hidx(int i, int j, int k, int n1, int n2) {
   return (size_t)i + (size_t)(n1 + 2) * ((size_t)j + (size_t)(n2 + 2) * (size_t)k);

@@ -575,8 +575,8 @@ __device__ __forceinline__ T r2r_post(const DirParams &P, const cplx_t<T> *__res
   switch (kind) {
     case K_R2HC: {
       const T2 a = L[zpos<M, LAY>(k)], b = L[zpos<M, LAY>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
-      if (2 * k <= n) return wsel == 0 ? T(0.5) * (a.x + b.x) : T(0.5) * (a.y + b.y);
-      return wsel == 0 ? T(0.5) * (b.y - a.y) : T(0.5) * (a.x - b.x);
+      if (2 * k <= n) return wsel == 0 ? pow2_scale<1>(a.x + b.x) : pow2_scale<1>(a.y + b.y);
+      return wsel == 0 ? pow2_scale<1>(b.y - a.y) : pow2_scale<1>(a.x - b.x);
     }
     case K_REDFT10:
     case K_RODFT10: {
@@ -619,8 +619,9 @@ __device__ __forceinline__ void r2r_post2(const DirParams &P, const cplx_t<T> *_
   switch (kind) {
     case K_R2HC: {
       const T2 a = L[zpos<M, LAY>(k)], b = L[zpos<M, LAY>(M ? ((m - k) & (M - 1)) : ((m - k) % m))];
-      if (2 * k <= n) { v0 = T(0.5) * (a.x + b.x); v1 = T(0.5) * (a.y + b.y); }
-      else { v0 = T(0.5) * (b.y - a.y); v1 = T(0.5) * (a.x - b.x); }
+      // the halves exactly (pow2_scale: off the FP64 pipe for FP64 transforms)
+      if (2 * k <= n) { v0 = pow2_scale<1>(a.x + b.x); v1 = pow2_scale<1>(a.y + b.y); }
+      else { v0 = pow2_scale<1>(b.y - a.y); v1 = pow2_scale<1>(a.x - b.x); }
     } break;
     case K_REDFT10:
     case K_RODFT10: {

@@ -69,18 +69,6 @@ __device__ __forceinline__ void updatep_cell(const Dims &d, double dxi, double d
   }
 }
 
-// 0.25 x, exactly: for FP64 the exponent field is lowered by 2 on the integer pipe (GB300
-// issues FP64 multiplies at 1/58 of its FP32 rate); zero, results that would be subnormal,
-// infinities and NaNs take the multiply, out of line so that it is not issued for the rest
-static __device__ __noinline__ double quarter_mul(double x) { return 0.25 * x; }
-template <typename T> __device__ __forceinline__ T quarter(T x) { return T(0.25) * x; }
-template <> __device__ __forceinline__ double quarter<double>(double x) {
-  const long long b = __double_as_longlong(x);
-  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
-  if (e > 2u && e < 0x7ffu) return __longlong_as_double(b - (2LL << 52));
-  return quarter_mul(x);
-}
-
 // The 27 velocity values, 4 pressure values and 4 grid factors the fused momentum update of
 // one cell reads: name suffix = offset in (x, y, z), m = -1, c = 0, p = +1.
 template <typename T> struct MomIn {
@@ -133,9 +121,9 @@ __device__ __forceinline__ void mom_rk_point(const MomIn<T> &m, T dxi, T dyi, T 
   const T dudxp = (m.u_pcc - m.u_ccc) * dxi, dudxm = (m.u_ccc - m.u_mcc) * dxi;
   const T dudyp = (m.u_cpc - m.u_ccc) * dyi, dudym = (m.u_ccc - m.u_cmc) * dyi;
   const T dudzp = (m.u_ccp - m.u_ccc) * dzci_k, dudzm = (m.u_ccc - m.u_ccm) * dzci_km;
-  const T uuip = quarter<T>(m.u_ccc + m.u_pcc) * m.u_pcc, uuim = quarter<T>(m.u_ccc + m.u_mcc) * m.u_mcc;
-  const T vujp = quarter<T>(m.v_ccc + m.v_pcc) * m.u_cpc, vujm = quarter<T>(m.v_cmc + m.v_pmc) * m.u_cmc;
-  const T wukp = quarter<T>(m.w_ccc + m.w_pcc) * m.u_ccp, wukm = quarter<T>(m.w_ccm + m.w_pcm) * m.u_ccm;
+  const T uuip = pow2_scale<2>(m.u_ccc + m.u_pcc) * m.u_pcc, uuim = pow2_scale<2>(m.u_ccc + m.u_mcc) * m.u_mcc;
+  const T vujp = pow2_scale<2>(m.v_ccc + m.v_pcc) * m.u_cpc, vujm = pow2_scale<2>(m.v_cmc + m.v_pmc) * m.u_cmc;
+  const T wukp = pow2_scale<2>(m.w_ccc + m.w_pcc) * m.u_ccp, wukm = pow2_scale<2>(m.w_ccm + m.w_pcm) * m.u_ccm;
   const T dudtd_xy = visc * (dudxp - dudxm) * dxi + visc * (dudyp - dudym) * dyi;
   const T dudtd_z = visc * (dudzp - dudzm) * dzfi_k;
   dudt = -(uuip - uuim) * dxi - (vujp - vujm) * dyi - (wukp - wukm) * dzfi_k;
@@ -143,9 +131,9 @@ __device__ __forceinline__ void mom_rk_point(const MomIn<T> &m, T dxi, T dyi, T 
   const T dvdxp = (m.v_pcc - m.v_ccc) * dxi, dvdxm = (m.v_ccc - m.v_mcc) * dxi;
   const T dvdyp = (m.v_cpc - m.v_ccc) * dyi, dvdym = (m.v_ccc - m.v_cmc) * dyi;
   const T dvdzp = (m.v_ccp - m.v_ccc) * dzci_k, dvdzm = (m.v_ccc - m.v_ccm) * dzci_km;
-  const T uvip = quarter<T>(m.u_ccc + m.u_cpc) * m.v_pcc, uvim = quarter<T>(m.u_mcc + m.u_mpc) * m.v_mcc;
-  const T vvjp = quarter<T>(m.v_ccc + m.v_cpc) * m.v_cpc, vvjm = quarter<T>(m.v_ccc + m.v_cmc) * m.v_cmc;
-  const T wvkp = quarter<T>(m.w_ccc + m.w_cpc) * m.v_ccp, wvkm = quarter<T>(m.w_ccm + m.w_cpm) * m.v_ccm;
+  const T uvip = pow2_scale<2>(m.u_ccc + m.u_cpc) * m.v_pcc, uvim = pow2_scale<2>(m.u_mcc + m.u_mpc) * m.v_mcc;
+  const T vvjp = pow2_scale<2>(m.v_ccc + m.v_cpc) * m.v_cpc, vvjm = pow2_scale<2>(m.v_ccc + m.v_cmc) * m.v_cmc;
+  const T wvkp = pow2_scale<2>(m.w_ccc + m.w_cpc) * m.v_ccp, wvkm = pow2_scale<2>(m.w_ccm + m.w_cpm) * m.v_ccm;
   const T dvdtd_xy = visc * (dvdxp - dvdxm) * dxi + visc * (dvdyp - dvdym) * dyi;
   const T dvdtd_z = visc * (dvdzp - dvdzm) * dzfi_k;
   dvdt = -(uvip - uvim) * dxi - (vvjp - vvjm) * dyi - (wvkp - wvkm) * dzfi_k;
@@ -153,11 +141,11 @@ __device__ __forceinline__ void mom_rk_point(const MomIn<T> &m, T dxi, T dyi, T 
   const T dwdxp = (m.w_pcc - m.w_ccc) * dxi, dwdxm = (m.w_ccc - m.w_mcc) * dxi;
   const T dwdyp = (m.w_cpc - m.w_ccc) * dyi, dwdym = (m.w_ccc - m.w_cmc) * dyi;
   const T dwdzp = (m.w_ccp - m.w_ccc) * dzfi_kp, dwdzm = (m.w_ccc - m.w_ccm) * dzfi_k;
-  const T uwip = quarter<T>(rdzm * m.u_ccc + rdzp * m.u_ccp) * m.w_pcc;
-  const T uwim = quarter<T>(rdzm * m.u_mcc + rdzp * m.u_mcp) * m.w_mcc;
-  const T vwjp = quarter<T>(rdzm * m.v_ccc + rdzp * m.v_ccp) * m.w_cpc;
-  const T vwjm = quarter<T>(rdzm * m.v_cmc + rdzp * m.v_cmp) * m.w_cmc;
-  const T wwkp = quarter<T>(m.w_ccc + m.w_ccp) * m.w_ccp, wwkm = quarter<T>(m.w_ccc + m.w_ccm) * m.w_ccm;
+  const T uwip = pow2_scale<2>(rdzm * m.u_ccc + rdzp * m.u_ccp) * m.w_pcc;
+  const T uwim = pow2_scale<2>(rdzm * m.u_mcc + rdzp * m.u_mcp) * m.w_mcc;
+  const T vwjp = pow2_scale<2>(rdzm * m.v_ccc + rdzp * m.v_ccp) * m.w_cpc;
+  const T vwjm = pow2_scale<2>(rdzm * m.v_cmc + rdzp * m.v_cmp) * m.w_cmc;
+  const T wwkp = pow2_scale<2>(m.w_ccc + m.w_ccp) * m.w_ccp, wwkm = pow2_scale<2>(m.w_ccc + m.w_ccm) * m.w_ccm;
   const T dwdtd_xy = visc * (dwdxp - dwdxm) * dxi + visc * (dwdyp - dwdym) * dyi;
   const T dwdtd_z = visc * (dwdzp - dwdzm) * dzci_k;
   dwdt = -(uwip - uwim) * dxi - (vwjp - vwjm) * dyi - (wwkp - wwkm) * dzci_k;
