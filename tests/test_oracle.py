@@ -21,7 +21,7 @@ def _hc(x):
     return hc
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 5, 8, 13, 16, 48, 64, 97, 112, 384])
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 8, 13, 16, 22, 34, 48, 61, 64, 69, 97, 112, 384])
 def test_r2r_kinds_match_scipy(n):
     """FFTW r2r semantics (src/fft.f90:260-313 kinds) vs pocketfft and numpy."""
     rng = np.random.default_rng(n)
