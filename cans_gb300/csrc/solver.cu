@@ -840,11 +840,14 @@ template <typename T> static int set_smem(const void *fn, size_t bytes) {
 
 // CTAs of a persistent pass kernel: resident CTAs per SM x SMs, at most one per tile
 static int resident_grid(const void *fn, size_t smem, long tiles, unsigned *grid) {
-  static int nsm = 0;
+  // SM count per device, read once (atomics: plans may launch from several host threads)
+  static std::atomic<int> s_nsm[64];
+  int dev = 0;
+  CANS_CUDA_TRY(cudaGetDevice(&dev));
+  int nsm = dev >= 0 && dev < 64 ? s_nsm[dev].load(std::memory_order_relaxed) : 0;
   if (!nsm) {
-    int dev = 0;
-    CANS_CUDA_TRY(cudaGetDevice(&dev));
     CANS_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    if (dev >= 0 && dev < 64) s_nsm[dev].store(nsm, std::memory_order_relaxed);
   }
   // resident CTAs per SM of (kernel, shared memory), computed once
   static std::mutex mu;
